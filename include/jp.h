@@ -1,0 +1,179 @@
+/*
+ * jp.h - C ABI of the GB300 lattice Boltzmann engine (libjpsolver.so).
+ *
+ * The reference (josepedro/jp-solver) has no library interface: its "API" is the command line of
+ * two programs, src/tgv3d_uniform.cu and src/tgv3d_amr.cu, whose main() parses flags, allocates the
+ * populations, runs the time loop and prints diagnostics. Every entry point below replaces one piece
+ * of those main() functions (cited per entry), so that the drop-in `uniform` / `amr` programs and any
+ * other host (Python ctypes, cgo, JNI) drive the same device code through plain pointers and sizes.
+ *
+ * Conventions
+ *   - Every call returns jp_status; JP_OK is 0.  On failure jp_last_error() gives a message (per
+ *     host thread).  No entry point calls exit().
+ *   - A solver owns all of its device memory and one CUDA stream; host buffers belong to the caller.
+ *   - One solver is driven by one host thread at a time.
+ *   - Populations cross the boundary in the reference's D3Q19 velocity order
+ *     (q: 0 rest, 1..6 faces +x -x +y -y +z -z, 7..18 edges; src/tgv3d_uniform.cu:28-33) and either
+ *     in the flat layout [q][z][y][x] or in the reference's blocked layout [block][q][cell]
+ *     (block = (bz*gx+by)*gx+bx, cell = (k*MB+j)*MB+i; src/tgv3d_uniform.cu:43-53).
+ */
+#ifndef JP_H
+#define JP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JP_ABI_VERSION 1
+
+typedef enum jp_status {
+    JP_OK = 0,
+    JP_ERR_INVALID = 1,     /* bad argument: the reference exits 2 on N%MB (src/tgv3d_uniform.cu:148) */
+    JP_ERR_CUDA = 2,        /* a CUDA runtime error: the reference's CK() exits 2 (src/tgv3d_uniform.cu:25) */
+    JP_ERR_CAPACITY = 3,    /* a block pool or a fixed-size buffer would overflow */
+    JP_ERR_NOMEM = 4,       /* the device or the HBM budget cannot hold the request */
+    JP_ERR_STATE = 5,       /* call not valid in the solver's current state */
+    JP_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
+    JP_ERR_UNSUPPORTED = 7  /* valid request this build does not implement */
+} jp_status;
+
+typedef enum jp_kind { JP_UNIFORM = 0, JP_AMR = 1 } jp_kind;
+
+/* Population storage.  FP32 is the reference's format.  FP16/BF16 store the shifted value f - w_q
+ * (w_q the lattice weight) and collide in FP32; FP64 stores and computes in double. */
+typedef enum jp_storage { JP_FP32 = 0, JP_FP16 = 1, JP_BF16 = 2, JP_FP64 = 3 } jp_storage;
+
+typedef enum jp_layout { JP_LAYOUT_FLAT = 0, JP_LAYOUT_BLOCKED = 1 } jp_layout;
+
+/* Host element type of a population copy. */
+typedef enum jp_dtype { JP_F32 = 0, JP_F64 = 1 } jp_dtype;
+
+/* Refinement mode of one AMR level (--l1/--l2 all|slab|sensor, src/tgv3d_amr.cu:651). */
+typedef enum jp_refine { JP_REFINE_ALL = 0, JP_REFINE_SLAB = 1, JP_REFINE_SENSOR = 2 } jp_refine;
+
+/* Solver configuration.  Defaults (jp_config_default) are the reference's flag defaults:
+ * uniform --n 128 --re 1600 --u0 0.05 --tstar 12 (src/tgv3d_uniform.cu:143-147);
+ * amr --n 32 --re 800 --frac1 0.35 --frac2 0.35 --l1 all --l2 all --adapt 100 --maxgb 0
+ * (src/tgv3d_amr.cu:644-656,674,685). */
+typedef struct jp_config {
+    int32_t kind;            /* jp_kind */
+    int32_t n;               /* uniform edge, or AMR coarse edge; a multiple of mb */
+    double re;               /* Reynolds number */
+    double u0;               /* TGV velocity amplitude (lattice units) */
+    double tstar;            /* end time in t* = s * u0 * 2pi/n */
+    int32_t storage;         /* jp_storage */
+    int32_t mb;              /* block edge (4, 8 or 16); the reference's -DMB */
+    int32_t l1_mode;         /* jp_refine, AMR only */
+    int32_t l2_mode;         /* jp_refine, AMR only */
+    double frac1, frac2;     /* target refined fractions (sensor mode) */
+    int32_t adapt_every;     /* regrid period in coarse steps (sensor mode) */
+    int32_t develop_steps;   /* uncounted coarse steps before the first sensor build (300) */
+    double max_gb;           /* HBM ceiling for the fine pools in GiB; 0 = 75% of free memory */
+    int32_t device;          /* CUDA device ordinal */
+    int32_t threads_per_block; /* 0 = tuned default */
+    int32_t vec;             /* cells per thread along x in the uniform step; 0 = tuned default */
+    int32_t reserved[8];
+} jp_config;
+
+/* Derived quantities of a solver (src/tgv3d_uniform.cu:151-153, src/tgv3d_amr.cu:658-664). */
+typedef struct jp_info {
+    int32_t kind, n, mb, storage;
+    int64_t cells;           /* uniform: n^3; AMR: coarse n^3 */
+    int64_t steps;           /* round(tstar / (u0 * 2pi/n)) */
+    double nu, tau, omega;   /* level-0 viscosity, relaxation time, 1/tau */
+    double tau1, tau2;       /* AMR level 1/2 relaxation times */
+    double kf;               /* 2pi/n */
+    int64_t bytes_state;     /* device bytes of the double-buffered populations */
+    int64_t step_count;      /* time steps taken so far */
+    int32_t reserved[8];
+} jp_info;
+
+typedef struct jp_solver jp_solver;
+
+/* ---- lifecycle ---------------------------------------------------------------------------- */
+
+/* Fill *cfg with the reference's defaults for `kind`. */
+void jp_config_default(jp_config* cfg, int32_t kind);
+
+/* Allocate a solver and put the Taylor-Green initial state in it.
+ * Replaces the allocation and k_init_tgv3d launch of src/tgv3d_uniform.cu:157-161
+ * (AMR: src/tgv3d_amr.cu:669-670 and the initial build gpurce_init, :776-816). */
+jp_status jp_create(const jp_config* cfg, jp_solver** out);
+
+/* Free all device memory of a solver.  Accepts NULL. */
+void jp_destroy(jp_solver* s);
+
+/* Last error message of the calling host thread ("" if none). */
+const char* jp_last_error(void);
+
+/* ABI version and build description. */
+int32_t jp_abi_version(void);
+const char* jp_build_info(void);
+
+/* sizeof(jp_config) for which=0, sizeof(jp_info) for which=1, else 0: lets an FFI binding check
+ * its struct mirrors against the library it loaded. */
+size_t jp_sizeof(int32_t which);
+
+/* Derived quantities (nu, tau, steps...). */
+jp_status jp_get_info(const jp_solver* s, jp_info* out);
+
+/* Re-initialise the populations with the Taylor-Green state and reset the step counter
+ * (src/tgv3d_uniform.cu:63-77, src/tgv3d_amr.cu:431-440). */
+jp_status jp_init_tgv(jp_solver* s);
+
+/* ---- time stepping ------------------------------------------------------------------------ */
+
+/* Advance `nsteps` time steps (uniform: the k_step launch of src/tgv3d_uniform.cu:194;
+ * AMR: base_step, src/tgv3d_amr.cu:821-837, one coarse step each).  Asynchronous on the solver's
+ * stream; errors of the launches are reported here or by the next synchronising call. */
+jp_status jp_step(jp_solver* s, int64_t nsteps);
+
+/* Wait for all work of the solver. */
+jp_status jp_sync(jp_solver* s);
+
+/* Mean kinetic energy 1/2|u|^2, mean enstrophy 1/2|omega|^2 (central differences, periodic) and
+ * mean density of the current state, computed on the device in FP64 with a deterministic reduction.
+ * out[0]=E, out[1]=enstrophy, out[2]=mass.  Replaces k_macro + the host loop of
+ * src/tgv3d_uniform.cu:169-189 and k_composite + k_diag_reduce of src/tgv3d_amr.cu:882-888. */
+jp_status jp_diag(jp_solver* s, double out[3]);
+
+/* ---- population I/O (parity checks, checkpoint/restart, host-resident workloads) ----------- */
+
+/* Number of population values (19 per cell) of AMR level `level` (0 for uniform). */
+jp_status jp_population_count(const jp_solver* s, int32_t level, int64_t* count);
+
+/* Copy the populations of `level` to a host buffer of `count` values of type `dtype`, in `layout`.
+ * Shifted FP16/BF16 storage is returned unshifted (f = w_q + stored). */
+jp_status jp_get_populations(jp_solver* s, int32_t level, int32_t layout, int32_t dtype,
+                             void* host, int64_t count);
+
+/* Overwrite the populations of `level` from a host buffer (the inverse of jp_get_populations).
+ * From pinned memory in the native layout and type the copy is one asynchronous DMA. */
+jp_status jp_set_populations(jp_solver* s, int32_t level, int32_t layout, int32_t dtype,
+                             const void* host, int64_t count);
+
+/* Macroscopic field of the current uniform state: `host` receives n^3 float4 (rho, ux, uy, uz) in
+ * the linear order (z*n+y)*n+x, as k_macro writes it (src/tgv3d_uniform.cu:80-90). */
+jp_status jp_get_macro(jp_solver* s, float* host, int64_t count);
+
+/* Pinned host memory for asynchronous copies (cudaMallocHost / cudaFreeHost). */
+jp_status jp_host_alloc(void** ptr, size_t bytes);
+void jp_host_free(void* ptr);
+
+/* ---- measurement ---------------------------------------------------------------------------- */
+
+/* Advance `nsteps` steps and return the device time of those launches, measured with CUDA events
+ * recorded on the solver's own stream (the stream the kernels run on). */
+jp_status jp_step_timed(jp_solver* s, int64_t nsteps, float* ms);
+
+/* Number of kernel launches this library has issued in this process. */
+int64_t jp_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JP_H */

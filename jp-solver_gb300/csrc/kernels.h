@@ -1,0 +1,61 @@
+// Internal launch interface between the C ABI (capi.cu) and the kernel translation units.
+// Nothing here is exported from the shared library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+namespace jp {
+
+// ---- uniform periodic cube, flat SoA layout [q][z][y][x] ----------------------------------------
+
+// One periodic cube of a batched stream-collide launch.
+struct UniSolve {
+    const void* src;         // populations at t   (19 * n^3 elements)
+    void* dst;               // populations at t+1
+    int n;                   // edge
+    int nxs;                 // n / V: x segments per row
+    float omega;             // 1/tau (FP32 and shifted storages)
+    int pad;
+    double omega_d;          // 1/tau (FP64 storage)
+    long long blk_begin;     // first CUDA block of this cube in the launch
+    long long nseg;          // n^3 / V threads
+};
+constexpr int kMaxBatch = 48;
+struct UniBatch {
+    int count;
+    int pad;
+    UniSolve s[kMaxBatch];
+};
+
+// Launch one stream-collide over `count` cubes of the same storage format (storage id of jp_storage).
+// vec: cells per thread along x (0 = default), tpb: threads per block (0 = default).
+// Returns the CUDA error of the launch.
+cudaError_t launch_stream_collide(int storage, const UniSolve* solves, int count, int vec, int tpb,
+                                  cudaStream_t st);
+
+// Largest supported vec for a storage; a valid vec divides n and keeps n^3/vec a multiple of 32.
+int default_vec(int storage);
+bool vec_supported(int storage, int vec);
+
+// TGV initial state (src/tgv3d_uniform.cu:63-77) into flat storage.
+cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, cudaStream_t st);
+
+// Macroscopic field (rho, ux, uy, uz) per cell, linear (z*n+y)*n+x.  FP64 storage writes double4,
+// every other storage float4 (k_macro, src/tgv3d_uniform.cu:80-90).
+cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStream_t st);
+
+// Energy, enstrophy, mass of a macro field, reduced deterministically to out_dev[3] (device).
+// partials_dev holds kDiagBlocks*3 doubles.  float_diff=true takes the velocity differences in
+// float before widening (the uniform host loop, src/tgv3d_uniform.cu:103-105); false in double
+// (k_diag_reduce, src/tgv3d_amr.cu:542-546).
+constexpr int kDiagBlocks = 1216;   // 152 SMs x 8
+constexpr int kDiagThreads = 256;
+cudaError_t launch_diag_field(bool field_is_double, bool float_diff, const void* field, int n,
+                              double* partials_dev, double* out_dev, cudaStream_t st);
+
+// Count of kernel launches issued by this library (for the bench's launch accounting).
+void note_launch(int k = 1);
+long long launch_count();
+
+}  // namespace jp

@@ -1,0 +1,66 @@
+// Solver object behind the opaque jp_solver handle, and the per-kind implementations the C ABI
+// dispatches to.  Internal to libjpsolver.so.
+#pragma once
+#include "jp.h"
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace jp {
+struct AmrState;
+
+jp_status fail(jp_status st, const char* fmt, ...);
+jp_status cuda_fail(cudaError_t e, const char* what);
+size_t storage_bytes(int storage);
+double stored_to_double(int storage, const void* base, size_t idx, int q);
+void double_to_stored(int storage, void* base, size_t idx, int q, double v);
+}  // namespace jp
+
+struct jp_solver {
+    jp_config cfg{};
+    jp_info info{};
+    int kind = 0;
+    int device = 0;
+    int storage = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int64_t step_count = 0;
+
+    // uniform cube (flat [q][z][y][x])
+    int n = 0;
+    long long cells = 0;
+    size_t elem = 0;           // bytes per stored population
+    void* fa = nullptr;        // state at the current time
+    void* fb = nullptr;        // next state
+    void* field = nullptr;     // macro field (float4 or double4 per cell), allocated on first use
+    double* partials = nullptr;  // diagnostic block partials (kDiagBlocks*3)
+    double* diag_dev = nullptr;  // 3 doubles
+    double* diag_host = nullptr; // 3 doubles, pinned
+    int vec = 0, tpb = 0;
+
+    jp::AmrState* amr = nullptr;
+};
+
+namespace jp {
+// uniform (solver_uniform.cu)
+jp_status uniform_create(jp_solver* s);
+void uniform_free(jp_solver* s);
+jp_status uniform_init(jp_solver* s);
+jp_status uniform_step(jp_solver* s, int64_t nsteps);
+jp_status uniform_diag(jp_solver* s, double out[3]);
+jp_status uniform_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count);
+jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype, const void* host, int64_t count);
+jp_status uniform_get_macro(jp_solver* s, float* host, int64_t count);
+jp_status common_setup(jp_solver* s);
+
+// AMR (solver_amr.cu)
+jp_status amr_create(jp_solver* s);
+void amr_destroy(jp_solver* s);
+jp_status amr_init(jp_solver* s);
+jp_status amr_step(jp_solver* s, int64_t nsteps);
+jp_status amr_diag(jp_solver* s, double out[3]);
+jp_status amr_population_count(const jp_solver* s, int level, int64_t* count);
+jp_status amr_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count);
+jp_status amr_set_populations(jp_solver* s, int level, int layout, int dtype, const void* host, int64_t count);
+}  // namespace jp

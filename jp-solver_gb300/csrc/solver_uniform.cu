@@ -1,0 +1,228 @@
+// Uniform periodic solver: one cube in the flat layout, double-buffered, stepped by the batched
+// stream-collide kernel (batch of one), with the device diagnostic reduction.
+// Reference: main() of src/tgv3d_uniform.cu:142-203.
+#include "jp.h"
+#include "kernels.h"
+#include "lattice.cuh"
+#include "solver.h"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace jp {
+
+#define JP_CK(call, what)                                   \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what);  \
+    } while (0)
+
+// nu, tau and the step count exactly as the reference derives them (src/tgv3d_uniform.cu:151-153,
+// src/tgv3d_amr.cu:659-664).
+jp_status common_setup(jp_solver* s) {
+    const jp_config& c = s->cfg;
+    s->kind = c.kind;
+    s->device = c.device;
+    s->storage = c.storage;
+    int ndev = 0;
+    JP_CK(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+    if (c.device < 0 || c.device >= ndev) return fail(JP_ERR_INVALID, "device %d out of range (%d devices)", c.device, ndev);
+    JP_CK(cudaSetDevice(c.device), "cudaSetDevice");
+    JP_CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    JP_CK(cudaEventCreate(&s->ev0), "cudaEventCreate");
+    JP_CK(cudaEventCreate(&s->ev1), "cudaEventCreate");
+    jp_info& in = s->info;
+    std::memset(&in, 0, sizeof in);
+    in.kind = c.kind;
+    in.n = c.n;
+    in.mb = c.mb;
+    in.storage = c.storage;
+    in.cells = (int64_t)c.n * c.n * c.n;
+    const double N = double(c.n);
+    in.nu = c.u0 * N / (2.0 * M_PI * c.re);
+    in.tau = 3.0 * in.nu + 0.5;
+    in.omega = double(float(1.0 / in.tau));
+    if (c.storage == JP_FP64) in.omega = 1.0 / in.tau;
+    in.tau1 = 2.0 * in.tau - 0.5;
+    in.tau2 = 2.0 * in.tau1 - 0.5;
+    in.kf = 2.0 * M_PI / N;
+    in.steps = (int64_t)(long)(c.tstar / (c.u0 * in.kf) + 0.5);
+    return JP_OK;
+}
+
+static int pick_vec(int storage, int n, int want) {
+    const int cand[4] = {8, 4, 2, 1};
+    for (int v : cand) {
+        if (want && v != want) continue;
+        if (!vec_supported(storage, v)) continue;
+        if (want == 0 && v > default_vec(storage)) continue;
+        if (n % v) continue;
+        if (((long long)n * n * n / v) % 32) continue;
+        return v;
+    }
+    return 0;
+}
+
+jp_status uniform_create(jp_solver* s) {
+    jp_status st = common_setup(s);
+    if (st != JP_OK) return st;
+    const jp_config& c = s->cfg;
+    s->n = c.n;
+    s->cells = (long long)c.n * c.n * c.n;
+    s->elem = storage_bytes(c.storage);
+    s->vec = pick_vec(c.storage, c.n, c.vec);
+    if (!s->vec) return fail(JP_ERR_INVALID, "no vector width fits n=%d (requested vec=%d)", c.n, c.vec);
+    s->tpb = c.threads_per_block ? c.threads_per_block : 256;
+    if (s->tpb != 64 && s->tpb != 128 && s->tpb != 256 && s->tpb != 512)
+        return fail(JP_ERR_INVALID, "threads_per_block must be 64, 128, 256 or 512");
+    const size_t bytes = (size_t)Q * s->cells * s->elem;
+    s->info.bytes_state = (int64_t)(2 * bytes);
+    JP_CK(cudaMalloc(&s->fa, bytes), "cudaMalloc populations");
+    JP_CK(cudaMalloc(&s->fb, bytes), "cudaMalloc populations");
+    JP_CK(cudaMalloc(&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
+    JP_CK(cudaMalloc(&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
+    JP_CK(cudaMallocHost(&s->diag_host, sizeof(double) * 3), "cudaMallocHost diag");
+    return uniform_init(s);
+}
+
+void uniform_free(jp_solver* s) {
+    if (s->fa) cudaFree(s->fa);
+    if (s->fb) cudaFree(s->fb);
+    if (s->field) cudaFree(s->field);
+    if (s->partials) cudaFree(s->partials);
+    if (s->diag_dev) cudaFree(s->diag_dev);
+    if (s->diag_host) cudaFreeHost(s->diag_host);
+    s->fa = s->fb = s->field = nullptr;
+    s->partials = s->diag_dev = s->diag_host = nullptr;
+}
+
+jp_status uniform_init(jp_solver* s) {
+    JP_CK(launch_init_tgv(s->storage, s->fa, s->n, s->cfg.u0, s->info.kf, s->stream), "init_tgv");
+    JP_CK(cudaStreamSynchronize(s->stream), "init_tgv");
+    s->step_count = 0;
+    return JP_OK;
+}
+
+jp_status uniform_step(jp_solver* s, int64_t nsteps) {
+    UniSolve u;
+    std::memset(&u, 0, sizeof u);
+    u.n = s->n;
+    u.omega = float(s->info.omega);
+    u.omega_d = s->info.omega;
+    for (int64_t i = 0; i < nsteps; ++i) {
+        u.src = s->fa;
+        u.dst = s->fb;
+        cudaError_t e = launch_stream_collide(s->storage, &u, 1, s->vec, s->tpb, s->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "stream_collide launch");
+        std::swap(s->fa, s->fb);
+        ++s->step_count;
+    }
+    return JP_OK;
+}
+
+static jp_status ensure_field(jp_solver* s) {
+    if (s->field) return JP_OK;
+    const size_t fb = (s->storage == JP_FP64 ? sizeof(double) : sizeof(float)) * 4 * (size_t)s->cells;
+    JP_CK(cudaMalloc(&s->field, fb), "cudaMalloc macro field");
+    return JP_OK;
+}
+
+jp_status uniform_diag(jp_solver* s, double out[3]) {
+    jp_status st = ensure_field(s);
+    if (st != JP_OK) return st;
+    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream), "macro");
+    const bool dbl = s->storage == JP_FP64;
+    JP_CK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, s->diag_dev, s->stream), "diag");
+    JP_CK(cudaMemcpyAsync(s->diag_host, s->diag_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "diag D2H");
+    JP_CK(cudaStreamSynchronize(s->stream), "diag");
+    out[0] = s->diag_host[0];
+    out[1] = s->diag_host[1];
+    out[2] = s->diag_host[2];
+    return JP_OK;
+}
+
+// index of population q of cell (x,y,z) in the blocked layout [block][q][cell] of edge mb
+static inline size_t blocked_index(int n, int mb, int q, int x, int y, int z) {
+    const int gx = n / mb;
+    const size_t b = ((size_t)(z / mb) * gx + (y / mb)) * gx + (x / mb);
+    const size_t cell = ((size_t)(z % mb) * mb + (y % mb)) * mb + (x % mb);
+    return (b * Q + q) * (size_t)mb * mb * mb + cell;
+}
+
+jp_status uniform_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count) {
+    if (level != 0) return fail(JP_ERR_INVALID, "uniform solver has only level 0");
+    if (count != (int64_t)Q * s->cells) return fail(JP_ERR_INVALID, "count %lld != 19*n^3", (long long)count);
+    if (layout != JP_LAYOUT_FLAT && layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_INVALID, "bad layout %d", layout);
+    const size_t bytes = (size_t)count * s->elem;
+    const bool native = layout == JP_LAYOUT_FLAT &&
+                        ((dtype == JP_F32 && s->storage == JP_FP32) || (dtype == JP_F64 && s->storage == JP_FP64));
+    if (native) {
+        JP_CK(cudaMemcpyAsync(host, s->fa, bytes, cudaMemcpyDeviceToHost, s->stream), "populations D2H");
+        JP_CK(cudaStreamSynchronize(s->stream), "populations D2H");
+        return JP_OK;
+    }
+    std::vector<unsigned char> raw(bytes);
+    JP_CK(cudaMemcpyAsync(raw.data(), s->fa, bytes, cudaMemcpyDeviceToHost, s->stream), "populations D2H");
+    JP_CK(cudaStreamSynchronize(s->stream), "populations D2H");
+    const int n = s->n, mb = s->cfg.mb;
+    for (int q = 0; q < Q; ++q)
+        for (int z = 0; z < n; ++z)
+            for (int y = 0; y < n; ++y)
+                for (int x = 0; x < n; ++x) {
+                    const size_t src = (size_t)q * s->cells + ((size_t)z * n + y) * n + x;
+                    const size_t dst = layout == JP_LAYOUT_FLAT ? src : blocked_index(n, mb, q, x, y, z);
+                    const double v = stored_to_double(s->storage, raw.data(), src, q);
+                    if (dtype == JP_F32) static_cast<float*>(host)[dst] = float(v);
+                    else static_cast<double*>(host)[dst] = v;
+                }
+    return JP_OK;
+}
+
+jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype, const void* host, int64_t count) {
+    if (level != 0) return fail(JP_ERR_INVALID, "uniform solver has only level 0");
+    if (count != (int64_t)Q * s->cells) return fail(JP_ERR_INVALID, "count %lld != 19*n^3", (long long)count);
+    if (layout != JP_LAYOUT_FLAT && layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_INVALID, "bad layout %d", layout);
+    const size_t bytes = (size_t)count * s->elem;
+    const bool native = layout == JP_LAYOUT_FLAT &&
+                        ((dtype == JP_F32 && s->storage == JP_FP32) || (dtype == JP_F64 && s->storage == JP_FP64));
+    if (native) {
+        // asynchronous from pinned memory; stream order puts it before the next step
+        JP_CK(cudaMemcpyAsync(s->fa, host, bytes, cudaMemcpyHostToDevice, s->stream), "populations H2D");
+        return JP_OK;
+    }
+    std::vector<unsigned char> raw(bytes);
+    const int n = s->n, mb = s->cfg.mb;
+    for (int q = 0; q < Q; ++q)
+        for (int z = 0; z < n; ++z)
+            for (int y = 0; y < n; ++y)
+                for (int x = 0; x < n; ++x) {
+                    const size_t dst = (size_t)q * s->cells + ((size_t)z * n + y) * n + x;
+                    const size_t src = layout == JP_LAYOUT_FLAT ? dst : blocked_index(n, mb, q, x, y, z);
+                    const double v = dtype == JP_F32 ? double(static_cast<const float*>(host)[src])
+                                                     : static_cast<const double*>(host)[src];
+                    double_to_stored(s->storage, raw.data(), dst, q, v);
+                }
+    JP_CK(cudaMemcpyAsync(s->fa, raw.data(), bytes, cudaMemcpyHostToDevice, s->stream), "populations H2D");
+    JP_CK(cudaStreamSynchronize(s->stream), "populations H2D");
+    return JP_OK;
+}
+
+jp_status uniform_get_macro(jp_solver* s, float* host, int64_t count) {
+    if (count != 4 * (int64_t)s->cells) return fail(JP_ERR_INVALID, "count %lld != 4*n^3", (long long)count);
+    jp_status st = ensure_field(s);
+    if (st != JP_OK) return st;
+    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream), "macro");
+    if (s->storage == JP_FP64) {
+        std::vector<double> tmp((size_t)count);
+        JP_CK(cudaMemcpyAsync(tmp.data(), s->field, (size_t)count * 8, cudaMemcpyDeviceToHost, s->stream), "macro D2H");
+        JP_CK(cudaStreamSynchronize(s->stream), "macro D2H");
+        for (int64_t i = 0; i < count; ++i) host[i] = float(tmp[(size_t)i]);
+        return JP_OK;
+    }
+    JP_CK(cudaMemcpyAsync(host, s->field, (size_t)count * 4, cudaMemcpyDeviceToHost, s->stream), "macro D2H");
+    JP_CK(cudaStreamSynchronize(s->stream), "macro D2H");
+    return JP_OK;
+}
+
+}  // namespace jp

@@ -1,0 +1,443 @@
+// Uniform periodic D3Q19 BGK: Taylor-Green initial state, fused pull stream-collide, macro field and
+// the energy / enstrophy / mass reduction.
+//
+// Reference: src/tgv3d_uniform.cu.  The reference keeps populations as [block][q][8^3 cells] and
+// launches one CUDA block per 8^3 block with a modulo per population to find the pulled cell
+// (k_step, :40-61).  Here a cube lives in the flat SoA layout [q][z][y][x]: a thread owns V
+// consecutive cells of one x-row, reads each of the 19 source rows as one aligned 16-byte vector,
+// and gets the one value that a +-x pull needs from outside its vector from the neighbouring lane by
+// a warp shuffle (a direct load only at the warp and row edges, which wrap periodically).  Every
+// population is therefore read from HBM once and written once per step, with full 128-byte lines
+// on both sides: 152 B per lattice update in FP32, 76 B in FP16/BF16, 304 B in FP64.
+#include "kernels.h"
+#include "lattice.cuh"
+
+#include <atomic>
+
+namespace jp {
+
+static std::atomic<long long> g_launches{0};
+void note_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+// ---- vector access helpers ---------------------------------------------------------------------
+
+template <class RAW, int V>
+struct Pack {
+    static constexpr int bytes = int(sizeof(RAW)) * V;
+    using word = typename std::conditional<bytes == 16, uint4,
+                 typename std::conditional<bytes == 8, uint2,
+                 typename std::conditional<bytes == 4, unsigned int, unsigned short>::type>::type>::type;
+    union {
+        word w;
+        RAW v[V];
+    };
+};
+
+template <class RAW, int V>
+__device__ __forceinline__ Pack<RAW, V> ld_pack(const RAW* p) {
+    Pack<RAW, V> r;
+    r.w = __ldg(reinterpret_cast<const typename Pack<RAW, V>::word*>(p));
+    return r;
+}
+template <class RAW, int V>
+__device__ __forceinline__ void st_pack(RAW* p, const Pack<RAW, V>& r) {
+    __stcs(reinterpret_cast<typename Pack<RAW, V>::word*>(p), r.w);
+}
+
+template <class RAW> __device__ __forceinline__ RAW ld_one(const RAW* p) { return __ldg(p); }
+template <> __device__ __forceinline__ uint16_t ld_one<uint16_t>(const uint16_t* p) {
+    return __ldg(reinterpret_cast<const unsigned short*>(p));
+}
+
+template <class RAW> __device__ __forceinline__ RAW shfl_up1(RAW v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+template <class RAW> __device__ __forceinline__ RAW shfl_dn1(RAW v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+template <> __device__ __forceinline__ uint16_t shfl_up1<uint16_t>(uint16_t v) {
+    return (uint16_t)__shfl_up_sync(0xffffffffu, (unsigned)v, 1);
+}
+template <> __device__ __forceinline__ uint16_t shfl_dn1<uint16_t>(uint16_t v) {
+    return (uint16_t)__shfl_down_sync(0xffffffffu, (unsigned)v, 1);
+}
+
+// ---- stream-collide ---------------------------------------------------------------------------
+
+template <class ST, int V, int TPB>
+__global__ void __launch_bounds__(TPB) k_stream_collide(const __grid_constant__ UniBatch b) {
+    using raw = typename ST::raw;
+    using R = typename ST::real;
+    constexpr bool SH = ST::shifted;
+
+    // which cube this CUDA block belongs to (uniform over the block)
+    int si = 0;
+#pragma unroll 1
+    for (int i = 1; i < b.count; ++i) si = (b.s[i].blk_begin <= (long long)blockIdx.x) ? i : si;
+    const UniSolve& d = b.s[si];
+    const long long seg = ((long long)blockIdx.x - d.blk_begin) * TPB + threadIdx.x;
+    if (seg >= d.nseg) return;  // whole warps: nseg is a multiple of 32
+
+    const int n = d.n;
+    const int nxs = d.nxs;
+    const raw* __restrict__ src = static_cast<const raw*>(d.src);
+    raw* __restrict__ dst = static_cast<raw*>(d.dst);
+    const int xs = int(seg % nxs);
+    const long long r = seg / nxs;
+    const int y = int(r % n);
+    const int z = int(r / n);
+    const int x0 = xs * V;
+    const int lane = threadIdx.x & 31;
+    const size_t qs = (size_t)n * n * n;
+    const int ym = y == 0 ? n - 1 : y - 1, yp = y == n - 1 ? 0 : y + 1;
+    const int zm = z == 0 ? n - 1 : z - 1, zp = z == n - 1 ? 0 : z + 1;
+    const bool prev_direct = (lane == 0) || (x0 == 0);
+    const bool next_direct = (lane == 31) || (x0 + V == n);
+    const int xprev = x0 == 0 ? n - 1 : x0 - 1;
+    const int xnext = (x0 + V == n) ? 0 : x0 + V;
+
+    // 1. issue every load: 19 row vectors + the edge values of the 10 populations with c_x != 0
+    Pack<raw, V> L[Q];
+    raw E[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int sy = cy(q) > 0 ? ym : (cy(q) < 0 ? yp : y);   // pull from y - c_y
+        const int sz = cz(q) > 0 ? zm : (cz(q) < 0 ? zp : z);
+        const raw* p = src + q * qs + ((size_t)sz * n + sy) * n;
+        L[q] = ld_pack<raw, V>(p + x0);
+        E[q] = raw(0);
+        if (cx(q) > 0 && prev_direct) E[q] = ld_one(p + xprev);
+        if (cx(q) < 0 && next_direct) E[q] = ld_one(p + xnext);
+    }
+    // 2. neighbour values across the vector edge from the adjacent lanes
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (cx(q) > 0) {
+            raw t = shfl_up1(L[q].v[V - 1]);
+            if (!prev_direct) E[q] = t;
+        } else if (cx(q) < 0) {
+            raw t = shfl_dn1(L[q].v[0]);
+            if (!next_direct) E[q] = t;
+        }
+    }
+    // value of population q pulled into cell x0+v
+    auto val = [&](int q, int v) -> R {
+        raw e;
+        if (cx(q) > 0) e = (v == 0) ? E[q] : L[q].v[v - 1];
+        else if (cx(q) < 0) e = (v == V - 1) ? E[q] : L[q].v[v + 1];
+        else e = L[q].v[v];
+        return ST::load(e);
+    };
+
+    // 3. moments per cell
+    R rho[V], ux[V], uy[V], uz[V], s[V], usq[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        R f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) f[q] = val(q, v);
+        R sm = f[0];
+#pragma unroll
+        for (int q = 1; q < Q; ++q) sm += f[q];
+        const R jx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+        const R jy = f[3] - f[4] + f[7] - f[8] - f[9] + f[10] + f[15] - f[16] + f[17] - f[18];
+        const R jz = f[5] - f[6] + f[11] - f[12] - f[13] + f[14] + f[15] - f[16] - f[17] + f[18];
+        const R rh = SH ? R(1) + sm : sm;
+        s[v] = sm;
+        rho[v] = rh;
+        ux[v] = jx / rh;
+        uy[v] = jy / rh;
+        uz[v] = jz / rh;
+        usq[v] = R(1.5) * (ux[v] * ux[v] + uy[v] * uy[v] + uz[v] * uz[v]);
+    }
+
+    // 4. relax and store, one population pair at a time
+    const R om = sizeof(R) == 8 ? R(d.omega_d) : R(d.omega);
+    const size_t orow = ((size_t)z * n + y) * n + x0;
+    {
+        Pack<raw, V> o;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const R w0 = wgt<R>(0);
+            const R feq = SH ? w0 * (s[v] - rho[v] * usq[v]) : w0 * rho[v] * (R(1) - usq[v]);
+            const R f = val(0, v);
+            o.v[v] = ST::store(f - om * (f - feq));
+        }
+        st_pack<raw, V>(dst + orow, o);
+    }
+#pragma unroll
+    for (int q = 1; q < Q; q += 2) {
+        Pack<raw, V> op, om_;
+        const R w = wgt<R>(q);
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const R cu = R(3) * (R(cx(q)) * ux[v] + R(cy(q)) * uy[v] + R(cz(q)) * uz[v]);
+            const R wr = w * rho[v];
+            const R sym = SH ? w * s[v] + wr * (R(0.5) * cu * cu - usq[v])
+                             : wr * (R(1) + R(0.5) * cu * cu - usq[v]);
+            const R asym = wr * cu;
+            const R fa = val(q, v), fb = val(q + 1, v);
+            op.v[v] = ST::store(fa - om * (fa - (sym + asym)));
+            om_.v[v] = ST::store(fb - om * (fb - (sym - asym)));
+        }
+        st_pack<raw, V>(dst + q * qs + orow, op);
+        st_pack<raw, V>(dst + (q + 1) * qs + orow, om_);
+    }
+}
+
+int default_vec(int storage) {
+    switch (storage) {
+        case 0: return 4;   // float4
+        case 1: return 8;   // 8 x half
+        case 2: return 8;   // 8 x bf16
+        case 3: return 2;   // double2
+    }
+    return 0;
+}
+bool vec_supported(int storage, int vec) {
+    switch (storage) {
+        case 0: return vec == 1 || vec == 2 || vec == 4;
+        case 1: case 2: return vec == 2 || vec == 4 || vec == 8;
+        case 3: return vec == 1 || vec == 2;
+    }
+    return false;
+}
+
+template <class ST, int V, int TPB>
+static cudaError_t launch_sc(const UniSolve* solves, int count, cudaStream_t st) {
+    UniBatch b;
+    b.count = count;
+    b.pad = 0;
+    long long blocks = 0;
+    for (int i = 0; i < count; ++i) {
+        b.s[i] = solves[i];
+        b.s[i].nxs = solves[i].n / V;
+        b.s[i].nseg = (long long)solves[i].n * solves[i].n * solves[i].n / V;
+        b.s[i].blk_begin = blocks;
+        blocks += (b.s[i].nseg + TPB - 1) / TPB;
+    }
+    if (blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    k_stream_collide<ST, V, TPB><<<(unsigned)blocks, TPB, 0, st>>>(b);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <class ST, int V>
+static cudaError_t launch_sc_tpb(int tpb, const UniSolve* s, int c, cudaStream_t st) {
+    switch (tpb) {
+        case 64: return launch_sc<ST, V, 64>(s, c, st);
+        case 128: return launch_sc<ST, V, 128>(s, c, st);
+        case 512: return launch_sc<ST, V, 512>(s, c, st);
+        default: return launch_sc<ST, V, 256>(s, c, st);
+    }
+}
+
+cudaError_t launch_stream_collide(int storage, const UniSolve* solves, int count, int vec, int tpb,
+                                  cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    if (count > kMaxBatch) return cudaErrorInvalidValue;
+    if (vec == 0) vec = default_vec(storage);
+    if (!vec_supported(storage, vec)) return cudaErrorInvalidValue;
+    for (int i = 0; i < count; ++i)
+        if (solves[i].n % vec != 0 || ((long long)solves[i].n * solves[i].n * solves[i].n / vec) % 32 != 0)
+            return cudaErrorInvalidValue;
+    switch (storage) {
+        case 0:
+            if (vec == 4) return launch_sc_tpb<StF32, 4>(tpb, solves, count, st);
+            if (vec == 2) return launch_sc_tpb<StF32, 2>(tpb, solves, count, st);
+            return launch_sc_tpb<StF32, 1>(tpb, solves, count, st);
+        case 1:
+            if (vec == 8) return launch_sc_tpb<StF16, 8>(tpb, solves, count, st);
+            if (vec == 4) return launch_sc_tpb<StF16, 4>(tpb, solves, count, st);
+            return launch_sc_tpb<StF16, 2>(tpb, solves, count, st);
+        case 2:
+            if (vec == 8) return launch_sc_tpb<StBF16, 8>(tpb, solves, count, st);
+            if (vec == 4) return launch_sc_tpb<StBF16, 4>(tpb, solves, count, st);
+            return launch_sc_tpb<StBF16, 2>(tpb, solves, count, st);
+        case 3:
+            if (vec == 2) return launch_sc_tpb<StF64, 2>(tpb, solves, count, st);
+            return launch_sc_tpb<StF64, 1>(tpb, solves, count, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// ---- Taylor-Green initial state ------------------------------------------------------------------
+// u = u0 sin x cos y cos z, v = -u0 cos x sin y cos z, w = 0 at cell centres (i+0.5)kf, pressure folded
+// into rho = 1 + 3p, p = u0^2/16 (cos2x + cos2y)(cos2z + 2), equilibrium populations
+// (src/tgv3d_uniform.cu:63-77).  FP32 storage rounds rho and u to float and evaluates the float
+// equilibrium as the reference does; FP64 keeps double; shifted formats store the double deviation.
+template <class ST>
+__global__ void k_init_tgv(typename ST::raw* __restrict__ f, int n, double u0, double kf) {
+    const long long cells = (long long)n * n * n;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
+    const double x = (i + 0.5) * kf, y = (j + 0.5) * kf, z = (k + 0.5) * kf;
+    const double ux = u0 * sin(x) * cos(y) * cos(z);
+    const double uy = -u0 * cos(x) * sin(y) * cos(z);
+    const double p = (u0 * u0 / 16.0) * (cos(2 * x) + cos(2 * y)) * (cos(2 * z) + 2.0);
+    const double rho = 1.0 + 3.0 * p;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        typename ST::raw v;
+        if constexpr (ST::id == 0) {
+            v = feq_ref(q, float(rho), float(ux), float(uy), 0.f);
+        } else if constexpr (ST::id == 3) {
+            v = feq_ref_d(q, rho, ux, uy, 0.0);
+        } else {
+            const double cu = 3.0 * (cx(q) * ux + cy(q) * uy);
+            const double g = wd(q) * (3.0 * p + rho * (cu + 0.5 * cu * cu - 1.5 * (ux * ux + uy * uy)));
+            v = ST::store(float(g));
+        }
+        f[(size_t)q * cells + c] = v;
+    }
+}
+
+cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, cudaStream_t st) {
+    const long long cells = (long long)n * n * n;
+    const unsigned blocks = (unsigned)((cells + 255) / 256);
+    switch (storage) {
+        case 0: k_init_tgv<StF32><<<blocks, 256, 0, st>>>((float*)f, n, u0, kf); break;
+        case 1: k_init_tgv<StF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, kf); break;
+        case 2: k_init_tgv<StBF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, kf); break;
+        case 3: k_init_tgv<StF64><<<blocks, 256, 0, st>>>((double*)f, n, u0, kf); break;
+        default: return cudaErrorInvalidValue;
+    }
+    note_launch();
+    return cudaGetLastError();
+}
+
+// ---- macro field ---------------------------------------------------------------------------------
+template <class ST, class FT>
+__global__ void k_macro(const typename ST::raw* __restrict__ f, FT* __restrict__ out, int n) {
+    using R = typename ST::real;
+    const long long cells = (long long)n * n * n;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    R v[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q] = ST::load(f[(size_t)q * cells + c]);
+    R sm = v[0];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) sm += v[q];
+    const R jx = v[1] - v[2] + v[7] - v[8] + v[9] - v[10] + v[11] - v[12] + v[13] - v[14];
+    const R jy = v[3] - v[4] + v[7] - v[8] - v[9] + v[10] + v[15] - v[16] + v[17] - v[18];
+    const R jz = v[5] - v[6] + v[11] - v[12] - v[13] + v[14] + v[15] - v[16] - v[17] + v[18];
+    const R rho = ST::shifted ? R(1) + sm : sm;
+    FT* o = out + 4 * c;
+    o[0] = FT(rho);
+    o[1] = FT(jx / rho);
+    o[2] = FT(jy / rho);
+    o[3] = FT(jz / rho);
+}
+
+cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStream_t st) {
+    const long long cells = (long long)n * n * n;
+    const unsigned blocks = (unsigned)((cells + 255) / 256);
+    switch (storage) {
+        case 0: k_macro<StF32, float><<<blocks, 256, 0, st>>>((const float*)f, (float*)field, n); break;
+        case 1: k_macro<StF16, float><<<blocks, 256, 0, st>>>((const uint16_t*)f, (float*)field, n); break;
+        case 2: k_macro<StBF16, float><<<blocks, 256, 0, st>>>((const uint16_t*)f, (float*)field, n); break;
+        case 3: k_macro<StF64, double><<<blocks, 256, 0, st>>>((const double*)f, (double*)field, n); break;
+        default: return cudaErrorInvalidValue;
+    }
+    note_launch();
+    return cudaGetLastError();
+}
+
+// ---- energy / enstrophy / mass ---------------------------------------------------------------------
+// Per cell: 1/2|u|^2, 1/2|curl u|^2 with central differences (periodic), rho; all in FP64.  Each
+// thread walks a fixed grid-stride sequence of cells, blocks reduce in a fixed tree, and one block
+// sums the block partials in a fixed order, so the result is the same on every run.
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <class FT, bool FLOAT_DIFF>
+__global__ void __launch_bounds__(kDiagThreads) k_diag_field(const FT* __restrict__ F, int n,
+                                                             double* __restrict__ partials) {
+    const long long cells = (long long)n * n * n;
+    double e = 0.0, ens = 0.0, mass = 0.0;
+    for (long long c = (long long)blockIdx.x * kDiagThreads + threadIdx.x; c < cells;
+         c += (long long)gridDim.x * kDiagThreads) {
+        const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
+        const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
+        const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
+        const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
+        auto at = [&](int a, int b, int cc, int comp) -> FT {
+            return F[(((size_t)cc * n + b) * n + a) * 4 + comp];
+        };
+        auto dif = [&](FT a, FT b) -> double {
+            if (FLOAT_DIFF) return double(FT(a - b)) * 0.5;
+            return (double(a) - double(b)) * 0.5;
+        };
+        const double rho = double(F[c * 4 + 0]);
+        const double u = double(F[c * 4 + 1]), v = double(F[c * 4 + 2]), w = double(F[c * 4 + 3]);
+        const double dudy = dif(at(i, jp, k, 1), at(i, jm, k, 1)), dudz = dif(at(i, j, kp, 1), at(i, j, km, 1));
+        const double dvdx = dif(at(ip, j, k, 2), at(im, j, k, 2)), dvdz = dif(at(i, j, kp, 2), at(i, j, km, 2));
+        const double dwdx = dif(at(ip, j, k, 3), at(im, j, k, 3)), dwdy = dif(at(i, jp, k, 3), at(i, jm, k, 3));
+        const double ox = dwdy - dvdz, oy = dudz - dwdx, oz = dvdx - dudy;
+        e += 0.5 * (u * u + v * v + w * w);
+        ens += 0.5 * (ox * ox + oy * oy + oz * oz);
+        mass += rho;
+    }
+    __shared__ double sh[3][kDiagThreads / 32];
+    e = warp_sum(e);
+    ens = warp_sum(ens);
+    mass = warp_sum(mass);
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sh[0][wid] = e;
+        sh[1][wid] = ens;
+        sh[2][wid] = mass;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int i = 0; i < kDiagThreads / 32; ++i) t += sh[threadIdx.x][i];
+        partials[blockIdx.x * 3 + threadIdx.x] = t;
+    }
+}
+
+// Sum `nparts` partial triples in a fixed order and scale by 1/cells.
+__global__ void __launch_bounds__(256) k_diag_finish(const double* __restrict__ partials, int nparts,
+                                                     double inv_cells, double* __restrict__ out) {
+    double a[3] = {0.0, 0.0, 0.0};
+    for (int p = threadIdx.x; p < nparts; p += 256) {
+        a[0] += partials[p * 3 + 0];
+        a[1] += partials[p * 3 + 1];
+        a[2] += partials[p * 3 + 2];
+    }
+    __shared__ double sh[3][8];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double t = warp_sum(a[k]);
+        if (lane == 0) sh[k][wid] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int i = 0; i < 8; ++i) t += sh[threadIdx.x][i];
+        out[threadIdx.x] = t * inv_cells;
+    }
+}
+
+cudaError_t launch_diag_field(bool field_is_double, bool float_diff, const void* field, int n,
+                              double* partials_dev, double* out_dev, cudaStream_t st) {
+    const long long cells = (long long)n * n * n;
+    const int blocks = (int)std::min<long long>(kDiagBlocks, (cells + kDiagThreads - 1) / kDiagThreads);
+    if (field_is_double) {
+        k_diag_field<double, false><<<blocks, kDiagThreads, 0, st>>>((const double*)field, n, partials_dev);
+    } else if (float_diff) {
+        k_diag_field<float, true><<<blocks, kDiagThreads, 0, st>>>((const float*)field, n, partials_dev);
+    } else {
+        k_diag_field<float, false><<<blocks, kDiagThreads, 0, st>>>((const float*)field, n, partials_dev);
+    }
+    k_diag_finish<<<1, 256, 0, st>>>(partials_dev, blocks, 1.0 / double(cells), out_dev);
+    note_launch(2);
+    return cudaGetLastError();
+}
+
+}  // namespace jp

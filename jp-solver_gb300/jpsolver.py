@@ -1,0 +1,217 @@
+"""ctypes binding of libjpsolver.so (the C ABI in include/jp.h).
+
+This is the reference-facing boundary seen from Python: tests and bench.py drive the engine only
+through these calls.  There is no fallback: if the shared library is missing, importing works but
+creating a solver raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libjpsolver.so")
+
+UNIFORM, AMR = 0, 1
+STORAGE = {"fp32": 0, "fp16": 1, "bf16": 2, "fp64": 3}
+REFINE = {"all": 0, "slab": 1, "sensor": 2}
+LAYOUT = {"flat": 0, "blocked": 1}
+Q = 19
+
+
+class JPError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("jp status %d: %s" % (status, msg))
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32), ("n", C.c_int32),
+        ("re", C.c_double), ("u0", C.c_double), ("tstar", C.c_double),
+        ("storage", C.c_int32), ("mb", C.c_int32),
+        ("l1_mode", C.c_int32), ("l2_mode", C.c_int32),
+        ("frac1", C.c_double), ("frac2", C.c_double),
+        ("adapt_every", C.c_int32), ("develop_steps", C.c_int32),
+        ("max_gb", C.c_double),
+        ("device", C.c_int32), ("threads_per_block", C.c_int32), ("vec", C.c_int32),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32), ("n", C.c_int32), ("mb", C.c_int32), ("storage", C.c_int32),
+        ("cells", C.c_int64), ("steps", C.c_int64),
+        ("nu", C.c_double), ("tau", C.c_double), ("omega", C.c_double),
+        ("tau1", C.c_double), ("tau2", C.c_double), ("kf", C.c_double),
+        ("bytes_state", C.c_int64), ("step_count", C.c_int64),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+
+_lib: Optional[C.CDLL] = None
+
+# exported symbol -> (restype, argtypes)
+SIGNATURES = {
+    "jp_config_default": (None, [C.POINTER(Config), C.c_int32]),
+    "jp_create": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
+    "jp_destroy": (None, [C.c_void_p]),
+    "jp_last_error": (C.c_char_p, []),
+    "jp_abi_version": (C.c_int32, []),
+    "jp_build_info": (C.c_char_p, []),
+    "jp_sizeof": (C.c_size_t, [C.c_int32]),
+    "jp_get_info": (C.c_int, [C.c_void_p, C.POINTER(Info)]),
+    "jp_init_tgv": (C.c_int, [C.c_void_p]),
+    "jp_step": (C.c_int, [C.c_void_p, C.c_int64]),
+    "jp_sync": (C.c_int, [C.c_void_p]),
+    "jp_diag": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "jp_population_count": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
+    "jp_get_populations": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]),
+    "jp_set_populations": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]),
+    "jp_get_macro": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
+    "jp_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
+    "jp_host_free": (None, [C.c_void_p]),
+    "jp_step_timed": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
+    "jp_launch_count": (C.c_int64, []),
+}
+
+
+def lib() -> C.CDLL:
+    """Load libjpsolver.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libjpsolver.so not found at %s: run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(st: int) -> None:
+    if st != 0:
+        raise JPError(st, lib().jp_last_error().decode())
+
+
+def config(kind: str = "uniform", **kw) -> Config:
+    c = Config()
+    lib().jp_config_default(C.byref(c), UNIFORM if kind == "uniform" else AMR)
+    for k, v in kw.items():
+        if k == "storage" and isinstance(v, str):
+            v = STORAGE[v]
+        if k in ("l1_mode", "l2_mode") and isinstance(v, str):
+            v = REFINE[v]
+        if not hasattr(c, k):
+            raise KeyError("unknown config field %r" % k)
+        setattr(c, k, v)
+    return c
+
+
+class Solver:
+    """One solve on the GPU (uniform periodic cube or 3-level AMR)."""
+
+    def __init__(self, kind: str = "uniform", **kw):
+        self.cfg = config(kind, **kw)
+        h = C.c_void_p()
+        _check(lib().jp_create(C.byref(self.cfg), C.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().jp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def info(self) -> dict:
+        i = Info()
+        _check(lib().jp_get_info(self.h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in Info._fields_ if k != "reserved"}
+
+    def init_tgv(self) -> None:
+        _check(lib().jp_init_tgv(self.h))
+
+    def step(self, n: int = 1) -> None:
+        _check(lib().jp_step(self.h, n))
+
+    def sync(self) -> None:
+        _check(lib().jp_sync(self.h))
+
+    def step_timed(self, n: int) -> float:
+        ms = C.c_float()
+        _check(lib().jp_step_timed(self.h, n, C.byref(ms)))
+        return ms.value
+
+    def diag(self) -> tuple:
+        out = (C.c_double * 3)()
+        _check(lib().jp_diag(self.h, out))
+        return out[0], out[1], out[2]
+
+    def population_count(self, level: int = 0) -> int:
+        c = C.c_int64()
+        _check(lib().jp_population_count(self.h, level, C.byref(c)))
+        return c.value
+
+    def get_populations(self, level: int = 0, layout: str = "flat", dtype=np.float32) -> np.ndarray:
+        cnt = self.population_count(level)
+        a = np.empty(cnt, dtype=dtype)
+        dt = 0 if a.dtype == np.float32 else 1
+        _check(lib().jp_get_populations(self.h, level, LAYOUT[layout], dt, a.ctypes.data_as(C.c_void_p), cnt))
+        return a
+
+    def set_populations(self, a: np.ndarray, level: int = 0, layout: str = "flat") -> None:
+        a = np.ascontiguousarray(a)
+        if a.dtype not in (np.float32, np.float64):
+            raise TypeError("populations must be float32 or float64")
+        dt = 0 if a.dtype == np.float32 else 1
+        _check(lib().jp_set_populations(self.h, level, LAYOUT[layout], dt, a.ctypes.data_as(C.c_void_p), a.size))
+        self.sync()
+
+    def macro(self) -> np.ndarray:
+        n = self.cfg.n
+        a = np.empty(4 * n ** 3, dtype=np.float32)
+        _check(lib().jp_get_macro(self.h, a.ctypes.data_as(C.POINTER(C.c_float)), a.size))
+        return a.reshape(n, n, n, 4)
+
+
+def launch_count() -> int:
+    return int(lib().jp_launch_count())
+
+
+class PinnedBuffer:
+    """Page-locked host memory from jp_host_alloc, viewed as a numpy array."""
+
+    def __init__(self, count: int, dtype=np.float32):
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(count) * self.dtype.itemsize
+        p = C.c_void_p()
+        _check(lib().jp_host_alloc(C.byref(p), self.nbytes))
+        self.ptr = p
+        buf = (C.c_char * self.nbytes).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=self.dtype, count=int(count))
+
+    def free(self) -> None:
+        if self.ptr:
+            self.array = None
+            lib().jp_host_free(self.ptr)
+            self.ptr = None
