@@ -163,6 +163,56 @@ jp_status jp_get_macro(jp_solver* s, float* host, int64_t count);
 jp_status jp_host_alloc(void** ptr, size_t bytes);
 void jp_host_free(void* ptr);
 
+/* ---- AMR: adaptation and block tables ----------------------------------------------------------- */
+
+/* Block tables of the three-level AMR, int32 with -1 = absent (src/tgv3d_amr.cu:695-701). */
+typedef enum jp_table {
+    JP_TABLE_REF0 = 0,   /* [cnb0] coarse block refined to level 1 */
+    JP_TABLE_FOF0 = 1,   /* [cnb0] first level-1 block of a coarse block, -1 */
+    JP_TABLE_RL0 = 2,    /* [nref0] refined coarse blocks in rank order */
+    JP_TABLE_L1PCB = 3,  /* [nf1] parent coarse block of a level-1 block */
+    JP_TABLE_L1OCT = 4,  /* [nf1] octant of a level-1 block in its parent */
+    JP_TABLE_F1POS = 5,  /* [nf1] level-1 grid position of a level-1 block */
+    JP_TABLE_L1GRID = 6, /* [(2N/MB)^3] level-1 block at a grid position, -1 */
+    JP_TABLE_REF1 = 7,   /* [nf1] level-1 block refined to level 2 */
+    JP_TABLE_FOF1 = 8,   /* [nf1] first level-2 block of a level-1 block, -1 */
+    JP_TABLE_RL1 = 9,    /* [nref1] refined level-1 blocks in rank order */
+    JP_TABLE_L2PL1 = 10, /* [nf2] parent level-1 block of a level-2 block */
+    JP_TABLE_L2OCT = 11, /* [nf2] octant of a level-2 block */
+    JP_TABLE_SKIN0 = 12, /* [n_skin0] coarse blocks refined or next to a refined one, ascending */
+    JP_TABLE_SKIN1 = 13, /* [n_skin1] level-1 blocks refined or next to a refined one, ascending */
+    JP_TABLE_DEEP = 14   /* [nf1] level-1 block whose 6 face neighbours exist (2:1 balance) */
+} jp_table;
+
+typedef struct jp_amr_counts {
+    int32_t nref0, nf1, nref1, nf2, n_skin0, n_skin1, ndeep;
+    int32_t cnb0, ng1, cap_nref0, cap1, cap_nref1, cap2;
+    int32_t pad;
+    int64_t hw_nf1, hw_nf2;   /* pool high-water marks (src/tgv3d_amr.cu:901-902) */
+    int32_t reserved[8];
+} jp_amr_counts;
+
+/* Rebuild the refinement from the current state: sensor, exact threshold, marks, tables, migration of
+ * the fine payloads, skin lists (gpurce_regrid, src/tgv3d_amr.cu:722-764).  Synchronous; only block
+ * counts cross to the host.  JP_ERR_CAPACITY if a pool would overflow. */
+jp_status jp_regrid(jp_solver* s);
+
+/* Block counts, capacities and high-water marks of an AMR solver. */
+jp_status jp_amr_get_counts(jp_solver* s, jp_amr_counts* out);
+
+/* Copy one block table to `host` (capacity entries); *count receives its length. */
+jp_status jp_get_table(jp_solver* s, int32_t table, int32_t* host, int64_t capacity, int64_t* count);
+
+/* The refinement sensor of the last adaptation: level 0 per coarse block (cnb0 values), level 1 per
+ * level-1 block (nf1 values); block max of |f - feq|_2 / rho (k_sensor, src/tgv3d_amr.cu:442-453). */
+jp_status jp_get_sensor(jp_solver* s, int32_t level, float* host, int64_t capacity, int64_t* count);
+
+/* Replace the computed sensor by supplied values in every later adaptation (initial build by
+ * jp_init_tgv, regrid): sen0 per coarse block (cnb0 values), sen1_by_pos per level-1 grid position
+ * ((2N/MB)^3 values, so a level-1 block takes the value of its position).  NULL, NULL clears.  Feeds
+ * two implementations the same sensor field for bit-exact table comparisons. */
+jp_status jp_set_sensor_override(jp_solver* s, const float* sen0, const float* sen1_by_pos);
+
 /* ---- measurement ---------------------------------------------------------------------------- */
 
 /* Advance `nsteps` steps and return the device time of those launches, measured with CUDA events

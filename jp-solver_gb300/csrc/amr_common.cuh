@@ -1,0 +1,137 @@
+// Device helpers of the three-level block AMR (reference: src/tgv3d_amr.cu).
+//
+// Block payloads keep the reference's layout float[blk][19][MB^3] (cell = (k*MB+j)*MB+i), so block
+// tables index the same way on both sides.  Ghost layers differ: the reference stores a full
+// (MB+2)^3 box per fine block of which only the shell is ever written or read; here a fine block's
+// ghosts are the shell's faces and edges only (6*MB^2 + 12*MB cells; D3Q19 never pulls across a
+// corner), stored as float[blk][19][SH], so the fill writes and the step reads a dense array.
+#pragma once
+#include <cmath>
+
+#include "lattice.cuh"
+
+namespace jp {
+namespace amr {
+
+template <int MB> struct Geo {
+    static constexpr int MB3 = MB * MB * MB;
+    static constexpr int HALF = MB / 2;
+    static constexpr int SH = 6 * MB * MB + 12 * MB;   // ghost shell cells per fine block
+    static constexpr int TPB = MB3 < 512 ? MB3 : 512;  // threads per CTA for per-cell kernels
+};
+
+// Shell index of a ghost cell at block-local (i, j, k), each in [-1, MB]; -1 for interior/corner.
+template <int MB>
+__host__ __device__ __forceinline__ int shell_index(int i, int j, int k) {
+    const bool bx = (i < 0) | (i >= MB), by = (j < 0) | (j >= MB), bz = (k < 0) | (k >= MB);
+    const int cnt = int(bx) + int(by) + int(bz);
+    if (cnt == 1) {
+        if (bx) return (i < 0 ? 0 : 1) * MB * MB + k * MB + j;
+        if (by) return (j < 0 ? 2 : 3) * MB * MB + k * MB + i;
+        return (k < 0 ? 4 : 5) * MB * MB + j * MB + i;
+    }
+    if (cnt == 2) {
+        const int base = 6 * MB * MB;
+        if (!bx) return base + ((j < 0 ? 0 : 1) + 2 * (k < 0 ? 0 : 1)) * MB + i;
+        if (!by) return base + (4 + (i < 0 ? 0 : 1) + 2 * (k < 0 ? 0 : 1)) * MB + j;
+        return base + (8 + (i < 0 ? 0 : 1) + 2 * (j < 0 ? 0 : 1)) * MB + k;
+    }
+    return -1;
+}
+// Inverse of shell_index for t in [0, SH).
+template <int MB>
+__host__ __device__ __forceinline__ void shell_coord(int t, int& i, int& j, int& k) {
+    if (t < 6 * MB * MB) {
+        const int f = t / (MB * MB), r = t % (MB * MB), a = r % MB, b = r / MB;
+        switch (f) {
+            case 0: i = -1; j = a; k = b; break;
+            case 1: i = MB; j = a; k = b; break;
+            case 2: i = a; j = -1; k = b; break;
+            case 3: i = a; j = MB; k = b; break;
+            case 4: i = a; j = b; k = -1; break;
+            default: i = a; j = b; k = MB; break;
+        }
+        return;
+    }
+    const int u = t - 6 * MB * MB, e = u / MB, a = u % MB;
+    if (e < 4) {
+        i = a; j = (e & 1) ? MB : -1; k = (e & 2) ? MB : -1;
+    } else if (e < 8) {
+        j = a; i = ((e - 4) & 1) ? MB : -1; k = ((e - 4) & 2) ? MB : -1;
+    } else {
+        k = a; i = ((e - 8) & 1) ? MB : -1; j = ((e - 8) & 2) ? MB : -1;
+    }
+}
+
+__device__ __forceinline__ int pmod(int a, int n) {
+    const int r = a % n;
+    return r < 0 ? r + n : r;
+}
+
+// rho, u of one cell, summed in q order as the reference's loops do
+__device__ __forceinline__ void moments(const float (&f)[Q], float& rho, float& ux, float& uy, float& uz) {
+    float r = f[0];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) r += f[q];
+    const float jx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+    const float jy = f[3] - f[4] + f[7] - f[8] - f[9] + f[10] + f[15] - f[16] + f[17] - f[18];
+    const float jz = f[5] - f[6] + f[11] - f[12] - f[13] + f[14] + f[15] - f[16] - f[17] + f[18];
+    rho = r;
+    ux = jx / r;
+    uy = jy / r;
+    uz = jz / r;
+}
+
+// Hermite regularisation of a non-equilibrium vector: project onto the second-order moments
+// Pi = sum c c n and rebuild n_q = 4.5 w_q Q_q : Pi, Q_q = c c - I/3 (src/tgv3d_amr.cu:56-67).
+__device__ __forceinline__ void regularize(float (&n)[Q]) {
+    const float Pxx = n[1] + n[2] + n[7] + n[8] + n[9] + n[10] + n[11] + n[12] + n[13] + n[14];
+    const float Pyy = n[3] + n[4] + n[7] + n[8] + n[9] + n[10] + n[15] + n[16] + n[17] + n[18];
+    const float Pzz = n[5] + n[6] + n[11] + n[12] + n[13] + n[14] + n[15] + n[16] + n[17] + n[18];
+    const float Pxy = n[7] + n[8] - n[9] - n[10];
+    const float Pxz = n[11] + n[12] - n[13] - n[14];
+    const float Pyz = n[15] + n[16] - n[17] - n[18];
+    const float third = 1.f / 3.f;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float Qxx = float(cx(q) * cx(q)) - third, Qyy = float(cy(q) * cy(q)) - third,
+                    Qzz = float(cz(q) * cz(q)) - third;
+        const float Qxy = float(cx(q) * cy(q)), Qxz = float(cx(q) * cz(q)), Qyz = float(cy(q) * cz(q));
+        n[q] = 4.5f * wf(q) * (Qxx * Pxx + Qyy * Pyy + Qzz * Pzz + 2.f * (Qxy * Pxy + Qxz * Pxz + Qyz * Pyz));
+    }
+}
+
+// Prolongation source of one parent cell: feq + nqs * regularize(f - feq).
+__device__ __forceinline__ void prep_cell(float (&f)[Q], float nqs) {
+    float rho, ux, uy, uz;
+    moments(f, rho, ux, uy, uz);
+    float fe[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        fe[q] = feq_ref(q, rho, ux, uy, uz);
+        f[q] = f[q] - fe[q];
+    }
+    regularize(f);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q] = fe[q] + nqs * f[q];
+}
+
+// BGK collide of one cell in the reference's form out = f - omega (f - feq)
+__device__ __forceinline__ void bgk(float (&f)[Q], float om) {
+    float rho, ux, uy, uz;
+    moments(f, rho, ux, uy, uz);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q] = f[q] - om * (f[q] - feq_ref(q, rho, ux, uy, uz));
+}
+
+// Trilinear weights of the cell-centred 2:1 prolongation: fine index g maps to the parent position
+// (g+0.5)/2-0.5, so the lower parent is floor of that and the weight of the upper one is 0.25 or
+// 0.75 (src/tgv3d_amr.cu:71-73).  Both are exact in float.
+__device__ __forceinline__ void tri_axis(int g, int& lo, float& t) {
+    const double xc = (double(g) + 0.5) / 2.0 - 0.5;
+    lo = int(floor(xc));
+    t = float(xc - lo);
+}
+
+}  // namespace amr
+}  // namespace jp

@@ -1,0 +1,606 @@
+// AMR level kernels: coarse step, prolongation sources ("prep"), ghost-shell fill, fine steps,
+// restriction, seeding and migration, sensor and the composite macro field.
+// Reference: src/tgv3d_amr.cu:69-453, 514-536.  One CTA per block; a thread owns one cell (MB<=8)
+// or several (MB=16).  Arithmetic follows the reference's expressions so results agree within
+// round-off; loop orders of the trilinear and the 8-child average are the reference's.
+#include "amr_common.cuh"
+#include "amr_kernels.h"
+#include "kernels.h"
+
+namespace jp {
+namespace amr {
+
+#define CELL_LOOP(c) for (int c = threadIdx.x; c < G::MB3; c += G::TPB)
+
+// ---- TGV initial state of the coarse grid (src/tgv3d_amr.cu:431-440) ---------------------------
+template <int MB>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_init(float* __restrict__ f, int cgx, double u0, double kf) {
+    using G = Geo<MB>;
+    const int b = blockIdx.x;
+    const int bx = b % cgx, by = (b / cgx) % cgx, bz = b / (cgx * cgx);
+    CELL_LOOP(cell) {
+        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+        const double x = (bx * MB + i + 0.5) * kf, y = (by * MB + j + 0.5) * kf, z = (bz * MB + k + 0.5) * kf;
+        const double ux = u0 * sin(x) * cos(y) * cos(z), uy = -u0 * cos(x) * sin(y) * cos(z);
+        const double p = (u0 * u0 / 16.0) * (cos(2 * x) + cos(2 * y)) * (cos(2 * z) + 2.0), rho = 1.0 + 3.0 * p;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) f[((size_t)b * Q + q) * G::MB3 + cell] = feq_ref(q, float(rho), float(ux), float(uy), 0.f);
+    }
+}
+
+// ---- dense periodic coarse step (src/tgv3d_amr.cu:203-220) ---------------------------------------
+template <int MB>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l0(const float* __restrict__ fa, float* __restrict__ fb, int cgx,
+                                                         int N, float om) {
+    using G = Geo<MB>;
+    const int b = blockIdx.x;
+    const int bx = b % cgx, by = (b / cgx) % cgx, bz = b / (cgx * cgx);
+    CELL_LOOP(cell) {
+        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+        const int gi = bx * MB + i, gj = by * MB + j, gk = bz * MB + k;
+        float f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            int si = gi - cx(q), sj = gj - cy(q), sk = gk - cz(q);
+            si += si < 0 ? N : (si >= N ? -N : 0);
+            sj += sj < 0 ? N : (sj >= N ? -N : 0);
+            sk += sk < 0 ? N : (sk >= N ? -N : 0);
+            const int sb = ((sk / MB) * cgx + sj / MB) * cgx + si / MB;
+            const int sc = ((sk % MB) * MB + sj % MB) * MB + si % MB;
+            f[q] = __ldg(fa + ((size_t)sb * Q + q) * G::MB3 + sc);
+        }
+        bgk(f, om);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) fb[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
+    }
+}
+
+// ---- prolongation sources on a block list (src/tgv3d_amr.cu:160-171) -----------------------------
+template <int MB>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const float* __restrict__ fin, float* __restrict__ pr,
+                                                      const int* __restrict__ list, float nqs) {
+    using G = Geo<MB>;
+    const int b = list[blockIdx.x];
+    CELL_LOOP(cell) {
+        float f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) f[q] = __ldg(fin + ((size_t)b * Q + q) * G::MB3 + cell);
+        prep_cell(f, nqs);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) pr[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
+    }
+}
+
+// trilinear of a precomputed source on the dense coarse grid (src/tgv3d_amr.cu:122-132)
+template <int MB>
+__device__ __forceinline__ void prolong_prep_l0(const float* __restrict__ pr, int cgx, int N, int gfi, int gfj, int gfk,
+                                                float (&out)[Q]) {
+    constexpr int MB3 = MB * MB * MB;
+    int ib, jb, kb;
+    float tx, ty, tz;
+    tri_axis(gfi, ib, tx);
+    tri_axis(gfj, jb, ty);
+    tri_axis(gfk, kb, tz);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) out[q] = 0.f;
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+        const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
+        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
+        const int ci = pmod(ib + di, N), cj = pmod(jb + dj, N), ck = pmod(kb + dk, N);
+        const int cb = ((ck / MB) * cgx + cj / MB) * cgx + ci / MB;
+        const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
+        const float* p = pr + (size_t)cb * Q * MB3 + cc;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) out[q] += wgt * __ldg(p + q * MB3);
+    }
+}
+
+// trilinear of a precomputed source on the scattered L1 level, dropping absent corners and
+// renormalising (src/tgv3d_amr.cu:133-144)
+template <int MB>
+__device__ __forceinline__ void prolong_prep_l1(const float* __restrict__ pr, const int* __restrict__ l1grid, int l1gx,
+                                                int N1, int g2i, int g2j, int g2k, float (&out)[Q]) {
+    constexpr int MB3 = MB * MB * MB;
+    int ib, jb, kb;
+    float tx, ty, tz, wsum = 0.f;
+    tri_axis(g2i, ib, tx);
+    tri_axis(g2j, jb, ty);
+    tri_axis(g2k, kb, tz);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) out[q] = 0.f;
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+        const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
+        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
+        const int ci = pmod(ib + di, N1), cj = pmod(jb + dj, N1), ck = pmod(kb + dk, N1);
+        const int lb = __ldg(l1grid + ((ck / MB) * l1gx + cj / MB) * l1gx + ci / MB);
+        if (lb < 0) continue;
+        const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
+        wsum += wgt;
+        const float* p = pr + (size_t)lb * Q * MB3 + cc;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) out[q] += wgt * __ldg(p + q * MB3);
+    }
+    if (wsum > 0.f && wsum < 0.999f) {
+        const float inv = 1.f / wsum;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) out[q] *= inv;
+    }
+}
+
+// ---- ghost shells (src/tgv3d_amr.cu:173-202) -------------------------------------------------------
+// One CTA per fine block, one thread per shell cell; a shell cell whose source parent block is
+// refined is left alone (the step gathers it from the same level instead).
+template <int MB>
+__global__ void __launch_bounds__(256) k_fill_l1(const float* __restrict__ pr, float* __restrict__ gh,
+                                                const int* __restrict__ pcb, const int* __restrict__ poct,
+                                                const int* __restrict__ ref0, int cgx, int N) {
+    using G = Geo<MB>;
+    const int fb = blockIdx.x;
+    const int cb = pcb[fb], oct = poct[fb];
+    const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
+    const int ox = cbx * 2 * MB + (oct & 1) * MB, oy = cby * 2 * MB + ((oct >> 1) & 1) * MB, oz = cbz * 2 * MB + (oct >> 2) * MB;
+    const int N1 = 2 * N;
+    for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
+        int i, j, k;
+        shell_coord<MB>(t, i, j, k);
+        const int gfi = pmod(ox + i, N1), gfj = pmod(oy + j, N1), gfk = pmod(oz + k, N1);
+        const int scb = ((gfk / (2 * MB)) * cgx + gfj / (2 * MB)) * cgx + gfi / (2 * MB);
+        if (__ldg(ref0 + scb)) continue;
+        float out[Q];
+        prolong_prep_l0<MB>(pr, cgx, N, gfi, gfj, gfk, out);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) gh[((size_t)fb * Q + q) * G::SH + t] = out[q];
+    }
+}
+
+template <int MB>
+__global__ void __launch_bounds__(256) k_fill_l2(const float* __restrict__ pr, float* __restrict__ gh,
+                                                const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
+                                                const int* __restrict__ f1pos, const int* __restrict__ l1grid,
+                                                const int* __restrict__ ref1, int l1gx, int N1) {
+    using G = Geo<MB>;
+    const int b = blockIdx.x;
+    const int pl1 = l2pl1[b], oct = l2oct[b];
+    const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
+    const int ox = px * 2 * MB + (oct & 1) * MB, oy = py * 2 * MB + ((oct >> 1) & 1) * MB, oz = pz * 2 * MB + (oct >> 2) * MB;
+    const int N2 = 2 * N1;
+    for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
+        int i, j, k;
+        shell_coord<MB>(t, i, j, k);
+        const int g2i = pmod(ox + i, N2), g2j = pmod(oy + j, N2), g2k = pmod(oz + k, N2);
+        const int lb = __ldg(l1grid + ((g2k / (2 * MB)) * l1gx + g2j / (2 * MB)) * l1gx + g2i / (2 * MB));
+        if (lb >= 0 && __ldg(ref1 + lb)) continue;
+        float out[Q];
+        prolong_prep_l1<MB>(pr, l1grid, l1gx, N1, g2i, g2j, g2k, out);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) gh[((size_t)b * Q + q) * G::SH + t] = out[q];
+    }
+}
+
+// ---- fine steps (src/tgv3d_amr.cu:241-274, 331-356) -----------------------------------------------
+// Level 1: the 27 coarse neighbours of the parent say whether a pulled cell lives on level 1 (gather
+// from its block) or not (read the ghost shell).
+template <int MB>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l1(const float* __restrict__ fa, float* __restrict__ fbuf,
+                                                         const float* __restrict__ gh, const int* __restrict__ pcb,
+                                                         const int* __restrict__ poct, const int* __restrict__ ref0,
+                                                         const int* __restrict__ fof0, int cgx, int N, float om) {
+    using G = Geo<MB>;
+    const int b = blockIdx.x;
+    const int cb = pcb[b], oct = poct[b];
+    const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
+    __shared__ int sfof[27];  // fine block base of each coarse neighbour, -1 if not refined
+    if (threadIdx.x < 27) {
+        const int dx = threadIdx.x % 3 - 1, dy = (threadIdx.x / 3) % 3 - 1, dz = threadIdx.x / 9 - 1;
+        const int nx = (cbx + dx + cgx) % cgx, ny = (cby + dy + cgx) % cgx, nz = (cbz + dz + cgx) % cgx;
+        const int ncb = (nz * cgx + ny) * cgx + nx;
+        sfof[threadIdx.x] = ref0[ncb] ? fof0[ncb] : -1;
+    }
+    __syncthreads();
+    const int ox = cbx * 2 * MB + (oct & 1) * MB, oy = cby * 2 * MB + ((oct >> 1) & 1) * MB, oz = cbz * 2 * MB + (oct >> 2) * MB;
+    const int N1 = 2 * N;
+    CELL_LOOP(cell) {
+        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+        float f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int li = i - cx(q), lj = j - cy(q), lk = k - cz(q);
+            if (li >= 0 && li < MB && lj >= 0 && lj < MB && lk >= 0 && lk < MB) {
+                f[q] = __ldg(fa + ((size_t)b * Q + q) * G::MB3 + (lk * MB + lj) * MB + li);
+                continue;
+            }
+            int sfi = ox + li, sfj = oy + lj, sfk = oz + lk;
+            sfi += sfi < 0 ? N1 : (sfi >= N1 ? -N1 : 0);
+            sfj += sfj < 0 ? N1 : (sfj >= N1 ? -N1 : 0);
+            sfk += sfk < 0 ? N1 : (sfk >= N1 ? -N1 : 0);
+            int ddx = sfi / (2 * MB) - cbx, ddy = sfj / (2 * MB) - cby, ddz = sfk / (2 * MB) - cbz;
+            if (ddx > 1) ddx -= cgx; else if (ddx < -1) ddx += cgx;
+            if (ddy > 1) ddy -= cgx; else if (ddy < -1) ddy += cgx;
+            if (ddz > 1) ddz -= cgx; else if (ddz < -1) ddz += cgx;
+            const int base = sfof[(ddz + 1) * 9 + (ddy + 1) * 3 + (ddx + 1)];
+            if (base >= 0) {
+                const int sq = (((sfk % (2 * MB)) / MB) * 4 + ((sfj % (2 * MB)) / MB) * 2 + (sfi % (2 * MB)) / MB);
+                const int sc = ((sfk % MB) * MB + sfj % MB) * MB + sfi % MB;
+                f[q] = __ldg(fa + ((size_t)(base + sq) * Q + q) * G::MB3 + sc);
+            } else {
+                f[q] = __ldg(gh + ((size_t)b * Q + q) * G::SH + shell_index<MB>(li, lj, lk));
+            }
+        }
+        bgk(f, om);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
+    }
+}
+
+// Level 2: the level-1 grid map says where a pulled cell lives.
+template <int MB>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l2(const float* __restrict__ fa, float* __restrict__ fbuf,
+                                                         const float* __restrict__ gh, const int* __restrict__ l2pl1,
+                                                         const int* __restrict__ l2oct, const int* __restrict__ f1pos,
+                                                         const int* __restrict__ l1grid, const int* __restrict__ ref1,
+                                                         const int* __restrict__ fof1, int l1gx, int N1, float om) {
+    using G = Geo<MB>;
+    const int b = blockIdx.x;
+    const int pl1 = l2pl1[b], oct = l2oct[b];
+    const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
+    const int ox = px * 2 * MB + (oct & 1) * MB, oy = py * 2 * MB + ((oct >> 1) & 1) * MB, oz = pz * 2 * MB + (oct >> 2) * MB;
+    // fine-block base of the 27 level-1 grid neighbours of the parent (-1: not on level 2)
+    __shared__ int sbase[27];
+    if (threadIdx.x < 27) {
+        const int dx = threadIdx.x % 3 - 1, dy = (threadIdx.x / 3) % 3 - 1, dz = threadIdx.x / 9 - 1;
+        const int nx = (px + dx + l1gx) % l1gx, ny = (py + dy + l1gx) % l1gx, nz = (pz + dz + l1gx) % l1gx;
+        const int lb = l1grid[(nz * l1gx + ny) * l1gx + nx];
+        sbase[threadIdx.x] = (lb >= 0 && ref1[lb]) ? fof1[lb] : -1;
+    }
+    __syncthreads();
+    const int N2 = 2 * N1;
+    CELL_LOOP(cell) {
+        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+        float f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int li = i - cx(q), lj = j - cy(q), lk = k - cz(q);
+            if (li >= 0 && li < MB && lj >= 0 && lj < MB && lk >= 0 && lk < MB) {
+                f[q] = __ldg(fa + ((size_t)b * Q + q) * G::MB3 + (lk * MB + lj) * MB + li);
+                continue;
+            }
+            int sfi = ox + li, sfj = oy + lj, sfk = oz + lk;
+            sfi += sfi < 0 ? N2 : (sfi >= N2 ? -N2 : 0);
+            sfj += sfj < 0 ? N2 : (sfj >= N2 ? -N2 : 0);
+            sfk += sfk < 0 ? N2 : (sfk >= N2 ? -N2 : 0);
+            int ddx = sfi / (2 * MB) - px, ddy = sfj / (2 * MB) - py, ddz = sfk / (2 * MB) - pz;
+            if (ddx > 1) ddx -= l1gx; else if (ddx < -1) ddx += l1gx;
+            if (ddy > 1) ddy -= l1gx; else if (ddy < -1) ddy += l1gx;
+            if (ddz > 1) ddz -= l1gx; else if (ddz < -1) ddz += l1gx;
+            const int base = sbase[(ddz + 1) * 9 + (ddy + 1) * 3 + (ddx + 1)];
+            if (base >= 0) {
+                const int sq = (((sfk % (2 * MB)) / MB) * 4 + ((sfj % (2 * MB)) / MB) * 2 + (sfi % (2 * MB)) / MB);
+                const int sc = ((sfk % MB) * MB + sfj % MB) * MB + sfi % MB;
+                f[q] = __ldg(fa + ((size_t)(base + sq) * Q + q) * G::MB3 + sc);
+            } else {
+                f[q] = __ldg(gh + ((size_t)b * Q + q) * G::SH + shell_index<MB>(li, lj, lk));
+            }
+        }
+        bgk(f, om);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
+    }
+}
+
+// ---- restriction (src/tgv3d_amr.cu:275-298, 357-381) -------------------------------------------------
+// One CTA per refined parent block; each parent cell becomes feq + nqi*regularize(avg - feq) of the
+// average of its 8 children (summed in the reference's dk, dj, di order).
+template <int MB>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_restrict(float* __restrict__ cf, const float* __restrict__ ff,
+                                                          const int* __restrict__ rl, const int* __restrict__ fof,
+                                                          float nqi) {
+    using G = Geo<MB>;
+    const int cb = rl[blockIdx.x];
+    const int fbase = fof[cb];
+    CELL_LOOP(cell) {
+        const int lci = cell % MB, lcj = (cell / MB) % MB, lck = cell / (MB * MB);
+        const int oct = (lck / G::HALF) * 4 + (lcj / G::HALF) * 2 + lci / G::HALF;
+        const int fi0 = 2 * (lci % G::HALF), fj0 = 2 * (lcj % G::HALF), fk0 = 2 * (lck % G::HALF);
+        const float* src = ff + (size_t)(fbase + oct) * Q * G::MB3;
+        float a[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) a[q] = 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
+            const int sc = ((fk0 + dk) * MB + (fj0 + dj)) * MB + (fi0 + di);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) a[q] += 0.125f * __ldg(src + q * G::MB3 + sc);
+        }
+        float rho, ux, uy, uz;
+        moments(a, rho, ux, uy, uz);
+        float fe[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            fe[q] = feq_ref(q, rho, ux, uy, uz);
+            a[q] = a[q] - fe[q];
+        }
+        regularize(a);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) cf[((size_t)cb * Q + q) * G::MB3 + cell] = fe[q] + nqi * a[q];
+    }
+}
+
+// ---- on-the-fly prolongation for seeding and migration (src/tgv3d_amr.cu:70-118) ----------------
+template <int MB>
+__device__ __forceinline__ void prolong_l0(const float* __restrict__ cf, int cgx, int N, int gfi, int gfj, int gfk,
+                                           float nqs, float (&out)[Q]) {
+    constexpr int MB3 = MB * MB * MB;
+    int ib, jb, kb;
+    float tx, ty, tz;
+    tri_axis(gfi, ib, tx);
+    tri_axis(gfj, jb, ty);
+    tri_axis(gfk, kb, tz);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) out[q] = 0.f;
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+        const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
+        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
+        const int ci = pmod(ib + di, N), cj = pmod(jb + dj, N), ck = pmod(kb + dk, N);
+        const int cb = ((ck / MB) * cgx + cj / MB) * cgx + ci / MB;
+        const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
+        float f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) f[q] = __ldg(cf + ((size_t)cb * Q + q) * MB3 + cc);
+        prep_cell(f, nqs);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) out[q] += wgt * f[q];
+    }
+}
+template <int MB>
+__device__ __forceinline__ void prolong_l1(const float* __restrict__ f1, const int* __restrict__ l1grid, int l1gx,
+                                           int N1, int g2i, int g2j, int g2k, float nqs, float (&out)[Q]) {
+    constexpr int MB3 = MB * MB * MB;
+    int ib, jb, kb;
+    float tx, ty, tz, wsum = 0.f;
+    tri_axis(g2i, ib, tx);
+    tri_axis(g2j, jb, ty);
+    tri_axis(g2k, kb, tz);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) out[q] = 0.f;
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+        const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
+        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
+        const int ci = pmod(ib + di, N1), cj = pmod(jb + dj, N1), ck = pmod(kb + dk, N1);
+        const int lb = __ldg(l1grid + ((ck / MB) * l1gx + cj / MB) * l1gx + ci / MB);
+        if (lb < 0) continue;
+        const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
+        float f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) f[q] = __ldg(f1 + ((size_t)lb * Q + q) * MB3 + cc);
+        prep_cell(f, nqs);
+        wsum += wgt;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) out[q] += wgt * f[q];
+    }
+    if (wsum > 0.f && wsum < 0.999f) {
+        const float inv = 1.f / wsum;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) out[q] *= inv;
+    }
+}
+
+// seed (old_ref == nullptr) or migrate level 1: a block whose parent was refined before copies its old
+// payload, a new one is prolonged from the coarse level (src/tgv3d_amr.cu:299-308, 397-411)
+template <int MB>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_seed_l1(const float* __restrict__ oldf, float* __restrict__ newf,
+                                                         const float* __restrict__ c0, const int* __restrict__ pcb,
+                                                         const int* __restrict__ poct, const int* __restrict__ old_ref0,
+                                                         const int* __restrict__ old_fof0, int cgx, int N, float nqs) {
+    using G = Geo<MB>;
+    const int nfb = blockIdx.x;
+    const int cb = pcb[nfb], oct = poct[nfb];
+    const bool copy = old_ref0 != nullptr && old_ref0[cb];
+    const int ofb = copy ? old_fof0[cb] + oct : 0;
+    const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
+    CELL_LOOP(cell) {
+        if (copy) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                newf[((size_t)nfb * Q + q) * G::MB3 + cell] = __ldg(oldf + ((size_t)ofb * Q + q) * G::MB3 + cell);
+            continue;
+        }
+        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+        float out[Q];
+        prolong_l0<MB>(c0, cgx, N, cbx * 2 * MB + (oct & 1) * MB + i, cby * 2 * MB + ((oct >> 1) & 1) * MB + j,
+                       cbz * 2 * MB + (oct >> 2) * MB + k, nqs, out);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) newf[((size_t)nfb * Q + q) * G::MB3 + cell] = out[q];
+    }
+}
+
+// seed or migrate level 2, keyed by the level-1 grid position (src/tgv3d_amr.cu:382-393, 414-430)
+template <int MB>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_seed_l2(const float* __restrict__ oldf, float* __restrict__ newf,
+                                                         const float* __restrict__ f1, const int* __restrict__ l2pl1,
+                                                         const int* __restrict__ l2oct, const int* __restrict__ f1pos,
+                                                         const int* __restrict__ old_l1grid, const int* __restrict__ old_ref1,
+                                                         const int* __restrict__ old_fof1, const int* __restrict__ l1grid,
+                                                         int l1gx, int N1, float nqs) {
+    using G = Geo<MB>;
+    const int nfb = blockIdx.x;
+    const int pl1 = l2pl1[nfb], oct = l2oct[nfb], p = f1pos[pl1];
+    bool copy = false;
+    int of2 = 0;
+    if (old_l1grid != nullptr) {
+        const int old_l1b = old_l1grid[p];
+        copy = old_l1b >= 0 && old_ref1[old_l1b];
+        if (copy) of2 = old_fof1[old_l1b] + oct;
+    }
+    const int px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
+    CELL_LOOP(cell) {
+        if (copy) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                newf[((size_t)nfb * Q + q) * G::MB3 + cell] = __ldg(oldf + ((size_t)of2 * Q + q) * G::MB3 + cell);
+            continue;
+        }
+        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+        float out[Q];
+        prolong_l1<MB>(f1, l1grid, l1gx, N1, px * 2 * MB + (oct & 1) * MB + i, py * 2 * MB + ((oct >> 1) & 1) * MB + j,
+                       pz * 2 * MB + (oct >> 2) * MB + k, nqs, out);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) newf[((size_t)nfb * Q + q) * G::MB3 + cell] = out[q];
+    }
+}
+
+// ---- refinement sensor (src/tgv3d_amr.cu:442-453) -----------------------------------------------
+// Block max over cells of |f - feq|_2 / rho.  With `override_pos` set, block b takes the supplied
+// value of its grid position instead (pos == nullptr: position = block index).
+template <int MB>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_sensor(const float* __restrict__ ff, float* __restrict__ d,
+                                                        const float* __restrict__ override_val,
+                                                        const int* __restrict__ pos) {
+    using G = Geo<MB>;
+    const int b = blockIdx.x;
+    if (override_val) {
+        if (threadIdx.x == 0) d[b] = override_val[pos ? pos[b] : b];
+        return;
+    }
+    float m = -INFINITY;
+    CELL_LOOP(cell) {
+        float f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) f[q] = __ldg(ff + ((size_t)b * Q + q) * G::MB3 + cell);
+        float rho, ux, uy, uz;
+        moments(f, rho, ux, uy, uz);
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const float d2 = f[q] - feq_ref(q, rho, ux, uy, uz);
+            s += d2 * d2;
+        }
+        m = fmaxf(m, sqrtf(s) / rho);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float sm[32];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = sm[0];
+        for (int w = 1; w < (G::TPB + 31) / 32; ++w) r = fmaxf(r, sm[w]);
+        d[b] = r;
+    }
+}
+
+// ---- composite macro field at 4*N0 (src/tgv3d_amr.cu:514-536) ----------------------------------
+template <int MB>
+__global__ void __launch_bounds__(256) k_composite(const float* __restrict__ c0, const float* __restrict__ f1,
+                                                  const float* __restrict__ f2, const int* __restrict__ ref1,
+                                                  const int* __restrict__ fof1, const int* __restrict__ l1grid, int cgx,
+                                                  int l1gx, int N2, float* __restrict__ F) {
+    constexpr int MB3 = MB * MB * MB;
+    const long long NN = (long long)N2 * N2 * N2;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= NN) return;
+    const int gi = int(idx % N2), gj = int((idx / N2) % N2), gk = int(idx / ((long long)N2 * N2));
+    const int lb = l1grid[((gk / (2 * MB)) * l1gx + gj / (2 * MB)) * l1gx + gi / (2 * MB)];
+    const float* src;
+    size_t blk;
+    int sc;
+    if (lb >= 0 && ref1[lb]) {
+        blk = fof1[lb] + (((gk % (2 * MB)) / MB) * 4 + ((gj % (2 * MB)) / MB) * 2 + (gi % (2 * MB)) / MB);
+        sc = ((gk % MB) * MB + gj % MB) * MB + gi % MB;
+        src = f2;
+    } else if (lb >= 0) {
+        const int g1i = gi / 2, g1j = gj / 2, g1k = gk / 2;
+        blk = lb;
+        sc = ((g1k % MB) * MB + g1j % MB) * MB + g1i % MB;
+        src = f1;
+    } else {
+        const int c0i = gi / 4, c0j = gj / 4, c0k = gk / 4;
+        blk = ((c0k / MB) * cgx + c0j / MB) * cgx + c0i / MB;
+        sc = ((c0k % MB) * MB + c0j % MB) * MB + c0i % MB;
+        src = c0;
+    }
+    float f[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q] = __ldg(src + (blk * Q + q) * MB3 + sc);
+    float rho, ux, uy, uz;
+    moments(f, rho, ux, uy, uz);
+    F[idx * 4 + 0] = rho;
+    F[idx * 4 + 1] = ux;
+    F[idx * 4 + 2] = uy;
+    F[idx * 4 + 3] = uz;
+}
+
+// ---- launchers ------------------------------------------------------------------------------------
+
+template <int MB>
+static cudaError_t dispatch(const AmrLaunch& L, int op) {
+    using G = Geo<MB>;
+    const dim3 cta(G::TPB);
+    const dim3 shl(G::SH < 256 ? ((G::SH + 31) / 32) * 32 : 256);
+    switch (op) {
+        case OP_INIT:
+            k_init<MB><<<L.nblocks, cta, 0, L.st>>>(L.out, L.cgx, L.u0, L.kf);
+            break;
+        case OP_STEP_L0:
+            k_step_l0<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.cgx, L.n, L.omega);
+            break;
+        case OP_PREP:
+            k_prep<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.list, L.scale);
+            break;
+        case OP_FILL_L1:
+            k_fill_l1<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.t2, L.cgx, L.n);
+            break;
+        case OP_FILL_L2:
+            k_fill_l2<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.t2, L.t3, L.t4, L.l1gx, L.n1);
+            break;
+        case OP_STEP_L1:
+            k_step_l1<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.cgx, L.n, L.omega);
+            break;
+        case OP_STEP_L2:
+            k_step_l2<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.t4, L.t5, L.l1gx,
+                                                       L.n1, L.omega);
+            break;
+        case OP_RESTRICT:
+            k_restrict<MB><<<L.nblocks, cta, 0, L.st>>>(L.out, L.in, L.list, L.t0, L.scale);
+            break;
+        case OP_SEED_L1:
+            k_seed_l1<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.cgx, L.n, L.scale);
+            break;
+        case OP_SEED_L2:
+            k_seed_l2<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.t4, L.t5, L.t6,
+                                                       L.l1gx, L.n1, L.scale);
+            break;
+        case OP_SENSOR:
+            k_sensor<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0);
+            break;
+        case OP_COMPOSITE: {
+            const long long NN = (long long)L.n2 * L.n2 * L.n2;
+            k_composite<MB><<<(unsigned)((NN + 255) / 256), 256, 0, L.st>>>(L.in, L.aux, L.aux2, L.t0, L.t1, L.t2,
+                                                                          L.cgx, L.l1gx, L.n2, L.out);
+            break;
+        }
+        default:
+            return cudaErrorInvalidValue;
+    }
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t amr_launch(int mb, int op, const AmrLaunch& L) {
+    if (L.nblocks <= 0 && op != OP_COMPOSITE) return cudaSuccess;
+    switch (mb) {
+        case 4: return dispatch<4>(L, op);
+        case 8: return dispatch<8>(L, op);
+        case 16: return dispatch<16>(L, op);
+    }
+    return cudaErrorInvalidValue;
+}
+
+int shell_cells(int mb) { return 6 * mb * mb + 12 * mb; }
+
+}  // namespace amr
+}  // namespace jp

@@ -1,0 +1,76 @@
+// Launch interface of the AMR kernels (amr_kernels.cu) and the adaptation pipeline (adapt.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace jp {
+namespace amr {
+
+enum AmrOp {
+    OP_INIT = 0,       // out = TGV state of the coarse grid
+    OP_STEP_L0,        // in -> out, dense periodic coarse step
+    OP_PREP,           // out[list] = prolongation source of in[list]; scale = nqs
+    OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, t2 ref0
+    OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, t4 ref1
+    OP_STEP_L1,        // in -> out, aux = gh1; t0 pcb, t1 oct, t2 ref0, t3 fof0
+    OP_STEP_L2,        // in -> out, aux = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, t4 ref1, t5 fof1
+    OP_RESTRICT,       // out = coarse, in = fine; list = refined coarse blocks, t0 = fof; scale = nqi
+    OP_SEED_L1,        // in = old f1 (migrate) , out = new f1, aux = c0; t0 pcb, t1 oct, t2 old ref0|null, t3 old fof0
+    OP_SEED_L2,        // in = old f2, out = new f2, aux = f1; t0 l2pl1, t1 l2oct, t2 f1pos, t3 old l1grid|null,
+                       // t4 old ref1, t5 old fof1, t6 l1grid
+    OP_SENSOR,         // in = level, out = sensor; aux = override values|null, t0 = override position map|null
+    OP_COMPOSITE       // in = c0, aux = f1, aux2 = f2, out = field; t0 ref1, t1 fof1, t2 l1grid
+};
+
+struct AmrLaunch {
+    cudaStream_t st = nullptr;
+    int nblocks = 0;
+    const float* in = nullptr;
+    float* out = nullptr;
+    const float* aux = nullptr;
+    const float* aux2 = nullptr;
+    const int* list = nullptr;
+    const int *t0 = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr, *t6 = nullptr;
+    int cgx = 0, n = 0, l1gx = 0, n1 = 0, n2 = 0;
+    float omega = 0.f, scale = 0.f;
+    double u0 = 0.0, kf = 0.0;
+};
+
+cudaError_t amr_launch(int mb, int op, const AmrLaunch& L);
+int shell_cells(int mb);
+
+// ---- adaptation pipeline (adapt.cu) ------------------------------------------------------------
+// Device counters shared by the pipeline; the host reads them once per stage.
+struct AdaptCounts {
+    int nref0, nf1, nref1, nf2, n_skin0, n_skin1, ndeep, err;
+    float thr0, thr1;
+    int pad[6];
+};
+enum { ADAPT_ERR_CAP1 = 1, ADAPT_ERR_CAP2 = 2 };
+
+// ref[i] = 1 for all (mode 0) or the lower half in z (mode 1, k_mark_slab)
+cudaError_t adapt_mark_mode(int mode, int* ref, int cnb0, int cgx, cudaStream_t st);
+// Exact threshold: thr = the (n - tgt)-th smallest of the sensors (ascending, 0-based) where
+// tgt = min(cap, max(1, int(frac * n))), n = count of entries with mask != 0 (all if mask is null);
+// then ref[i] = (mask[i] && sen[i] >= thr).  Writes n to counts->ndeep when mask is given and the
+// threshold to counts->thr0/thr1.  If n == 0 ref is zeroed.
+cudaError_t adapt_threshold_mark(const float* sen, const int* mask, int n, double frac, int cap, int* ref,
+                                 AdaptCounts* counts, int which, cudaStream_t st);
+// deep[b] = all six face neighbours of block b's level-1 grid position are present
+cudaError_t adapt_deepmask(const int* f1pos, const int* l1grid, int l1gx, int nf1, int* deep, cudaStream_t st);
+// exclusive scan of ref0 -> level-1 tables (k_scatter_L1, l1grid reset first); nref0/nf1 into counts.
+// If nf1 > cap1 the error bit is set and no table is written.
+cudaError_t adapt_build_l1(const int* ref0, int cnb0, int cgx, int l1gx, int cap1, int* rank, int* fof0, int* rl0,
+                           int* pcb, int* oct, int* l1grid, int* f1pos, AdaptCounts* counts, cudaStream_t st);
+// exclusive scan of ref1 into rank (counts only): nref1/nf2 into counts
+cudaError_t adapt_scan_l2(const int* ref1, int nf1, int* rank, AdaptCounts* counts, cudaStream_t st);
+// k_scatter_L2 from the ranks of adapt_scan_l2; error and no scatter if nf2 > cap2
+cudaError_t adapt_scatter_l2(const int* ref1, const int* rank, int nf1, int cap2, int* fof1, int* rl1, int* l2pl1,
+                             int* l2oct, AdaptCounts* counts, cudaStream_t st);
+// skin lists: blocks that are refined or have a refined 26-neighbour, ascending (k_dilate + copy_if)
+cudaError_t adapt_skins(const int* ref0, int cnb0, int cgx, const int* ref1, const int* f1pos, const int* l1grid,
+                        int nf1, int l1gx, int* flags, int* skin0, int* skin1, AdaptCounts* counts, cudaStream_t st);
+// set n ints to v
+cudaError_t adapt_fill(int* p, int v, long long n, cudaStream_t st);
+
+}  // namespace amr
+}  // namespace jp

@@ -224,6 +224,49 @@ jp_status jp_get_macro(jp_solver* s, float* host, int64_t count) {
     return uniform_get_macro(s, host, count);
 }
 
+static jp_status need_amr(const jp_solver* s) {
+    if (!s) return fail(JP_ERR_INVALID, "null solver");
+    if (s->kind != JP_AMR) return fail(JP_ERR_INVALID, "not an AMR solver");
+    return JP_OK;
+}
+
+jp_status jp_regrid(jp_solver* s) {
+    jp_status st = need_amr(s);
+    if (st != JP_OK) return st;
+    cudaSetDevice(s->device);
+    return amr_regrid(s);
+}
+
+jp_status jp_amr_get_counts(jp_solver* s, jp_amr_counts* out) {
+    jp_status st = need_amr(s);
+    if (st != JP_OK) return st;
+    if (!out) return fail(JP_ERR_INVALID, "null argument");
+    return amr_get_counts(s, out);
+}
+
+jp_status jp_get_table(jp_solver* s, int32_t table, int32_t* host, int64_t capacity, int64_t* count) {
+    jp_status st = need_amr(s);
+    if (st != JP_OK) return st;
+    if (!host && capacity > 0) return fail(JP_ERR_INVALID, "null buffer");
+    cudaSetDevice(s->device);
+    return amr_get_table(s, table, host, capacity, count);
+}
+
+jp_status jp_get_sensor(jp_solver* s, int32_t level, float* host, int64_t capacity, int64_t* count) {
+    jp_status st = need_amr(s);
+    if (st != JP_OK) return st;
+    if (!host && capacity > 0) return fail(JP_ERR_INVALID, "null buffer");
+    cudaSetDevice(s->device);
+    return amr_get_sensor(s, level, host, capacity, count);
+}
+
+jp_status jp_set_sensor_override(jp_solver* s, const float* sen0, const float* sen1_by_pos) {
+    jp_status st = need_amr(s);
+    if (st != JP_OK) return st;
+    cudaSetDevice(s->device);
+    return amr_set_sensor_override(s, sen0, sen1_by_pos);
+}
+
 jp_status jp_host_alloc(void** ptr, size_t bytes) {
     if (!ptr) return fail(JP_ERR_INVALID, "null argument");
     cudaError_t e = cudaMallocHost(ptr, bytes);

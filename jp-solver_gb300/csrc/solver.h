@@ -63,4 +63,9 @@ jp_status amr_diag(jp_solver* s, double out[3]);
 jp_status amr_population_count(const jp_solver* s, int level, int64_t* count);
 jp_status amr_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count);
 jp_status amr_set_populations(jp_solver* s, int level, int layout, int dtype, const void* host, int64_t count);
+jp_status amr_regrid(jp_solver* s);
+jp_status amr_get_counts(jp_solver* s, jp_amr_counts* out);
+jp_status amr_get_table(jp_solver* s, int table, int32_t* host, int64_t capacity, int64_t* count);
+jp_status amr_get_sensor(jp_solver* s, int level, float* host, int64_t capacity, int64_t* count);
+jp_status amr_set_sensor_override(jp_solver* s, const float* sen0, const float* sen1_by_pos);
 }  // namespace jp

@@ -1,16 +1,702 @@
-// Three-level block AMR solver (reference: src/tgv3d_amr.cu).
+// Three-level block AMR solver: pools, the initial build, regrid, the 1:2:4 subcycled step and the
+// composite diagnostics.  Reference: main() of src/tgv3d_amr.cu (pool sizing :675-709, gpurce_regrid
+// :722-764, gpurce_init :776-815, base_step :821-837, diagnostics :866-888).  The launch sequence and
+// the pool policy are the reference's, so block tables come out identical; the kernels are this
+// library's (amr_kernels.cu, adapt.cu).
+#include "amr_kernels.h"
 #include "jp.h"
+#include "kernels.h"
+#include "lattice.cuh"
 #include "solver.h"
 
-namespace jp {
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <vector>
 
-jp_status amr_create(jp_solver*) { return fail(JP_ERR_UNSUPPORTED, "AMR solver not built yet"); }
-void amr_destroy(jp_solver*) {}
-jp_status amr_init(jp_solver*) { return fail(JP_ERR_UNSUPPORTED, "AMR solver not built yet"); }
-jp_status amr_step(jp_solver*, int64_t) { return fail(JP_ERR_UNSUPPORTED, "AMR solver not built yet"); }
-jp_status amr_diag(jp_solver*, double*) { return fail(JP_ERR_UNSUPPORTED, "AMR solver not built yet"); }
-jp_status amr_population_count(const jp_solver*, int, int64_t*) { return fail(JP_ERR_UNSUPPORTED, "AMR solver not built yet"); }
-jp_status amr_get_populations(jp_solver*, int, int, int, void*, int64_t) { return fail(JP_ERR_UNSUPPORTED, "AMR solver not built yet"); }
-jp_status amr_set_populations(jp_solver*, int, int, int, const void*, int64_t) { return fail(JP_ERR_UNSUPPORTED, "AMR solver not built yet"); }
+namespace jp {
+using namespace amr;
+
+struct AmrState {
+    int MB = 8, MB3 = 512, SH = 480, N = 0, cgx = 0, cnb0 = 0, l1gx = 0, N1 = 0, N2 = 0, NG1 = 0;
+    double tau0 = 0, tau1 = 0, tau2 = 0, nqs01 = 0, nqi10 = 0, nqs12 = 0, nqi21 = 0;
+    float om0 = 0, om1 = 0, om2 = 0;
+    int l1mode = 0, l2mode = 0;
+    bool dynamic = false;
+    int cap_nref0 = 0, cap1 = 0, cap_nref1 = INT_MAX, cap2 = 0;
+    long long hw_nf1 = 0, hw_nf2 = 0;
+    double budget = 0;
+    size_t PB = 0;
+    float *c0a = nullptr, *c0b = nullptr, *f1a = nullptr, *f1b = nullptr, *gh1 = nullptr, *prep0 = nullptr,
+          *prep1 = nullptr, *f2a = nullptr, *f2b = nullptr, *gh2 = nullptr;
+    int *ref0 = nullptr, *fof0 = nullptr, *rl0 = nullptr, *pcb = nullptr, *oct = nullptr, *f1pos = nullptr,
+        *l1grid = nullptr, *ref1 = nullptr, *fof1 = nullptr, *rl1 = nullptr, *l2pl1 = nullptr, *l2oct = nullptr,
+        *skin0 = nullptr, *skin1 = nullptr;
+    int *o_ref0 = nullptr, *o_fof0 = nullptr, *o_l1grid = nullptr, *o_ref1 = nullptr, *o_fof1 = nullptr;
+    int *rank = nullptr, *deep = nullptr, *flags = nullptr;
+    float *sen0 = nullptr, *sen1 = nullptr;
+    float *ov_sen0 = nullptr, *ov_sen1pos = nullptr;
+    AdaptCounts* cnt_dev = nullptr;
+    AdaptCounts* cnt_host = nullptr;
+    int nref0 = 0, nf1 = 0, nref1 = 0, nf2 = 0, n_skin0 = 0, n_skin1 = 0, ndeep = 0;
+    float* field = nullptr;
+    std::vector<void*> owned;
+};
+
+#define ACK(call, what)                                     \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what);  \
+    } while (0)
+
+template <class T>
+static jp_status dalloc(AmrState* a, T** p, size_t count, const char* what) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    a->owned.push_back(*p);
+    return JP_OK;
+}
+template <class T>
+static void dfree(AmrState* a, T*& p) {
+    if (!p) return;
+    auto it = std::find(a->owned.begin(), a->owned.end(), (void*)p);
+    if (it != a->owned.end()) a->owned.erase(it);
+    cudaFree(p);
+    p = nullptr;
+}
+
+#define TRY(x)                      \
+    do {                            \
+        jp_status s_ = (x);         \
+        if (s_ != JP_OK) return s_; \
+    } while (0)
+
+static jp_status launch(jp_solver* s, int op, AmrLaunch L) {
+    L.st = s->stream;
+    cudaError_t e = amr_launch(s->amr->MB, op, L);
+    if (e != cudaSuccess) return cuda_fail(e, "AMR kernel launch");
+    return JP_OK;
+}
+
+static jp_status read_counts(jp_solver* s) {
+    AmrState* a = s->amr;
+    ACK(cudaMemcpyAsync(a->cnt_host, a->cnt_dev, sizeof(AdaptCounts), cudaMemcpyDeviceToHost, s->stream), "counts D2H");
+    ACK(cudaStreamSynchronize(s->stream), "adaptation");
+    return JP_OK;
+}
+
+static bool pool_fits(const AmrState* a, long long c1, long long c2) {
+    return (double)((size_t)(c1 + c2) * a->PB * 6 / 5) < a->budget;
+}
+
+// sensor of level 0 (all coarse blocks) or level 1 (active fine blocks), override-aware
+static jp_status sensor(jp_solver* s, int level) {
+    AmrState* a = s->amr;
+    AmrLaunch L;
+    if (level == 0) {
+        L.nblocks = a->cnb0;
+        L.in = a->c0a;
+        L.out = a->sen0;
+        L.aux = a->ov_sen0;
+        L.t0 = nullptr;
+    } else {
+        L.nblocks = a->nf1;
+        L.in = a->f1a;
+        L.out = a->sen1;
+        L.aux = a->ov_sen1pos;
+        L.t0 = a->ov_sen1pos ? a->f1pos : nullptr;
+    }
+    return launch(s, OP_SENSOR, L);
+}
+
+static jp_status step_l0(jp_solver* s) {
+    AmrState* a = s->amr;
+    AmrLaunch L;
+    L.nblocks = a->cnb0;
+    L.in = a->c0a;
+    L.out = a->c0b;
+    L.cgx = a->cgx;
+    L.n = a->N;
+    L.omega = a->om0;
+    TRY(launch(s, OP_STEP_L0, L));
+    std::swap(a->c0a, a->c0b);
+    return JP_OK;
+}
+
+static jp_status skins(jp_solver* s) {
+    AmrState* a = s->amr;
+    ACK(adapt_skins(a->ref0, a->cnb0, a->cgx, a->ref1, a->f1pos, a->l1grid, a->nf1, a->l1gx, a->flags, a->skin0,
+                    a->skin1, a->cnt_dev, s->stream), "skins");
+    TRY(read_counts(s));
+    a->n_skin0 = a->cnt_host->n_skin0;
+    a->n_skin1 = a->cnt_host->n_skin1;
+    return JP_OK;
+}
+
+static jp_status check_err(jp_solver* s) {
+    const int e = s->amr->cnt_host->err;
+    if (e & ADAPT_ERR_CAP1) return fail(JP_ERR_CAPACITY, "level-1 pool overflow: %d blocks > capacity %d", s->amr->cnt_host->nf1, s->amr->cap1);
+    if (e & ADAPT_ERR_CAP2) return fail(JP_ERR_CAPACITY, "level-2 pool overflow: %d blocks > capacity %d", s->amr->cnt_host->nf2, s->amr->cap2);
+    return JP_OK;
+}
+
+static jp_status mark_l0_by_sensor(jp_solver* s) {
+    AmrState* a = s->amr;
+    TRY(sensor(s, 0));
+    ACK(adapt_threshold_mark(a->sen0, nullptr, a->cnb0, s->cfg.frac1, a->cap_nref0, a->ref0, a->cnt_dev, 0, s->stream),
+        "threshold L0");
+    return JP_OK;
+}
+
+// exclusive scan of the marks and the level-1 tables.  On overflow of the level-1 pool nothing is
+// written and, in a regrid (restore_marks), the previous marks come back: the old grid stays valid.
+static jp_status build_l1(jp_solver* s, bool restore_marks) {
+    AmrState* a = s->amr;
+    ACK(adapt_build_l1(a->ref0, a->cnb0, a->cgx, a->l1gx, a->cap1, a->rank, a->fof0, a->rl0, a->pcb, a->oct, a->l1grid,
+                       a->f1pos, a->cnt_dev, s->stream), "build L1");
+    TRY(read_counts(s));
+    if (a->cnt_host->err && restore_marks) {
+        ACK(cudaMemcpyAsync(a->ref0, a->o_ref0, sizeof(int) * a->cnb0, cudaMemcpyDeviceToDevice, s->stream), "restore");
+        ACK(cudaStreamSynchronize(s->stream), "restore");
+    }
+    TRY(check_err(s));
+    a->nref0 = a->cnt_host->nref0;
+    a->nf1 = a->cnt_host->nf1;
+    a->hw_nf1 = std::max(a->hw_nf1, (long long)a->nf1);
+    return JP_OK;
+}
+
+// gpurce_init (src/tgv3d_amr.cu:776-815)
+static jp_status initial_build(jp_solver* s) {
+    AmrState* a = s->amr;
+    const jp_config& c = s->cfg;
+    ACK(cudaMemsetAsync(a->cnt_dev, 0, sizeof(AdaptCounts), s->stream), "counts");
+    if (a->l1mode == JP_REFINE_ALL || a->l1mode == JP_REFINE_SLAB) {
+        ACK(adapt_mark_mode(a->l1mode == JP_REFINE_ALL ? 0 : 1, a->ref0, a->cnb0, a->cgx, s->stream), "mark L0");
+    } else {
+        for (int i = 0; i < c.develop_steps; ++i) TRY(step_l0(s));  // uncounted coarse steps (:711,779)
+        TRY(mark_l0_by_sensor(s));
+    }
+    TRY(build_l1(s, false));
+    if (a->nf1) {
+        ACK(cudaMemsetAsync(a->gh1, 0, sizeof(float) * (size_t)a->nf1 * Q * a->SH, s->stream), "memset gh1");
+        AmrLaunch L;
+        L.nblocks = a->nf1;
+        L.out = a->f1a;
+        L.aux = a->c0a;
+        L.t0 = a->pcb;
+        L.t1 = a->oct;
+        L.cgx = a->cgx;
+        L.n = a->N;
+        L.scale = float(a->nqs01);
+        TRY(launch(s, OP_SEED_L1, L));
+    }
+    a->nref1 = a->nf2 = 0;
+    if (a->nf1) {
+        TRY(sensor(s, 1));
+        ACK(adapt_deepmask(a->f1pos, a->l1grid, a->l1gx, a->nf1, a->deep, s->stream), "deepmask");
+        ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * a->cap1, s->stream), "memset ref1");
+        if (a->l2mode == JP_REFINE_ALL) {
+            ACK(cudaMemcpyAsync(a->ref1, a->deep, sizeof(int) * a->nf1, cudaMemcpyDeviceToDevice, s->stream), "ref1=deep");
+        } else {
+            ACK(adapt_threshold_mark(a->sen1, a->deep, a->nf1, c.frac2, INT_MAX, a->ref1, a->cnt_dev, 1, s->stream),
+                "threshold L1");
+        }
+        ACK(adapt_scan_l2(a->ref1, a->nf1, a->rank, a->cnt_dev, s->stream), "scan L2");
+        TRY(read_counts(s));
+        a->nref1 = a->cnt_host->nref1;
+        a->nf2 = a->cnt_host->nf2;
+        a->ndeep = a->cnt_host->ndeep;
+        a->hw_nf2 = std::max(a->hw_nf2, (long long)a->nf2);
+        a->cap_nref1 = std::max(1, (int)std::ceil(a->nref1 * 2.5));
+        if (a->l2mode == JP_REFINE_ALL) a->cap_nref1 = std::max(a->cap_nref1, a->nf1);
+        a->cap_nref1 = std::min(a->cap_nref1, a->cap1);
+        while (a->cap_nref1 > 1 && !pool_fits(a, a->cap1, 8LL * a->cap_nref1)) a->cap_nref1--;
+        a->cap2 = 8 * a->cap_nref1;
+    } else {
+        a->cap_nref1 = 1;
+        a->cap2 = 8;
+    }
+    if (a->nf2 > a->cap2) return fail(JP_ERR_CAPACITY, "level-2 pool overflow: %d > %d", a->nf2, a->cap2);
+    dfree(a, a->f2a);
+    dfree(a, a->f2b);
+    dfree(a, a->gh2);
+    dfree(a, a->l2pl1);
+    dfree(a, a->l2oct);
+    const size_t blk = (size_t)Q * a->MB3;
+    TRY(dalloc(a, &a->f2a, (size_t)a->cap2 * blk, "cudaMalloc f2"));
+    TRY(dalloc(a, &a->f2b, (size_t)a->cap2 * blk, "cudaMalloc f2"));
+    TRY(dalloc(a, &a->gh2, (size_t)a->cap2 * Q * a->SH, "cudaMalloc gh2"));
+    TRY(dalloc(a, &a->l2pl1, (size_t)a->cap2, "cudaMalloc l2pl1"));
+    TRY(dalloc(a, &a->l2oct, (size_t)a->cap2, "cudaMalloc l2oct"));
+    ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset fof1");
+    if (a->nf2) {
+        ACK(adapt_scatter_l2(a->ref1, a->rank, a->nf1, a->cap2, a->fof1, a->rl1, a->l2pl1, a->l2oct, a->cnt_dev,
+                             s->stream), "scatter L2");
+        ACK(cudaMemsetAsync(a->gh2, 0, sizeof(float) * (size_t)a->nf2 * Q * a->SH, s->stream), "memset gh2");
+        AmrLaunch L;
+        L.nblocks = a->nf2;
+        L.out = a->f2a;
+        L.aux = a->f1a;
+        L.t0 = a->l2pl1;
+        L.t1 = a->l2oct;
+        L.t2 = a->f1pos;
+        L.t6 = a->l1grid;
+        L.l1gx = a->l1gx;
+        L.n1 = a->N1;
+        L.scale = float(a->nqs12);
+        TRY(launch(s, OP_SEED_L2, L));
+    }
+    TRY(skins(s));
+    return JP_OK;
+}
+
+// gpurce_regrid (src/tgv3d_amr.cu:722-764)
+static jp_status regrid(jp_solver* s) {
+    AmrState* a = s->amr;
+    const jp_config& c = s->cfg;
+    ACK(cudaMemsetAsync(a->cnt_dev, 0, sizeof(AdaptCounts), s->stream), "counts");
+    ACK(cudaMemcpyAsync(a->o_ref0, a->ref0, sizeof(int) * a->cnb0, cudaMemcpyDeviceToDevice, s->stream), "snapshot");
+    ACK(cudaMemcpyAsync(a->o_fof0, a->fof0, sizeof(int) * a->cnb0, cudaMemcpyDeviceToDevice, s->stream), "snapshot");
+    ACK(cudaMemcpyAsync(a->o_l1grid, a->l1grid, sizeof(int) * a->NG1, cudaMemcpyDeviceToDevice, s->stream), "snapshot");
+    ACK(cudaMemcpyAsync(a->o_ref1, a->ref1, sizeof(int) * a->cap1, cudaMemcpyDeviceToDevice, s->stream), "snapshot");
+    ACK(cudaMemcpyAsync(a->o_fof1, a->fof1, sizeof(int) * a->cap1, cudaMemcpyDeviceToDevice, s->stream), "snapshot");
+    TRY(mark_l0_by_sensor(s));
+    TRY(build_l1(s, true));
+    if (a->nf1) {
+        AmrLaunch L;
+        L.nblocks = a->nf1;
+        L.in = a->f1a;
+        L.out = a->f1b;
+        L.aux = a->c0a;
+        L.t0 = a->pcb;
+        L.t1 = a->oct;
+        L.t2 = a->o_ref0;
+        L.t3 = a->o_fof0;
+        L.cgx = a->cgx;
+        L.n = a->N;
+        L.scale = float(a->nqs01);
+        TRY(launch(s, OP_SEED_L1, L));
+        std::swap(a->f1a, a->f1b);
+    }
+    a->nref1 = a->nf2 = 0;
+    if (a->nf1) {
+        TRY(sensor(s, 1));
+        ACK(adapt_deepmask(a->f1pos, a->l1grid, a->l1gx, a->nf1, a->deep, s->stream), "deepmask");
+        ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * a->cap1, s->stream), "memset ref1");
+        ACK(adapt_threshold_mark(a->sen1, a->deep, a->nf1, c.frac2, a->cap_nref1, a->ref1, a->cnt_dev, 1, s->stream),
+            "threshold L1");
+        ACK(adapt_scan_l2(a->ref1, a->nf1, a->rank, a->cnt_dev, s->stream), "scan L2");
+        TRY(read_counts(s));
+        a->nref1 = a->cnt_host->nref1;
+        a->nf2 = a->cnt_host->nf2;
+        a->ndeep = a->cnt_host->ndeep;
+        a->hw_nf2 = std::max(a->hw_nf2, (long long)a->nf2);
+        if (a->nf2 > a->cap2) return fail(JP_ERR_CAPACITY, "level-2 pool overflow: %d > %d", a->nf2, a->cap2);
+        ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset fof1");
+        if (a->nref1)
+            ACK(adapt_scatter_l2(a->ref1, a->rank, a->nf1, a->cap2, a->fof1, a->rl1, a->l2pl1, a->l2oct, a->cnt_dev,
+                                 s->stream), "scatter L2");
+        if (a->nf2) {
+            AmrLaunch L;
+            L.nblocks = a->nf2;
+            L.in = a->f2a;
+            L.out = a->f2b;
+            L.aux = a->f1a;
+            L.t0 = a->l2pl1;
+            L.t1 = a->l2oct;
+            L.t2 = a->f1pos;
+            L.t3 = a->o_l1grid;
+            L.t4 = a->o_ref1;
+            L.t5 = a->o_fof1;
+            L.t6 = a->l1grid;
+            L.l1gx = a->l1gx;
+            L.n1 = a->N1;
+            L.scale = float(a->nqs12);
+            TRY(launch(s, OP_SEED_L2, L));
+            std::swap(a->f2a, a->f2b);
+        }
+    }
+    TRY(skins(s));
+    return JP_OK;
+}
+
+// base_step (src/tgv3d_amr.cu:821-837): coarse once, level 1 twice, level 2 four times, restricting
+// level 2 into level 1 after each pair and level 1 into level 0 at the end.
+static jp_status base_step(jp_solver* s) {
+    AmrState* a = s->amr;
+    TRY(step_l0(s));
+    if (!a->nf1) return JP_OK;
+    {
+        AmrLaunch L;
+        L.nblocks = a->n_skin0;
+        L.in = a->c0a;
+        L.out = a->prep0;
+        L.list = a->skin0;
+        L.scale = float(a->nqs01);
+        TRY(launch(s, OP_PREP, L));
+        AmrLaunch F;
+        F.nblocks = a->nf1;
+        F.in = a->prep0;
+        F.out = a->gh1;
+        F.t0 = a->pcb;
+        F.t1 = a->oct;
+        F.t2 = a->ref0;
+        F.cgx = a->cgx;
+        F.n = a->N;
+        TRY(launch(s, OP_FILL_L1, F));
+    }
+    for (int s1 = 0; s1 < 2; ++s1) {
+        if (a->nf2) {
+            AmrLaunch L;
+            L.nblocks = a->n_skin1;
+            L.in = a->f1a;
+            L.out = a->prep1;
+            L.list = a->skin1;
+            L.scale = float(a->nqs12);
+            TRY(launch(s, OP_PREP, L));
+            AmrLaunch F;
+            F.nblocks = a->nf2;
+            F.in = a->prep1;
+            F.out = a->gh2;
+            F.t0 = a->l2pl1;
+            F.t1 = a->l2oct;
+            F.t2 = a->f1pos;
+            F.t3 = a->l1grid;
+            F.t4 = a->ref1;
+            F.l1gx = a->l1gx;
+            F.n1 = a->N1;
+            TRY(launch(s, OP_FILL_L2, F));
+            for (int s2 = 0; s2 < 2; ++s2) {
+                AmrLaunch S;
+                S.nblocks = a->nf2;
+                S.in = a->f2a;
+                S.out = a->f2b;
+                S.aux = a->gh2;
+                S.t0 = a->l2pl1;
+                S.t1 = a->l2oct;
+                S.t2 = a->f1pos;
+                S.t3 = a->l1grid;
+                S.t4 = a->ref1;
+                S.t5 = a->fof1;
+                S.l1gx = a->l1gx;
+                S.n1 = a->N1;
+                S.omega = a->om2;
+                TRY(launch(s, OP_STEP_L2, S));
+                std::swap(a->f2a, a->f2b);
+            }
+            AmrLaunch R;
+            R.nblocks = a->nref1;
+            R.out = a->f1a;
+            R.in = a->f2a;
+            R.list = a->rl1;
+            R.t0 = a->fof1;
+            R.scale = float(a->nqi21);
+            TRY(launch(s, OP_RESTRICT, R));
+        }
+        AmrLaunch S;
+        S.nblocks = a->nf1;
+        S.in = a->f1a;
+        S.out = a->f1b;
+        S.aux = a->gh1;
+        S.t0 = a->pcb;
+        S.t1 = a->oct;
+        S.t2 = a->ref0;
+        S.t3 = a->fof0;
+        S.cgx = a->cgx;
+        S.n = a->N;
+        S.omega = a->om1;
+        TRY(launch(s, OP_STEP_L1, S));
+        std::swap(a->f1a, a->f1b);
+    }
+    AmrLaunch R;
+    R.nblocks = a->nref0;
+    R.out = a->c0a;
+    R.in = a->f1a;
+    R.list = a->rl0;
+    R.t0 = a->fof0;
+    R.scale = float(a->nqi10);
+    return launch(s, OP_RESTRICT, R);
+}
+
+// ---- lifecycle -------------------------------------------------------------------------------------
+
+jp_status amr_create(jp_solver* s) {
+    TRY(common_setup(s));
+    const jp_config& c = s->cfg;
+    if (c.storage != JP_FP32) return fail(JP_ERR_UNSUPPORTED, "AMR solver: FP32 storage only in this build");
+    if (c.l1_mode < 0 || c.l1_mode > 2 || c.l2_mode < 0 || c.l2_mode > 2) return fail(JP_ERR_INVALID, "bad refine mode");
+    AmrState* a = new (std::nothrow) AmrState();
+    if (!a) return fail(JP_ERR_NOMEM, "host allocation");
+    s->amr = a;
+    a->MB = c.mb;
+    a->MB3 = c.mb * c.mb * c.mb;
+    a->SH = shell_cells(c.mb);
+    a->N = c.n;
+    a->cgx = c.n / c.mb;
+    a->cnb0 = a->cgx * a->cgx * a->cgx;
+    a->l1gx = 2 * a->cgx;
+    a->N1 = 2 * c.n;
+    a->N2 = 4 * c.n;
+    a->NG1 = a->l1gx * a->l1gx * a->l1gx;
+    a->l1mode = c.l1_mode;
+    a->l2mode = c.l2_mode;
+    a->dynamic = c.l1_mode == JP_REFINE_SENSOR || c.l2_mode == JP_REFINE_SENSOR;
+    const double tau0 = s->info.tau;
+    a->tau0 = tau0;
+    a->tau1 = 2.0 * tau0 - 0.5;
+    a->tau2 = 2.0 * a->tau1 - 0.5;
+    a->om0 = float(1.0 / a->tau0);
+    a->om1 = float(1.0 / a->tau1);
+    a->om2 = float(1.0 / a->tau2);
+    a->nqs01 = (a->tau1 - 1.0) / (2.0 * (a->tau0 - 1.0));
+    a->nqi10 = (2.0 * (a->tau0 - 1.0)) / (a->tau1 - 1.0);
+    a->nqs12 = (a->tau2 - 1.0) / (2.0 * (a->tau1 - 1.0));
+    a->nqi21 = (2.0 * (a->tau1 - 1.0)) / (a->tau2 - 1.0);
+    s->cells = (long long)a->cnb0 * a->MB3;
+    s->n = c.n;
+    const size_t blk = (size_t)Q * a->MB3;
+    TRY(dalloc(a, &a->c0a, (size_t)a->cnb0 * blk, "cudaMalloc c0"));
+    TRY(dalloc(a, &a->c0b, (size_t)a->cnb0 * blk, "cudaMalloc c0"));
+    TRY(dalloc(a, &a->sen0, (size_t)a->cnb0, "cudaMalloc sen0"));
+    // HBM budget for the fine pools: --maxgb, else 75% of free memory (src/tgv3d_amr.cu:684-688)
+    size_t freeB = 0, totB = 0;
+    ACK(cudaMemGetInfo(&freeB, &totB), "cudaMemGetInfo");
+    a->budget = c.max_gb > 0 ? c.max_gb * double(1ull << 30) : double(freeB) * 0.75;
+    a->PB = (size_t)Q * 4 * (2 * a->MB3 + (a->MB + 2) * (a->MB + 2) * (a->MB + 2));
+    a->cap_nref0 = (a->l1mode == JP_REFINE_ALL) ? a->cnb0
+                                                : std::min(a->cnb0, std::max(1, (int)std::ceil(c.frac1 * a->cnb0 * 1.4)));
+    while (a->cap_nref0 > 1 && !pool_fits(a, 8LL * a->cap_nref0, 0)) a->cap_nref0--;
+    a->cap1 = 8 * a->cap_nref0;
+    TRY(dalloc(a, &a->f1a, (size_t)a->cap1 * blk, "cudaMalloc f1"));
+    TRY(dalloc(a, &a->f1b, (size_t)a->cap1 * blk, "cudaMalloc f1"));
+    TRY(dalloc(a, &a->gh1, (size_t)a->cap1 * Q * a->SH, "cudaMalloc gh1"));
+    TRY(dalloc(a, &a->prep0, (size_t)a->cnb0 * blk, "cudaMalloc prep0"));
+    TRY(dalloc(a, &a->prep1, (size_t)a->cap1 * blk, "cudaMalloc prep1"));
+    int** cnb_tabs[] = {&a->ref0, &a->fof0, &a->o_ref0, &a->o_fof0, &a->skin0};
+    for (int** t : cnb_tabs) TRY(dalloc(a, t, (size_t)a->cnb0, "cudaMalloc table"));
+    int** cap_tabs[] = {&a->pcb, &a->oct, &a->rl0, &a->f1pos, &a->ref1, &a->fof1, &a->o_ref1, &a->o_fof1,
+                        &a->rl1, &a->skin1, &a->deep};
+    for (int** t : cap_tabs) TRY(dalloc(a, t, (size_t)a->cap1, "cudaMalloc table"));
+    TRY(dalloc(a, &a->l1grid, (size_t)a->NG1, "cudaMalloc l1grid"));
+    TRY(dalloc(a, &a->o_l1grid, (size_t)a->NG1, "cudaMalloc l1grid"));
+    TRY(dalloc(a, &a->rank, (size_t)std::max(a->cnb0, a->cap1), "cudaMalloc rank"));
+    TRY(dalloc(a, &a->flags, (size_t)a->cnb0 + a->cap1, "cudaMalloc flags"));
+    TRY(dalloc(a, &a->sen1, (size_t)a->cap1, "cudaMalloc sen1"));
+    TRY(dalloc(a, &a->cnt_dev, 1, "cudaMalloc counts"));
+    ACK(cudaMallocHost(&a->cnt_host, sizeof(AdaptCounts)), "cudaMallocHost counts");
+    ACK(cudaMalloc(&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
+    ACK(cudaMalloc(&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
+    ACK(cudaMallocHost(&s->diag_host, sizeof(double) * 3), "cudaMallocHost diag");
+    ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset");
+    ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * a->cap1, s->stream), "memset");
+    ACK(cudaMemsetAsync(a->l1grid, 0xFF, sizeof(int) * a->NG1, s->stream), "memset");
+    return amr_init(s);
+}
+
+void amr_destroy(jp_solver* s) {
+    AmrState* a = s->amr;
+    if (!a) return;
+    for (void* p : a->owned) cudaFree(p);
+    if (a->cnt_host) cudaFreeHost(a->cnt_host);
+    if (a->field) cudaFree(a->field);
+    delete a;
+    s->amr = nullptr;
+}
+
+// TGV state on the coarse grid and the initial build (with the sensor override, if one is set)
+jp_status amr_init(jp_solver* s) {
+    AmrState* a = s->amr;
+    AmrLaunch L;
+    L.nblocks = a->cnb0;
+    L.out = a->c0a;
+    L.cgx = a->cgx;
+    L.u0 = s->cfg.u0;
+    L.kf = s->info.kf;
+    TRY(launch(s, OP_INIT, L));
+    a->hw_nf1 = a->hw_nf2 = 0;
+    TRY(initial_build(s));
+    ACK(cudaStreamSynchronize(s->stream), "initial build");
+    s->step_count = 0;
+    s->info.bytes_state = (int64_t)(((size_t)2 * a->cnb0 + 2 * (size_t)a->cap1 + 2 * (size_t)a->cap2) * Q * a->MB3 * 4 +
+                                    ((size_t)a->cap1 + a->cap2) * Q * a->SH * 4);
+    return JP_OK;
+}
+
+jp_status amr_step(jp_solver* s, int64_t nsteps) {
+    for (int64_t i = 0; i < nsteps; ++i) {
+        TRY(base_step(s));
+        ++s->step_count;
+    }
+    return JP_OK;
+}
+
+jp_status amr_regrid(jp_solver* s) {
+    TRY(regrid(s));
+    ACK(cudaStreamSynchronize(s->stream), "regrid");
+    return JP_OK;
+}
+
+jp_status amr_diag(jp_solver* s, double out[3]) {
+    AmrState* a = s->amr;
+    if (!a->field) ACK(cudaMalloc(&a->field, sizeof(float) * 4 * (size_t)a->N2 * a->N2 * a->N2), "cudaMalloc composite");
+    AmrLaunch L;
+    L.in = a->c0a;
+    L.aux = a->f1a;
+    L.aux2 = a->f2a;
+    L.out = a->field;
+    L.t0 = a->ref1;
+    L.t1 = a->fof1;
+    L.t2 = a->l1grid;
+    L.cgx = a->cgx;
+    L.l1gx = a->l1gx;
+    L.n2 = a->N2;
+    TRY(launch(s, OP_COMPOSITE, L));
+    ACK(launch_diag_field(false, false, a->field, a->N2, s->partials, s->diag_dev, s->stream), "diag");
+    ACK(cudaMemcpyAsync(s->diag_host, s->diag_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "diag D2H");
+    ACK(cudaStreamSynchronize(s->stream), "diag");
+    out[0] = s->diag_host[0];
+    out[1] = s->diag_host[1];
+    out[2] = s->diag_host[2];
+    return JP_OK;
+}
+
+static float* level_ptr(AmrState* a, int level, long long* nblk) {
+    switch (level) {
+        case 0: *nblk = a->cnb0; return a->c0a;
+        case 1: *nblk = a->nf1; return a->f1a;
+        case 2: *nblk = a->nf2; return a->f2a;
+    }
+    *nblk = -1;
+    return nullptr;
+}
+
+jp_status amr_population_count(const jp_solver* s, int level, int64_t* count) {
+    long long nb;
+    if (!level_ptr(s->amr, level, &nb) && nb < 0) return fail(JP_ERR_INVALID, "AMR level must be 0, 1 or 2");
+    *count = (int64_t)nb * Q * s->amr->MB3;
+    return JP_OK;
+}
+
+jp_status amr_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count) {
+    AmrState* a = s->amr;
+    long long nb;
+    float* p = level_ptr(a, level, &nb);
+    if (nb < 0) return fail(JP_ERR_INVALID, "AMR level must be 0, 1 or 2");
+    if (layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_UNSUPPORTED, "AMR populations are exported in the blocked layout");
+    if (count != nb * Q * a->MB3) return fail(JP_ERR_INVALID, "count %lld != %lld", (long long)count, nb * Q * a->MB3);
+    if (count == 0) return JP_OK;
+    if (dtype == JP_F32) {
+        ACK(cudaMemcpyAsync(host, p, sizeof(float) * count, cudaMemcpyDeviceToHost, s->stream), "D2H");
+        ACK(cudaStreamSynchronize(s->stream), "D2H");
+        return JP_OK;
+    }
+    std::vector<float> tmp((size_t)count);
+    ACK(cudaMemcpyAsync(tmp.data(), p, sizeof(float) * count, cudaMemcpyDeviceToHost, s->stream), "D2H");
+    ACK(cudaStreamSynchronize(s->stream), "D2H");
+    for (int64_t i = 0; i < count; ++i) static_cast<double*>(host)[i] = tmp[(size_t)i];
+    return JP_OK;
+}
+
+jp_status amr_set_populations(jp_solver* s, int level, int layout, int dtype, const void* host, int64_t count) {
+    AmrState* a = s->amr;
+    long long nb;
+    float* p = level_ptr(a, level, &nb);
+    if (nb < 0) return fail(JP_ERR_INVALID, "AMR level must be 0, 1 or 2");
+    if (layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_UNSUPPORTED, "AMR populations are imported in the blocked layout");
+    if (count != nb * Q * a->MB3) return fail(JP_ERR_INVALID, "count %lld != %lld", (long long)count, nb * Q * a->MB3);
+    if (count == 0) return JP_OK;
+    if (dtype == JP_F32) {
+        ACK(cudaMemcpyAsync(p, host, sizeof(float) * count, cudaMemcpyHostToDevice, s->stream), "H2D");
+        ACK(cudaStreamSynchronize(s->stream), "H2D");
+        return JP_OK;
+    }
+    std::vector<float> tmp((size_t)count);
+    for (int64_t i = 0; i < count; ++i) tmp[(size_t)i] = float(static_cast<const double*>(host)[i]);
+    ACK(cudaMemcpyAsync(p, tmp.data(), sizeof(float) * count, cudaMemcpyHostToDevice, s->stream), "H2D");
+    ACK(cudaStreamSynchronize(s->stream), "H2D");
+    return JP_OK;
+}
+
+jp_status amr_get_counts(jp_solver* s, jp_amr_counts* o) {
+    AmrState* a = s->amr;
+    std::memset(o, 0, sizeof *o);
+    o->nref0 = a->nref0;
+    o->nf1 = a->nf1;
+    o->nref1 = a->nref1;
+    o->nf2 = a->nf2;
+    o->n_skin0 = a->n_skin0;
+    o->n_skin1 = a->n_skin1;
+    o->ndeep = a->ndeep;
+    o->cnb0 = a->cnb0;
+    o->ng1 = a->NG1;
+    o->cap_nref0 = a->cap_nref0;
+    o->cap1 = a->cap1;
+    o->cap_nref1 = a->cap_nref1;
+    o->cap2 = a->cap2;
+    o->hw_nf1 = a->hw_nf1;
+    o->hw_nf2 = a->hw_nf2;
+    return JP_OK;
+}
+
+jp_status amr_get_table(jp_solver* s, int table, int32_t* host, int64_t capacity, int64_t* count) {
+    AmrState* a = s->amr;
+    const int* p = nullptr;
+    long long n = 0;
+    switch (table) {
+        case JP_TABLE_REF0: p = a->ref0; n = a->cnb0; break;
+        case JP_TABLE_FOF0: p = a->fof0; n = a->cnb0; break;
+        case JP_TABLE_RL0: p = a->rl0; n = a->nref0; break;
+        case JP_TABLE_L1PCB: p = a->pcb; n = a->nf1; break;
+        case JP_TABLE_L1OCT: p = a->oct; n = a->nf1; break;
+        case JP_TABLE_F1POS: p = a->f1pos; n = a->nf1; break;
+        case JP_TABLE_L1GRID: p = a->l1grid; n = a->NG1; break;
+        case JP_TABLE_REF1: p = a->ref1; n = a->nf1; break;
+        case JP_TABLE_FOF1: p = a->fof1; n = a->nf1; break;
+        case JP_TABLE_RL1: p = a->rl1; n = a->nref1; break;
+        case JP_TABLE_L2PL1: p = a->l2pl1; n = a->nf2; break;
+        case JP_TABLE_L2OCT: p = a->l2oct; n = a->nf2; break;
+        case JP_TABLE_SKIN0: p = a->skin0; n = a->n_skin0; break;
+        case JP_TABLE_SKIN1: p = a->skin1; n = a->n_skin1; break;
+        case JP_TABLE_DEEP: p = a->deep; n = a->nf1; break;
+        default: return fail(JP_ERR_INVALID, "unknown table %d", table);
+    }
+    if (count) *count = n;
+    if (n > capacity) return fail(JP_ERR_CAPACITY, "table %d has %lld entries, buffer holds %lld", table, n, (long long)capacity);
+    if (n == 0) return JP_OK;
+    ACK(cudaMemcpyAsync(host, p, sizeof(int) * n, cudaMemcpyDeviceToHost, s->stream), "table D2H");
+    ACK(cudaStreamSynchronize(s->stream), "table D2H");
+    return JP_OK;
+}
+
+jp_status amr_get_sensor(jp_solver* s, int level, float* host, int64_t capacity, int64_t* count) {
+    AmrState* a = s->amr;
+    if (level != 0 && level != 1) return fail(JP_ERR_INVALID, "sensor level must be 0 or 1");
+    const long long n = level == 0 ? a->cnb0 : a->nf1;
+    if (count) *count = n;
+    if (n > capacity) return fail(JP_ERR_CAPACITY, "sensor has %lld entries", n);
+    if (n == 0) return JP_OK;
+    ACK(cudaMemcpyAsync(host, level == 0 ? a->sen0 : a->sen1, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream), "D2H");
+    ACK(cudaStreamSynchronize(s->stream), "D2H");
+    return JP_OK;
+}
+
+jp_status amr_set_sensor_override(jp_solver* s, const float* sen0, const float* sen1_by_pos) {
+    AmrState* a = s->amr;
+    if (!sen0 || !sen1_by_pos) {
+        dfree(a, a->ov_sen0);
+        dfree(a, a->ov_sen1pos);
+        return JP_OK;
+    }
+    if (!a->ov_sen0) TRY(dalloc(a, &a->ov_sen0, (size_t)a->cnb0, "cudaMalloc override"));
+    if (!a->ov_sen1pos) TRY(dalloc(a, &a->ov_sen1pos, (size_t)a->NG1, "cudaMalloc override"));
+    ACK(cudaMemcpyAsync(a->ov_sen0, sen0, sizeof(float) * a->cnb0, cudaMemcpyHostToDevice, s->stream), "H2D");
+    ACK(cudaMemcpyAsync(a->ov_sen1pos, sen1_by_pos, sizeof(float) * a->NG1, cudaMemcpyHostToDevice, s->stream), "H2D");
+    ACK(cudaStreamSynchronize(s->stream), "H2D");
+    return JP_OK;
+}
 
 }  // namespace jp

@@ -53,6 +53,20 @@ class Info(C.Structure):
     ]
 
 
+class AmrCounts(C.Structure):
+    _fields_ = [
+        ("nref0", C.c_int32), ("nf1", C.c_int32), ("nref1", C.c_int32), ("nf2", C.c_int32),
+        ("n_skin0", C.c_int32), ("n_skin1", C.c_int32), ("ndeep", C.c_int32),
+        ("cnb0", C.c_int32), ("ng1", C.c_int32), ("cap_nref0", C.c_int32), ("cap1", C.c_int32),
+        ("cap_nref1", C.c_int32), ("cap2", C.c_int32), ("pad", C.c_int32),
+        ("hw_nf1", C.c_int64), ("hw_nf2", C.c_int64),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+
+TABLES = {"ref0": 0, "fof0": 1, "rl0": 2, "l1pcb": 3, "l1oct": 4, "f1pos": 5, "l1grid": 6, "ref1": 7, "fof1": 8,
+          "rl1": 9, "l2pl1": 10, "l2oct": 11, "skin0": 12, "skin1": 13, "deep": 14}
+
 _lib: Optional[C.CDLL] = None
 
 # exported symbol -> (restype, argtypes)
@@ -77,6 +91,11 @@ SIGNATURES = {
     "jp_host_free": (None, [C.c_void_p]),
     "jp_step_timed": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
     "jp_launch_count": (C.c_int64, []),
+    "jp_regrid": (C.c_int, [C.c_void_p]),
+    "jp_amr_get_counts": (C.c_int, [C.c_void_p, C.POINTER(AmrCounts)]),
+    "jp_get_table": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int64)]),
+    "jp_get_sensor": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_int64)]),
+    "jp_set_sensor_override": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
 }
 
 
@@ -174,6 +193,8 @@ class Solver:
 
     def get_populations(self, level: int = 0, layout: str = "flat", dtype=np.float32) -> np.ndarray:
         cnt = self.population_count(level)
+        if cnt == 0:
+            return np.empty(0, dtype=dtype)
         a = np.empty(cnt, dtype=dtype)
         dt = 0 if a.dtype == np.float32 else 1
         _check(lib().jp_get_populations(self.h, level, LAYOUT[layout], dt, a.ctypes.data_as(C.c_void_p), cnt))
@@ -186,6 +207,38 @@ class Solver:
         dt = 0 if a.dtype == np.float32 else 1
         _check(lib().jp_set_populations(self.h, level, LAYOUT[layout], dt, a.ctypes.data_as(C.c_void_p), a.size))
         self.sync()
+
+    # ---- AMR ----
+    def regrid(self) -> None:
+        _check(lib().jp_regrid(self.h))
+
+    def counts(self) -> dict:
+        c = AmrCounts()
+        _check(lib().jp_amr_get_counts(self.h, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in AmrCounts._fields_ if k not in ("reserved", "pad")}
+
+    def table(self, name: str) -> np.ndarray:
+        n = C.c_int64()
+        lib().jp_get_table(self.h, TABLES[name], None, 0, C.byref(n))
+        a = np.empty(max(n.value, 1), dtype=np.int32)
+        _check(lib().jp_get_table(self.h, TABLES[name], a.ctypes.data_as(C.POINTER(C.c_int32)), a.size, C.byref(n)))
+        return a[:n.value]
+
+    def sensor(self, level: int) -> np.ndarray:
+        n = C.c_int64()
+        lib().jp_get_sensor(self.h, level, None, 0, C.byref(n))
+        a = np.empty(max(n.value, 1), dtype=np.float32)
+        _check(lib().jp_get_sensor(self.h, level, a.ctypes.data_as(C.POINTER(C.c_float)), a.size, C.byref(n)))
+        return a[:n.value]
+
+    def set_sensor_override(self, sen0=None, sen1_by_pos=None) -> None:
+        if sen0 is None or sen1_by_pos is None:
+            _check(lib().jp_set_sensor_override(self.h, None, None))
+            return
+        s0 = np.ascontiguousarray(sen0, dtype=np.float32)
+        s1 = np.ascontiguousarray(sen1_by_pos, dtype=np.float32)
+        _check(lib().jp_set_sensor_override(self.h, s0.ctypes.data_as(C.POINTER(C.c_float)),
+                                            s1.ctypes.data_as(C.POINTER(C.c_float))))
 
     def macro(self) -> np.ndarray:
         n = self.cfg.n

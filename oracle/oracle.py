@@ -172,3 +172,175 @@ def ref_time(n: int, omega: float, warmup: int, nsteps: int, u0: float = 0.05) -
     ms = C.c_float()
     _rck(ref().ref_uniform_time(n, u0, omega, warmup, nsteps, C.byref(ms)))
     return ms.value
+
+
+# ---- AMR: CPU restatement (liboracle) and the reference's kernels (librefrun) ----------------------
+
+TABLES = {"ref0": 0, "fof0": 1, "rl0": 2, "l1pcb": 3, "l1oct": 4, "f1pos": 5, "l1grid": 6, "ref1": 7, "fof1": 8,
+          "rl1": 9, "l2pl1": 10, "l2oct": 11, "skin0": 12, "skin1": 13, "deep": 14}
+COUNTS = ["nref0", "nf1", "nref1", "nf2", "n_skin0", "n_skin1", "cap1", "cap2", "cnb0", "ng1", "hw_nf1", "hw_nf2",
+          "ndeep", "cap_nref0", "cap_nref1", "steps"]
+MODES = {"all": 0, "slab": 1, "sensor": 2}
+BIG_BUDGET = float(1 << 40)
+
+
+def _amr_sigs(L, prefix):
+    vp = C.c_void_p
+    getattr(L, prefix + "_destroy").argtypes = [vp]
+    getattr(L, prefix + "_set_sensor_override").argtypes = [vp, _F, _F]
+    getattr(L, prefix + "_regrid").argtypes = [vp]
+    getattr(L, prefix + "_step").argtypes = [vp, C.c_long]
+    getattr(L, prefix + "_diag").argtypes = [vp, _D]
+    getattr(L, prefix + "_counts").argtypes = [vp, C.POINTER(C.c_long)]
+    getattr(L, prefix + "_get_table").argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.c_long]
+    getattr(L, prefix + "_get_sensor").argtypes = [vp, C.c_int, _F, C.c_long]
+    getattr(L, prefix + "_get_pops").argtypes = [vp, C.c_int, _F, C.c_long]
+    getattr(L, prefix + "_get_pops").restype = C.c_long
+    getattr(L, prefix + "_set_pops").argtypes = [vp, C.c_int, _F, C.c_long]
+    getattr(L, prefix + "_set_pops").restype = C.c_long
+
+
+_amr_orc_ready = False
+
+
+class AmrBackend:
+    """Common driver of the CPU oracle ('oracle') and of the reference's kernels ('reference')."""
+
+    def __init__(self, which: str, n: int, re: float, l1: str = "all", l2: str = "all", frac1: float = 0.35,
+                 frac2: float = 0.35, u0: float = 0.05, tstar: float = 12.0, develop: int = 300,
+                 budget: float = BIG_BUDGET, mb: int = 8, build: bool = True):
+        global _amr_orc_ready
+        self.which = which
+        self.n, self.mb = n, mb
+        if which == "oracle":
+            L = orc()
+            if not _amr_orc_ready:
+                L.orc_amr_create.restype = C.c_void_p
+                L.orc_amr_create.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                             C.c_double, C.c_double, C.c_int, C.c_double]
+                L.orc_amr_initial_build.argtypes = [C.c_void_p]
+                _amr_sigs(L, "orc_amr")
+                _amr_orc_ready = True
+            self.L, self.p = L, "orc_amr"
+            self.h = L.orc_amr_create(n, mb, re, u0, tstar, MODES[l1], MODES[l2], frac1, frac2, develop, budget)
+        else:
+            L = ref_amr()
+            if mb != 8:
+                raise ValueError("the reference cubin is built with MB=8")
+            self.L, self.p = L, "ref_amr"
+            self.h = L.ref_amr_create(n, re, u0, tstar, MODES[l1], MODES[l2], frac1, frac2, develop, budget)
+        if not self.h:
+            raise RuntimeError("AMR %s create failed" % which)
+        if build:
+            self.initial_build()
+
+    def _f(self, name):
+        return getattr(self.L, self.p + "_" + name)
+
+    def initial_build(self):
+        rc = self._f("initial_build")(C.c_void_p(self.h))
+        if rc:
+            raise RuntimeError("%s initial build failed (%d)" % (self.which, rc))
+
+    def close(self):
+        if self.h:
+            self._f("destroy")(C.c_void_p(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_sensor_override(self, sen0, sen1pos):
+        s0 = np.ascontiguousarray(sen0, dtype=np.float32)
+        s1 = np.ascontiguousarray(sen1pos, dtype=np.float32)
+        self._keep = (s0, s1)
+        self._f("set_sensor_override")(C.c_void_p(self.h), _fp(s0), _fp(s1))
+
+    def regrid(self):
+        rc = self._f("regrid")(C.c_void_p(self.h))
+        if rc:
+            raise RuntimeError("%s regrid failed (%d)" % (self.which, rc))
+
+    def step(self, k: int = 1):
+        rc = self._f("step")(C.c_void_p(self.h), k)
+        if rc:
+            raise RuntimeError("%s step failed (%d)" % (self.which, rc))
+
+    def diag(self):
+        out = np.empty(3)
+        self._f("diag")(C.c_void_p(self.h), _dp(out))
+        return tuple(float(x) for x in out)
+
+    def counts(self) -> dict:
+        v = (C.c_long * 16)()
+        self._f("counts")(C.c_void_p(self.h), v)
+        return dict(zip(COUNTS, list(v)))
+
+    def table(self, name: str) -> np.ndarray:
+        c = self.counts()
+        cap = max(c["ng1"], c["cnb0"], c["cap1"], c["cap2"], 1)
+        a = np.empty(cap, dtype=np.int32)
+        n = self._f("get_table")(C.c_void_p(self.h), TABLES[name], a.ctypes.data_as(C.POINTER(C.c_int)), cap)
+        if n < 0:
+            raise RuntimeError("table %s: %d" % (name, n))
+        return a[:n].copy()
+
+    def sensor(self, level: int) -> np.ndarray:
+        c = self.counts()
+        a = np.empty(max(c["cnb0"], c["cap1"], 1), dtype=np.float32)
+        n = self._f("get_sensor")(C.c_void_p(self.h), level, _fp(a), a.size)
+        return a[:n].copy()
+
+    def pops(self, level: int) -> np.ndarray:
+        c = self.counts()
+        nb = {0: c["cnb0"], 1: c["nf1"], 2: c["nf2"]}[level]
+        a = np.empty(max(nb * Q * self.mb ** 3, 1), dtype=np.float32)
+        n = self._f("get_pops")(C.c_void_p(self.h), level, _fp(a), a.size)
+        if n < 0:
+            raise RuntimeError("pops: %d" % n)
+        return a[:n].copy()
+
+    def set_pops(self, level: int, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        n = self._f("set_pops")(C.c_void_p(self.h), level, _fp(a), a.size)
+        if n < 0:
+            raise RuntimeError("set_pops: %d" % n)
+
+
+_ref_amr_ready = False
+
+
+def ref_amr_available() -> bool:
+    return os.path.exists(REFRUN_LIB) and os.path.exists(REF_AMR_CUBIN)
+
+
+def ref_amr() -> C.CDLL:
+    global _ref_amr_ready
+    L = ref()
+    if not _ref_amr_ready:
+        L.refrun_load_amr.argtypes = [C.c_char_p]
+        rc = L.refrun_load_amr(REF_AMR_CUBIN.encode())
+        if rc:
+            raise RuntimeError("reference AMR cubin load failed: %s" % L.refrun_last_error().decode())
+        L.ref_amr_create.restype = C.c_void_p
+        L.ref_amr_create.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_double,
+                                     C.c_double, C.c_int, C.c_double]
+        L.ref_amr_initial_build.argtypes = [C.c_void_p]
+        L.ref_amr_time.argtypes = [C.c_void_p, C.c_long, C.c_long, _F]
+        _amr_sigs(L, "ref_amr")
+        _ref_amr_ready = True
+    return L
+
+
+def random_sensor_fields(n: int, mb: int = 8, seed: int = 0, ties: bool = False):
+    """Seeded sensor fields for bit-exact table comparisons: one value per coarse block and one per
+    level-1 grid position.  ties=True draws from a few levels so thresholds fall on ties."""
+    rng = np.random.default_rng(seed)
+    cgx = n // mb
+    cnb0, ng1 = cgx ** 3, (2 * cgx) ** 3
+    if ties:
+        return (rng.integers(0, 4, cnb0).astype(np.float32) * 0.25, rng.integers(0, 5, ng1).astype(np.float32) * 0.2)
+    return rng.random(cnb0, dtype=np.float32), rng.random(ng1, dtype=np.float32)

@@ -1,0 +1,90 @@
+"""CPU checks of the AMR oracle (restatement of src/tgv3d_amr.cu): golden fixtures made by the
+reference's own AMR kernels on a GB300 (tests/golden/make_golden.py), and invariants of the block
+tables that hold by construction."""
+import glob
+import os
+
+import numpy as np
+import oracle as O
+import pytest
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TABLES = ["ref0", "fof0", "rl0", "l1pcb", "l1oct", "f1pos", "l1grid", "ref1", "fof1", "rl1", "l2pl1", "l2oct",
+          "skin0", "skin1"]
+
+
+def block_sums(f, mb=8):
+    return f.reshape(-1, O.Q, mb ** 3).astype(np.float64).sum(axis=2)
+
+
+FIXTURES = sorted(glob.glob(os.path.join(GOLD, "amr_*.npz")))
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p) for p in FIXTURES])
+def test_oracle_reproduces_reference_amr(path):
+    g = np.load(path)
+    n = int(g["n"])
+    o = O.AmrBackend("oracle", n, float(g["re"]), str(g["l1"]), str(g["l2"]), float(g["frac1"]), float(g["frac2"]),
+                     develop=int(g["develop"]), budget=1024.0 * 2 ** 30, build=False)
+    o.set_sensor_override(g["sen0"], g["sen1"])
+    o.initial_build()
+    for t in TABLES:                                   # integer tables: bit-exact
+        np.testing.assert_array_equal(o.table(t), g["init_" + t], err_msg="init " + t)
+    for lv in range(3):
+        np.testing.assert_allclose(block_sums(o.pops(lv)), g["init_sums%d" % lv], rtol=1e-6)
+    o.step(1)
+    for lv in range(3):
+        np.testing.assert_allclose(block_sums(o.pops(lv)), g["step1_sums%d" % lv], rtol=1e-5)
+    d = o.diag()
+    np.testing.assert_allclose(d, g["step1_diag"], rtol=1e-9)
+    o.set_sensor_override(g["sen0_b"], g["sen1_b"])
+    o.regrid()
+    for t in TABLES:
+        np.testing.assert_array_equal(o.table(t), g["regrid_" + t], err_msg="regrid " + t)
+    for lv in range(3):
+        np.testing.assert_allclose(block_sums(o.pops(lv)), g["regrid_sums%d" % lv], rtol=1e-5)
+
+
+@pytest.mark.parametrize("l1,l2", [("all", "all"), ("slab", "sensor"), ("sensor", "sensor")])
+def test_table_invariants(l1, l2):
+    n = 32
+    s0, s1 = O.random_sensor_fields(n, seed=5)
+    o = O.AmrBackend("oracle", n, 800.0, l1, l2, 0.4, 0.4, develop=2, build=False)
+    o.set_sensor_override(s0, s1)
+    o.initial_build()
+    c = o.counts()
+    ref0, fof0, rl0 = o.table("ref0"), o.table("fof0"), o.table("rl0")
+    assert c["nref0"] == ref0.sum() and c["nf1"] == 8 * c["nref0"]
+    assert np.all(np.diff(rl0) > 0)                         # rank order = ascending block index
+    np.testing.assert_array_equal(fof0[rl0], 8 * np.arange(c["nref0"]))
+    assert np.all(fof0[ref0 == 0] == -1)
+    pcb, oc, f1pos, grid = o.table("l1pcb"), o.table("l1oct"), o.table("f1pos"), o.table("l1grid")
+    np.testing.assert_array_equal(grid[f1pos], np.arange(c["nf1"]))
+    assert (grid >= 0).sum() == c["nf1"]
+    np.testing.assert_array_equal(pcb, np.repeat(rl0, 8))
+    np.testing.assert_array_equal(oc, np.tile(np.arange(8), c["nref0"]))
+    # 2:1 balance: every refined level-1 block is deep (its six face neighbours exist)
+    ref1, deep = o.table("ref1"), o.table("deep")
+    assert np.all(deep[ref1 == 1] == 1)
+    # skins contain every refined block, ascending
+    for skin, ref in ((o.table("skin0"), ref0), (o.table("skin1"), ref1)):
+        assert np.all(np.diff(skin) > 0)
+        assert set(np.flatnonzero(ref)) <= set(skin)
+    o.close()
+
+
+def test_threshold_is_exact_order_statistic_with_ties():
+    # tgt0 = max(1, int(frac1 * cnb0)); marks use >= so ties over-admit (src/tgv3d_amr.cu:455-457,728)
+    n = 32
+    cnb0 = (n // 8) ** 3
+    s0 = np.zeros(cnb0, dtype=np.float32)
+    s0[:10] = 3.0
+    s0[10:30] = 2.0
+    s1 = np.ones((2 * n // 8) ** 3, dtype=np.float32)
+    o = O.AmrBackend("oracle", n, 800.0, "sensor", "sensor", 0.35, 0.1, develop=0, build=False)
+    o.set_sensor_override(s0, s1)
+    o.initial_build()
+    # int(0.35*64)=22 -> threshold is the 22nd largest = 2.0 -> all 30 blocks >= 2.0 are refined
+    # (the pool holds ceil(0.35*64*1.4)=32 parents, so the over-admission still fits)
+    assert o.counts()["nref0"] == 30
+    o.close()
