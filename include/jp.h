@@ -75,8 +75,14 @@ typedef struct jp_config {
     int32_t device;          /* CUDA device ordinal */
     int32_t threads_per_block; /* 0 = tuned default */
     int32_t vec;             /* cells per thread along x in the uniform step; 0 = tuned default */
-    int32_t reserved[8];
+    int32_t flags;           /* JP_FLAG_* */
+    int32_t reserved[7];
 } jp_config;
+
+/* jp_config.flags */
+#define JP_FLAG_SKIP_PREP 1      /* AMR profiling: skip prep + ghost fill (breaks physics; --skipprep, src/tgv3d_amr.cu:654) */
+#define JP_FLAG_SKIP_RESTRICT 2  /* AMR profiling: skip restriction (breaks physics; --skiprestr, :655) */
+#define JP_FLAG_GRAPH 4          /* replay the step from captured CUDA graphs (--graph, :656) */
 
 /* Derived quantities of a solver (src/tgv3d_uniform.cu:151-153, src/tgv3d_amr.cu:658-664). */
 typedef struct jp_info {
@@ -158,6 +164,16 @@ jp_status jp_set_populations(jp_solver* s, int32_t level, int32_t layout, int32_
 /* Macroscopic field of the current uniform state: `host` receives n^3 float4 (rho, ux, uy, uz) in
  * the linear order (z*n+y)*n+x, as k_macro writes it (src/tgv3d_uniform.cu:80-90). */
 jp_status jp_get_macro(jp_solver* s, float* host, int64_t count);
+
+/* Output fields for VTK frames, computed on the device: Q-criterion -1/2 g_ab g_ba of the central-
+ * difference velocity gradient, speed |u| and (optional, may be NULL) the velocity vector, in the
+ * linear order (z*n+y)*n+x.  Uniform: n = N, as write_vti computes them on the host
+ * (src/tgv3d_uniform.cu:110-121); AMR: n = 4*N0 on the composite field, as k_qspeed
+ * (src/tgv3d_amr.cu:553-564).  `count` = n^3. */
+jp_status jp_get_output_fields(jp_solver* s, float* q, float* speed, float* velocity, int64_t count);
+
+/* Free and total bytes of the solver's device (cudaMemGetInfo). */
+jp_status jp_memory_info(jp_solver* s, int64_t* free_bytes, int64_t* total_bytes);
 
 /* Pinned host memory for asynchronous copies (cudaMallocHost / cudaFreeHost). */
 jp_status jp_host_alloc(void** ptr, size_t bytes);

@@ -224,6 +224,24 @@ jp_status jp_get_macro(jp_solver* s, float* host, int64_t count) {
     return uniform_get_macro(s, host, count);
 }
 
+jp_status jp_get_output_fields(jp_solver* s, float* q, float* speed, float* velocity, int64_t count) {
+    if (!s) return fail(JP_ERR_INVALID, "null solver");
+    cudaSetDevice(s->device);
+    return s->kind == JP_UNIFORM ? uniform_get_output_fields(s, q, speed, velocity, count)
+                                 : amr_get_output_fields(s, q, speed, velocity, count);
+}
+
+jp_status jp_memory_info(jp_solver* s, int64_t* free_bytes, int64_t* total_bytes) {
+    if (!s || !free_bytes || !total_bytes) return fail(JP_ERR_INVALID, "null argument");
+    cudaSetDevice(s->device);
+    size_t f = 0, t = 0;
+    cudaError_t e = cudaMemGetInfo(&f, &t);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
+    *free_bytes = (int64_t)f;
+    *total_bytes = (int64_t)t;
+    return JP_OK;
+}
+
 static jp_status need_amr(const jp_solver* s) {
     if (!s) return fail(JP_ERR_INVALID, "null solver");
     if (s->kind != JP_AMR) return fail(JP_ERR_INVALID, "not an AMR solver");

@@ -54,6 +54,10 @@ constexpr int kDiagThreads = 256;
 cudaError_t launch_diag_field(bool field_is_double, bool float_diff, const void* field, int n,
                               double* partials_dev, double* out_dev, cudaStream_t st);
 
+// Q-criterion, speed and (vel != nullptr) velocity of a macro field of edge n into device arrays.
+cudaError_t launch_qspeed(bool field_is_double, bool float_diff, const void* field, int n, float* Q, float* speed,
+                          float* vel, cudaStream_t st);
+
 // Count of kernel launches issued by this library (for the bench's launch accounting).
 void note_launch(int k = 1);
 long long launch_count();

@@ -38,6 +38,7 @@ struct jp_solver {
     double* diag_dev = nullptr;  // 3 doubles
     double* diag_host = nullptr; // 3 doubles, pinned
     int vec = 0, tpb = 0;
+    float* outbuf = nullptr;   // device Q / speed / velocity for output frames, allocated on first use
 
     jp::AmrState* amr = nullptr;
 };
@@ -52,6 +53,9 @@ jp_status uniform_diag(jp_solver* s, double out[3]);
 jp_status uniform_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count);
 jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype, const void* host, int64_t count);
 jp_status uniform_get_macro(jp_solver* s, float* host, int64_t count);
+jp_status uniform_get_output_fields(jp_solver* s, float* q, float* speed, float* vel, int64_t count);
+jp_status output_fields_from(jp_solver* s, const void* field, bool field_is_double, bool float_diff, int n, float* q,
+                             float* speed, float* vel);
 jp_status common_setup(jp_solver* s);
 
 // AMR (solver_amr.cu)
@@ -68,4 +72,5 @@ jp_status amr_get_counts(jp_solver* s, jp_amr_counts* out);
 jp_status amr_get_table(jp_solver* s, int table, int32_t* host, int64_t capacity, int64_t* count);
 jp_status amr_get_sensor(jp_solver* s, int level, float* host, int64_t capacity, int64_t* count);
 jp_status amr_set_sensor_override(jp_solver* s, const float* sen0, const float* sen1_by_pos);
+jp_status amr_get_output_fields(jp_solver* s, float* q, float* speed, float* vel, int64_t count);
 }  // namespace jp

@@ -42,7 +42,19 @@ struct AmrState {
     int nref0 = 0, nf1 = 0, nref1 = 0, nf2 = 0, n_skin0 = 0, n_skin1 = 0, ndeep = 0;
     float* field = nullptr;
     std::vector<void*> owned;
+    // captured base_step graphs, one per parity of the coarse ping-pong (the fine levels swap an even
+    // number of times per step and return to their buffers); dropped whenever the grid changes
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    float* c0_home = nullptr;
 };
+
+static void drop_graphs(AmrState* a) {
+    for (auto& g : a->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
 
 #define ACK(call, what)                                     \
     do {                                                    \
@@ -328,9 +340,10 @@ static jp_status regrid(jp_solver* s) {
 // level 2 into level 1 after each pair and level 1 into level 0 at the end.
 static jp_status base_step(jp_solver* s) {
     AmrState* a = s->amr;
+    const bool skip_prep = s->cfg.flags & JP_FLAG_SKIP_PREP, skip_restrict = s->cfg.flags & JP_FLAG_SKIP_RESTRICT;
     TRY(step_l0(s));
     if (!a->nf1) return JP_OK;
-    {
+    if (!skip_prep) {
         AmrLaunch L;
         L.nblocks = a->n_skin0;
         L.in = a->c0a;
@@ -350,7 +363,7 @@ static jp_status base_step(jp_solver* s) {
         TRY(launch(s, OP_FILL_L1, F));
     }
     for (int s1 = 0; s1 < 2; ++s1) {
-        if (a->nf2) {
+        if (a->nf2 && !skip_prep) {
             AmrLaunch L;
             L.nblocks = a->n_skin1;
             L.in = a->f1a;
@@ -370,6 +383,8 @@ static jp_status base_step(jp_solver* s) {
             F.l1gx = a->l1gx;
             F.n1 = a->N1;
             TRY(launch(s, OP_FILL_L2, F));
+        }
+        if (a->nf2) {
             for (int s2 = 0; s2 < 2; ++s2) {
                 AmrLaunch S;
                 S.nblocks = a->nf2;
@@ -395,7 +410,7 @@ static jp_status base_step(jp_solver* s) {
             R.list = a->rl1;
             R.t0 = a->fof1;
             R.scale = float(a->nqi21);
-            TRY(launch(s, OP_RESTRICT, R));
+            if (!skip_restrict) TRY(launch(s, OP_RESTRICT, R));
         }
         AmrLaunch S;
         S.nblocks = a->nf1;
@@ -419,7 +434,35 @@ static jp_status base_step(jp_solver* s) {
     R.list = a->rl0;
     R.t0 = a->fof0;
     R.scale = float(a->nqi10);
+    if (skip_restrict) return JP_OK;
     return launch(s, OP_RESTRICT, R);
+}
+
+// base_step replayed from a captured graph (captured on first use for each coarse parity)
+static jp_status graph_step(jp_solver* s) {
+    AmrState* a = s->amr;
+    const int par = a->c0a == a->c0_home ? 0 : 1;
+    if (!a->graph[par]) {
+        float* c0a = a->c0a;
+        float* c0b = a->c0b;
+        ACK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        jp_status st = base_step(s);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+        a->c0a = c0a;  // the capture only recorded the step; the replay below performs it
+        a->c0b = c0b;
+        if (st != JP_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "end capture");
+        e = cudaGraphInstantiate(&a->graph[par], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+    }
+    ACK(cudaGraphLaunch(a->graph[par], s->stream), "graph launch");
+    std::swap(a->c0a, a->c0b);
+    return JP_OK;
 }
 
 // ---- lifecycle -------------------------------------------------------------------------------------
@@ -500,6 +543,7 @@ jp_status amr_create(jp_solver* s) {
 void amr_destroy(jp_solver* s) {
     AmrState* a = s->amr;
     if (!a) return;
+    drop_graphs(a);
     for (void* p : a->owned) cudaFree(p);
     if (a->cnt_host) cudaFreeHost(a->cnt_host);
     if (a->field) cudaFree(a->field);
@@ -510,6 +554,7 @@ void amr_destroy(jp_solver* s) {
 // TGV state on the coarse grid and the initial build (with the sensor override, if one is set)
 jp_status amr_init(jp_solver* s) {
     AmrState* a = s->amr;
+    drop_graphs(a);
     AmrLaunch L;
     L.nblocks = a->cnb0;
     L.out = a->c0a;
@@ -520,6 +565,7 @@ jp_status amr_init(jp_solver* s) {
     a->hw_nf1 = a->hw_nf2 = 0;
     TRY(initial_build(s));
     ACK(cudaStreamSynchronize(s->stream), "initial build");
+    a->c0_home = a->c0a;
     s->step_count = 0;
     s->info.bytes_state = (int64_t)(((size_t)2 * a->cnb0 + 2 * (size_t)a->cap1 + 2 * (size_t)a->cap2) * Q * a->MB3 * 4 +
                                     ((size_t)a->cap1 + a->cap2) * Q * a->SH * 4);
@@ -527,20 +573,22 @@ jp_status amr_init(jp_solver* s) {
 }
 
 jp_status amr_step(jp_solver* s, int64_t nsteps) {
+    const bool graph = s->cfg.flags & JP_FLAG_GRAPH;
     for (int64_t i = 0; i < nsteps; ++i) {
-        TRY(base_step(s));
+        TRY(graph ? graph_step(s) : base_step(s));
         ++s->step_count;
     }
     return JP_OK;
 }
 
 jp_status amr_regrid(jp_solver* s) {
+    drop_graphs(s->amr);
     TRY(regrid(s));
     ACK(cudaStreamSynchronize(s->stream), "regrid");
     return JP_OK;
 }
 
-jp_status amr_diag(jp_solver* s, double out[3]) {
+static jp_status composite(jp_solver* s) {
     AmrState* a = s->amr;
     if (!a->field) ACK(cudaMalloc(&a->field, sizeof(float) * 4 * (size_t)a->N2 * a->N2 * a->N2), "cudaMalloc composite");
     AmrLaunch L;
@@ -554,7 +602,19 @@ jp_status amr_diag(jp_solver* s, double out[3]) {
     L.cgx = a->cgx;
     L.l1gx = a->l1gx;
     L.n2 = a->N2;
-    TRY(launch(s, OP_COMPOSITE, L));
+    return launch(s, OP_COMPOSITE, L);
+}
+
+jp_status amr_get_output_fields(jp_solver* s, float* q, float* speed, float* vel, int64_t count) {
+    AmrState* a = s->amr;
+    if (count != (int64_t)a->N2 * a->N2 * a->N2) return fail(JP_ERR_INVALID, "count %lld != (4 N0)^3", (long long)count);
+    TRY(composite(s));
+    return output_fields_from(s, a->field, false, false, a->N2, q, speed, vel);
+}
+
+jp_status amr_diag(jp_solver* s, double out[3]) {
+    AmrState* a = s->amr;
+    TRY(composite(s));
     ACK(launch_diag_field(false, false, a->field, a->N2, s->partials, s->diag_dev, s->stream), "diag");
     ACK(cudaMemcpyAsync(s->diag_host, s->diag_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "diag D2H");
     ACK(cudaStreamSynchronize(s->stream), "diag");

@@ -93,6 +93,8 @@ void uniform_free(jp_solver* s) {
     if (s->partials) cudaFree(s->partials);
     if (s->diag_dev) cudaFree(s->diag_dev);
     if (s->diag_host) cudaFreeHost(s->diag_host);
+    if (s->outbuf) cudaFree(s->outbuf);
+    s->outbuf = nullptr;
     s->fa = s->fb = s->field = nullptr;
     s->partials = s->diag_dev = s->diag_host = nullptr;
 }
@@ -206,6 +208,31 @@ jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype
     JP_CK(cudaMemcpyAsync(s->fa, raw.data(), bytes, cudaMemcpyHostToDevice, s->stream), "populations H2D");
     JP_CK(cudaStreamSynchronize(s->stream), "populations H2D");
     return JP_OK;
+}
+
+// Q / speed / velocity of a device macro field of edge n, copied to host arrays of n^3 (vel: 3 n^3).
+jp_status output_fields_from(jp_solver* s, const void* field, bool field_is_double, bool float_diff, int n, float* q,
+                             float* speed, float* vel) {
+    const size_t cells = (size_t)n * n * n;
+    if (!s->outbuf) JP_CK(cudaMalloc(&s->outbuf, sizeof(float) * 5 * cells), "cudaMalloc output fields");
+    float* dq = s->outbuf;
+    float* ds = dq + cells;
+    float* dv = ds + cells;
+    JP_CK(launch_qspeed(field_is_double, float_diff, field, n, dq, ds, vel ? dv : nullptr, s->stream), "qspeed");
+    if (q) JP_CK(cudaMemcpyAsync(q, dq, sizeof(float) * cells, cudaMemcpyDeviceToHost, s->stream), "Q D2H");
+    if (speed) JP_CK(cudaMemcpyAsync(speed, ds, sizeof(float) * cells, cudaMemcpyDeviceToHost, s->stream), "speed D2H");
+    if (vel) JP_CK(cudaMemcpyAsync(vel, dv, sizeof(float) * 3 * cells, cudaMemcpyDeviceToHost, s->stream), "vel D2H");
+    JP_CK(cudaStreamSynchronize(s->stream), "output fields");
+    return JP_OK;
+}
+
+jp_status uniform_get_output_fields(jp_solver* s, float* q, float* speed, float* vel, int64_t count) {
+    if (count != (int64_t)s->cells) return fail(JP_ERR_INVALID, "count %lld != n^3", (long long)count);
+    jp_status st = ensure_field(s);
+    if (st != JP_OK) return st;
+    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream), "macro");
+    const bool dbl = s->storage == JP_FP64;
+    return output_fields_from(s, s->field, dbl, !dbl, s->n, q, speed, vel);
 }
 
 jp_status uniform_get_macro(jp_solver* s, float* host, int64_t count) {

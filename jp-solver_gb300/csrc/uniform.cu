@@ -424,6 +424,58 @@ __global__ void __launch_bounds__(256) k_diag_finish(const double* __restrict__ 
     }
 }
 
+// ---- output fields: Q-criterion, speed, velocity ---------------------------------------------------
+// Q = -1/2 sum_ab g_ab g_ba of the central-difference gradient g_cd = d u_c / d x_d (periodic), in FP64;
+// FLOAT_DIFF takes each difference in the field's float first, as the uniform reference's host writer
+// (src/tgv3d_uniform.cu:98-121); otherwise in double, as k_qspeed (src/tgv3d_amr.cu:553-564).
+template <class FT, bool FLOAT_DIFF>
+__global__ void __launch_bounds__(256) k_qspeed(const FT* __restrict__ F, int n, float* __restrict__ Qo,
+                                               float* __restrict__ spd, float* __restrict__ vel) {
+    const long long cells = (long long)n * n * n;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
+    const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
+    const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
+    const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
+    auto at = [&](int a, int b, int cc, int comp) -> FT { return F[(((size_t)cc * n + b) * n + a) * 4 + 1 + comp]; };
+    auto dif = [&](FT a, FT b) -> double {
+        if (FLOAT_DIFF) return double(FT(a - b)) * 0.5;
+        return (double(a) - double(b)) * 0.5;
+    };
+    const double u = double(F[c * 4 + 1]), v = double(F[c * 4 + 2]), w = double(F[c * 4 + 3]);
+    spd[c] = float(sqrt(u * u + v * v + w * w));
+    if (vel) {
+        vel[c * 3 + 0] = float(u);
+        vel[c * 3 + 1] = float(v);
+        vel[c * 3 + 2] = float(w);
+    }
+    double g[3][3];
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+        g[cc][0] = dif(at(ip, j, k, cc), at(im, j, k, cc));
+        g[cc][1] = dif(at(i, jp, k, cc), at(i, jm, k, cc));
+        g[cc][2] = dif(at(i, j, kp, cc), at(i, j, km, cc));
+    }
+    double Q = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) Q -= 0.5 * g[a][b] * g[b][a];
+    Qo[c] = float(Q);
+}
+
+cudaError_t launch_qspeed(bool field_is_double, bool float_diff, const void* field, int n, float* Q, float* speed,
+                          float* vel, cudaStream_t st) {
+    const long long cells = (long long)n * n * n;
+    const unsigned blocks = (unsigned)((cells + 255) / 256);
+    if (field_is_double) k_qspeed<double, false><<<blocks, 256, 0, st>>>((const double*)field, n, Q, speed, vel);
+    else if (float_diff) k_qspeed<float, true><<<blocks, 256, 0, st>>>((const float*)field, n, Q, speed, vel);
+    else k_qspeed<float, false><<<blocks, 256, 0, st>>>((const float*)field, n, Q, speed, vel);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_diag_field(bool field_is_double, bool float_diff, const void* field, int n,
                               double* partials_dev, double* out_dev, cudaStream_t st) {
     const long long cells = (long long)n * n * n;

