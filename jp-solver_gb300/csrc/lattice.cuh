@@ -70,6 +70,11 @@ struct StF16 {
     static constexpr int id = 1;
     __device__ static __forceinline__ float load(raw v) { return __half2float(__ushort_as_half(v)); }
     __device__ static __forceinline__ raw store(float v) { return __half_as_ushort(__float2half_rn(v)); }
+    // two values rounded and packed in one conversion (a in the low half)
+    __device__ static __forceinline__ unsigned int store2(float a, float b) {
+        const __half2 h = __floats2half2_rn(a, b);
+        return *reinterpret_cast<const unsigned int*>(&h);
+    }
 };
 struct StBF16 {
     using raw = uint16_t;
@@ -78,6 +83,10 @@ struct StBF16 {
     static constexpr int id = 2;
     __device__ static __forceinline__ float load(raw v) { return __bfloat162float(__ushort_as_bfloat16(v)); }
     __device__ static __forceinline__ raw store(float v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
+    __device__ static __forceinline__ unsigned int store2(float a, float b) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        return *reinterpret_cast<const unsigned int*>(&h);
+    }
 };
 struct StF64 {
     using raw = double;

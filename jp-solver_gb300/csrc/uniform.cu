@@ -31,6 +31,7 @@ struct Pack {
     union {
         word w;
         RAW v[V];
+        unsigned int u32[(bytes + 3) / 4];
     };
 };
 
@@ -117,54 +118,68 @@ __global__ void __launch_bounds__(TPB) k_stream_collide(const __grid_constant__ 
             if (!next_direct) E[q] = t;
         }
     }
-    // value of population q pulled into cell x0+v
-    auto val = [&](int q, int v) -> R {
-        raw e;
-        if (cx(q) > 0) e = (v == 0) ? E[q] : L[q].v[v - 1];
-        else if (cx(q) < 0) e = (v == V - 1) ? E[q] : L[q].v[v + 1];
-        else e = L[q].v[v];
-        return ST::load(e);
-    };
+    // 3. the pulled values of every cell, converted to the collision type once
+    R f[V][Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            raw e;
+            if (cx(q) > 0) e = (v == 0) ? E[q] : L[q].v[v - 1];
+            else if (cx(q) < 0) e = (v == V - 1) ? E[q] : L[q].v[v + 1];
+            else e = L[q].v[v];
+            f[v][q] = ST::load(e);
+        }
 
-    // 3. moments per cell
+    // 4. moments per cell (one reciprocal of rho instead of three divisions)
     R rho[V], ux[V], uy[V], uz[V], s[V], usq[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-        R f[Q];
+        const R* g = f[v];
+        R sm = g[0];
 #pragma unroll
-        for (int q = 0; q < Q; ++q) f[q] = val(q, v);
-        R sm = f[0];
-#pragma unroll
-        for (int q = 1; q < Q; ++q) sm += f[q];
-        const R jx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
-        const R jy = f[3] - f[4] + f[7] - f[8] - f[9] + f[10] + f[15] - f[16] + f[17] - f[18];
-        const R jz = f[5] - f[6] + f[11] - f[12] - f[13] + f[14] + f[15] - f[16] - f[17] + f[18];
+        for (int q = 1; q < Q; ++q) sm += g[q];
+        const R jx = g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14];
+        const R jy = g[3] - g[4] + g[7] - g[8] - g[9] + g[10] + g[15] - g[16] + g[17] - g[18];
+        const R jz = g[5] - g[6] + g[11] - g[12] - g[13] + g[14] + g[15] - g[16] - g[17] + g[18];
         const R rh = SH ? R(1) + sm : sm;
+        const R inv = R(1) / rh;
         s[v] = sm;
         rho[v] = rh;
-        ux[v] = jx / rh;
-        uy[v] = jy / rh;
-        uz[v] = jz / rh;
+        ux[v] = jx * inv;
+        uy[v] = jy * inv;
+        uz[v] = jz * inv;
         usq[v] = R(1.5) * (ux[v] * ux[v] + uy[v] * uy[v] + uz[v] * uz[v]);
     }
 
-    // 4. relax and store, one population pair at a time
+    // 5. relax and store, one population pair at a time; 16-bit formats convert two cells per
+    //    instruction
     const R om = sizeof(R) == 8 ? R(d.omega_d) : R(d.omega);
     const size_t orow = ((size_t)z * n + y) * n + x0;
+    auto put = [&](Pack<raw, V>& p, const R (&o)[V]) {
+        if constexpr (SH && V % 2 == 0) {
+#pragma unroll
+            for (int v = 0; v < V; v += 2) p.u32[v / 2] = ST::store2(o[v], o[v + 1]);
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) p.v[v] = ST::store(o[v]);
+        }
+    };
     {
-        Pack<raw, V> o;
+        R o[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) {
             const R w0 = wgt<R>(0);
             const R feq = SH ? w0 * (s[v] - rho[v] * usq[v]) : w0 * rho[v] * (R(1) - usq[v]);
-            const R f = val(0, v);
-            o.v[v] = ST::store(f - om * (f - feq));
+            o[v] = f[v][0] - om * (f[v][0] - feq);
         }
-        st_pack<raw, V>(dst + orow, o);
+        Pack<raw, V> p;
+        put(p, o);
+        st_pack<raw, V>(dst + orow, p);
     }
 #pragma unroll
     for (int q = 1; q < Q; q += 2) {
-        Pack<raw, V> op, om_;
+        R oa[V], ob[V];
         const R w = wgt<R>(q);
 #pragma unroll
         for (int v = 0; v < V; ++v) {
@@ -173,12 +188,15 @@ __global__ void __launch_bounds__(TPB) k_stream_collide(const __grid_constant__ 
             const R sym = SH ? w * s[v] + wr * (R(0.5) * cu * cu - usq[v])
                              : wr * (R(1) + R(0.5) * cu * cu - usq[v]);
             const R asym = wr * cu;
-            const R fa = val(q, v), fb = val(q + 1, v);
-            op.v[v] = ST::store(fa - om * (fa - (sym + asym)));
-            om_.v[v] = ST::store(fb - om * (fb - (sym - asym)));
+            const R fa = f[v][q], fb = f[v][q + 1];
+            oa[v] = fa - om * (fa - (sym + asym));
+            ob[v] = fb - om * (fb - (sym - asym));
         }
-        st_pack<raw, V>(dst + q * qs + orow, op);
-        st_pack<raw, V>(dst + (q + 1) * qs + orow, om_);
+        Pack<raw, V> pa, pb;
+        put(pa, oa);
+        put(pb, ob);
+        st_pack<raw, V>(dst + q * qs + orow, pa);
+        st_pack<raw, V>(dst + (q + 1) * qs + orow, pb);
     }
 }
 
