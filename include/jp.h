@@ -175,6 +175,20 @@ jp_status jp_get_output_fields(jp_solver* s, float* q, float* speed, float* velo
 /* Free and total bytes of the solver's device (cudaMemGetInfo). */
 jp_status jp_memory_info(jp_solver* s, int64_t* free_bytes, int64_t* total_bytes);
 
+/* Diagnostics of a caller-owned macro field with no device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc when they need the numbers (a host
+ * framework that owns all device memory through its own pool, a loop that must not allocate after
+ * start-up, work recorded into a CUDA graph).  `field_dev` holds n^3 float4 (rho, ux, uy, uz) in the
+ * order of jp_get_macro; `out_dev` receives 3 doubles (mean E, mean enstrophy, mean rho), written on
+ * `stream` (a cudaStream_t; NULL = default stream) without host synchronisation.  float_diff = 1 takes
+ * velocity differences in float (the uniform solver's jp_diag), 0 in double (the AMR composite).
+ * Scratch lives in a fixed 384 KiB device array inside the library, so fields above 268,435,456 cells
+ * (n > 645) are rejected with JP_ERR_CAPACITY.  The first call on each device looks up that array's
+ * address and should come before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller. */
+jp_status jp_diag_field_noalloc(const float* field_dev, int32_t n, int32_t float_diff, double* out_dev,
+                                void* stream);
+
 /* Pinned host memory for asynchronous copies (cudaMallocHost / cudaFreeHost). */
 jp_status jp_host_alloc(void** ptr, size_t bytes);
 void jp_host_free(void* ptr);

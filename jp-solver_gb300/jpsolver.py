@@ -98,6 +98,7 @@ SIGNATURES = {
     "jp_get_output_fields": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                        C.c_int64]),
     "jp_memory_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "jp_diag_field_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "jp_amr_get_counts": (C.c_int, [C.c_void_p, C.POINTER(AmrCounts)]),
     "jp_get_table": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int64)]),
     "jp_get_sensor": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_int64)]),
