@@ -73,7 +73,7 @@ jp_status uniform_create(jp_solver* s) {
     s->elem = storage_bytes(c.storage);
     s->vec = pick_vec(c.storage, c.n, c.vec);
     if (!s->vec) return fail(JP_ERR_INVALID, "no vector width fits n=%d (requested vec=%d)", c.n, c.vec);
-    s->tpb = c.threads_per_block ? c.threads_per_block : 256;
+    s->tpb = c.threads_per_block ? c.threads_per_block : 128;
     if (s->tpb != 64 && s->tpb != 128 && s->tpb != 256 && s->tpb != 512)
         return fail(JP_ERR_INVALID, "threads_per_block must be 64, 128, 256 or 512");
     const size_t bytes = (size_t)Q * s->cells * s->elem;

@@ -62,8 +62,17 @@ template <> __device__ __forceinline__ uint16_t shfl_dn1<uint16_t>(uint16_t v) {
 
 // ---- stream-collide ---------------------------------------------------------------------------
 
+// Occupancy floor per SM for a variant: the wide-vector variants need warps (to keep 19 vector
+// loads per thread in flight, and for the issue-bound 16-bit collision) more than registers:
+// FP32 V=4 and 16-bit V=4 to 128 registers, 16-bit V=8 to 168.
 template <class ST, int V, int TPB>
-__global__ void __launch_bounds__(TPB) k_stream_collide(const __grid_constant__ UniBatch b) {
+constexpr int min_blocks() {
+    return (sizeof(typename ST::raw) * V == 16 && sizeof(typename ST::raw) == 2) ? (384 / TPB > 0 ? 384 / TPB : 1)
+         : (sizeof(typename ST::raw) * V >= 8 && sizeof(typename ST::raw) <= 4) ? (512 / TPB > 0 ? 512 / TPB : 1) : 1;
+}
+
+template <class ST, int V, int TPB>
+__global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_collide(const __grid_constant__ UniBatch b) {
     using raw = typename ST::raw;
     using R = typename ST::real;
     constexpr bool SH = ST::shifted;
@@ -153,8 +162,10 @@ __global__ void __launch_bounds__(TPB) k_stream_collide(const __grid_constant__ 
     }
 
     // 5. relax and store, one population pair at a time; 16-bit formats convert two cells per
-    //    instruction
+    //    instruction.  BGK as out = (1 - omega) f + omega feq with omega*w*rho folded per weight
+    //    class: with a = c.u, feq_pm = w rho (1 - 1.5|u|^2 + 4.5 a^2) +- 3 w rho a.
     const R om = sizeof(R) == 8 ? R(d.omega_d) : R(d.omega);
+    const R omc = R(1) - om;
     const size_t orow = ((size_t)z * n + y) * n + x0;
     auto put = [&](Pack<raw, V>& p, const R (&o)[V]) {
         if constexpr (SH && V % 2 == 0) {
@@ -165,13 +176,24 @@ __global__ void __launch_bounds__(TPB) k_stream_collide(const __grid_constant__ 
             for (int v = 0; v < V; ++v) p.v[v] = ST::store(o[v]);
         }
     };
+    // per cell: omega*w*rho and (shifted) omega*w*s for the face (1/18) and edge (1/36) classes, and
+    // the base term 1 - 1.5|u|^2 (or -1.5|u|^2 shifted)
+    R owr1[V], owr2[V], owr3a[V], owr3b[V], ows1[V], ows2[V], base[V];
     {
         R o[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) {
             const R w0 = wgt<R>(0);
             const R feq = SH ? w0 * (s[v] - rho[v] * usq[v]) : w0 * rho[v] * (R(1) - usq[v]);
-            o[v] = f[v][0] - om * (f[v][0] - feq);
+            o[v] = omc * f[v][0] + om * feq;
+            const R orho = om * rho[v];
+            owr1[v] = orho * wgt<R>(1);
+            owr2[v] = orho * wgt<R>(7);
+            owr3a[v] = R(3) * owr1[v];
+            owr3b[v] = R(3) * owr2[v];
+            ows1[v] = SH ? om * wgt<R>(1) * s[v] : R(0);
+            ows2[v] = SH ? om * wgt<R>(7) * s[v] : R(0);
+            base[v] = SH ? -usq[v] : R(1) - usq[v];
         }
         Pack<raw, V> p;
         put(p, o);
@@ -180,17 +202,15 @@ __global__ void __launch_bounds__(TPB) k_stream_collide(const __grid_constant__ 
 #pragma unroll
     for (int q = 1; q < Q; q += 2) {
         R oa[V], ob[V];
-        const R w = wgt<R>(q);
 #pragma unroll
         for (int v = 0; v < V; ++v) {
-            const R cu = R(3) * (R(cx(q)) * ux[v] + R(cy(q)) * uy[v] + R(cz(q)) * uz[v]);
-            const R wr = w * rho[v];
-            const R sym = SH ? w * s[v] + wr * (R(0.5) * cu * cu - usq[v])
-                             : wr * (R(1) + R(0.5) * cu * cu - usq[v]);
-            const R asym = wr * cu;
-            const R fa = f[v][q], fb = f[v][q + 1];
-            oa[v] = fa - om * (fa - (sym + asym));
-            ob[v] = fb - om * (fb - (sym - asym));
+            const R a = cdot<R>(q, ux[v], uy[v], uz[v]);
+            const R owr = q < 7 ? owr1[v] : owr2[v];
+            const R t = owr * (R(4.5) * a * a + base[v]);
+            const R osym = SH ? (q < 7 ? ows1[v] : ows2[v]) + t : t;  // omega * symmetric part
+            const R oasym = (q < 7 ? owr3a[v] : owr3b[v]) * a;           // omega * antisymmetric part
+            oa[v] = omc * f[v][q] + (osym + oasym);
+            ob[v] = omc * f[v][q + 1] + (osym - oasym);
         }
         Pack<raw, V> pa, pb;
         put(pa, oa);
@@ -203,8 +223,8 @@ __global__ void __launch_bounds__(TPB) k_stream_collide(const __grid_constant__ 
 int default_vec(int storage) {
     switch (storage) {
         case 0: return 4;   // float4
-        case 1: return 8;   // 8 x half
-        case 2: return 8;   // 8 x bf16
+        case 1: return 4;   // 4 x half
+        case 2: return 4;   // 4 x bf16
         case 3: return 2;   // double2
     }
     return 0;
