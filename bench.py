@@ -134,8 +134,9 @@ def load_traffic(key: str):
     return d.get(key)
 
 
-def bench_storage(J, n: int, storage: str, steps: int, warmup: int, device: int, pg, sampler=None) -> dict:
-    s = J.Solver("uniform", n=n, re=RE, u0=U0, storage=storage, device=device)
+def bench_storage(J, n: int, storage: str, steps: int, warmup: int, device: int, pg, sampler=None, vec: int = 0,
+                  tpb: int = 0) -> dict:
+    s = J.Solver("uniform", n=n, re=RE, u0=U0, storage=storage, device=device, vec=vec, threads_per_block=tpb)
     try:
         s.step(warmup)
         s.sync()
@@ -193,6 +194,74 @@ def bench_e2e(J, n: int, calls: int, k: int, device: int, pg) -> dict:
     return {"seconds": dt, "glups": n ** 3 * k * calls / dt / 1e9, "h2d_bytes": cnt * 4, "d2h_bytes": 24}
 
 
+def c5_requests(J, n_req: int, rate: float, seed: int) -> list:
+    """The served-ensemble workload: Poisson(rate) arrivals from a seed; each request a uniform solve
+    with N in {32,48,64,96,128} or an AMR solve with coarse N in {16,24,32,48} (sensor refinement on
+    both levels, frac1 0.3, frac2 0.1, regrid every 20 coarse steps, graph replay); Re log-uniform in
+    [200, 3200]; t* uniform in [2, 10]; FP32 or FP16 storage 50/50 (AMR solves store FP32)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    out = []
+    for i in range(n_req):
+        amr = bool(rng.random() < 0.5)
+        n = int(rng.choice([16, 24, 32, 48] if amr else [32, 48, 64, 96, 128]))
+        re = float(np.exp(rng.uniform(np.log(200.0), np.log(3200.0))))
+        ts = float(rng.uniform(2.0, 10.0))
+        half = bool(rng.random() < 0.5)
+        r = dict(rid=i, kind="amr" if amr else "uniform", n=n, re=re, tstar=ts)
+        if amr:
+            r.update(l1_mode="sensor", l2_mode="sensor", frac1=0.3, frac2=0.1, adapt_every=20, flags=J.FLAG_GRAPH)
+        else:
+            r.update(storage="fp16" if half else "fp32")
+        out.append((float(t[i]), r))
+    return out
+
+
+def serve_run(J, reqs: list, device: int, open_loop: bool, max_active: int = 0, tick: int = 64) -> dict:
+    """Drive the server: open loop submits each request at its arrival time, closed loop submits all
+    at once.  Returns throughput and latency percentiles (submit to result)."""
+    import numpy as np
+
+    sv = J.Server(device=device, pool_gb=120.0, max_active=max_active, tick_steps=tick)
+    t0 = time.perf_counter()
+    i, res = 0, {}
+    if not open_loop:
+        for _, r in reqs:
+            sv.submit(**r)
+        i = len(reqs)
+    while len(res) < len(reqs):
+        now = time.perf_counter() - t0
+        while i < len(reqs) and reqs[i][0] <= now:
+            sv.submit(**reqs[i][1])
+            i += 1
+        a, q = sv.tick()
+        for r in sv.poll(1024):
+            res[r["id"]] = r
+        if a == 0 and q == 0 and i < len(reqs):
+            time.sleep(min(0.002, max(0.0, reqs[i][0] - (time.perf_counter() - t0))))
+    span = time.perf_counter() - t0
+    sv.close()
+    lat = np.array([r["t_end"] - r["t_submit"] for r in res.values()])
+    ok = sum(1 for r in res.values() if r["status"] == 0)
+    return {"solves": len(res), "ok": ok, "seconds": span, "solves_per_s": len(res) / span,
+            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "valid": sum(1 for r in res.values() if r["valid"])}
+
+
+def bench_serve(J, args, device: int) -> dict:
+    reqs = c5_requests(J, args.requests, args.rate, args.seed)
+    open_r = serve_run(J, reqs, device, open_loop=True)
+    m = min(args.compare, len(reqs))
+    sample = reqs[:m]
+    batched = serve_run(J, sample, device, open_loop=False)
+    single = serve_run(J, sample, device, open_loop=False, max_active=1)
+    return {"open_loop": open_r, "closed_loop": {"sample": m, "batched_solves_per_s": batched["solves_per_s"],
+                                                 "one_at_a_time_solves_per_s": single["solves_per_s"],
+                                                 "speedup": batched["solves_per_s"] / single["solves_per_s"]}}
+
+
 def cpu_baseline(n: int, steps: int) -> dict:
     """The oracle (CPU restatement of the reference's step, OpenMP) on this host's cores."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -221,14 +290,23 @@ def main() -> int:
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--no-variants", action="store_true", help="skip the FP16/BF16 lines")
     ap.add_argument("--e2e-calls", type=int, default=4)
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=3, help="0 skips the CPU baseline")
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16", "bf16", "fp64"],
+                    help="storage of the timed run (the headline is fp32)")
+    ap.add_argument("--vec", type=int, default=0)
+    ap.add_argument("--tpb", type=int, default=0)
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "serve"])
+    ap.add_argument("--requests", type=int, default=2000)
+    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--compare", type=int, default=200, help="requests in the batched vs one-at-a-time comparison")
     a = ap.parse_args()
     if a.warmup < 3:
         a.warmup = 3
     rank, local, world, pg = dist_setup(a.gpus)
     n = a.n
     config = {"workload": "uniform TGV D3Q19 BGK, N=%d, Re=%g, u0=%g, periodic" % (n, RE, U0),
-              "n": n, "re": RE, "storage": "fp32", "cells": n ** 3,
+              "n": n, "re": RE, "storage": a.storage, "cells": n ** 3,
               "l2": "inputs larger than L2 (%.1f GB of populations per step)" % (2 * Q * 4 * n ** 3 / 1e9),
               "parallelism": "replicas x%d" % world}
 
@@ -248,9 +326,23 @@ def main() -> int:
 
     import jpsolver as J
 
+    if a.workload == "serve":
+        sv = bench_serve(J, a, local)
+        o = sv["open_loop"]
+        line = {"metric": "ensemble solves/s", "value": o["solves_per_s"], "unit": "solves/s", "n_gpus": world,
+                "steps": o["solves"], "warmup": 0, "ms_per_step": 1e3 / o["solves_per_s"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded Poisson requests of Taylor-Green solves)",
+                "config": {"workload": "served TGV ensemble: %d requests, Poisson %.0f/s, seed %d, 120 GB pool"
+                                       % (a.requests, a.rate, a.seed)},
+                "serving": sv, "p50_latency_s": o["p50_s"], "p99_latency_s": o["p99_s"]}
+        if rank == 0:
+            print(json.dumps(line))
+        return 0
+
     peaks = load_peaks()
     sampler = ClockSampler(local)
-    main_r = bench_storage(J, n, "fp32", a.steps, a.warmup, local, pg, sampler)
+    main_r = bench_storage(J, n, a.storage, a.steps, a.warmup, local, pg, sampler, a.vec, a.tpb)
     variants = {}
     if not a.no_variants:
         for st in ("fp16", "bf16"):
@@ -260,27 +352,27 @@ def main() -> int:
                             "achieved_gbs": r["achieved_gbs"], "frac": r["achieved_gbs"] / peaks["hbm_gbs"],
                             "speedup_vs_fp32": r["glups"] / main_r["glups"]}
     k = max(1, int(O_diag_every(n)))
-    e2e = bench_e2e(J, n, a.e2e_calls, k, local, pg)
-    traffic = load_traffic("stream_collide_fp32")
+    e2e = bench_e2e(J, n, a.e2e_calls, k, local, pg) if a.e2e_calls > 0 else None
+    traffic = load_traffic("stream_collide_" + a.storage)
     value = main_r["glups"] * world
     line = {
         "metric": "GLUPS", "value": value, "unit": "GLUPS", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": main_r["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (analytic Taylor-Green initial state)", "config": config,
-        "roofline": {"bound": "hbm", "kernel": "k_stream_collide<fp32>", "achieved": main_r["achieved_gbs"],
+        "roofline": {"bound": "hbm", "kernel": "k_stream_collide<%s>" % a.storage, "achieved": main_r["achieved_gbs"],
                      "peak": peaks["hbm_gbs"], "peak_source": peaks["source"], "unit": "GB/s",
                      "frac": main_r["achieved_gbs"] / peaks["hbm_gbs"],
-                     "bytes_per_update": BYTES_PER_UPDATE["fp32"],
+                     "bytes_per_update": BYTES_PER_UPDATE[a.storage],
                      "traffic": (traffic * n ** 3) if traffic else None},
         "variants": variants,
-        "e2e": {"value": e2e["glups"] * world, "unit": "GLUPS", "h2d_bytes_per_step": e2e["h2d_bytes"],
-                "d2h_bytes_per_step": e2e["d2h_bytes"], "lattice_steps_per_call": k,
-                "calls": a.e2e_calls},
+        "e2e": ({"value": e2e["glups"] * world, "unit": "GLUPS", "h2d_bytes_per_step": e2e["h2d_bytes"],
+                 "d2h_bytes_per_step": e2e["d2h_bytes"], "lattice_steps_per_call": k,
+                 "calls": a.e2e_calls} if e2e else None),
         "gpu_launches": main_r["launches"],
         "clocks": main_r["clocks"],
     }
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and a.cpu_steps > 0:
         line["cpu_baseline"] = cpu_baseline(n, a.cpu_steps)
     if rank == 0:
         print(json.dumps(line))

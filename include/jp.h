@@ -119,8 +119,9 @@ const char* jp_last_error(void);
 int32_t jp_abi_version(void);
 const char* jp_build_info(void);
 
-/* sizeof(jp_config) for which=0, sizeof(jp_info) for which=1, else 0: lets an FFI binding check
- * its struct mirrors against the library it loaded. */
+/* sizeof of the ABI structs: 0 jp_config, 1 jp_info, 2 jp_amr_counts, 3 jp_server_config,
+ * 4 jp_request, 5 jp_result; else 0.  Lets an FFI binding check its struct mirrors against the
+ * library it loaded. */
 size_t jp_sizeof(int32_t which);
 
 /* Derived quantities (nu, tau, steps...). */
@@ -242,6 +243,59 @@ jp_status jp_get_sensor(jp_solver* s, int32_t level, float* host, int64_t capaci
  * ((2N/MB)^3 values, so a level-1 block takes the value of its position).  NULL, NULL clears.  Feeds
  * two implementations the same sensor field for bit-exact table comparisons. */
 jp_status jp_set_sensor_override(jp_solver* s, const float* sen0, const float* sen1_by_pos);
+
+/* ---- ensembles and serving (spec extensions; no counterpart in the reference) ------------- */
+
+/* An ensemble steps many uniform solvers of the same device together: every lattice step is one
+ * batched stream-collide launch per storage format (up to 48 cubes of any sizes per launch) on the
+ * ensemble's stream, ordered after each member's pending work and before its later work. */
+typedef struct jp_ensemble jp_ensemble;
+jp_status jp_ensemble_create(int32_t device, jp_ensemble** out);
+void jp_ensemble_destroy(jp_ensemble* e);
+jp_status jp_ensemble_add(jp_ensemble* e, jp_solver* s);     /* uniform solvers only */
+jp_status jp_ensemble_remove(jp_ensemble* e, jp_solver* s);
+jp_status jp_ensemble_step(jp_ensemble* e, int64_t nsteps);
+
+/* A server runs whole Taylor-Green solves (the `uniform` / `amr` programs' runs) for a stream of
+ * requests with continuous batching: requests wait in a queue until their HBM estimate fits the
+ * pool budget and a slot is free, are admitted between ticks while others run, advance together
+ * (uniform solves in batched launches, AMR solves concurrently on their own streams), and leave a
+ * result with their diagnostics summary and timestamps when they finish. */
+typedef struct jp_server jp_server;
+typedef struct jp_server_config {
+    int32_t device;
+    int32_t max_active;      /* slots; 0 = unlimited */
+    double pool_gb;          /* HBM budget for admitted solves, GiB (0 = 75% of free memory) */
+    int32_t tick_steps;      /* lattice steps a uniform solve advances per tick (AMR: coarse steps / 4) */
+    int32_t reserved[7];
+} jp_server_config;
+typedef struct jp_request {
+    int64_t id;
+    jp_config cfg;           /* kind, n, re, tstar, storage, refinement... as for jp_create */
+    int32_t diag_every;      /* 0 = the programs' cadence: steps/240 (uniform), steps/160 (AMR) */
+    int32_t reserved[7];
+} jp_request;
+typedef struct jp_result {
+    int64_t id;
+    int32_t status;          /* jp_status of the solve */
+    int32_t valid;           /* the programs' VALID gate (src/tgv3d_uniform.cu:199) */
+    int64_t steps;
+    int32_t samples;         /* diagnostic samples taken */
+    int32_t pad;
+    double peak_tstar, peak_enstrophy, energy_ratio, mass_drift;  /* energy_ratio = E_end / E0 */
+    double t_submit, t_start, t_end;   /* seconds on the server clock */
+    int64_t bytes;           /* HBM estimate the solve was admitted with */
+    int32_t reserved[8];
+} jp_result;
+jp_status jp_server_create(const jp_server_config* cfg, jp_server** out);
+void jp_server_destroy(jp_server* sv);
+jp_status jp_server_submit(jp_server* sv, const jp_request* req);  /* never blocks */
+/* One scheduling round: retire finished solves, admit queued ones that fit, advance the active ones. */
+jp_status jp_server_tick(jp_server* sv, int32_t* active, int32_t* queued);
+/* Move up to `max` finished results to `out`; returns how many. */
+int32_t jp_server_poll(jp_server* sv, jp_result* out, int32_t max);
+/* Seconds since the server was created (the clock of jp_result timestamps). */
+double jp_server_clock(const jp_server* sv);
 
 /* ---- measurement ---------------------------------------------------------------------------- */
 

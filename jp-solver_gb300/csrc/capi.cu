@@ -95,7 +95,17 @@ const char* jp_build_info(void) {
     return "jp-solver GB300 engine: D3Q19 BGK, sm_103a, storages fp32/fp16s/bf16s/fp64";
 }
 int64_t jp_launch_count(void) { return launch_count(); }
-size_t jp_sizeof(int32_t which) { return which == 0 ? sizeof(jp_config) : (which == 1 ? sizeof(jp_info) : 0); }
+size_t jp_sizeof(int32_t which) {
+    switch (which) {
+        case 0: return sizeof(jp_config);
+        case 1: return sizeof(jp_info);
+        case 2: return sizeof(jp_amr_counts);
+        case 3: return sizeof(jp_server_config);
+        case 4: return sizeof(jp_request);
+        case 5: return sizeof(jp_result);
+    }
+    return 0;
+}
 
 void jp_config_default(jp_config* c, int32_t kind) {
     if (!c) return;

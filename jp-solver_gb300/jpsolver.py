@@ -67,6 +67,23 @@ class AmrCounts(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_active", C.c_int32), ("pool_gb", C.c_double),
+                ("tick_steps", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class Request(C.Structure):
+    _fields_ = [("id", C.c_int64), ("cfg", Config), ("diag_every", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class Result(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("valid", C.c_int32), ("steps", C.c_int64),
+                ("samples", C.c_int32), ("pad", C.c_int32),
+                ("peak_tstar", C.c_double), ("peak_enstrophy", C.c_double), ("energy_ratio", C.c_double),
+                ("mass_drift", C.c_double), ("t_submit", C.c_double), ("t_start", C.c_double),
+                ("t_end", C.c_double), ("bytes", C.c_int64), ("reserved", C.c_int32 * 8)]
+
+
 TABLES = {"ref0": 0, "fof0": 1, "rl0": 2, "l1pcb": 3, "l1oct": 4, "f1pos": 5, "l1grid": 6, "ref1": 7, "fof1": 8,
           "rl1": 9, "l2pl1": 10, "l2oct": 11, "skin0": 12, "skin1": 13, "deep": 14}
 
@@ -95,6 +112,17 @@ SIGNATURES = {
     "jp_step_timed": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
     "jp_launch_count": (C.c_int64, []),
     "jp_regrid": (C.c_int, [C.c_void_p]),
+    "jp_ensemble_create": (C.c_int, [C.c_int32, C.POINTER(C.c_void_p)]),
+    "jp_ensemble_destroy": (None, [C.c_void_p]),
+    "jp_ensemble_add": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "jp_ensemble_remove": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "jp_ensemble_step": (C.c_int, [C.c_void_p, C.c_int64]),
+    "jp_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "jp_server_destroy": (None, [C.c_void_p]),
+    "jp_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request)]),
+    "jp_server_tick": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "jp_server_poll": (C.c_int32, [C.c_void_p, C.POINTER(Result), C.c_int32]),
+    "jp_server_clock": (C.c_double, [C.c_void_p]),
     "jp_get_output_fields": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                        C.c_int64]),
     "jp_memory_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
@@ -292,3 +320,77 @@ class PinnedBuffer:
             self.array = None
             lib().jp_host_free(self.ptr)
             self.ptr = None
+
+
+class Ensemble:
+    """Uniform solvers stepped together in batched launches."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().jp_ensemble_create(device, C.byref(h)))
+        self.h = h
+        self.members = []
+
+    def add(self, s: Solver) -> None:
+        _check(lib().jp_ensemble_add(self.h, s.h))
+        self.members.append(s)
+
+    def remove(self, s: Solver) -> None:
+        _check(lib().jp_ensemble_remove(self.h, s.h))
+        self.members.remove(s)
+
+    def step(self, n: int = 1) -> None:
+        _check(lib().jp_ensemble_step(self.h, n))
+
+    def close(self) -> None:
+        if self.h:
+            lib().jp_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching solve server (jp_server_*)."""
+
+    def __init__(self, device: int = 0, max_active: int = 0, pool_gb: float = 0.0, tick_steps: int = 64):
+        c = ServerConfig()
+        c.device, c.max_active, c.pool_gb, c.tick_steps = device, max_active, pool_gb, tick_steps
+        h = C.c_void_p()
+        _check(lib().jp_server_create(C.byref(c), C.byref(h)))
+        self.h = h
+
+    def submit(self, rid: int, kind: str = "uniform", diag_every: int = 0, **kw) -> int:
+        r = Request()
+        r.id = rid
+        r.cfg = config(kind, **kw)
+        r.diag_every = diag_every
+        return lib().jp_server_submit(self.h, C.byref(r))
+
+    def tick(self) -> tuple:
+        a, q = C.c_int32(), C.c_int32()
+        _check(lib().jp_server_tick(self.h, C.byref(a), C.byref(q)))
+        return a.value, q.value
+
+    def poll(self, max_results: int = 256) -> list:
+        buf = (Result * max_results)()
+        n = lib().jp_server_poll(self.h, buf, max_results)
+        return [{k: getattr(buf[i], k) for k, _ in Result._fields_ if k not in ("reserved", "pad")} for i in range(n)]
+
+    def clock(self) -> float:
+        return lib().jp_server_clock(self.h)
+
+    def close(self) -> None:
+        if self.h:
+            lib().jp_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -43,9 +43,11 @@ def test_binding_covers_every_declared_symbol():
 def test_abi_version_and_struct_sizes():
     L = jpsolver.lib()
     assert L.jp_abi_version() == 1
-    assert L.jp_sizeof(0) == ctypes.sizeof(jpsolver.Config)
-    assert L.jp_sizeof(1) == ctypes.sizeof(jpsolver.Info)
-    assert L.jp_sizeof(7) == 0
+    mirrors = [jpsolver.Config, jpsolver.Info, jpsolver.AmrCounts, jpsolver.ServerConfig, jpsolver.Request,
+               jpsolver.Result]
+    for i, m in enumerate(mirrors):
+        assert L.jp_sizeof(i) == ctypes.sizeof(m), m.__name__
+    assert L.jp_sizeof(17) == 0
 
 
 def test_config_defaults_match_reference_flags():

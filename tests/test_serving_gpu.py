@@ -1,0 +1,139 @@
+"""Ensembles (batched launches over many cubes) and the continuous-batching server, on a GB300.
+
+Bars: a cube stepped inside a batch gives the same bits as stepped alone (same kernel, same per-cell
+arithmetic); a solve's result is identical alone and in a mix; admission never exceeds the pool
+budget; an oversized request is refused, not run."""
+import numpy as np
+import pytest
+
+import jpsolver as J
+
+pytestmark = pytest.mark.gpu
+
+
+def test_ensemble_step_matches_individual_steps_bit_exact():
+    cfgs = [dict(n=16, re=400.0), dict(n=24, re=800.0, storage="fp16"), dict(n=32, re=1600.0),
+            dict(n=40, re=200.0, storage="bf16"), dict(n=8, re=400.0)]
+    alone = []
+    for c in cfgs:
+        with J.Solver("uniform", **c) as s:
+            s.step(13)
+            alone.append(s.get_populations(dtype=np.float64))
+    solvers = [J.Solver("uniform", **c) for c in cfgs]
+    ens = J.Ensemble()
+    for s in solvers:
+        ens.add(s)
+    ens.step(5)
+    solvers[0].step(3)            # a member's own steps interleave with the ensemble's
+    ens.remove(solvers[0])
+    ens.step(5)
+    solvers[0].step(2)
+    ens.add(solvers[0])
+    ens.step(3)
+    for s, ref, c in zip(solvers, alone, cfgs):
+        got = s.get_populations(dtype=np.float64)
+        assert s.info["step_count"] == 13
+        np.testing.assert_array_equal(got, ref, err_msg=str(c))
+    ens.close()
+    for s in solvers:
+        s.close()
+
+
+def test_ensemble_with_more_members_than_one_launch():
+    cfgs = [dict(n=8 + 8 * (i % 3), re=400.0 + 10 * i) for i in range(60)]   # > 48 cubes: two launches
+    solvers = [J.Solver("uniform", **c) for c in cfgs]
+    ens = J.Ensemble()
+    for s in solvers:
+        ens.add(s)
+    ens.step(4)
+    for s, c in zip(solvers, cfgs):
+        with J.Solver("uniform", **c) as r:
+            r.step(4)
+            np.testing.assert_array_equal(s.get_populations(), r.get_populations())
+    ens.close()
+    for s in solvers:
+        s.close()
+
+
+def run_server(requests, **kw):
+    sv = J.Server(**kw)
+    for r in requests:
+        assert sv.submit(**r) == 0
+    results, peak_active = {}, 0
+    while len(results) < len(requests):
+        a, q = sv.tick()
+        peak_active = max(peak_active, a)
+        for res in sv.poll():
+            results[res["id"]] = res
+    sv.close()
+    return results, peak_active
+
+
+R0 = dict(rid=1, kind="uniform", n=32, re=400.0, tstar=2.0)
+MIX = [dict(rid=10, kind="uniform", n=48, re=800.0, tstar=1.5, storage="fp16"),
+       dict(rid=11, kind="uniform", n=16, re=300.0, tstar=3.0),
+       dict(rid=12, kind="amr", n=16, re=800.0, tstar=1.0, l1_mode="sensor", l2_mode="sensor", frac1=0.3,
+            frac2=0.2, develop_steps=20, adapt_every=20),
+       dict(rid=13, kind="uniform", n=64, re=1600.0, tstar=0.5, storage="bf16"),
+       dict(rid=14, kind="amr", n=16, re=400.0, tstar=1.0),
+       dict(rid=15, kind="uniform", n=24, re=200.0, tstar=2.5)]
+
+
+def test_server_result_same_alone_and_in_mix():
+    alone, _ = run_server([R0], tick_steps=16)
+    mixed, peak = run_server([MIX[0], MIX[1], R0] + MIX[2:], tick_steps=16)
+    a, m = alone[1], mixed[1]
+    assert a["status"] == 0 and m["status"] == 0
+    for k in ("steps", "samples", "peak_tstar", "peak_enstrophy", "energy_ratio", "mass_drift", "valid"):
+        assert a[k] == m[k], k
+    assert peak >= 3                                   # solves really ran concurrently
+    assert all(r["status"] == 0 for r in mixed.values())
+
+
+def test_server_amr_result_matches_program_loop():
+    req = MIX[2]
+    res, _ = run_server([req], tick_steps=16)
+    r = res[12]
+    # the `amr` program's loop: regrid (s>0, s % adapt == 0), diagnostic (s % diagK == 0), step
+    cfg = {k: v for k, v in req.items() if k not in ("rid", "kind")}
+    with J.Solver("amr", **cfg) as s:
+        steps = s.info["steps"]
+        diagK = max(1, steps // 160)
+        E0, peak, peak_ts, samples, Elast = None, -1.0, -1.0, 0, None
+        kf = s.info["kf"]
+        for step in range(steps + 1):
+            if step > 0 and step % cfg["adapt_every"] == 0:
+                s.regrid()
+            if step % diagK == 0:
+                E, ens, mass = s.diag()
+                E0 = E if E0 is None else E0
+                Elast = E
+                samples += 1
+                if ens > peak:
+                    peak, peak_ts = ens, step * 0.05 * kf
+            if step < steps:
+                s.step(1)
+    assert r["samples"] == samples
+    assert r["peak_enstrophy"] == peak and r["peak_tstar"] == peak_ts
+    assert r["energy_ratio"] == Elast / E0
+
+
+def test_server_admission_respects_budget():
+    big = [dict(rid=100 + i, kind="uniform", n=96, re=800.0, tstar=0.3) for i in range(4)]
+    one = 2 * 19 * 4 * 96 ** 3 + 16 * 96 ** 3 + (1 << 20)
+    budget_gb = 2.5 * one / 2 ** 30                   # room for two at a time
+    res, peak = run_server(big, pool_gb=budget_gb, tick_steps=32)
+    assert peak == 2
+    assert all(r["status"] == 0 for r in res.values())
+    # later requests started only after earlier ones ended
+    starts = sorted(r["t_start"] for r in res.values())
+    ends = sorted(r["t_end"] for r in res.values())
+    assert starts[2] >= ends[0]
+
+
+def test_server_refuses_request_larger_than_pool():
+    sv = J.Server(pool_gb=0.001)
+    assert sv.submit(rid=7, kind="uniform", n=64, re=400.0, tstar=0.2) == 4     # JP_ERR_NOMEM
+    res = sv.poll()
+    assert len(res) == 1 and res[0]["id"] == 7 and res[0]["status"] == 4
+    sv.close()
