@@ -262,6 +262,51 @@ def bench_serve(J, args, device: int) -> dict:
                                                  "speedup": batched["solves_per_s"] / single["solves_per_s"]}}
 
 
+def precision_run(J, n: int, storage: str, every: int, device: int, tstar: float = 12.0) -> dict:
+    """One full TGV run (Re=1600) with diagnostics every `every` steps: the energy and enstrophy
+    histories, the enstrophy peak time and the mass drift."""
+    import numpy as np
+
+    with J.Solver("uniform", n=n, re=RE, u0=U0, tstar=tstar, storage=storage, device=device) as s:
+        info = s.info
+        steps, kf = info["steps"], info["kf"]
+        ts, E, Z, M = [], [], [], []
+        t0 = time.perf_counter()
+        for k in range(0, steps + 1, every):
+            e, z, m = s.diag()
+            ts.append(k * U0 * kf)
+            E.append(e)
+            Z.append(z)
+            M.append(m)
+            if k + every <= steps:
+                s.step(every)
+        wall = time.perf_counter() - t0
+    E, Z, M = np.array(E), np.array(Z), np.array(M)
+    i = int(np.argmax(Z))
+    return {"storage": storage, "n": n, "steps": steps, "seconds": wall, "t": np.array(ts), "E": E / E[0], "Z": Z,
+            "peak_tstar": float(ts[i]), "peak_enstrophy": float(Z[i]),
+            "mass_drift": float(np.max(np.abs(M - M[0]) / M[0])), "energy_monotonic": bool(np.all(np.diff(E) <= 0))}
+
+
+def bench_precision(J, args, device: int) -> dict:
+    """Storage precision study (configs[1]): FP32, shifted FP16 and BF16 storage against an FP64 run at
+    the same N, Re=1600, t*=12; errors of the enstrophy peak time, the energy curve and the enstrophy
+    curve relative to FP64."""
+    import numpy as np
+
+    n, every = args.n, args.every
+    ref = precision_run(J, n, "fp64", every, device)
+    out = {"n": n, "every_steps": every, "dt_star_per_sample": float(ref["t"][1] - ref["t"][0]),
+           "fp64": {k: ref[k] for k in ("peak_tstar", "peak_enstrophy", "mass_drift", "energy_monotonic", "seconds")}}
+    for st in ("fp32", "fp16", "bf16"):
+        r = precision_run(J, n, st, every, device)
+        out[st] = {k: r[k] for k in ("peak_tstar", "peak_enstrophy", "mass_drift", "energy_monotonic", "seconds")}
+        out[st]["peak_tstar_error"] = r["peak_tstar"] - ref["peak_tstar"]
+        out[st]["energy_max_rel_error"] = float(np.max(np.abs(r["E"] - ref["E"]) / ref["E"]))
+        out[st]["enstrophy_max_rel_error"] = float(np.max(np.abs(r["Z"] - ref["Z"]) / ref["Z"]))
+    return out
+
+
 def cpu_baseline(n: int, steps: int) -> dict:
     """The oracle (CPU restatement of the reference's step, OpenMP) on this host's cores."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -295,7 +340,8 @@ def main() -> int:
                     help="storage of the timed run (the headline is fp32)")
     ap.add_argument("--vec", type=int, default=0)
     ap.add_argument("--tpb", type=int, default=0)
-    ap.add_argument("--workload", default="uniform", choices=["uniform", "serve"])
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "serve", "precision"])
+    ap.add_argument("--every", type=int, default=10, help="precision study: steps between diagnostics")
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--seed", type=int, default=20261203)
@@ -325,6 +371,18 @@ def main() -> int:
         return 0
 
     import jpsolver as J
+
+    if a.workload == "precision":
+        pr = bench_precision(J, a, local)
+        line = {"metric": "enstrophy-peak t* error vs FP64 storage", "value": pr["fp16"]["peak_tstar_error"],
+                "unit": "t*", "n_gpus": world, "steps": pr["fp64"]["seconds"], "warmup": 0, "ms_per_step": None,
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (analytic Taylor-Green initial state)",
+                "config": {"workload": "uniform TGV N=%d Re=%g t*=12, FP64/FP32/FP16/BF16 storage" % (a.n, RE)},
+                "precision": pr}
+        if rank == 0:
+            print(json.dumps(line))
+        return 0
 
     if a.workload == "serve":
         sv = bench_serve(J, a, local)

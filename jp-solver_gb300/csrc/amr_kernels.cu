@@ -179,14 +179,53 @@ __global__ void __launch_bounds__(256) k_fill_l2(const float* __restrict__ pr, f
     }
 }
 
+// Restriction of one fine block, staged in shared memory as sf[q * MB^3 + cell] after its last
+// substep, into the octant `oct` of its parent block: each covered parent cell becomes
+// feq + nqi*regularize(avg - feq) of its 8 children, summed in the reference's dk, dj, di order
+// (k_restrict_L1/L2, src/tgv3d_amr.cu:275-298, 357-381).
+template <int MB>
+__device__ __forceinline__ void restrict_octant(const float* __restrict__ sf, float* __restrict__ parent, int oct,
+                                                float nqi) {
+    constexpr int H = MB / 2, MB3 = MB * MB * MB;
+    for (int t = threadIdx.x; t < H * H * H; t += blockDim.x) {
+        const int i = t % H, j = (t / H) % H, k = t / (H * H);
+        float a[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) a[q] = 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
+            const int sc = ((2 * k + dk) * MB + (2 * j + dj)) * MB + (2 * i + di);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) a[q] += 0.125f * sf[q * MB3 + sc];
+        }
+        float rho, ux, uy, uz;
+        moments(a, rho, ux, uy, uz);
+        float fe[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            fe[q] = feq_ref(q, rho, ux, uy, uz);
+            a[q] = a[q] - fe[q];
+        }
+        regularize(a);
+        const int pc = (((oct >> 2) * H + k) * MB + (((oct >> 1) & 1) * H + j)) * MB + ((oct & 1) * H + i);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) parent[q * MB3 + pc] = fe[q] + nqi * a[q];
+    }
+}
+
 // ---- fine steps (src/tgv3d_amr.cu:241-274, 331-356) -----------------------------------------------
 // Level 1: the 27 coarse neighbours of the parent say whether a pulled cell lives on level 1 (gather
-// from its block) or not (read the ghost shell).
-template <int MB>
+// from its block) or not (read the ghost shell).  FUSE: this is the last substep before the
+// restriction into the coarse level, so the block also restricts itself into its parent octant
+// (saves re-reading the level from HBM in a separate restriction kernel).
+template <int MB, bool FUSE>
 __global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l1(const float* __restrict__ fa, float* __restrict__ fbuf,
                                                          const float* __restrict__ gh, const int* __restrict__ pcb,
                                                          const int* __restrict__ poct, const int* __restrict__ ref0,
-                                                         const int* __restrict__ fof0, int cgx, int N, float om) {
+                                                         const int* __restrict__ fof0, int cgx, int N, float om,
+                                                         float* __restrict__ parent_pool, float nqi) {
+    extern __shared__ float sf[];
     using G = Geo<MB>;
     const int b = blockIdx.x;
     const int cb = pcb[b], oct = poct[b];
@@ -230,17 +269,27 @@ __global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l1(const float* __restric
         }
         bgk(f, om);
 #pragma unroll
-        for (int q = 0; q < Q; ++q) fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
+        for (int q = 0; q < Q; ++q) {
+            fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
+            if (FUSE) sf[q * G::MB3 + cell] = f[q];
+        }
+    }
+    if (FUSE) {
+        __syncthreads();
+        restrict_octant<MB>(sf, parent_pool + (size_t)cb * Q * G::MB3, oct, nqi);
     }
 }
 
-// Level 2: the level-1 grid map says where a pulled cell lives.
-template <int MB>
+// Level 2: the level-1 grid map says where a pulled cell lives.  FUSE as for level 1, into the
+// parent level-1 block.
+template <int MB, bool FUSE>
 __global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l2(const float* __restrict__ fa, float* __restrict__ fbuf,
                                                          const float* __restrict__ gh, const int* __restrict__ l2pl1,
                                                          const int* __restrict__ l2oct, const int* __restrict__ f1pos,
                                                          const int* __restrict__ l1grid, const int* __restrict__ ref1,
-                                                         const int* __restrict__ fof1, int l1gx, int N1, float om) {
+                                                         const int* __restrict__ fof1, int l1gx, int N1, float om,
+                                                         float* __restrict__ parent_pool, float nqi) {
+    extern __shared__ float sf[];
     using G = Geo<MB>;
     const int b = blockIdx.x;
     const int pl1 = l2pl1[b], oct = l2oct[b];
@@ -285,7 +334,14 @@ __global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l2(const float* __restric
         }
         bgk(f, om);
 #pragma unroll
-        for (int q = 0; q < Q; ++q) fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
+        for (int q = 0; q < Q; ++q) {
+            fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
+            if (FUSE) sf[q * G::MB3 + cell] = f[q];
+        }
+    }
+    if (FUSE) {
+        __syncthreads();
+        restrict_octant<MB>(sf, parent_pool + (size_t)pl1 * Q * G::MB3, oct, nqi);
     }
 }
 
@@ -558,11 +614,20 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
             k_fill_l2<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.t2, L.t3, L.t4, L.l1gx, L.n1);
             break;
         case OP_STEP_L1:
-            k_step_l1<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.cgx, L.n, L.omega);
+            if (L.out2 && MB <= 8)
+                k_step_l1<MB, true><<<L.nblocks, cta, sizeof(float) * Q * G::MB3, L.st>>>(
+                    L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.cgx, L.n, L.omega, L.out2, L.scale);
+            else
+                k_step_l1<MB, false><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.cgx,
+                                                                  L.n, L.omega, nullptr, 0.f);
             break;
         case OP_STEP_L2:
-            k_step_l2<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.t4, L.t5, L.l1gx,
-                                                       L.n1, L.omega);
+            if (L.out2 && MB <= 8)
+                k_step_l2<MB, true><<<L.nblocks, cta, sizeof(float) * Q * G::MB3, L.st>>>(
+                    L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.t4, L.t5, L.l1gx, L.n1, L.omega, L.out2, L.scale);
+            else
+                k_step_l2<MB, false><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.t4,
+                                                                  L.t5, L.l1gx, L.n1, L.omega, nullptr, 0.f);
             break;
         case OP_RESTRICT:
             k_restrict<MB><<<L.nblocks, cta, 0, L.st>>>(L.out, L.in, L.list, L.t0, L.scale);
@@ -601,6 +666,7 @@ cudaError_t amr_launch(int mb, int op, const AmrLaunch& L) {
 }
 
 int shell_cells(int mb) { return 6 * mb * mb + 12 * mb; }
+bool can_fuse_restrict(int mb) { return mb <= 8; }
 
 }  // namespace amr
 }  // namespace jp

@@ -11,8 +11,9 @@ enum AmrOp {
     OP_PREP,           // out[list] = prolongation source of in[list]; scale = nqs
     OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, t2 ref0
     OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, t4 ref1
-    OP_STEP_L1,        // in -> out, aux = gh1; t0 pcb, t1 oct, t2 ref0, t3 fof0
-    OP_STEP_L2,        // in -> out, aux = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, t4 ref1, t5 fof1
+    OP_STEP_L1,        // in -> out, aux = gh1; t0 pcb, t1 oct, t2 ref0, t3 fof0; out2 = c0 restricts (scale nqi)
+    OP_STEP_L2,        // in -> out, aux = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, t4 ref1, t5 fof1;
+                       // out2 = f1 restricts (scale nqi)
     OP_RESTRICT,       // out = coarse, in = fine; list = refined coarse blocks, t0 = fof; scale = nqi
     OP_SEED_L1,        // in = old f1 (migrate) , out = new f1, aux = c0; t0 pcb, t1 oct, t2 old ref0|null, t3 old fof0
     OP_SEED_L2,        // in = old f2, out = new f2, aux = f1; t0 l2pl1, t1 l2oct, t2 f1pos, t3 old l1grid|null,
@@ -26,6 +27,7 @@ struct AmrLaunch {
     int nblocks = 0;
     const float* in = nullptr;
     float* out = nullptr;
+    float* out2 = nullptr;   // fused restriction target of the last fine substep (nullptr: none)
     const float* aux = nullptr;
     const float* aux2 = nullptr;
     const int* list = nullptr;
@@ -37,6 +39,8 @@ struct AmrLaunch {
 
 cudaError_t amr_launch(int mb, int op, const AmrLaunch& L);
 int shell_cells(int mb);
+// the fused restriction stages a block in shared memory: MB <= 8 (38 KiB at MB = 8)
+bool can_fuse_restrict(int mb);
 
 // ---- adaptation pipeline (adapt.cu) ------------------------------------------------------------
 // Device counters shared by the pipeline; the host reads them once per stage.

@@ -147,6 +147,7 @@ struct Job {
     jp_info info{};
     long long step = 0, steps = 0, diagK = 1, adapt = 0;
     bool dynamic = false, need_diag = true, regridded = false;
+    jp_status error = JP_OK;
     int samples = 0;
     double E0 = -1, prevE = 1e30, Elast = 0, peak = -1, peak_ts = -1, mass0 = -1, drift = 0;
     bool mono = true;
@@ -340,17 +341,25 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
     }
     // 2. regrid (AMR, before the diagnostic of the same step) and diagnostics due now
     std::vector<Job*> uni_diag;
+    // a failing call ends only its own solve: the job leaves with that status at the next retirement
     for (Job* j : sv->active) {
+        if (j->error != JP_OK) continue;
         if (j->req.cfg.kind == JP_AMR && j->dynamic && j->step > 0 && j->step % j->adapt == 0 && !j->regridded) {
             jp_status st = jp_regrid(j->s);
-            if (st != JP_OK) return st;
             j->regridded = true;
+            if (st != JP_OK) {
+                j->error = st;
+                continue;
+            }
         }
         if (!j->need_diag) continue;
         if (j->req.cfg.kind == JP_AMR) {
             double d[3];
             jp_status st = jp_diag(j->s, d);
-            if (st != JP_OK) return st;
+            if (st != JP_OK) {
+                j->error = st;
+                continue;
+            }
             record(j, d);
         } else {
             uni_diag.push_back(j);
@@ -381,13 +390,13 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
     }
     // 3. retire finished solves (after the batched launches that touched them)
     bool any_done = false;
-    for (Job* j : sv->active) any_done |= j->step >= j->steps && !j->need_diag;
+    for (Job* j : sv->active) any_done |= (j->step >= j->steps && !j->need_diag) || j->error != JP_OK;
     if (any_done) ECK(cudaStreamSynchronize(sv->stream), "retire");
     for (size_t i = 0; i < sv->active.size();) {
         Job* j = sv->active[i];
-        if (j->step >= j->steps && !j->need_diag) {
+        if ((j->step >= j->steps && !j->need_diag) || j->error != JP_OK) {
             sv->active.erase(sv->active.begin() + i);
-            finish(sv, j, JP_OK);
+            finish(sv, j, j->error);
         } else {
             ++i;
         }
@@ -396,12 +405,16 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
     std::vector<std::pair<Job*, long long>> uni;
     long long kmax = 0;
     for (Job* j : sv->active) {
+        if (j->error != JP_OK) continue;
         const long long target = next_event(j);
         if (j->req.cfg.kind == JP_AMR) {
             const long long k = std::min(target - j->step, std::max(1LL, (long long)sv->cfg.tick_steps / 4));
             if (k <= 0) continue;
             jp_status st = jp_step(j->s, k);
-            if (st != JP_OK) return st;
+            if (st != JP_OK) {
+                j->error = st;
+                continue;
+            }
             j->step += k;
             j->regridded = false;
         } else {

@@ -163,16 +163,94 @@ static jp_status mark_l0_by_sensor(jp_solver* s) {
     return JP_OK;
 }
 
-// exclusive scan of the marks and the level-1 tables.  On overflow of the level-1 pool nothing is
-// written and, in a regrid (restore_marks), the previous marks come back: the old grid stays valid.
+// Replace a device array by one of `count` elements that keeps the first `keep` elements.
+template <class T>
+static jp_status regrow(jp_solver* s, T*& p, size_t count, size_t keep) {
+    AmrState* a = s->amr;
+    T* q = nullptr;
+    TRY(dalloc(a, &q, count, "cudaMalloc (pool growth)"));
+    if (keep && p) ACK(cudaMemcpyAsync(q, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s->stream), "pool growth copy");
+    ACK(cudaStreamSynchronize(s->stream), "pool growth");
+    dfree(a, p);
+    p = q;
+    return JP_OK;
+}
+
+static void update_bytes(jp_solver* s) {
+    const AmrState* a = s->amr;
+    s->info.bytes_state = (int64_t)(((size_t)3 * a->cnb0 + 3 * (size_t)a->cap1 + 2 * (size_t)a->cap2) * Q * a->MB3 * 4 +
+                                    ((size_t)a->cap1 + a->cap2) * Q * a->SH * 4);
+}
+
+// Pools grow on overflow instead of being written past their end (the reference sizes them with
+// margins and does not check: ties at the threshold over-admit).  The new capacity is at least
+// twice the old one and must fit the HBM budget; payloads and the snapshots of the previous grid
+// that a regrid still reads are kept.
+static jp_status grow_l1(jp_solver* s, int needed) {
+    AmrState* a = s->amr;
+    const int cap = ((std::max(needed, 2 * a->cap1) + 7) / 8) * 8;
+    if (!pool_fits(a, cap, a->cap2))
+        return fail(JP_ERR_CAPACITY, "level-1 pool overflow: %d blocks needed, %d held, budget allows no growth", needed,
+                    a->cap1);
+    const size_t blk = (size_t)Q * a->MB3, old = a->cap1;
+    TRY(regrow(s, a->f1a, cap * blk, old * blk));  // payload the migration reads
+    TRY(regrow(s, a->f1b, cap * blk, 0));
+    TRY(regrow(s, a->gh1, (size_t)cap * Q * a->SH, 0));
+    TRY(regrow(s, a->prep1, cap * blk, 0));
+    TRY(regrow(s, a->o_ref1, cap, old));           // snapshots of the previous grid
+    TRY(regrow(s, a->o_fof1, cap, old));
+    int** scratch[] = {&a->pcb, &a->oct, &a->rl0, &a->f1pos, &a->ref1, &a->fof1, &a->rl1, &a->skin1, &a->deep};
+    for (int** t : scratch) TRY(regrow(s, *t, cap, 0));
+    TRY(regrow(s, a->sen1, cap, 0));
+    TRY(regrow(s, a->rank, std::max(a->cnb0, cap), 0));
+    TRY(regrow(s, a->flags, (size_t)a->cnb0 + cap, 0));
+    ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * cap, s->stream), "memset");
+    ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * cap, s->stream), "memset");
+    a->cap1 = cap;
+    update_bytes(s);
+    return JP_OK;
+}
+
+static jp_status grow_l2(jp_solver* s, int needed) {
+    AmrState* a = s->amr;
+    const int cap = ((std::max(needed, 2 * a->cap2) + 7) / 8) * 8;
+    if (!pool_fits(a, a->cap1, cap))
+        return fail(JP_ERR_CAPACITY, "level-2 pool overflow: %d blocks needed, %d held, budget allows no growth", needed,
+                    a->cap2);
+    const size_t blk = (size_t)Q * a->MB3, old = a->cap2;
+    TRY(regrow(s, a->f2a, cap * blk, old * blk));  // payload the migration reads
+    TRY(regrow(s, a->f2b, cap * blk, 0));
+    TRY(regrow(s, a->gh2, (size_t)cap * Q * a->SH, 0));
+    TRY(regrow(s, a->l2pl1, cap, 0));
+    TRY(regrow(s, a->l2oct, cap, 0));
+    a->cap2 = cap;
+    update_bytes(s);
+    return JP_OK;
+}
+
+// exclusive scan of the marks and the level-1 tables; on overflow of the level-1 pool nothing is
+// written, the pool grows and the tables are built again.  If the pool cannot grow the error stands
+// and, in a regrid (restore_marks), the previous marks come back: the old grid stays valid.
 static jp_status build_l1(jp_solver* s, bool restore_marks) {
     AmrState* a = s->amr;
     ACK(adapt_build_l1(a->ref0, a->cnb0, a->cgx, a->l1gx, a->cap1, a->rank, a->fof0, a->rl0, a->pcb, a->oct, a->l1grid,
                        a->f1pos, a->cnt_dev, s->stream), "build L1");
     TRY(read_counts(s));
-    if (a->cnt_host->err && restore_marks) {
-        ACK(cudaMemcpyAsync(a->ref0, a->o_ref0, sizeof(int) * a->cnb0, cudaMemcpyDeviceToDevice, s->stream), "restore");
-        ACK(cudaStreamSynchronize(s->stream), "restore");
+    if (a->cnt_host->err & ADAPT_ERR_CAP1) {
+        jp_status g = grow_l1(s, a->cnt_host->nf1);
+        if (g == JP_OK) {
+            a->cnt_host->err = 0;
+            ACK(cudaMemsetAsync(&a->cnt_dev->err, 0, sizeof(int), s->stream), "counts");
+            ACK(adapt_build_l1(a->ref0, a->cnb0, a->cgx, a->l1gx, a->cap1, a->rank, a->fof0, a->rl0, a->pcb, a->oct,
+                               a->l1grid, a->f1pos, a->cnt_dev, s->stream), "build L1");
+            TRY(read_counts(s));
+        } else if (restore_marks) {
+            ACK(cudaMemcpyAsync(a->ref0, a->o_ref0, sizeof(int) * a->cnb0, cudaMemcpyDeviceToDevice, s->stream), "restore");
+            ACK(cudaStreamSynchronize(s->stream), "restore");
+            return g;
+        } else {
+            return g;
+        }
     }
     TRY(check_err(s));
     a->nref0 = a->cnt_host->nref0;
@@ -307,7 +385,7 @@ static jp_status regrid(jp_solver* s) {
         a->nf2 = a->cnt_host->nf2;
         a->ndeep = a->cnt_host->ndeep;
         a->hw_nf2 = std::max(a->hw_nf2, (long long)a->nf2);
-        if (a->nf2 > a->cap2) return fail(JP_ERR_CAPACITY, "level-2 pool overflow: %d > %d", a->nf2, a->cap2);
+        if (a->nf2 > a->cap2) TRY(grow_l2(s, a->nf2));  // on failure the solver needs jp_init_tgv
         ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset fof1");
         if (a->nref1)
             ACK(adapt_scatter_l2(a->ref1, a->rank, a->nf1, a->cap2, a->fof1, a->rl1, a->l2pl1, a->l2oct, a->cnt_dev,
@@ -341,6 +419,8 @@ static jp_status regrid(jp_solver* s) {
 static jp_status base_step(jp_solver* s) {
     AmrState* a = s->amr;
     const bool skip_prep = s->cfg.flags & JP_FLAG_SKIP_PREP, skip_restrict = s->cfg.flags & JP_FLAG_SKIP_RESTRICT;
+    // restrictions fused into the last substep of each fine level (same values, one pass less)
+    const bool fuse = !skip_restrict && can_fuse_restrict(a->MB);
     TRY(step_l0(s));
     if (!a->nf1) return JP_OK;
     if (!skip_prep) {
@@ -400,6 +480,10 @@ static jp_status base_step(jp_solver* s) {
                 S.l1gx = a->l1gx;
                 S.n1 = a->N1;
                 S.omega = a->om2;
+                if (s2 == 1 && fuse) {  // last level-2 substep restricts itself into level 1
+                    S.out2 = a->f1a;
+                    S.scale = float(a->nqi21);
+                }
                 TRY(launch(s, OP_STEP_L2, S));
                 std::swap(a->f2a, a->f2b);
             }
@@ -410,7 +494,7 @@ static jp_status base_step(jp_solver* s) {
             R.list = a->rl1;
             R.t0 = a->fof1;
             R.scale = float(a->nqi21);
-            if (!skip_restrict) TRY(launch(s, OP_RESTRICT, R));
+            if (!skip_restrict && !fuse) TRY(launch(s, OP_RESTRICT, R));
         }
         AmrLaunch S;
         S.nblocks = a->nf1;
@@ -424,6 +508,10 @@ static jp_status base_step(jp_solver* s) {
         S.cgx = a->cgx;
         S.n = a->N;
         S.omega = a->om1;
+        if (s1 == 1 && fuse) {  // last level-1 substep restricts itself into the coarse level
+            S.out2 = a->c0a;
+            S.scale = float(a->nqi10);
+        }
         TRY(launch(s, OP_STEP_L1, S));
         std::swap(a->f1a, a->f1b);
     }
@@ -434,7 +522,7 @@ static jp_status base_step(jp_solver* s) {
     R.list = a->rl0;
     R.t0 = a->fof0;
     R.scale = float(a->nqi10);
-    if (skip_restrict) return JP_OK;
+    if (skip_restrict || fuse) return JP_OK;
     return launch(s, OP_RESTRICT, R);
 }
 
@@ -567,8 +655,7 @@ jp_status amr_init(jp_solver* s) {
     ACK(cudaStreamSynchronize(s->stream), "initial build");
     a->c0_home = a->c0a;
     s->step_count = 0;
-    s->info.bytes_state = (int64_t)(((size_t)2 * a->cnb0 + 2 * (size_t)a->cap1 + 2 * (size_t)a->cap2) * Q * a->MB3 * 4 +
-                                    ((size_t)a->cap1 + a->cap2) * Q * a->SH * 4);
+    update_bytes(s);
     return JP_OK;
 }
 

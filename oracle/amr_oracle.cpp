@@ -87,6 +87,36 @@ struct Amr {
     bool ov = false;
     std::vector<float> ov_sen0, ov_sen1pos;
     int error = 0;  // 3 = pool capacity exceeded
+    // off: the reference's behaviour (an overflow is an error here, an out-of-bounds write there);
+    // on: the engine's pool growth (capacity at least doubled, budget permitting, payloads kept)
+    bool grow = false;
+
+    bool grow_l1(int needed) {
+        int cap = ((std::max(needed, 2 * cap1) + 7) / 8) * 8;
+        if (!pool_fits(cap, cap2)) return false;
+        size_t blkn = (size_t)Q * MB3;
+        f1a.resize(cap * blkn, 0.f);
+        f1b.resize(cap * blkn, 0.f);
+        prep1.resize(cap * blkn, 0.f);
+        gh1.resize((size_t)cap * Q * EB3, 0.f);
+        for (std::vector<int>* t : {&rl0, &l1pcb, &l1oct, &f1pos, &ref1, &rl1, &deep, &skin1}) t->resize(cap, 0);
+        fof1.resize(cap, -1);
+        sen1.resize(cap, 0.f);
+        cap1 = cap;
+        return true;
+    }
+    bool grow_l2(int needed) {
+        int cap = ((std::max(needed, 2 * cap2) + 7) / 8) * 8;
+        if (!pool_fits(cap1, cap)) return false;
+        size_t blkn = (size_t)Q * MB3;
+        f2a.resize(cap * blkn, 0.f);
+        f2b.resize(cap * blkn, 0.f);
+        gh2.resize((size_t)cap * Q * EB3, 0.f);
+        l2pl1.resize(cap, 0);
+        l2oct.resize(cap, 0);
+        cap2 = cap;
+        return true;
+    }
 
     size_t blk(int b, int q) const { return ((size_t)b * Q + q) * MB3; }
     size_t gblk(int b, int q) const { return ((size_t)b * Q + q) * EB3; }
@@ -509,7 +539,7 @@ struct Amr {
         nref0 = acc;
         nf1 = 8 * nref0;
         hw_nf1 = std::max(hw_nf1, (long)nf1);
-        if (nf1 > cap1) { error = 3; return false; }
+        if (nf1 > cap1 && !(grow && grow_l1(nf1))) { error = 3; return false; }
         std::fill(l1grid.begin(), l1grid.end(), -1);
         std::fill(fof0.begin(), fof0.end(), -1);
         for (int cb = 0; cb < cnb0; ++cb) {
@@ -661,7 +691,7 @@ struct Amr {
         if (nf1) {
             mark_l1(false, false);
             scan_l2();
-            if (nf2 > cap2) { error = 3; return; }
+            if (nf2 > cap2 && !(grow && grow_l2(nf2))) { error = 3; return; }
             scatter_l2();
             if (nf2) migrate_L2();
         }
@@ -844,6 +874,7 @@ void orc_amr_set_sensor_override(void* h, const float* sen0, const float* sen1po
     a->ov_sen0.assign(sen0, sen0 + a->cnb0);
     a->ov_sen1pos.assign(sen1pos, sen1pos + a->NG1);
 }
+void orc_amr_set_growth(void* h, int on) { static_cast<Amr*>(h)->grow = on != 0; }
 int orc_amr_initial_build(void* h) {
     Amr* a = static_cast<Amr*>(h);
     a->initial_build();

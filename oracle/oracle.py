@@ -208,7 +208,7 @@ class AmrBackend:
 
     def __init__(self, which: str, n: int, re: float, l1: str = "all", l2: str = "all", frac1: float = 0.35,
                  frac2: float = 0.35, u0: float = 0.05, tstar: float = 12.0, develop: int = 300,
-                 budget: float = BIG_BUDGET, mb: int = 8, build: bool = True):
+                 budget: float = BIG_BUDGET, mb: int = 8, build: bool = True, grow: bool = False):
         global _amr_orc_ready
         self.which = which
         self.n, self.mb = n, mb
@@ -223,6 +223,9 @@ class AmrBackend:
                 _amr_orc_ready = True
             self.L, self.p = L, "orc_amr"
             self.h = L.orc_amr_create(n, mb, re, u0, tstar, MODES[l1], MODES[l2], frac1, frac2, develop, budget)
+            if self.h and grow:
+                L.orc_amr_set_growth.argtypes = [C.c_void_p, C.c_int]
+                L.orc_amr_set_growth(C.c_void_p(self.h), 1)
         else:
             L = ref_amr()
             if mb != 8:

@@ -55,22 +55,15 @@ CASES = [  # n, l1, l2, frac1, frac2, ties
 
 
 def build_both(n, l1, l2, f1, f2, s0, s1, develop=5):
-    """Initial build on both sides with the same sensor.  Ties can over-admit past the pool (the
-    reference sizes it with a 1.4 margin and then writes out of bounds); both sides must then report
-    the overflow instead.  Returns (engine, oracle) or None after checking that both refused."""
+    """Initial build on both sides with the same sensor.  Ties can over-admit past a pool (the
+    reference sizes it with a 1.4 margin and then writes out of bounds); the engine grows the pool,
+    and so does the oracle here (grow=True), so tables still compare bit for bit."""
     e = engine(n, 800.0, l1, l2, f1, f2, develop=develop)
     e.set_sensor_override(s0, s1)
-    o = oracle(n, 800.0, l1, l2, f1, f2, develop=develop, build=False)
+    o = O.AmrBackend("oracle", n, 800.0, l1, l2, f1, f2, develop=develop, budget=1024.0 * 2 ** 30, build=False,
+                     grow=True)
     o.set_sensor_override(s0, s1)
-    try:
-        o.initial_build()
-    except RuntimeError:
-        with pytest.raises(J.JPError) as exc:
-            e.init_tgv()
-        assert exc.value.status == 3
-        e.close()
-        o.close()
-        return None
+    o.initial_build()
     e.init_tgv()
     return e, o
 
@@ -78,10 +71,7 @@ def build_both(n, l1, l2, f1, f2, s0, s1, develop=5):
 @pytest.mark.parametrize("n,l1,l2,f1,f2,ties", CASES)
 def test_tables_bit_exact_with_shared_sensor(n, l1, l2, f1, f2, ties):
     s0, s1 = O.random_sensor_fields(n, seed=n + len(l1) + len(l2), ties=ties)
-    pair = build_both(n, l1, l2, f1, f2, s0, s1)
-    if pair is None:
-        return
-    e, o = pair
+    e, o = build_both(n, l1, l2, f1, f2, s0, s1)
     with e:
         assert_tables_equal(e, o, "initial build")
         np.testing.assert_array_equal(e.sensor(0), o.sensor(0))
@@ -91,13 +81,7 @@ def test_tables_bit_exact_with_shared_sensor(n, l1, l2, f1, f2, ties):
             o.set_sensor_override(t0, t1)
             e.step(1)
             o.step(1)
-            try:
-                o.regrid()
-            except RuntimeError:            # over-admission past the pool: both refuse
-                with pytest.raises(J.JPError) as exc:
-                    e.regrid()
-                assert exc.value.status == 3
-                break
+            o.regrid()
             e.regrid()
             assert_tables_equal(e, o, "regrid %d" % r)
         o.close()
@@ -199,13 +183,39 @@ def test_static_gold_all_levels_track_uniform_4n():
     assert abs(ma - 1.0) < 1e-5
 
 
+def test_pool_grows_when_ties_over_admit():
+    # every coarse block ties at the threshold: 512 level-1 blocks against a pool of 72; the engine
+    # grows the pool (the reference would write past it) and the tables equal the growing oracle's
+    n = 32
+    cnb0, ng1 = (n // 8) ** 3, (2 * n // 8) ** 3
+    ones0, ones1 = np.ones(cnb0, dtype=np.float32), np.linspace(0, 1, ng1, dtype=np.float32)
+    with J.Solver("amr", n=n, re=800.0, l1_mode="sensor", l2_mode="sensor", frac1=0.1, frac2=0.2, develop_steps=2,
+                  max_gb=1024.0) as e:
+        o = O.AmrBackend("oracle", n, 800.0, "sensor", "sensor", 0.1, 0.2, develop=2, budget=1024.0 * 2 ** 30,
+                         grow=True)
+        assert e.counts()["cap1"] == 72
+        for lv in range(3):
+            e.set_populations(o.pops(lv), level=lv, layout="blocked")
+        for b in (e, o):
+            b.set_sensor_override(ones0, ones1)
+            b.regrid()
+        assert e.counts()["nf1"] == 512 and e.counts()["cap1"] >= 512
+        assert_tables_equal(e, o, "grown pool")
+        for lv in range(3):
+            assert rel_err(e.get_populations(lv, layout="blocked"), o.pops(lv)) < 2e-6
+        e.step(1)
+        o.step(1)
+        for lv in range(3):
+            assert rel_err(e.get_populations(lv, layout="blocked"), o.pops(lv)) < 1e-5
+        o.close()
+
+
 def test_capacity_overflow_is_reported_not_written():
-    # a regrid that would need more level-1 blocks than the pool holds is rejected before any table is
-    # written (the reference has no check: its marks use >=, so ties over-admit past the pool); the
-    # previous grid stays valid and the solver keeps stepping
+    # a regrid that would need more level-1 blocks than the pool holds, with no budget left to grow it,
+    # is rejected before any table is written; the previous grid stays valid and the solver steps on
     n = 32
     with J.Solver("amr", n=n, re=800.0, l1_mode="sensor", l2_mode="sensor", frac1=0.1, frac2=0.1, develop_steps=2,
-                  max_gb=1024.0) as e:
+                  max_gb=0.04) as e:
         cap1 = e.counts()["cap1"]
         cnb0 = e.counts()["cnb0"]
         ones0 = np.ones(cnb0, dtype=np.float32)              # every block ties at the threshold
