@@ -297,6 +297,15 @@ int32_t jp_server_poll(jp_server* sv, jp_result* out, int32_t max);
 /* Seconds since the server was created (the clock of jp_result timestamps). */
 double jp_server_clock(const jp_server* sv);
 
+/* ---- autotuning (spec extension; no counterpart in the reference) ------------------------- */
+
+/* Time `steps` steps of each candidate and write the fastest into *cfg: for a uniform solver the
+ * thread mapping (cells per thread `vec` x `threads_per_block`), for an AMR solver the block edge
+ * `mb` in {4, 8, 16} dividing n (the reference fixes MB at compile time; MB=16 cannot run there, its
+ * kernels would need 4096 threads per block).  *best receives the winner's lattice updates per second
+ * (AMR: work-normalised, (cnb0 + 2 nf1 + 4 nf2) MB^3 per coarse step). */
+jp_status jp_autotune(jp_config* cfg, int32_t steps, double* best);
+
 /* ---- measurement ---------------------------------------------------------------------------- */
 
 /* Advance `nsteps` steps and return the device time of those launches, measured with CUDA events

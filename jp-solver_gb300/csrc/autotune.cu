@@ -1,0 +1,79 @@
+// Autotuner: picks the uniform step's thread mapping or the AMR block edge by timing candidates on
+// the device (spec extension; the reference fixes MB and the mapping at compile time).
+#include <cstring>
+
+#include "jp.h"
+#include "kernels.h"
+#include "solver.h"
+
+using namespace jp;
+
+extern "C" jp_status jp_autotune(jp_config* cfg, int32_t steps, double* best) {
+    if (!cfg || !best) return fail(JP_ERR_INVALID, "jp_autotune: null argument");
+    if (steps <= 0) return fail(JP_ERR_INVALID, "jp_autotune: steps must be positive");
+    *best = 0.0;
+    if (cfg->kind == JP_UNIFORM) {
+        // one solver, the mapping switched between timings (same buffers, same state shape)
+        jp_config c = *cfg;
+        c.vec = 0;
+        c.threads_per_block = 0;
+        jp_solver* s = nullptr;
+        jp_status st = jp_create(&c, &s);
+        if (st != JP_OK) return st;
+        const int vecs[4] = {1, 2, 4, 8};
+        const int tpbs[4] = {64, 128, 256, 512};
+        int bv = s->vec, bt = s->tpb;
+        const double cells = double(s->cells);
+        for (int v : vecs) {
+            if (!vec_supported(s->storage, v) || s->n % v || ((long long)s->cells / v) % 32) continue;
+            for (int t : tpbs) {
+                s->vec = v;
+                s->tpb = t;
+                float ms = 0.f;
+                st = jp_step(s, 2);
+                if (st == JP_OK) st = jp_step_timed(s, steps, &ms);
+                if (st != JP_OK) {
+                    jp_destroy(s);
+                    return st;
+                }
+                const double lups = cells * steps / (double(ms) * 1e-3);
+                if (lups > *best) {
+                    *best = lups;
+                    bv = v;
+                    bt = t;
+                }
+            }
+        }
+        jp_destroy(s);
+        cfg->vec = bv;
+        cfg->threads_per_block = bt;
+        return JP_OK;
+    }
+    // AMR: block edges that divide n; work-normalised throughput of the 1:2:4 step
+    const int mbs[3] = {4, 8, 16};
+    int bmb = cfg->mb;
+    for (int mb : mbs) {
+        if (cfg->n % mb) continue;
+        jp_config c = *cfg;
+        c.mb = mb;
+        jp_solver* s = nullptr;
+        jp_status st = jp_create(&c, &s);
+        if (st == JP_ERR_NOMEM || st == JP_ERR_CAPACITY) continue;
+        if (st != JP_OK) return st;
+        float ms = 0.f;
+        st = jp_step(s, 1);
+        if (st == JP_OK) st = jp_step_timed(s, steps, &ms);
+        jp_amr_counts k;
+        if (st == JP_OK) st = jp_amr_get_counts(s, &k);
+        jp_destroy(s);
+        if (st != JP_OK) return st;
+        const double work = (double(k.cnb0) + 2.0 * k.nf1 + 4.0 * k.nf2) * double(mb) * mb * mb * steps;
+        const double lups = work / (double(ms) * 1e-3);
+        if (lups > *best) {
+            *best = lups;
+            bmb = mb;
+        }
+    }
+    cfg->mb = bmb;
+    return JP_OK;
+}

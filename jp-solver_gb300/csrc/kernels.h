@@ -38,8 +38,8 @@ cudaError_t launch_stream_collide(int storage, const UniSolve* solves, int count
 int default_vec(int storage);
 bool vec_supported(int storage, int vec);
 
-// TGV initial state (src/tgv3d_uniform.cu:63-77) into flat storage.
-cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, cudaStream_t st);
+// TGV initial state (src/tgv3d_uniform.cu:63-77) into flat storage; axis_tab: 3*n doubles of scratch.
+cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, double* axis_tab, cudaStream_t st);
 
 // Macroscopic field (rho, ux, uy, uz) per cell, linear (z*n+y)*n+x.  FP64 storage writes double4,
 // every other storage float4 (k_macro, src/tgv3d_uniform.cu:80-90).

@@ -100,7 +100,18 @@ void uniform_free(jp_solver* s) {
 }
 
 jp_status uniform_init(jp_solver* s) {
-    JP_CK(launch_init_tgv(s->storage, s->fa, s->n, s->cfg.u0, s->info.kf, s->stream), "init_tgv");
+    // the per-axis trigonometry table of the initial state lives in the diagnostic partials buffer
+    // (3n <= 3 * kDiagBlocks doubles for n <= kDiagBlocks), which is free between diagnostics
+    double* tab = s->partials;
+    double* own = nullptr;
+    if (s->n > kDiagBlocks) {
+        JP_CK(cudaMalloc(&own, sizeof(double) * 3 * s->n), "cudaMalloc init table");
+        tab = own;
+    }
+    cudaError_t e = launch_init_tgv(s->storage, s->fa, s->n, s->cfg.u0, s->info.kf, tab, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (own) cudaFree(own);
+    JP_CK(e, "init_tgv");
     JP_CK(cudaStreamSynchronize(s->stream), "init_tgv");
     s->step_count = 0;
     return JP_OK;

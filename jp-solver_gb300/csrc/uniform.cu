@@ -302,16 +302,29 @@ cudaError_t launch_stream_collide(int storage, const UniSolve* solves, int count
 // into rho = 1 + 3p, p = u0^2/16 (cos2x + cos2y)(cos2z + 2), equilibrium populations
 // (src/tgv3d_uniform.cu:63-77).  FP32 storage rounds rho and u to float and evaluates the float
 // equilibrium as the reference does; FP64 keeps double; shifted formats store the double deviation.
+// The field is separable: sin, cos and cos(2.) of (i+0.5)kf per axis index, tabulated once with the
+// same double expressions, give the same values as evaluating them per cell.
+__global__ void k_tgv_axis(double* __restrict__ tab, int n, double kf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = (i + 0.5) * kf;
+    tab[i] = sin(x);
+    tab[n + i] = cos(x);
+    tab[2 * n + i] = cos(2 * x);
+}
+
 template <class ST>
-__global__ void k_init_tgv(typename ST::raw* __restrict__ f, int n, double u0, double kf) {
+__global__ void k_init_tgv(typename ST::raw* __restrict__ f, int n, double u0, const double* __restrict__ tab) {
     const long long cells = (long long)n * n * n;
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cells) return;
     const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
-    const double x = (i + 0.5) * kf, y = (j + 0.5) * kf, z = (k + 0.5) * kf;
-    const double ux = u0 * sin(x) * cos(y) * cos(z);
-    const double uy = -u0 * cos(x) * sin(y) * cos(z);
-    const double p = (u0 * u0 / 16.0) * (cos(2 * x) + cos(2 * y)) * (cos(2 * z) + 2.0);
+    const double sx = tab[i], cxv = tab[n + i], c2x = tab[2 * n + i];
+    const double sy = tab[j], cyv = tab[n + j], c2y = tab[2 * n + j];
+    const double czv = tab[n + k], c2z = tab[2 * n + k];
+    const double ux = u0 * sx * cyv * czv;
+    const double uy = -u0 * cxv * sy * czv;
+    const double p = (u0 * u0 / 16.0) * (c2x + c2y) * (c2z + 2.0);
     const double rho = 1.0 + 3.0 * p;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -329,17 +342,18 @@ __global__ void k_init_tgv(typename ST::raw* __restrict__ f, int n, double u0, d
     }
 }
 
-cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, cudaStream_t st) {
+cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, double* axis_tab, cudaStream_t st) {
     const long long cells = (long long)n * n * n;
     const unsigned blocks = (unsigned)((cells + 255) / 256);
+    k_tgv_axis<<<(n + 255) / 256, 256, 0, st>>>(axis_tab, n, kf);
     switch (storage) {
-        case 0: k_init_tgv<StF32><<<blocks, 256, 0, st>>>((float*)f, n, u0, kf); break;
-        case 1: k_init_tgv<StF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, kf); break;
-        case 2: k_init_tgv<StBF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, kf); break;
-        case 3: k_init_tgv<StF64><<<blocks, 256, 0, st>>>((double*)f, n, u0, kf); break;
+        case 0: k_init_tgv<StF32><<<blocks, 256, 0, st>>>((float*)f, n, u0, axis_tab); break;
+        case 1: k_init_tgv<StF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, axis_tab); break;
+        case 2: k_init_tgv<StBF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, axis_tab); break;
+        case 3: k_init_tgv<StF64><<<blocks, 256, 0, st>>>((double*)f, n, u0, axis_tab); break;
         default: return cudaErrorInvalidValue;
     }
-    note_launch();
+    note_launch(2);
     return cudaGetLastError();
 }
 

@@ -82,6 +82,11 @@ int main(int argc, char** argv) {
     cfg.develop_steps = argi(argc, argv, "--develop", 300);
     cfg.device = argi(argc, argv, "--device", 0);
     cfg.flags = (skipprep ? JP_FLAG_SKIP_PREP : 0) | (skiprestr ? JP_FLAG_SKIP_RESTRICT : 0) | (usegraph ? JP_FLAG_GRAPH : 0);
+    if (argd(argc, argv, "--autotune", 0.0) > 0.5) {
+        double best = 0.0;
+        ck(jp_autotune(&cfg, 4, &best), "autotune");
+        std::printf("[autotune] MB=%d  %.1f MLUPS(work)\n", cfg.mb, best / 1e6);
+    }
     jp_solver* s = nullptr;
     ck(jp_create(&cfg, &s), "create");
     jp_info info;

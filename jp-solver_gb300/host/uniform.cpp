@@ -38,6 +38,11 @@ int main(int argc, char** argv) {
     cfg.threads_per_block = argi(argc, argv, "--tpb", 0);
     cfg.vec = argi(argc, argv, "--vec", 0);
     cfg.device = argi(argc, argv, "--device", 0);
+    if (argd(argc, argv, "--autotune", 0.0) > 0.5) {
+        double best = 0.0;
+        ck(jp_autotune(&cfg, 10, &best), "autotune");
+        std::printf("[autotune] vec=%d threads/block=%d  %.1f MLUPS\n", cfg.vec, cfg.threads_per_block, best / 1e6);
+    }
     jp_solver* s = nullptr;
     ck(jp_create(&cfg, &s), "create");
     jp_info info;

@@ -112,6 +112,7 @@ SIGNATURES = {
     "jp_step_timed": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
     "jp_launch_count": (C.c_int64, []),
     "jp_regrid": (C.c_int, [C.c_void_p]),
+    "jp_autotune": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(C.c_double)]),
     "jp_ensemble_create": (C.c_int, [C.c_int32, C.POINTER(C.c_void_p)]),
     "jp_ensemble_destroy": (None, [C.c_void_p]),
     "jp_ensemble_add": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -168,6 +169,14 @@ def config(kind: str = "uniform", **kw) -> Config:
             raise KeyError("unknown config field %r" % k)
         setattr(c, k, v)
     return c
+
+
+def autotune(kind: str = "uniform", steps: int = 10, **kw) -> tuple:
+    """(tuned config fields, lattice updates per second) from jp_autotune."""
+    c = config(kind, **kw)
+    best = C.c_double()
+    _check(lib().jp_autotune(C.byref(c), steps, C.byref(best)))
+    return {"vec": c.vec, "threads_per_block": c.threads_per_block, "mb": c.mb}, best.value
 
 
 class Solver:

@@ -189,10 +189,16 @@ def test_pool_grows_when_ties_over_admit():
     n = 32
     cnb0, ng1 = (n // 8) ** 3, (2 * n // 8) ** 3
     ones0, ones1 = np.ones(cnb0, dtype=np.float32), np.linspace(0, 1, ng1, dtype=np.float32)
+    s0, s1 = O.random_sensor_fields(n, seed=21)
     with J.Solver("amr", n=n, re=800.0, l1_mode="sensor", l2_mode="sensor", frac1=0.1, frac2=0.2, develop_steps=2,
                   max_gb=1024.0) as e:
         o = O.AmrBackend("oracle", n, 800.0, "sensor", "sensor", 0.1, 0.2, develop=2, budget=1024.0 * 2 ** 30,
-                         grow=True)
+                         grow=True, build=False)
+        for b in (e, o):                 # the same initial grid on both sides
+            b.set_sensor_override(s0, s1)
+        e.init_tgv()
+        o.initial_build()
+        assert_tables_equal(e, o, "initial build")
         assert e.counts()["cap1"] == 72
         for lv in range(3):
             e.set_populations(o.pops(lv), level=lv, layout="blocked")
@@ -230,3 +236,9 @@ def test_capacity_overflow_is_reported_not_written():
             np.testing.assert_array_equal(e.table(t), before[t], err_msg=t)
         e.step(2)
         assert np.isfinite(e.diag()[0])
+
+
+def test_autotune_amr_block_edge():
+    # the AMR tuner times the block edges that divide N0 and returns one of them
+    tuned, lups = J.autotune("amr", steps=2, n=32, re=800.0, l1_mode="all", l2_mode="all", max_gb=4.0)
+    assert tuned["mb"] in (4, 8, 16) and lups > 0

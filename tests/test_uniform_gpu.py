@@ -170,3 +170,18 @@ def test_full_size_512_conserves_mass():
     assert abs(m1 - m0) / m0 < 2e-6                 # FP32 round-off of 20 steps on 1.3e8 cells
     assert e1 < e0
     assert z1 > 0
+
+
+def test_autotune_picks_a_supported_mapping_that_matches_oracle():
+    # the tuner times the candidate (vec, threads/block) pairs and hands back one of them; a solver
+    # built with it steps like the oracle
+    n = 64
+    tuned, lups = J.autotune("uniform", steps=3, n=n, re=1600.0)
+    assert tuned["vec"] in (1, 2, 4, 8) and tuned["threads_per_block"] in (64, 128, 256, 512)
+    assert lups > 0
+    p = O.params(n, 1600.0)
+    with J.Solver("uniform", n=n, re=1600.0, vec=tuned["vec"], threads_per_block=tuned["threads_per_block"]) as s:
+        f0 = s.get_populations(layout="blocked")
+        s.step(2)
+        a = s.get_populations(layout="blocked")
+    assert rel_err(a, O.step(f0, n, 8, p["omega"], 2)) < 1.1e-5
