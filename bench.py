@@ -289,9 +289,9 @@ def precision_run(J, n: int, storage: str, every: int, device: int, tstar: float
 
 
 def bench_precision(J, args, device: int) -> dict:
-    """Storage precision study (configs[1]): FP32, shifted FP16 and BF16 storage against an FP64 run at
-    the same N, Re=1600, t*=12; errors of the enstrophy peak time, the energy curve and the enstrophy
-    curve relative to FP64."""
+    """Storage precision study: FP32, shifted FP16 and BF16 storage against an FP64 run at the same N
+    (256 by default), Re=1600, t*=12; errors of the enstrophy peak time, the energy curve and the
+    enstrophy curve relative to FP64."""
     import numpy as np
 
     n, every = args.n, args.every

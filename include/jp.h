@@ -244,7 +244,7 @@ jp_status jp_get_sensor(jp_solver* s, int32_t level, float* host, int64_t capaci
  * two implementations the same sensor field for bit-exact table comparisons. */
 jp_status jp_set_sensor_override(jp_solver* s, const float* sen0, const float* sen1_by_pos);
 
-/* ---- ensembles and serving (spec extensions; no counterpart in the reference) ------------- */
+/* ---- ensembles and serving (extensions; no counterpart in the reference) ------------- */
 
 /* An ensemble steps many uniform solvers of the same device together: every lattice step is one
  * batched stream-collide launch per storage format (up to 48 cubes of any sizes per launch) on the
@@ -297,7 +297,7 @@ int32_t jp_server_poll(jp_server* sv, jp_result* out, int32_t max);
 /* Seconds since the server was created (the clock of jp_result timestamps). */
 double jp_server_clock(const jp_server* sv);
 
-/* ---- autotuning (spec extension; no counterpart in the reference) ------------------------- */
+/* ---- autotuning (extension; no counterpart in the reference) ------------------------- */
 
 /* Time `steps` steps of each candidate and write the fastest into *cfg: for a uniform solver the
  * thread mapping (cells per thread `vec` x `threads_per_block`), for an AMR solver the block edge

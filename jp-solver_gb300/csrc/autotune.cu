@@ -1,5 +1,5 @@
 // Autotuner: picks the uniform step's thread mapping or the AMR block edge by timing candidates on
-// the device (spec extension; the reference fixes MB and the mapping at compile time).
+// the device (an extension: the reference fixes MB and the mapping at compile time).
 #include <cstring>
 
 #include "jp.h"
