@@ -349,6 +349,8 @@ def main() -> int:
     a = ap.parse_args()
     if a.warmup < 3:
         a.warmup = 3
+    if a.workload == "serve":  # concurrent AMR solves: one hardware queue per stream (before any CUDA call)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     rank, local, world, pg = dist_setup(a.gpus)
     n = a.n
     config = {"workload": "uniform TGV D3Q19 BGK, N=%d, Re=%g, u0=%g, periodic" % (n, RE, U0),

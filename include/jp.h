@@ -73,7 +73,7 @@ typedef struct jp_config {
     int32_t develop_steps;   /* uncounted coarse steps before the first sensor build (300) */
     double max_gb;           /* HBM ceiling for the fine pools in GiB; 0 = 75% of free memory */
     int32_t device;          /* CUDA device ordinal */
-    int32_t threads_per_block; /* 0 = tuned default */
+    int32_t threads_per_block; /* 0 = default; uniform: 64..512; AMR steps: 64 (MB=4), 128/256/512 */
     int32_t vec;             /* cells per thread along x in the uniform step; 0 = tuned default */
     int32_t flags;           /* JP_FLAG_* */
     int32_t reserved[7];
@@ -259,15 +259,20 @@ jp_status jp_ensemble_step(jp_ensemble* e, int64_t nsteps);
 /* A server runs whole Taylor-Green solves (the `uniform` / `amr` programs' runs) for a stream of
  * requests with continuous batching: requests wait in a queue until their HBM estimate fits the
  * pool budget and a slot is free, are admitted between ticks while others run, advance together
- * (uniform solves in batched launches, AMR solves concurrently on their own streams), and leave a
- * result with their diagnostics summary and timestamps when they finish. */
+ * (uniform solves in batched launches issued by jp_server_tick, AMR solves concurrently on worker
+ * threads, each on its own stream), and leave a result with their diagnostics summary and timestamps
+ * when they finish.  Device memory of served solves comes from one stream-ordered pool, so solves
+ * come and go without synchronising the device.  A process that serves many AMR solves at once
+ * should set CUDA_DEVICE_MAX_CONNECTIONS (e.g. 32) before its first CUDA call, so that their
+ * streams do not share the default 8 hardware queues. */
 typedef struct jp_server jp_server;
 typedef struct jp_server_config {
     int32_t device;
     int32_t max_active;      /* slots; 0 = unlimited */
     double pool_gb;          /* HBM budget for admitted solves, GiB (0 = 75% of free memory) */
-    int32_t tick_steps;      /* lattice steps a uniform solve advances per tick (AMR: coarse steps / 4) */
-    int32_t reserved[7];
+    int32_t tick_steps;      /* lattice steps the uniform solves advance per tick (default 64) */
+    int32_t workers;         /* host threads running AMR solves, one solve each (0 = one per core, 4..32) */
+    int32_t reserved[6];
 } jp_server_config;
 typedef struct jp_request {
     int64_t id;
@@ -301,9 +306,10 @@ double jp_server_clock(const jp_server* sv);
 
 /* Time `steps` steps of each candidate and write the fastest into *cfg: for a uniform solver the
  * thread mapping (cells per thread `vec` x `threads_per_block`), for an AMR solver the block edge
- * `mb` in {4, 8, 16} dividing n (the reference fixes MB at compile time; MB=16 cannot run there, its
- * kernels would need 4096 threads per block).  *best receives the winner's lattice updates per second
- * (AMR: work-normalised, (cnb0 + 2 nf1 + 4 nf2) MB^3 per coarse step). */
+ * `mb` in {4, 8, 16} dividing n and the threads per CTA of its level steps (`threads_per_block`
+ * 64 at MB=4, else 128, 256 or 512; the reference fixes MB at compile time and MB=16 cannot run
+ * there, its kernels would need 4096 threads per block).  *best receives the winner's lattice
+ * updates per second (AMR: work-normalised, (cnb0 + 2 nf1 + 4 nf2) MB^3 per coarse step). */
 jp_status jp_autotune(jp_config* cfg, int32_t steps, double* best);
 
 /* ---- measurement ---------------------------------------------------------------------------- */

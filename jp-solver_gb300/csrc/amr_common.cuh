@@ -124,6 +124,88 @@ __device__ __forceinline__ void bgk(float (&f)[Q], float om) {
     for (int q = 0; q < Q; ++q) f[q] = f[q] - om * (f[q] - feq_ref(q, rho, ux, uy, uz));
 }
 
+// The same BGK collide with the arithmetic of the uniform stream-collide: one reciprocal of rho,
+// out = (1 - omega) f + omega feq with omega*w*rho folded per weight class and
+// feq_pm = w rho (1 - 1.5|u|^2 + 4.5 a^2) +- 3 w rho a for a = c.u over the non-zero terms only.
+// Agrees with bgk() to FP32 round-off (a few ulp per population).
+__device__ __forceinline__ void bgk_fast(float (&f)[Q], float om) {
+    float sm = f[0];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) sm += f[q];
+    const float jx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+    const float jy = f[3] - f[4] + f[7] - f[8] - f[9] + f[10] + f[15] - f[16] + f[17] - f[18];
+    const float jz = f[5] - f[6] + f[11] - f[12] - f[13] + f[14] + f[15] - f[16] - f[17] + f[18];
+    const float inv = 1.f / sm;
+    const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+    const float base = 1.f - 1.5f * (ux * ux + uy * uy + uz * uz);
+    const float omc = 1.f - om, orho = om * sm;
+    const float owr1 = orho * wf(1), owr2 = orho * wf(7), owr3a = 3.f * owr1, owr3b = 3.f * owr2;
+    f[0] = omc * f[0] + orho * wf(0) * base;
+#pragma unroll
+    for (int q = 1; q < Q; q += 2) {
+        const float a = cdot<float>(q, ux, uy, uz);
+        const float t = (q < 7 ? owr1 : owr2) * (4.5f * a * a + base);
+        const float as = (q < 7 ? owr3a : owr3b) * a;
+        f[q] = omc * f[q] + (t + as);
+        f[q + 1] = omc * f[q + 1] + (t - as);
+    }
+}
+
+// Where population q of cell (i, j, k) is pulled from: the neighbour slot e = (dz+1)*9 + (dy+1)*3 +
+// (dx+1) of the same-level block at offset (dx, dy, dz) (13: the block itself) and the cell sc inside
+// that block.  MB is a power of two, so sc is the pulled coordinate masked by MB-1; with q unrolled,
+// which offsets a population can reach is known at compile time.
+template <int MB>
+__host__ __device__ __forceinline__ void pull_src(int q, int i, int j, int k, int& e, int& sc) {
+    constexpr int M = MB - 1;
+    static_assert((MB & M) == 0, "MB must be a power of two");
+    const int li = i - cx(q), lj = j - cy(q), lk = k - cz(q);
+    const int ex = cx(q) > 0 ? (li < 0 ? 0 : 1) : (cx(q) < 0 ? (li > M ? 2 : 1) : 1);
+    const int ey = cy(q) > 0 ? (lj < 0 ? 0 : 1) : (cy(q) < 0 ? (lj > M ? 2 : 1) : 1);
+    const int ez = cz(q) > 0 ? (lk < 0 ? 0 : 1) : (cz(q) < 0 ? (lk > M ? 2 : 1) : 1);
+    e = ez * 9 + ey * 3 + ex;
+    sc = ((lk & M) * MB + (lj & M)) * MB + (li & M);
+}
+
+#ifdef __CUDACC__
+// The pull of the 19 populations of cell (i, j, k) of pool block b in two halves: pull_own loads
+// the values that come from b itself (it needs no table), pull_nbr the rest.  nb[e] is the pool
+// index of the same-level neighbour in slot e (pull_src), or -1 where that neighbour is not on this
+// level; then the value comes from b's ghost shell gh (GHOST = false: every neighbour exists).
+template <int MB>
+__device__ __forceinline__ void pull_own(const float* __restrict__ fa, int b, int i, int j, int k, float (&f)[Q]) {
+    constexpr int MB3 = MB * MB * MB;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        int e, sc;
+        pull_src<MB>(q, i, j, k, e, sc);
+        if (e == 13) f[q] = __ldg(fa + ((size_t)b * Q + q) * MB3 + sc);
+    }
+}
+template <int MB, bool GHOST>
+__device__ __forceinline__ void pull_nbr(const float* __restrict__ fa, const float* __restrict__ gh, const int* nb,
+                                         int b, int i, int j, int k, float (&f)[Q]) {
+    constexpr int MB3 = MB * MB * MB, SH = Geo<MB>::SH;
+#pragma unroll
+    for (int q = 1; q < Q; ++q) {
+        int e, sc;
+        pull_src<MB>(q, i, j, k, e, sc);
+        if (e == 13) continue;
+        const int blk = nb[e];
+        if (!GHOST || blk >= 0) {
+            f[q] = __ldg(fa + ((size_t)blk * Q + q) * MB3 + sc);
+        } else {
+            f[q] = __ldg(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(i - cx(q), j - cy(q), k - cz(q)));
+        }
+    }
+}
+// Neighbour slot of a ghost-shell cell at block-local (i, j, k), each in [-1, MB].
+template <int MB>
+__device__ __forceinline__ int shell_slot(int i, int j, int k) {
+    return (k < 0 ? 0 : (k >= MB ? 2 : 1)) * 9 + (j < 0 ? 0 : (j >= MB ? 2 : 1)) * 3 + (i < 0 ? 0 : (i >= MB ? 2 : 1));
+}
+#endif
+
 // Trilinear weights of the cell-centred 2:1 prolongation: fine index g maps to the parent position
 // (g+0.5)/2-0.5, so the lower parent is floor of that and the weight of the upper one is 0.25 or
 // 0.75 (src/tgv3d_amr.cu:71-73).  Both are exact in float.

@@ -1,7 +1,7 @@
 // AMR level kernels: coarse step, prolongation sources ("prep"), ghost-shell fill, fine steps,
 // restriction, seeding and migration, sensor and the composite macro field.
 // Reference: src/tgv3d_amr.cu:69-453, 514-536.  One CTA per block; a thread owns one cell (MB<=8)
-// or several (MB=16).  Arithmetic follows the reference's expressions so results agree within
+// or several (MB=16), and the steps take 128, 256 or 512 threads per CTA at MB = 8 and 16.  Arithmetic follows the reference's expressions so results agree within
 // round-off; loop orders of the trilinear and the 8-child average are the reference's.
 #include "amr_common.cuh"
 #include "amr_kernels.h"
@@ -29,29 +29,33 @@ __global__ void __launch_bounds__(Geo<MB>::TPB) k_init(float* __restrict__ f, in
 }
 
 // ---- dense periodic coarse step (src/tgv3d_amr.cu:203-220) ---------------------------------------
-template <int MB>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l0(const float* __restrict__ fa, float* __restrict__ fb, int cgx,
-                                                         int N, float om) {
+template <int MB, int TPB>
+__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const float* __restrict__ fa, float* __restrict__ fb, int cgx,
+                                                 float om) {
     using G = Geo<MB>;
     const int b = blockIdx.x;
     const int bx = b % cgx, by = (b / cgx) % cgx, bz = b / (cgx * cgx);
-    CELL_LOOP(cell) {
-        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-        const int gi = bx * MB + i, gj = by * MB + j, gk = bz * MB + k;
-        float f[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            int si = gi - cx(q), sj = gj - cy(q), sk = gk - cz(q);
-            si += si < 0 ? N : (si >= N ? -N : 0);
-            sj += sj < 0 ? N : (sj >= N ? -N : 0);
-            sk += sk < 0 ? N : (sk >= N ? -N : 0);
-            const int sb = ((sk / MB) * cgx + sj / MB) * cgx + si / MB;
-            const int sc = ((sk % MB) * MB + sj % MB) * MB + si % MB;
-            f[q] = __ldg(fa + ((size_t)sb * Q + q) * G::MB3 + sc);
-        }
-        bgk(f, om);
+    __shared__ int snb[27];  // periodic neighbour blocks
+    if (threadIdx.x < 27) {
+        const int dx = threadIdx.x % 3 - 1, dy = (threadIdx.x / 3) % 3 - 1, dz = threadIdx.x / 9 - 1;
+        snb[threadIdx.x] = (((bz + dz + cgx) % cgx) * cgx + (by + dy + cgx) % cgx) * cgx + (bx + dx + cgx) % cgx;
+    }
+    int cell = threadIdx.x;
+    int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+    float f[Q];
+    pull_own<MB>(fa, b, i, j, k, f);
+    __syncthreads();
+    for (;;) {
+        pull_nbr<MB, false>(fa, nullptr, snb, b, i, j, k, f);
+        bgk_fast(f, om);
 #pragma unroll
         for (int q = 0; q < Q; ++q) fb[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
+        cell += TPB;
+        if (cell >= G::MB3) break;
+        i = cell % MB;
+        j = (cell / MB) % MB;
+        k = cell / (MB * MB);
+        pull_own<MB>(fa, b, i, j, k, f);
     }
 }
 
@@ -130,14 +134,17 @@ __device__ __forceinline__ void prolong_prep_l1(const float* __restrict__ pr, co
 }
 
 // ---- ghost shells (src/tgv3d_amr.cu:173-202) -------------------------------------------------------
-// One CTA per fine block, one thread per shell cell; a shell cell whose source parent block is
-// refined is left alone (the step gathers it from the same level instead).
+// One CTA per fine block, one thread per shell cell; a shell cell whose same-level neighbour block
+// exists (its parent is refined) is left alone: the step gathers it from that block instead.
 template <int MB>
 __global__ void __launch_bounds__(256) k_fill_l1(const float* __restrict__ pr, float* __restrict__ gh,
                                                 const int* __restrict__ pcb, const int* __restrict__ poct,
-                                                const int* __restrict__ ref0, int cgx, int N) {
+                                                const int* __restrict__ nbtab, int cgx, int N) {
     using G = Geo<MB>;
     const int fb = blockIdx.x;
+    __shared__ int snb[27];
+    if (threadIdx.x < 27) snb[threadIdx.x] = __ldg(nbtab + (size_t)fb * 27 + threadIdx.x);
+    __syncthreads();
     const int cb = pcb[fb], oct = poct[fb];
     const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
     const int ox = cbx * 2 * MB + (oct & 1) * MB, oy = cby * 2 * MB + ((oct >> 1) & 1) * MB, oz = cbz * 2 * MB + (oct >> 2) * MB;
@@ -145,9 +152,8 @@ __global__ void __launch_bounds__(256) k_fill_l1(const float* __restrict__ pr, f
     for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
+        if (snb[shell_slot<MB>(i, j, k)] >= 0) continue;
         const int gfi = pmod(ox + i, N1), gfj = pmod(oy + j, N1), gfk = pmod(oz + k, N1);
-        const int scb = ((gfk / (2 * MB)) * cgx + gfj / (2 * MB)) * cgx + gfi / (2 * MB);
-        if (__ldg(ref0 + scb)) continue;
         float out[Q];
         prolong_prep_l0<MB>(pr, cgx, N, gfi, gfj, gfk, out);
 #pragma unroll
@@ -159,9 +165,12 @@ template <int MB>
 __global__ void __launch_bounds__(256) k_fill_l2(const float* __restrict__ pr, float* __restrict__ gh,
                                                 const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
                                                 const int* __restrict__ f1pos, const int* __restrict__ l1grid,
-                                                const int* __restrict__ ref1, int l1gx, int N1) {
+                                                const int* __restrict__ nbtab, int l1gx, int N1) {
     using G = Geo<MB>;
     const int b = blockIdx.x;
+    __shared__ int snb[27];
+    if (threadIdx.x < 27) snb[threadIdx.x] = __ldg(nbtab + (size_t)b * 27 + threadIdx.x);
+    __syncthreads();
     const int pl1 = l2pl1[b], oct = l2oct[b];
     const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
     const int ox = px * 2 * MB + (oct & 1) * MB, oy = py * 2 * MB + ((oct >> 1) & 1) * MB, oz = pz * 2 * MB + (oct >> 2) * MB;
@@ -169,9 +178,8 @@ __global__ void __launch_bounds__(256) k_fill_l2(const float* __restrict__ pr, f
     for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
+        if (snb[shell_slot<MB>(i, j, k)] >= 0) continue;
         const int g2i = pmod(ox + i, N2), g2j = pmod(oy + j, N2), g2k = pmod(oz + k, N2);
-        const int lb = __ldg(l1grid + ((g2k / (2 * MB)) * l1gx + g2j / (2 * MB)) * l1gx + g2i / (2 * MB));
-        if (lb >= 0 && __ldg(ref1 + lb)) continue;
         float out[Q];
         prolong_prep_l1<MB>(pr, l1grid, l1gx, N1, g2i, g2j, g2k, out);
 #pragma unroll
@@ -214,134 +222,80 @@ __device__ __forceinline__ void restrict_octant(const float* __restrict__ sf, fl
     }
 }
 
-// ---- fine steps (src/tgv3d_amr.cu:241-274, 331-356) -----------------------------------------------
-// Level 1: the 27 coarse neighbours of the parent say whether a pulled cell lives on level 1 (gather
-// from its block) or not (read the ghost shell).  FUSE: this is the last substep before the
-// restriction into the coarse level, so the block also restricts itself into its parent octant
-// (saves re-reading the level from HBM in a separate restriction kernel).
-template <int MB, bool FUSE>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l1(const float* __restrict__ fa, float* __restrict__ fbuf,
-                                                         const float* __restrict__ gh, const int* __restrict__ pcb,
-                                                         const int* __restrict__ poct, const int* __restrict__ ref0,
-                                                         const int* __restrict__ fof0, int cgx, int N, float om,
-                                                         float* __restrict__ parent_pool, float nqi) {
-    extern __shared__ float sf[];
-    using G = Geo<MB>;
-    const int b = blockIdx.x;
-    const int cb = pcb[b], oct = poct[b];
+// ---- same-level neighbour tables -----------------------------------------------------------------
+// nb[b*27 + e] = pool index of the same-level block at offset slot e (pull_src) of fine block b, or
+// -1 where that neighbour is not on the block's level (its cells come from the ghost shell).  Built
+// once per grid change, so the steps and fills read one table instead of walking the block tables.
+__global__ void k_nbtab_l1(int* __restrict__ nb, const int* __restrict__ pcb, const int* __restrict__ poct,
+                           const int* __restrict__ ref0, const int* __restrict__ fof0, int cgx, int nf1) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 27LL * nf1) return;
+    const int b = int(idx / 27), e = int(idx % 27);
+    const int cb = pcb[b], oct = poct[b], l1gx = 2 * cgx;
     const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
-    __shared__ int sfof[27];  // fine block base of each coarse neighbour, -1 if not refined
-    if (threadIdx.x < 27) {
-        const int dx = threadIdx.x % 3 - 1, dy = (threadIdx.x / 3) % 3 - 1, dz = threadIdx.x / 9 - 1;
-        const int nx = (cbx + dx + cgx) % cgx, ny = (cby + dy + cgx) % cgx, nz = (cbz + dz + cgx) % cgx;
-        const int ncb = (nz * cgx + ny) * cgx + nx;
-        sfof[threadIdx.x] = ref0[ncb] ? fof0[ncb] : -1;
-    }
-    __syncthreads();
-    const int ox = cbx * 2 * MB + (oct & 1) * MB, oy = cby * 2 * MB + ((oct >> 1) & 1) * MB, oz = cbz * 2 * MB + (oct >> 2) * MB;
-    const int N1 = 2 * N;
-    CELL_LOOP(cell) {
-        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-        float f[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            const int li = i - cx(q), lj = j - cy(q), lk = k - cz(q);
-            if (li >= 0 && li < MB && lj >= 0 && lj < MB && lk >= 0 && lk < MB) {
-                f[q] = __ldg(fa + ((size_t)b * Q + q) * G::MB3 + (lk * MB + lj) * MB + li);
-                continue;
-            }
-            int sfi = ox + li, sfj = oy + lj, sfk = oz + lk;
-            sfi += sfi < 0 ? N1 : (sfi >= N1 ? -N1 : 0);
-            sfj += sfj < 0 ? N1 : (sfj >= N1 ? -N1 : 0);
-            sfk += sfk < 0 ? N1 : (sfk >= N1 ? -N1 : 0);
-            int ddx = sfi / (2 * MB) - cbx, ddy = sfj / (2 * MB) - cby, ddz = sfk / (2 * MB) - cbz;
-            if (ddx > 1) ddx -= cgx; else if (ddx < -1) ddx += cgx;
-            if (ddy > 1) ddy -= cgx; else if (ddy < -1) ddy += cgx;
-            if (ddz > 1) ddz -= cgx; else if (ddz < -1) ddz += cgx;
-            const int base = sfof[(ddz + 1) * 9 + (ddy + 1) * 3 + (ddx + 1)];
-            if (base >= 0) {
-                const int sq = (((sfk % (2 * MB)) / MB) * 4 + ((sfj % (2 * MB)) / MB) * 2 + (sfi % (2 * MB)) / MB);
-                const int sc = ((sfk % MB) * MB + sfj % MB) * MB + sfi % MB;
-                f[q] = __ldg(fa + ((size_t)(base + sq) * Q + q) * G::MB3 + sc);
-            } else {
-                f[q] = __ldg(gh + ((size_t)b * Q + q) * G::SH + shell_index<MB>(li, lj, lk));
-            }
-        }
-        bgk(f, om);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
-            if (FUSE) sf[q * G::MB3 + cell] = f[q];
-        }
-    }
-    if (FUSE) {
-        __syncthreads();
-        restrict_octant<MB>(sf, parent_pool + (size_t)cb * Q * G::MB3, oct, nqi);
-    }
+    const int dx = e % 3 - 1, dy = (e / 3) % 3 - 1, dz = e / 9 - 1;
+    const int nx = (2 * cbx + (oct & 1) + dx + l1gx) % l1gx, ny = (2 * cby + ((oct >> 1) & 1) + dy + l1gx) % l1gx,
+              nz = (2 * cbz + (oct >> 2) + dz + l1gx) % l1gx;
+    const int ncb = ((nz >> 1) * cgx + (ny >> 1)) * cgx + (nx >> 1);
+    nb[idx] = ref0[ncb] ? fof0[ncb] + ((nz & 1) * 4 + (ny & 1) * 2 + (nx & 1)) : -1;
 }
 
-// Level 2: the level-1 grid map says where a pulled cell lives.  FUSE as for level 1, into the
-// parent level-1 block.
-template <int MB, bool FUSE>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_step_l2(const float* __restrict__ fa, float* __restrict__ fbuf,
-                                                         const float* __restrict__ gh, const int* __restrict__ l2pl1,
-                                                         const int* __restrict__ l2oct, const int* __restrict__ f1pos,
-                                                         const int* __restrict__ l1grid, const int* __restrict__ ref1,
-                                                         const int* __restrict__ fof1, int l1gx, int N1, float om,
-                                                         float* __restrict__ parent_pool, float nqi) {
+__global__ void k_nbtab_l2(int* __restrict__ nb, const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
+                           const int* __restrict__ f1pos, const int* __restrict__ l1grid, const int* __restrict__ ref1,
+                           const int* __restrict__ fof1, int l1gx, int nf2) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 27LL * nf2) return;
+    const int b = int(idx / 27), e = int(idx % 27);
+    const int oct = l2oct[b], p = f1pos[l2pl1[b]], g2 = 2 * l1gx;
+    const int px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
+    const int dx = e % 3 - 1, dy = (e / 3) % 3 - 1, dz = e / 9 - 1;
+    const int nx = (2 * px + (oct & 1) + dx + g2) % g2, ny = (2 * py + ((oct >> 1) & 1) + dy + g2) % g2,
+              nz = (2 * pz + (oct >> 2) + dz + g2) % g2;
+    const int lb = l1grid[((nz >> 1) * l1gx + (ny >> 1)) * l1gx + (nx >> 1)];
+    nb[idx] = (lb >= 0 && ref1[lb]) ? fof1[lb] + ((nz & 1) * 4 + (ny & 1) * 2 + (nx & 1)) : -1;
+}
+
+// ---- fine steps (src/tgv3d_amr.cu:241-274, 331-356) -----------------------------------------------
+// One kernel for both fine levels: the neighbour table says, per offset, which pool block holds the
+// pulled cells or that they come from the ghost shell.  The CTA issues its own-block loads for its
+// first cells while the table is read, then the neighbour loads.  TPB threads share the block's
+// MB^3 cells.  FUSE: this is the last substep before the restriction into the parent level, so the
+// block also restricts itself into its parent octant (`parent`, `poct`), which saves re-reading the
+// level from HBM in a separate restriction kernel.
+template <int MB, int TPB, bool FUSE>
+__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_fine(const float* __restrict__ fa, float* __restrict__ fbuf,
+                                                   const float* __restrict__ gh, const int* __restrict__ nbtab,
+                                                   const int* __restrict__ parent, const int* __restrict__ poct,
+                                                   float om, float* __restrict__ parent_pool, float nqi) {
+    static_assert(Geo<MB>::MB3 % TPB == 0, "cells must split evenly over the CTA");
     extern __shared__ float sf[];
     using G = Geo<MB>;
     const int b = blockIdx.x;
-    const int pl1 = l2pl1[b], oct = l2oct[b];
-    const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
-    const int ox = px * 2 * MB + (oct & 1) * MB, oy = py * 2 * MB + ((oct >> 1) & 1) * MB, oz = pz * 2 * MB + (oct >> 2) * MB;
-    // fine-block base of the 27 level-1 grid neighbours of the parent (-1: not on level 2)
-    __shared__ int sbase[27];
-    if (threadIdx.x < 27) {
-        const int dx = threadIdx.x % 3 - 1, dy = (threadIdx.x / 3) % 3 - 1, dz = threadIdx.x / 9 - 1;
-        const int nx = (px + dx + l1gx) % l1gx, ny = (py + dy + l1gx) % l1gx, nz = (pz + dz + l1gx) % l1gx;
-        const int lb = l1grid[(nz * l1gx + ny) * l1gx + nx];
-        sbase[threadIdx.x] = (lb >= 0 && ref1[lb]) ? fof1[lb] : -1;
-    }
+    __shared__ int snb[27];
+    if (threadIdx.x < 27) snb[threadIdx.x] = __ldg(nbtab + (size_t)b * 27 + threadIdx.x);
+    int cell = threadIdx.x;
+    int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+    float f[Q];
+    pull_own<MB>(fa, b, i, j, k, f);
     __syncthreads();
-    const int N2 = 2 * N1;
-    CELL_LOOP(cell) {
-        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-        float f[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            const int li = i - cx(q), lj = j - cy(q), lk = k - cz(q);
-            if (li >= 0 && li < MB && lj >= 0 && lj < MB && lk >= 0 && lk < MB) {
-                f[q] = __ldg(fa + ((size_t)b * Q + q) * G::MB3 + (lk * MB + lj) * MB + li);
-                continue;
-            }
-            int sfi = ox + li, sfj = oy + lj, sfk = oz + lk;
-            sfi += sfi < 0 ? N2 : (sfi >= N2 ? -N2 : 0);
-            sfj += sfj < 0 ? N2 : (sfj >= N2 ? -N2 : 0);
-            sfk += sfk < 0 ? N2 : (sfk >= N2 ? -N2 : 0);
-            int ddx = sfi / (2 * MB) - px, ddy = sfj / (2 * MB) - py, ddz = sfk / (2 * MB) - pz;
-            if (ddx > 1) ddx -= l1gx; else if (ddx < -1) ddx += l1gx;
-            if (ddy > 1) ddy -= l1gx; else if (ddy < -1) ddy += l1gx;
-            if (ddz > 1) ddz -= l1gx; else if (ddz < -1) ddz += l1gx;
-            const int base = sbase[(ddz + 1) * 9 + (ddy + 1) * 3 + (ddx + 1)];
-            if (base >= 0) {
-                const int sq = (((sfk % (2 * MB)) / MB) * 4 + ((sfj % (2 * MB)) / MB) * 2 + (sfi % (2 * MB)) / MB);
-                const int sc = ((sfk % MB) * MB + sfj % MB) * MB + sfi % MB;
-                f[q] = __ldg(fa + ((size_t)(base + sq) * Q + q) * G::MB3 + sc);
-            } else {
-                f[q] = __ldg(gh + ((size_t)b * Q + q) * G::SH + shell_index<MB>(li, lj, lk));
-            }
-        }
-        bgk(f, om);
+    for (;;) {
+        pull_nbr<MB, true>(fa, gh, snb, b, i, j, k, f);
+        bgk_fast(f, om);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
             if (FUSE) sf[q * G::MB3 + cell] = f[q];
         }
+        cell += TPB;
+        if (cell >= G::MB3) break;
+        i = cell % MB;
+        j = (cell / MB) % MB;
+        k = cell / (MB * MB);
+        pull_own<MB>(fa, b, i, j, k, f);
     }
     if (FUSE) {
         __syncthreads();
-        restrict_octant<MB>(sf, parent_pool + (size_t)pl1 * Q * G::MB3, oct, nqi);
+        restrict_octant<MB>(sf, parent_pool + (size_t)parent[b] * Q * G::MB3, poct[b], nqi);
     }
 }
 
@@ -592,6 +546,26 @@ __global__ void __launch_bounds__(256) k_composite(const float* __restrict__ c0,
 
 // ---- launchers ------------------------------------------------------------------------------------
 
+// the steps with TPB threads per CTA (the block's MB^3 cells split evenly)
+template <int MB, int TPB>
+static void launch_steps(const AmrLaunch& L, int op) {
+    using G = Geo<MB>;
+    if (op == OP_STEP_L0) {
+        k_step_l0<MB, TPB><<<L.nblocks, TPB, 0, L.st>>>(L.in, L.out, L.cgx, L.omega);
+        return;
+    }
+    const int* parent = L.t0;  // pcb (level 1) or l2pl1 (level 2)
+    if constexpr (MB <= 8) {
+        if (L.out2) {
+            k_step_fine<MB, TPB, true><<<L.nblocks, TPB, sizeof(float) * Q * G::MB3, L.st>>>(
+                L.in, L.out, L.aux, L.nbt, parent, L.t1, L.omega, L.out2, L.scale);
+            return;
+        }
+    }
+    k_step_fine<MB, TPB, false><<<L.nblocks, TPB, 0, L.st>>>(L.in, L.out, L.aux, L.nbt, parent, L.t1, L.omega,
+                                                             nullptr, 0.f);
+}
+
 template <int MB>
 static cudaError_t dispatch(const AmrLaunch& L, int op) {
     using G = Geo<MB>;
@@ -602,32 +576,36 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
             k_init<MB><<<L.nblocks, cta, 0, L.st>>>(L.out, L.cgx, L.u0, L.kf);
             break;
         case OP_STEP_L0:
-            k_step_l0<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.cgx, L.n, L.omega);
+        case OP_STEP_L1:
+        case OP_STEP_L2: {
+            const int tpb = L.tpb ? L.tpb : G::TPB;
+            if constexpr (MB == 4) {
+                if (tpb != 64) return cudaErrorInvalidConfiguration;
+                launch_steps<MB, 64>(L, op);
+            } else {
+                if (tpb == 128) launch_steps<MB, 128>(L, op);
+                else if (tpb == 256) launch_steps<MB, 256>(L, op);
+                else if (tpb == 512) launch_steps<MB, 512>(L, op);
+                else return cudaErrorInvalidConfiguration;
+            }
+            break;
+        }
+        case OP_NBTAB_L1:
+            k_nbtab_l1<<<(unsigned)((27LL * L.nblocks + 255) / 256), 256, 0, L.st>>>(L.iout, L.t0, L.t1, L.t2, L.t3,
+                                                                                  L.cgx, L.nblocks);
+            break;
+        case OP_NBTAB_L2:
+            k_nbtab_l2<<<(unsigned)((27LL * L.nblocks + 255) / 256), 256, 0, L.st>>>(L.iout, L.t0, L.t1, L.t2, L.t3,
+                                                                                  L.t4, L.t5, L.l1gx, L.nblocks);
             break;
         case OP_PREP:
             k_prep<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.list, L.scale);
             break;
         case OP_FILL_L1:
-            k_fill_l1<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.t2, L.cgx, L.n);
+            k_fill_l1<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.nbt, L.cgx, L.n);
             break;
         case OP_FILL_L2:
-            k_fill_l2<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.t2, L.t3, L.t4, L.l1gx, L.n1);
-            break;
-        case OP_STEP_L1:
-            if (L.out2 && MB <= 8)
-                k_step_l1<MB, true><<<L.nblocks, cta, sizeof(float) * Q * G::MB3, L.st>>>(
-                    L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.cgx, L.n, L.omega, L.out2, L.scale);
-            else
-                k_step_l1<MB, false><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.cgx,
-                                                                  L.n, L.omega, nullptr, 0.f);
-            break;
-        case OP_STEP_L2:
-            if (L.out2 && MB <= 8)
-                k_step_l2<MB, true><<<L.nblocks, cta, sizeof(float) * Q * G::MB3, L.st>>>(
-                    L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.t4, L.t5, L.l1gx, L.n1, L.omega, L.out2, L.scale);
-            else
-                k_step_l2<MB, false><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.t4,
-                                                                  L.t5, L.l1gx, L.n1, L.omega, nullptr, 0.f);
+            k_fill_l2<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.t2, L.t3, L.nbt, L.l1gx, L.n1);
             break;
         case OP_RESTRICT:
             k_restrict<MB><<<L.nblocks, cta, 0, L.st>>>(L.out, L.in, L.list, L.t0, L.scale);
@@ -667,6 +645,10 @@ cudaError_t amr_launch(int mb, int op, const AmrLaunch& L) {
 
 int shell_cells(int mb) { return 6 * mb * mb + 12 * mb; }
 bool can_fuse_restrict(int mb) { return mb <= 8; }
+bool step_tpb_supported(int mb, int tpb) {
+    if (mb == 4) return tpb == 64;
+    return (mb == 8 || mb == 16) && (tpb == 128 || tpb == 256 || tpb == 512);
+}
 
 }  // namespace amr
 }  // namespace jp

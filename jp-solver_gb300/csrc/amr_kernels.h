@@ -9,17 +9,19 @@ enum AmrOp {
     OP_INIT = 0,       // out = TGV state of the coarse grid
     OP_STEP_L0,        // in -> out, dense periodic coarse step
     OP_PREP,           // out[list] = prolongation source of in[list]; scale = nqs
-    OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, t2 ref0
-    OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, t4 ref1
-    OP_STEP_L1,        // in -> out, aux = gh1; t0 pcb, t1 oct, t2 ref0, t3 fof0; out2 = c0 restricts (scale nqi)
-    OP_STEP_L2,        // in -> out, aux = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, t4 ref1, t5 fof1;
-                       // out2 = f1 restricts (scale nqi)
+    OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, nbt = level-1 neighbour table
+    OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, nbt = level-2 table
+    OP_STEP_L1,        // in -> out, aux = gh1, nbt = level-1 table; t0 pcb, t1 oct; out2 = c0 restricts (scale nqi)
+    OP_STEP_L2,        // in -> out, aux = gh2, nbt = level-2 table; t0 l2pl1, t1 l2oct; out2 = f1 restricts
     OP_RESTRICT,       // out = coarse, in = fine; list = refined coarse blocks, t0 = fof; scale = nqi
     OP_SEED_L1,        // in = old f1 (migrate) , out = new f1, aux = c0; t0 pcb, t1 oct, t2 old ref0|null, t3 old fof0
     OP_SEED_L2,        // in = old f2, out = new f2, aux = f1; t0 l2pl1, t1 l2oct, t2 f1pos, t3 old l1grid|null,
                        // t4 old ref1, t5 old fof1, t6 l1grid
     OP_SENSOR,         // in = level, out = sensor; aux = override values|null, t0 = override position map|null
-    OP_COMPOSITE       // in = c0, aux = f1, aux2 = f2, out = field; t0 ref1, t1 fof1, t2 l1grid
+    OP_COMPOSITE,      // in = c0, aux = f1, aux2 = f2, out = field; t0 ref1, t1 fof1, t2 l1grid
+    OP_NBTAB_L1,       // iout = level-1 neighbour table (nblocks = nf1); t0 pcb, t1 oct, t2 ref0, t3 fof0
+    OP_NBTAB_L2        // iout = level-2 neighbour table (nblocks = nf2); t0 l2pl1, t1 l2oct, t2 f1pos,
+                       // t3 l1grid, t4 ref1, t5 fof1
 };
 
 struct AmrLaunch {
@@ -32,6 +34,9 @@ struct AmrLaunch {
     const float* aux2 = nullptr;
     const int* list = nullptr;
     const int *t0 = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr, *t6 = nullptr;
+    const int* nbt = nullptr;  // same-level neighbour table of the fine level (27 per block)
+    int* iout = nullptr;
+    int tpb = 0;               // threads per CTA of the steps (0: min(MB^3, 512))
     int cgx = 0, n = 0, l1gx = 0, n1 = 0, n2 = 0;
     float omega = 0.f, scale = 0.f;
     double u0 = 0.0, kf = 0.0;
@@ -41,6 +46,8 @@ cudaError_t amr_launch(int mb, int op, const AmrLaunch& L);
 int shell_cells(int mb);
 // the fused restriction stages a block in shared memory: MB <= 8 (38 KiB at MB = 8)
 bool can_fuse_restrict(int mb);
+// threads per CTA a step of block edge mb can run with
+bool step_tpb_supported(int mb, int tpb);
 
 // ---- adaptation pipeline (adapt.cu) ------------------------------------------------------------
 // Device counters shared by the pipeline; the host reads them once per stage.

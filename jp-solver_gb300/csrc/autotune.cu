@@ -1,6 +1,7 @@
 // Autotuner: picks the uniform step's thread mapping or the AMR block edge by timing candidates on
 // the device (an extension: the reference fixes MB and the mapping at compile time).
 #include <cstring>
+#include <vector>
 
 #include "jp.h"
 #include "kernels.h"
@@ -49,31 +50,40 @@ extern "C" jp_status jp_autotune(jp_config* cfg, int32_t steps, double* best) {
         cfg->threads_per_block = bt;
         return JP_OK;
     }
-    // AMR: block edges that divide n; work-normalised throughput of the 1:2:4 step
+    // AMR: block edges that divide n x threads per CTA of the level steps; work-normalised
+    // throughput of the 1:2:4 step on the grid each edge builds
     const int mbs[3] = {4, 8, 16};
-    int bmb = cfg->mb;
+    int bmb = cfg->mb, btpb = cfg->threads_per_block;
     for (int mb : mbs) {
         if (cfg->n % mb) continue;
         jp_config c = *cfg;
         c.mb = mb;
+        c.threads_per_block = 0;
         jp_solver* s = nullptr;
         jp_status st = jp_create(&c, &s);
         if (st == JP_ERR_NOMEM || st == JP_ERR_CAPACITY) continue;
         if (st != JP_OK) return st;
-        float ms = 0.f;
-        st = jp_step(s, 1);
-        if (st == JP_OK) st = jp_step_timed(s, steps, &ms);
         jp_amr_counts k;
-        if (st == JP_OK) st = jp_amr_get_counts(s, &k);
+        st = jp_amr_get_counts(s, &k);
+        const double work = (double(k.cnb0) + 2.0 * k.nf1 + 4.0 * k.nf2) * double(mb) * mb * mb * steps;
+        const int tpbs[3] = {128, 256, 512};
+        for (int t : (mb == 4 ? std::vector<int>{64} : std::vector<int>(tpbs, tpbs + 3))) {
+            float ms = 0.f;
+            if (st == JP_OK) st = amr_set_step_tpb(s, t);
+            if (st == JP_OK) st = jp_step(s, 1);
+            if (st == JP_OK) st = jp_step_timed(s, steps, &ms);
+            if (st != JP_OK) break;
+            const double lups = work / (double(ms) * 1e-3);
+            if (lups > *best) {
+                *best = lups;
+                bmb = mb;
+                btpb = t;
+            }
+        }
         jp_destroy(s);
         if (st != JP_OK) return st;
-        const double work = (double(k.cnb0) + 2.0 * k.nf1 + 4.0 * k.nf2) * double(mb) * mb * mb * steps;
-        const double lups = work / (double(ms) * 1e-3);
-        if (lups > *best) {
-            *best = lups;
-            bmb = mb;
-        }
     }
     cfg->mb = bmb;
+    cfg->threads_per_block = btpb;
     return JP_OK;
 }

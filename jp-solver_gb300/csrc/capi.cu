@@ -87,6 +87,29 @@ using namespace jp;
 
 // ------------------------------------------------------------------------------------------------
 
+jp_status jp::create_solver(const jp_config* cfg, cudaMemPool_t pool, jp_solver** out) {
+    if (!cfg || !out) return fail(JP_ERR_INVALID, "jp_create: null argument");
+    *out = nullptr;
+    if (cfg->kind != JP_UNIFORM && cfg->kind != JP_AMR) return fail(JP_ERR_INVALID, "unknown solver kind %d", cfg->kind);
+    if (cfg->storage < 0 || cfg->storage > 3) return fail(JP_ERR_INVALID, "unknown storage %d", cfg->storage);
+    if (cfg->mb != 4 && cfg->mb != 8 && cfg->mb != 16) return fail(JP_ERR_INVALID, "mb must be 4, 8 or 16 (got %d)", cfg->mb);
+    if (cfg->n <= 0 || cfg->n % cfg->mb != 0) return fail(JP_ERR_INVALID, "N%%MB: n=%d is not a positive multiple of mb=%d", cfg->n, cfg->mb);
+    if (!(cfg->re > 0.0) || !(cfg->u0 > 0.0) || !(cfg->tstar >= 0.0)) return fail(JP_ERR_INVALID, "re, u0 must be > 0 and tstar >= 0");
+    jp_solver* s = new (std::nothrow) jp_solver();
+    if (!s) return fail(JP_ERR_NOMEM, "host allocation");
+    s->cfg = *cfg;
+    s->pool = pool;
+    jp_status st = (cfg->kind == JP_UNIFORM) ? uniform_create(s) : amr_create(s);
+    if (st != JP_OK) {
+        std::string keep = g_err;
+        jp_destroy(s);
+        g_err = keep;
+        return st;
+    }
+    *out = s;
+    return JP_OK;
+}
+
 extern "C" {
 
 const char* jp_last_error(void) { return g_err.c_str(); }
@@ -134,36 +157,19 @@ void jp_config_default(jp_config* c, int32_t kind) {
     }
 }
 
-jp_status jp_create(const jp_config* cfg, jp_solver** out) {
-    if (!cfg || !out) return fail(JP_ERR_INVALID, "jp_create: null argument");
-    *out = nullptr;
-    if (cfg->kind != JP_UNIFORM && cfg->kind != JP_AMR) return fail(JP_ERR_INVALID, "unknown solver kind %d", cfg->kind);
-    if (cfg->storage < 0 || cfg->storage > 3) return fail(JP_ERR_INVALID, "unknown storage %d", cfg->storage);
-    if (cfg->mb != 4 && cfg->mb != 8 && cfg->mb != 16) return fail(JP_ERR_INVALID, "mb must be 4, 8 or 16 (got %d)", cfg->mb);
-    if (cfg->n <= 0 || cfg->n % cfg->mb != 0) return fail(JP_ERR_INVALID, "N%%MB: n=%d is not a positive multiple of mb=%d", cfg->n, cfg->mb);
-    if (!(cfg->re > 0.0) || !(cfg->u0 > 0.0) || !(cfg->tstar >= 0.0)) return fail(JP_ERR_INVALID, "re, u0 must be > 0 and tstar >= 0");
-    jp_solver* s = new (std::nothrow) jp_solver();
-    if (!s) return fail(JP_ERR_NOMEM, "host allocation");
-    s->cfg = *cfg;
-    jp_status st = (cfg->kind == JP_UNIFORM) ? uniform_create(s) : amr_create(s);
-    if (st != JP_OK) {
-        std::string keep = g_err;
-        jp_destroy(s);
-        g_err = keep;
-        return st;
-    }
-    *out = s;
-    return JP_OK;
-}
+jp_status jp_create(const jp_config* cfg, jp_solver** out) { return create_solver(cfg, nullptr, out); }
+
 
 void jp_destroy(jp_solver* s) {
     if (!s) return;
     cudaSetDevice(s->device);
-    if (s->stream) cudaStreamSynchronize(s->stream);
+    // pooled memory is freed in stream order behind the solver's last work; plain cudaFree waits
+    if (s->stream && !s->pool) cudaStreamSynchronize(s->stream);
     if (s->kind == JP_AMR) amr_destroy(s);
     uniform_free(s);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->ev_wait) cudaEventDestroy(s->ev_wait);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }

@@ -8,11 +8,15 @@
 // exactly what the `uniform` / `amr` programs do for it (same steps, diagnostic cadence, regrid
 // cadence, VALID gate), so its numbers do not depend on what else is running.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
 #include <map>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "jp.h"
@@ -146,7 +150,9 @@ struct Job {
     jp_solver* s = nullptr;
     jp_info info{};
     long long step = 0, steps = 0, diagK = 1, adapt = 0;
-    bool dynamic = false, need_diag = true, regridded = false;
+    bool dynamic = false, need_diag = true;
+    bool admitted = false;  // holds `bytes` of the pool budget
+    bool requeue = false;   // an AMR worker could not get the memory: back to the queue head
     jp_status error = JP_OK;
     int samples = 0;
     double E0 = -1, prevE = 1e30, Elast = 0, peak = -1, peak_ts = -1, mass0 = -1, drift = 0;
@@ -183,9 +189,10 @@ long long estimate_bytes(const jp_config& c) {
 
 struct jp_server {
     jp_server_config cfg{};
-    cudaStream_t stream = nullptr;
-    std::deque<Job*> queue;
-    std::vector<Job*> active;
+    cudaStream_t stream = nullptr;     // batched uniform launches and their diagnostics
+    cudaMemPool_t pool = nullptr;      // device memory of every served solve (stream-ordered)
+    std::deque<Job*> queue;            // submitted, not admitted
+    std::vector<Job*> active;          // admitted uniform solves
     std::vector<jp_result> done;
     double budget = 0;
     long long used = 0;
@@ -193,6 +200,15 @@ struct jp_server {
     double* dev_diag = nullptr;   // 3 doubles per uniform job with a pending diagnostic
     double* host_diag = nullptr;
     int diag_cap = 0;
+    // AMR solves run whole on worker threads, each on its own stream; the tick thread admits and
+    // retires them.  amr_todo and amr_fin are guarded by mu.
+    std::vector<std::thread> workers;
+    std::mutex mu;
+    std::condition_variable cv_todo, cv_fin;
+    std::deque<Job*> amr_todo;
+    std::vector<Job*> amr_fin;
+    int amr_live = 0;                  // admitted AMR solves not yet retired (tick thread only)
+    std::atomic<bool> stop{false};
     double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 };
 
@@ -216,10 +232,8 @@ void finish(jp_server* sv, Job* j, jp_status status) {
     r.t_end = sv->now();
     r.bytes = j->bytes;
     sv->done.push_back(r);
-    if (j->s) {
-        jp_destroy(j->s);
-        sv->used -= j->bytes;
-    }
+    if (j->s) jp_destroy(j->s);
+    if (j->admitted) sv->used -= j->bytes;
     delete j;
 }
 
@@ -242,9 +256,76 @@ void record(Job* j, const double d[3]) {
 }
 
 long long next_event(const Job* j) {
-    long long e = std::min(j->steps, (j->step / j->diagK + 1) * j->diagK);
-    if (j->dynamic && j->adapt > 0) e = std::min(e, (j->step / j->adapt + 1) * j->adapt);
-    return e;
+    return std::min(j->steps, (j->step / j->diagK + 1) * j->diagK);
+}
+
+// One AMR solve from creation to destruction, on the calling worker thread: the loop of the `amr`
+// program (regrid every `adapt` coarse steps before the diagnostic of the same step, a diagnostic
+// every steps/160, two coarse steps per iteration with graph replay as the reference's graph holds
+// two), with the steps between two events issued in one call.
+void run_amr(jp_server* sv, Job* j) {
+    if (cudaSetDevice(sv->cfg.device) != cudaSuccess) {
+        j->error = JP_ERR_CUDA;
+        return;
+    }
+    jp_status st = create_solver(&j->req.cfg, sv->pool, &j->s);
+    if (st != JP_OK) {
+        j->s = nullptr;
+        if (st == JP_ERR_NOMEM) j->requeue = true;  // the estimate was optimistic: wait for memory
+        else j->error = st;
+        return;
+    }
+    jp_get_info(j->s, &j->info);
+    j->steps = j->info.steps;
+    j->diagK = j->req.diag_every > 0 ? j->req.diag_every : std::max(1LL, j->steps / 160);
+    j->dynamic = j->req.cfg.l1_mode == JP_REFINE_SENSOR || j->req.cfg.l2_mode == JP_REFINE_SENSOR;
+    j->adapt = j->req.cfg.adapt_every > 0 ? j->req.cfg.adapt_every : 100;
+    const long long sstep = (j->req.cfg.flags & JP_FLAG_GRAPH) ? 2 : 1;
+    long long pending = 0;
+    for (long long s_ = 0; s_ <= j->steps && st == JP_OK; s_ += sstep) {
+        if (sv->stop.load(std::memory_order_relaxed)) {
+            st = fail(JP_ERR_STATE, "server shut down during the solve");
+            break;
+        }
+        const bool rg = j->dynamic && s_ > 0 && s_ % j->adapt == 0, dg = s_ % j->diagK == 0;
+        if ((rg || dg) && pending) {
+            st = jp_step(j->s, pending);
+            pending = 0;
+        }
+        if (st == JP_OK && rg) st = jp_regrid(j->s);
+        if (st == JP_OK && dg) {
+            double d[3];
+            st = jp_diag(j->s, d);
+            if (st == JP_OK) {
+                j->step = s_;
+                record(j, d);
+            }
+        }
+        if (s_ < j->steps) pending += sstep;
+    }
+    if (st == JP_OK && pending) st = jp_step(j->s, pending);
+    j->error = st;
+    jp_destroy(j->s);  // pooled memory returns in stream order behind the last step
+    j->s = nullptr;
+}
+
+void worker_main(jp_server* sv) {
+    for (;;) {
+        Job* j = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(sv->mu);
+            sv->cv_todo.wait(lk, [sv] { return sv->stop.load() || !sv->amr_todo.empty(); });
+            if (sv->stop.load()) return;
+            j = sv->amr_todo.front();
+            sv->amr_todo.pop_front();
+        }
+        run_amr(sv, j);
+        {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            sv->amr_fin.push_back(j);
+        }
+        sv->cv_fin.notify_all();
+    }
 }
 
 }  // namespace
@@ -259,15 +340,29 @@ jp_status jp_server_create(const jp_server_config* cfg, jp_server** out) {
     if (!sv) return fail(JP_ERR_NOMEM, "host allocation");
     sv->cfg = *cfg;
     if (sv->cfg.tick_steps <= 0) sv->cfg.tick_steps = 64;
+    if (sv->cfg.workers <= 0) sv->cfg.workers = (int)std::min(32u, std::max(4u, std::thread::hardware_concurrency()));
     sv->t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
     size_t fr = 0, tot = 0;
     if (e == cudaSuccess) e = cudaMemGetInfo(&fr, &tot);
+    if (e == cudaSuccess) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = cfg->device;
+        e = cudaMemPoolCreate(&sv->pool, &props);
+    }
+    if (e == cudaSuccess) {  // keep freed memory in the pool for the next solves
+        uint64_t keep = UINT64_MAX;
+        e = cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (e != cudaSuccess) {
         jp_server_destroy(sv);
         return cuda_fail(e, "server setup");
     }
     sv->budget = cfg->pool_gb > 0 ? cfg->pool_gb * double(1ull << 30) : 0.75 * double(fr);
+    for (int w = 0; w < sv->cfg.workers; ++w) sv->workers.emplace_back(worker_main, sv);
     *out = sv;
     return JP_OK;
 }
@@ -275,15 +370,27 @@ jp_status jp_server_create(const jp_server_config* cfg, jp_server** out) {
 void jp_server_destroy(jp_server* sv) {
     if (!sv) return;
     cudaSetDevice(sv->cfg.device);
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop.store(true);
+    }
+    sv->cv_todo.notify_all();
+    for (std::thread& t : sv->workers) t.join();  // running solves stop at their next iteration
     if (sv->stream) cudaStreamSynchronize(sv->stream);
     for (Job* j : sv->active) {
         if (j->s) jp_destroy(j->s);
         delete j;
     }
+    for (Job* j : sv->amr_todo) delete j;
+    for (Job* j : sv->amr_fin) delete j;
     for (Job* j : sv->queue) delete j;
     if (sv->dev_diag) cudaFree(sv->dev_diag);
     if (sv->host_diag) cudaFreeHost(sv->host_diag);
     if (sv->stream) cudaStreamDestroy(sv->stream);
+    if (sv->pool) {
+        cudaDeviceSynchronize();
+        cudaMemPoolDestroy(sv->pool);
+    }
     delete sv;
 }
 
@@ -314,15 +421,53 @@ jp_status jp_server_submit(jp_server* sv, const jp_request* req) {
 jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
     if (!sv) return fail(JP_ERR_INVALID, "null server");
     ECK(cudaSetDevice(sv->cfg.device), "cudaSetDevice");
-    // 1. admission: FIFO while the head fits the budget and a slot is free
-    while (!sv->queue.empty() && (sv->cfg.max_active <= 0 || (int)sv->active.size() < sv->cfg.max_active)) {
-        Job* j = sv->queue.front();
-        if ((double)(sv->used + j->bytes) > sv->budget) break;
-        sv->queue.pop_front();
-        j->t_start = sv->now();
-        jp_status st = jp_create(&j->req.cfg, &j->s);
-        if (st == JP_ERR_NOMEM) {  // the estimate was optimistic: wait for memory to free up
+    // 1. retire the AMR solves the workers finished (their memory is back in the pool)
+    std::vector<Job*> fin, requeued;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        fin.swap(sv->amr_fin);
+    }
+    for (Job* j : fin) {
+        --sv->amr_live;
+        if (j->requeue) {
+            j->requeue = false;
+            j->admitted = false;
+            sv->used -= j->bytes;
             sv->queue.push_front(j);
+            requeued.push_back(j);
+        } else {
+            finish(sv, j, j->error);
+        }
+    }
+    // 2. admission in submission order while the budget and the slots allow.  An AMR solve also
+    //    needs a free worker; while none is free it keeps its place and later uniform solves may
+    //    pass it (they need no worker).  Memory is strictly first come, first served.
+    for (auto it = sv->queue.begin(); it != sv->queue.end();) {
+        if (sv->cfg.max_active > 0 && (int)sv->active.size() + sv->amr_live >= sv->cfg.max_active) break;
+        Job* j = *it;
+        if (std::find(requeued.begin(), requeued.end(), j) != requeued.end()) break;  // no memory: next tick
+        if (j->req.cfg.kind == JP_AMR && sv->amr_live >= sv->cfg.workers) {
+            ++it;
+            continue;
+        }
+        if ((double)(sv->used + j->bytes) > sv->budget) break;
+        it = sv->queue.erase(it);
+        j->t_start = sv->now();
+        if (j->req.cfg.kind == JP_AMR) {
+            j->admitted = true;
+            sv->used += j->bytes;
+            ++sv->amr_live;
+            {
+                std::lock_guard<std::mutex> lk(sv->mu);
+                sv->amr_todo.push_back(j);
+            }
+            sv->cv_todo.notify_one();
+            continue;
+        }
+        jp_status st = create_solver(&j->req.cfg, sv->pool, &j->s);
+        if (st == JP_ERR_NOMEM) {  // the estimate was optimistic: wait for memory to free up
+            j->s = nullptr;
+            sv->queue.insert(it, j);
             break;
         }
         if (st != JP_OK) {
@@ -330,55 +475,39 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
             finish(sv, j, st);
             continue;
         }
+        j->admitted = true;
         sv->used += j->bytes;
-        jp_get_info(j->s, &j->info);
+        jp_solver* s = j->s;
+        jp_get_info(s, &j->info);
         j->steps = j->info.steps;
-        const bool amr = j->req.cfg.kind == JP_AMR;
-        j->diagK = j->req.diag_every > 0 ? j->req.diag_every : std::max(1LL, j->steps / (amr ? 160 : 240));
-        j->dynamic = amr && (j->req.cfg.l1_mode == JP_REFINE_SENSOR || j->req.cfg.l2_mode == JP_REFINE_SENSOR);
-        j->adapt = j->req.cfg.adapt_every > 0 ? j->req.cfg.adapt_every : 100;
+        j->diagK = j->req.diag_every > 0 ? j->req.diag_every : std::max(1LL, j->steps / 240);
+        // the macro field of the diagnostics, ready before the server's stream uses it
+        const size_t fb = (s->storage == JP_FP64 ? 8 : 4) * 4 * (size_t)s->cells;
+        cudaError_t e = dev_alloc(s, &s->field, fb);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) {
+            finish(sv, j, cuda_fail(e, "macro field"));
+            continue;
+        }
         sv->active.push_back(j);
     }
-    // 2. regrid (AMR, before the diagnostic of the same step) and diagnostics due now
+    // 3. diagnostics due now (uniform), all to one pinned array with one read-back
     std::vector<Job*> uni_diag;
-    // a failing call ends only its own solve: the job leaves with that status at the next retirement
-    for (Job* j : sv->active) {
-        if (j->error != JP_OK) continue;
-        if (j->req.cfg.kind == JP_AMR && j->dynamic && j->step > 0 && j->step % j->adapt == 0 && !j->regridded) {
-            jp_status st = jp_regrid(j->s);
-            j->regridded = true;
-            if (st != JP_OK) {
-                j->error = st;
-                continue;
-            }
-        }
-        if (!j->need_diag) continue;
-        if (j->req.cfg.kind == JP_AMR) {
-            double d[3];
-            jp_status st = jp_diag(j->s, d);
-            if (st != JP_OK) {
-                j->error = st;
-                continue;
-            }
-            record(j, d);
-        } else {
-            uni_diag.push_back(j);
-        }
-    }
+    for (Job* j : sv->active)
+        if (j->error == JP_OK && j->need_diag) uni_diag.push_back(j);
     if (!uni_diag.empty()) {
         if ((int)uni_diag.size() > sv->diag_cap) {
+            ECK(cudaStreamSynchronize(sv->stream), "diag slots");
             if (sv->dev_diag) cudaFree(sv->dev_diag);
             if (sv->host_diag) cudaFreeHost(sv->host_diag);
+            sv->dev_diag = nullptr;
+            sv->host_diag = nullptr;
             sv->diag_cap = std::max<int>(2 * (int)uni_diag.size(), 64);
             ECK(cudaMalloc(&sv->dev_diag, sizeof(double) * 3 * sv->diag_cap), "cudaMalloc diag slots");
             ECK(cudaMallocHost(&sv->host_diag, sizeof(double) * 3 * sv->diag_cap), "cudaMallocHost diag slots");
         }
         for (size_t k = 0; k < uni_diag.size(); ++k) {
             jp_solver* s = uni_diag[k]->s;
-            if (!s->field) {
-                const size_t fb = (s->storage == JP_FP64 ? 8 : 4) * 4 * (size_t)s->cells;
-                ECK(cudaMalloc(&s->field, fb), "cudaMalloc macro field");
-            }
             const bool dbl = s->storage == JP_FP64;
             ECK(launch_macro(s->storage, s->fa, s->field, s->n, sv->stream), "macro");
             ECK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, sv->dev_diag + 3 * k, sv->stream), "diag");
@@ -388,7 +517,7 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
         ECK(cudaStreamSynchronize(sv->stream), "diag");
         for (size_t k = 0; k < uni_diag.size(); ++k) record(uni_diag[k], sv->host_diag + 3 * k);
     }
-    // 3. retire finished solves (after the batched launches that touched them)
+    // 4. retire finished uniform solves (after the batched launches that touched them)
     bool any_done = false;
     for (Job* j : sv->active) any_done |= (j->step >= j->steps && !j->need_diag) || j->error != JP_OK;
     if (any_done) ECK(cudaStreamSynchronize(sv->stream), "retire");
@@ -401,27 +530,14 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
             ++i;
         }
     }
-    // 4. advance: uniform solves in batched launches, AMR solves on their own streams
+    // 5. advance the uniform solves in batched launches
     std::vector<std::pair<Job*, long long>> uni;
     long long kmax = 0;
     for (Job* j : sv->active) {
-        if (j->error != JP_OK) continue;
-        const long long target = next_event(j);
-        if (j->req.cfg.kind == JP_AMR) {
-            const long long k = std::min(target - j->step, std::max(1LL, (long long)sv->cfg.tick_steps / 4));
-            if (k <= 0) continue;
-            jp_status st = jp_step(j->s, k);
-            if (st != JP_OK) {
-                j->error = st;
-                continue;
-            }
-            j->step += k;
-            j->regridded = false;
-        } else {
-            const long long k = std::min(target - j->step, (long long)sv->cfg.tick_steps);
-            uni.push_back({j, k});
-            kmax = std::max(kmax, k);
-        }
+        const long long k = std::min(next_event(j) - j->step, (long long)sv->cfg.tick_steps);
+        if (k <= 0) continue;
+        uni.push_back({j, k});
+        kmax = std::max(kmax, k);
     }
     std::vector<jp_solver*> members;
     for (long long t = 0; t < kmax; ++t) {
@@ -431,11 +547,16 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
         jp_status st = batched_step(members, sv->stream);
         if (st != JP_OK) return st;
     }
-    for (auto& p : uni) p.first->step += p.second;
-    for (Job* j : sv->active) {
-        if (j->step % j->diagK == 0) j->need_diag = true;  // diagnostics at the new step (next tick)
+    for (auto& p : uni) {
+        p.first->step += p.second;
+        if (p.first->step % p.first->diagK == 0) p.first->need_diag = true;  // at the new step, next tick
     }
-    if (n_active) *n_active = (int32_t)sv->active.size();
+    // 6. nothing to launch here while AMR solves run: wait briefly for one of them to finish
+    if (uni.empty() && sv->amr_live > 0) {
+        std::unique_lock<std::mutex> lk(sv->mu);
+        sv->cv_fin.wait_for(lk, std::chrono::milliseconds(1), [sv] { return !sv->amr_fin.empty(); });
+    }
+    if (n_active) *n_active = (int32_t)sv->active.size() + sv->amr_live;
     if (n_queued) *n_queued = (int32_t)sv->queue.size();
     return JP_OK;
 }

@@ -13,6 +13,23 @@ struct AmrState;
 jp_status fail(jp_status st, const char* fmt, ...);
 jp_status cuda_fail(cudaError_t e, const char* what);
 size_t storage_bytes(int storage);
+
+// Device memory of a solver: from its stream-ordered pool on its own stream when it has one (solves
+// run by a server: no device-wide synchronisation when they come and go), else cudaMalloc/cudaFree.
+cudaError_t dev_alloc(jp_solver* s, void** p, size_t bytes);
+void dev_free(jp_solver* s, void* p);
+// Small pinned host buffers (<= 256 bytes: diagnostic and count read-backs) from process-wide slabs
+// that are never returned to the driver, so creating and destroying solvers never calls
+// cudaFreeHost (which synchronises the device).
+void* pinned_slot_alloc();
+void pinned_slot_free(void* p);
+// jp_create with a stream-ordered memory pool (nullptr: plain allocations).  A solver with a pool
+// belongs to a server and waits for its stream politely (wait_stream).
+jp_status create_solver(const jp_config* cfg, cudaMemPool_t pool, jp_solver** out);
+// Wait until the solver's stream has drained.  A served solver polls an event, yielding the core and
+// then sleeping in short slices, so that many solves waiting at once leave the host cores to the
+// threads that issue work; otherwise cudaStreamSynchronize.
+cudaError_t wait_stream(jp_solver* s);
 double stored_to_double(int storage, const void* base, size_t idx, int q);
 void double_to_stored(int storage, void* base, size_t idx, int q, double v);
 }  // namespace jp
@@ -24,7 +41,9 @@ struct jp_solver {
     int device = 0;
     int storage = 0;
     cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;  // device allocations come from here when set (see dev_alloc)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_wait = nullptr;  // wait_stream of a served solver
     int64_t step_count = 0;
 
     // uniform cube (flat [q][z][y][x])
@@ -68,6 +87,7 @@ jp_status amr_population_count(const jp_solver* s, int level, int64_t* count);
 jp_status amr_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count);
 jp_status amr_set_populations(jp_solver* s, int level, int layout, int dtype, const void* host, int64_t count);
 jp_status amr_regrid(jp_solver* s);
+jp_status amr_set_step_tpb(jp_solver* s, int tpb);  // threads per CTA of the level steps (autotuner)
 jp_status amr_get_counts(jp_solver* s, jp_amr_counts* out);
 jp_status amr_get_table(jp_solver* s, int table, int32_t* host, int64_t capacity, int64_t* count);
 jp_status amr_get_sensor(jp_solver* s, int level, float* host, int64_t capacity, int64_t* count);

@@ -19,6 +19,7 @@ namespace jp {
 using namespace amr;
 
 struct AmrState {
+    jp_solver* owner = nullptr;  // allocations go through dev_alloc of the owning solver
     int MB = 8, MB3 = 512, SH = 480, N = 0, cgx = 0, cnb0 = 0, l1gx = 0, N1 = 0, N2 = 0, NG1 = 0;
     double tau0 = 0, tau1 = 0, tau2 = 0, nqs01 = 0, nqi10 = 0, nqs12 = 0, nqi21 = 0;
     float om0 = 0, om1 = 0, om2 = 0;
@@ -35,6 +36,8 @@ struct AmrState {
         *skin0 = nullptr, *skin1 = nullptr;
     int *o_ref0 = nullptr, *o_fof0 = nullptr, *o_l1grid = nullptr, *o_ref1 = nullptr, *o_fof1 = nullptr;
     int *rank = nullptr, *deep = nullptr, *flags = nullptr;
+    int *nb1 = nullptr, *nb2 = nullptr;  // same-level neighbour tables of the fine levels (27 per block)
+    int tpb = 0;                         // threads per CTA of the steps (0: min(MB^3, 512))
     float *sen0 = nullptr, *sen1 = nullptr;
     float *ov_sen0 = nullptr, *ov_sen1pos = nullptr;
     AdaptCounts* cnt_dev = nullptr;
@@ -66,7 +69,7 @@ template <class T>
 static jp_status dalloc(AmrState* a, T** p, size_t count, const char* what) {
     *p = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    cudaError_t e = dev_alloc(a->owner, (void**)p, count * sizeof(T));
     if (e != cudaSuccess) return cuda_fail(e, what);
     a->owned.push_back(*p);
     return JP_OK;
@@ -76,7 +79,7 @@ static void dfree(AmrState* a, T*& p) {
     if (!p) return;
     auto it = std::find(a->owned.begin(), a->owned.end(), (void*)p);
     if (it != a->owned.end()) a->owned.erase(it);
-    cudaFree(p);
+    dev_free(a->owner, p);
     p = nullptr;
 }
 
@@ -96,7 +99,7 @@ static jp_status launch(jp_solver* s, int op, AmrLaunch L) {
 static jp_status read_counts(jp_solver* s) {
     AmrState* a = s->amr;
     ACK(cudaMemcpyAsync(a->cnt_host, a->cnt_dev, sizeof(AdaptCounts), cudaMemcpyDeviceToHost, s->stream), "counts D2H");
-    ACK(cudaStreamSynchronize(s->stream), "adaptation");
+    ACK(wait_stream(s), "adaptation");
     return JP_OK;
 }
 
@@ -133,6 +136,7 @@ static jp_status step_l0(jp_solver* s) {
     L.cgx = a->cgx;
     L.n = a->N;
     L.omega = a->om0;
+    L.tpb = a->tpb;
     TRY(launch(s, OP_STEP_L0, L));
     std::swap(a->c0a, a->c0b);
     return JP_OK;
@@ -170,7 +174,7 @@ static jp_status regrow(jp_solver* s, T*& p, size_t count, size_t keep) {
     T* q = nullptr;
     TRY(dalloc(a, &q, count, "cudaMalloc (pool growth)"));
     if (keep && p) ACK(cudaMemcpyAsync(q, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s->stream), "pool growth copy");
-    ACK(cudaStreamSynchronize(s->stream), "pool growth");
+    ACK(wait_stream(s), "pool growth");
     dfree(a, p);
     p = q;
     return JP_OK;
@@ -204,6 +208,7 @@ static jp_status grow_l1(jp_solver* s, int needed) {
     TRY(regrow(s, a->sen1, cap, 0));
     TRY(regrow(s, a->rank, std::max(a->cnb0, cap), 0));
     TRY(regrow(s, a->flags, (size_t)a->cnb0 + cap, 0));
+    TRY(regrow(s, a->nb1, (size_t)cap * 27, 0));
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * cap, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * cap, s->stream), "memset");
     a->cap1 = cap;
@@ -223,6 +228,7 @@ static jp_status grow_l2(jp_solver* s, int needed) {
     TRY(regrow(s, a->gh2, (size_t)cap * Q * a->SH, 0));
     TRY(regrow(s, a->l2pl1, cap, 0));
     TRY(regrow(s, a->l2oct, cap, 0));
+    TRY(regrow(s, a->nb2, (size_t)cap * 27, 0));
     a->cap2 = cap;
     update_bytes(s);
     return JP_OK;
@@ -246,7 +252,7 @@ static jp_status build_l1(jp_solver* s, bool restore_marks) {
             TRY(read_counts(s));
         } else if (restore_marks) {
             ACK(cudaMemcpyAsync(a->ref0, a->o_ref0, sizeof(int) * a->cnb0, cudaMemcpyDeviceToDevice, s->stream), "restore");
-            ACK(cudaStreamSynchronize(s->stream), "restore");
+            ACK(wait_stream(s), "restore");
             return g;
         } else {
             return g;
@@ -257,6 +263,31 @@ static jp_status build_l1(jp_solver* s, bool restore_marks) {
     a->nf1 = a->cnt_host->nf1;
     a->hw_nf1 = std::max(a->hw_nf1, (long long)a->nf1);
     return JP_OK;
+}
+
+// same-level neighbour tables of both fine levels for the current grid
+static jp_status neighbour_tables(jp_solver* s) {
+    AmrState* a = s->amr;
+    AmrLaunch L;
+    L.nblocks = a->nf1;
+    L.iout = a->nb1;
+    L.t0 = a->pcb;
+    L.t1 = a->oct;
+    L.t2 = a->ref0;
+    L.t3 = a->fof0;
+    L.cgx = a->cgx;
+    TRY(launch(s, OP_NBTAB_L1, L));
+    AmrLaunch M;
+    M.nblocks = a->nf2;
+    M.iout = a->nb2;
+    M.t0 = a->l2pl1;
+    M.t1 = a->l2oct;
+    M.t2 = a->f1pos;
+    M.t3 = a->l1grid;
+    M.t4 = a->ref1;
+    M.t5 = a->fof1;
+    M.l1gx = a->l1gx;
+    return launch(s, OP_NBTAB_L2, M);
 }
 
 // gpurce_init (src/tgv3d_amr.cu:776-815)
@@ -316,7 +347,9 @@ static jp_status initial_build(jp_solver* s) {
     dfree(a, a->gh2);
     dfree(a, a->l2pl1);
     dfree(a, a->l2oct);
+    dfree(a, a->nb2);
     const size_t blk = (size_t)Q * a->MB3;
+    TRY(dalloc(a, &a->nb2, (size_t)a->cap2 * 27, "cudaMalloc nb2"));
     TRY(dalloc(a, &a->f2a, (size_t)a->cap2 * blk, "cudaMalloc f2"));
     TRY(dalloc(a, &a->f2b, (size_t)a->cap2 * blk, "cudaMalloc f2"));
     TRY(dalloc(a, &a->gh2, (size_t)a->cap2 * Q * a->SH, "cudaMalloc gh2"));
@@ -340,6 +373,7 @@ static jp_status initial_build(jp_solver* s) {
         L.scale = float(a->nqs12);
         TRY(launch(s, OP_SEED_L2, L));
     }
+    TRY(neighbour_tables(s));
     TRY(skins(s));
     return JP_OK;
 }
@@ -410,6 +444,7 @@ static jp_status regrid(jp_solver* s) {
             std::swap(a->f2a, a->f2b);
         }
     }
+    TRY(neighbour_tables(s));
     TRY(skins(s));
     return JP_OK;
 }
@@ -437,7 +472,7 @@ static jp_status base_step(jp_solver* s) {
         F.out = a->gh1;
         F.t0 = a->pcb;
         F.t1 = a->oct;
-        F.t2 = a->ref0;
+        F.nbt = a->nb1;
         F.cgx = a->cgx;
         F.n = a->N;
         TRY(launch(s, OP_FILL_L1, F));
@@ -459,7 +494,7 @@ static jp_status base_step(jp_solver* s) {
             F.t1 = a->l2oct;
             F.t2 = a->f1pos;
             F.t3 = a->l1grid;
-            F.t4 = a->ref1;
+            F.nbt = a->nb2;
             F.l1gx = a->l1gx;
             F.n1 = a->N1;
             TRY(launch(s, OP_FILL_L2, F));
@@ -471,15 +506,11 @@ static jp_status base_step(jp_solver* s) {
                 S.in = a->f2a;
                 S.out = a->f2b;
                 S.aux = a->gh2;
+                S.nbt = a->nb2;
                 S.t0 = a->l2pl1;
                 S.t1 = a->l2oct;
-                S.t2 = a->f1pos;
-                S.t3 = a->l1grid;
-                S.t4 = a->ref1;
-                S.t5 = a->fof1;
-                S.l1gx = a->l1gx;
-                S.n1 = a->N1;
                 S.omega = a->om2;
+                S.tpb = a->tpb;
                 if (s2 == 1 && fuse) {  // last level-2 substep restricts itself into level 1
                     S.out2 = a->f1a;
                     S.scale = float(a->nqi21);
@@ -501,13 +532,11 @@ static jp_status base_step(jp_solver* s) {
         S.in = a->f1a;
         S.out = a->f1b;
         S.aux = a->gh1;
+        S.nbt = a->nb1;
         S.t0 = a->pcb;
         S.t1 = a->oct;
-        S.t2 = a->ref0;
-        S.t3 = a->fof0;
-        S.cgx = a->cgx;
-        S.n = a->N;
         S.omega = a->om1;
+        S.tpb = a->tpb;
         if (s1 == 1 && fuse) {  // last level-1 substep restricts itself into the coarse level
             S.out2 = a->c0a;
             S.scale = float(a->nqi10);
@@ -560,9 +589,14 @@ jp_status amr_create(jp_solver* s) {
     const jp_config& c = s->cfg;
     if (c.storage != JP_FP32) return fail(JP_ERR_UNSUPPORTED, "AMR solver: FP32 storage only in this build");
     if (c.l1_mode < 0 || c.l1_mode > 2 || c.l2_mode < 0 || c.l2_mode > 2) return fail(JP_ERR_INVALID, "bad refine mode");
+    if (c.threads_per_block && !step_tpb_supported(c.mb, c.threads_per_block))
+        return fail(JP_ERR_INVALID, "threads_per_block %d does not split a block of edge %d (MB=4: 64; 8, 16: 128, 256, 512)",
+                    c.threads_per_block, c.mb);
     AmrState* a = new (std::nothrow) AmrState();
     if (!a) return fail(JP_ERR_NOMEM, "host allocation");
     s->amr = a;
+    a->owner = s;
+    a->tpb = c.threads_per_block;
     a->MB = c.mb;
     a->MB3 = c.mb * c.mb * c.mb;
     a->SH = shell_cells(c.mb);
@@ -617,11 +651,14 @@ jp_status amr_create(jp_solver* s) {
     TRY(dalloc(a, &a->rank, (size_t)std::max(a->cnb0, a->cap1), "cudaMalloc rank"));
     TRY(dalloc(a, &a->flags, (size_t)a->cnb0 + a->cap1, "cudaMalloc flags"));
     TRY(dalloc(a, &a->sen1, (size_t)a->cap1, "cudaMalloc sen1"));
+    TRY(dalloc(a, &a->nb1, (size_t)a->cap1 * 27, "cudaMalloc nb1"));
     TRY(dalloc(a, &a->cnt_dev, 1, "cudaMalloc counts"));
-    ACK(cudaMallocHost(&a->cnt_host, sizeof(AdaptCounts)), "cudaMallocHost counts");
-    ACK(cudaMalloc(&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
-    ACK(cudaMalloc(&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
-    ACK(cudaMallocHost(&s->diag_host, sizeof(double) * 3), "cudaMallocHost diag");
+    static_assert(sizeof(AdaptCounts) <= 256, "counts exceed a pinned slot");
+    a->cnt_host = (AdaptCounts*)pinned_slot_alloc();
+    s->diag_host = (double*)pinned_slot_alloc();
+    if (!a->cnt_host || !s->diag_host) return fail(JP_ERR_NOMEM, "pinned host slot");
+    ACK(dev_alloc(s, (void**)&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
+    ACK(dev_alloc(s, (void**)&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->l1grid, 0xFF, sizeof(int) * a->NG1, s->stream), "memset");
@@ -632,9 +669,9 @@ void amr_destroy(jp_solver* s) {
     AmrState* a = s->amr;
     if (!a) return;
     drop_graphs(a);
-    for (void* p : a->owned) cudaFree(p);
-    if (a->cnt_host) cudaFreeHost(a->cnt_host);
-    if (a->field) cudaFree(a->field);
+    for (void* p : a->owned) dev_free(s, p);
+    pinned_slot_free(a->cnt_host);
+    dev_free(s, a->field);
     delete a;
     s->amr = nullptr;
 }
@@ -652,7 +689,7 @@ jp_status amr_init(jp_solver* s) {
     TRY(launch(s, OP_INIT, L));
     a->hw_nf1 = a->hw_nf2 = 0;
     TRY(initial_build(s));
-    ACK(cudaStreamSynchronize(s->stream), "initial build");
+    ACK(wait_stream(s), "initial build");
     a->c0_home = a->c0a;
     s->step_count = 0;
     update_bytes(s);
@@ -668,16 +705,24 @@ jp_status amr_step(jp_solver* s, int64_t nsteps) {
     return JP_OK;
 }
 
+jp_status amr_set_step_tpb(jp_solver* s, int tpb) {
+    if (tpb && !step_tpb_supported(s->amr->MB, tpb)) return fail(JP_ERR_INVALID, "threads_per_block %d", tpb);
+    drop_graphs(s->amr);
+    s->amr->tpb = tpb;
+    s->cfg.threads_per_block = tpb;
+    return JP_OK;
+}
+
 jp_status amr_regrid(jp_solver* s) {
     drop_graphs(s->amr);
     TRY(regrid(s));
-    ACK(cudaStreamSynchronize(s->stream), "regrid");
+    ACK(wait_stream(s), "regrid");
     return JP_OK;
 }
 
 static jp_status composite(jp_solver* s) {
     AmrState* a = s->amr;
-    if (!a->field) ACK(cudaMalloc(&a->field, sizeof(float) * 4 * (size_t)a->N2 * a->N2 * a->N2), "cudaMalloc composite");
+    if (!a->field) ACK(dev_alloc(s, (void**)&a->field, sizeof(float) * 4 * (size_t)a->N2 * a->N2 * a->N2), "cudaMalloc composite");
     AmrLaunch L;
     L.in = a->c0a;
     L.aux = a->f1a;
@@ -704,7 +749,7 @@ jp_status amr_diag(jp_solver* s, double out[3]) {
     TRY(composite(s));
     ACK(launch_diag_field(false, false, a->field, a->N2, s->partials, s->diag_dev, s->stream), "diag");
     ACK(cudaMemcpyAsync(s->diag_host, s->diag_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "diag D2H");
-    ACK(cudaStreamSynchronize(s->stream), "diag");
+    ACK(wait_stream(s), "diag");
     out[0] = s->diag_host[0];
     out[1] = s->diag_host[1];
     out[2] = s->diag_host[2];

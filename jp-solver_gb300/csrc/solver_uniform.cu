@@ -78,22 +78,23 @@ jp_status uniform_create(jp_solver* s) {
         return fail(JP_ERR_INVALID, "threads_per_block must be 64, 128, 256 or 512");
     const size_t bytes = (size_t)Q * s->cells * s->elem;
     s->info.bytes_state = (int64_t)(2 * bytes);
-    JP_CK(cudaMalloc(&s->fa, bytes), "cudaMalloc populations");
-    JP_CK(cudaMalloc(&s->fb, bytes), "cudaMalloc populations");
-    JP_CK(cudaMalloc(&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
-    JP_CK(cudaMalloc(&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
-    JP_CK(cudaMallocHost(&s->diag_host, sizeof(double) * 3), "cudaMallocHost diag");
+    JP_CK(dev_alloc(s, &s->fa, bytes), "cudaMalloc populations");
+    JP_CK(dev_alloc(s, &s->fb, bytes), "cudaMalloc populations");
+    JP_CK(dev_alloc(s, (void**)&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
+    JP_CK(dev_alloc(s, (void**)&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
+    s->diag_host = (double*)pinned_slot_alloc();
+    if (!s->diag_host) return fail(JP_ERR_NOMEM, "pinned host slot");
     return uniform_init(s);
 }
 
 void uniform_free(jp_solver* s) {
-    if (s->fa) cudaFree(s->fa);
-    if (s->fb) cudaFree(s->fb);
-    if (s->field) cudaFree(s->field);
-    if (s->partials) cudaFree(s->partials);
-    if (s->diag_dev) cudaFree(s->diag_dev);
-    if (s->diag_host) cudaFreeHost(s->diag_host);
-    if (s->outbuf) cudaFree(s->outbuf);
+    dev_free(s, s->fa);
+    dev_free(s, s->fb);
+    dev_free(s, s->field);
+    dev_free(s, s->partials);
+    dev_free(s, s->diag_dev);
+    pinned_slot_free(s->diag_host);
+    dev_free(s, s->outbuf);
     s->outbuf = nullptr;
     s->fa = s->fb = s->field = nullptr;
     s->partials = s->diag_dev = s->diag_host = nullptr;
@@ -105,12 +106,12 @@ jp_status uniform_init(jp_solver* s) {
     double* tab = s->partials;
     double* own = nullptr;
     if (s->n > kDiagBlocks) {
-        JP_CK(cudaMalloc(&own, sizeof(double) * 3 * s->n), "cudaMalloc init table");
+        JP_CK(dev_alloc(s, (void**)&own, sizeof(double) * 3 * s->n), "cudaMalloc init table");
         tab = own;
     }
     cudaError_t e = launch_init_tgv(s->storage, s->fa, s->n, s->cfg.u0, s->info.kf, tab, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (own) cudaFree(own);
+    dev_free(s, own);
     JP_CK(e, "init_tgv");
     JP_CK(cudaStreamSynchronize(s->stream), "init_tgv");
     s->step_count = 0;
@@ -137,7 +138,7 @@ jp_status uniform_step(jp_solver* s, int64_t nsteps) {
 static jp_status ensure_field(jp_solver* s) {
     if (s->field) return JP_OK;
     const size_t fb = (s->storage == JP_FP64 ? sizeof(double) : sizeof(float)) * 4 * (size_t)s->cells;
-    JP_CK(cudaMalloc(&s->field, fb), "cudaMalloc macro field");
+    JP_CK(dev_alloc(s, &s->field, fb), "cudaMalloc macro field");
     return JP_OK;
 }
 
@@ -225,7 +226,7 @@ jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype
 jp_status output_fields_from(jp_solver* s, const void* field, bool field_is_double, bool float_diff, int n, float* q,
                              float* speed, float* vel) {
     const size_t cells = (size_t)n * n * n;
-    if (!s->outbuf) JP_CK(cudaMalloc(&s->outbuf, sizeof(float) * 5 * cells), "cudaMalloc output fields");
+    if (!s->outbuf) JP_CK(dev_alloc(s, (void**)&s->outbuf, sizeof(float) * 5 * cells), "cudaMalloc output fields");
     float* dq = s->outbuf;
     float* ds = dq + cells;
     float* dv = ds + cells;

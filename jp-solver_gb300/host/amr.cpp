@@ -1,7 +1,8 @@
 // `amr`: drop-in for the reference's three-level AMR Taylor-Green program (src/tgv3d_amr.cu:643-907),
 // driving the GB300 engine through the C ABI.  Same flags and defaults (including --adapt, --maxgb,
 // --graph, --skipprep, --skiprestr, --bench and the parsed-but-unused --buffer), same stdout lines,
-// exit codes and .vti/.vtp frames.  Additions: --mb, --develop, --device.
+// exit codes and .vti/.vtp frames.  Additions: --mb, --tpb (threads per CTA of the level steps),
+// --develop, --device, --autotune 1 (MB x threads per CTA), --diag-every.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -59,8 +60,8 @@ int main(int argc, char** argv) {
     const bool skipprep = argd(argc, argv, "--skipprep", 0.0) > 0.5;
     const bool skiprestr = argd(argc, argv, "--skiprestr", 0.0) > 0.5;
     const bool usegraph = argd(argc, argv, "--graph", 0.0) > 0.5;
-    const int MB = argi(argc, argv, "--mb", 8);
-    if (MB <= 0 || N % MB) {
+    const int MBarg = argi(argc, argv, "--mb", 8);
+    if (MBarg <= 0 || N % MBarg) {
         std::fprintf(stderr, "N%%MB\n");
         return 2;
     }
@@ -78,15 +79,17 @@ int main(int argc, char** argv) {
     cfg.l2_mode = refine_of(l2mode);
     cfg.adapt_every = adaptEvery;
     cfg.max_gb = argd(argc, argv, "--maxgb", 0.0);
-    cfg.mb = MB;
+    cfg.mb = MBarg;
     cfg.develop_steps = argi(argc, argv, "--develop", 300);
     cfg.device = argi(argc, argv, "--device", 0);
+    cfg.threads_per_block = argi(argc, argv, "--tpb", 0);
     cfg.flags = (skipprep ? JP_FLAG_SKIP_PREP : 0) | (skiprestr ? JP_FLAG_SKIP_RESTRICT : 0) | (usegraph ? JP_FLAG_GRAPH : 0);
     if (argd(argc, argv, "--autotune", 0.0) > 0.5) {
         double best = 0.0;
         ck(jp_autotune(&cfg, 4, &best), "autotune");
-        std::printf("[autotune] MB=%d  %.1f MLUPS(work)\n", cfg.mb, best / 1e6);
+        std::printf("[autotune] MB=%d threads/block=%d  %.1f MLUPS(work)\n", cfg.mb, cfg.threads_per_block, best / 1e6);
     }
+    const int MB = cfg.mb;  // the block edge in use (--mb, or the autotuner's pick)
     jp_solver* s = nullptr;
     ck(jp_create(&cfg, &s), "create");
     jp_info info;

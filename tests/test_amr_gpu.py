@@ -242,3 +242,22 @@ def test_autotune_amr_block_edge():
     # the AMR tuner times the block edges that divide N0 and returns one of them
     tuned, lups = J.autotune("amr", steps=2, n=32, re=800.0, l1_mode="all", l2_mode="all", max_gb=4.0)
     assert tuned["mb"] in (4, 8, 16) and lups > 0
+
+
+@pytest.mark.parametrize("mb,tpbs", [(8, (128, 256, 512)), (16, (128, 256, 512)), (4, (64,))])
+def test_step_threads_per_block_bit_exact(mb, tpbs):
+    # the level steps split a block's cells over 64..512 threads; every split computes the same
+    # per-cell arithmetic, so the populations agree bit for bit with the default split
+    n = 32
+    s0, s1 = O.random_sensor_fields(n, mb=mb, seed=5)
+    out = {}
+    for t in (0,) + tpbs:
+        with J.Solver("amr", n=n, re=800.0, l1_mode="sensor", l2_mode="sensor", frac1=0.3, frac2=0.3,
+                      develop_steps=2, max_gb=1024.0, mb=mb, threads_per_block=t) as e:
+            e.set_sensor_override(s0, s1)
+            e.init_tgv()
+            e.step(2)
+            out[t] = [e.get_populations(lv, layout="blocked") for lv in range(3)]
+    for t in tpbs:
+        for lv in range(3):
+            np.testing.assert_array_equal(out[t][lv], out[0][lv], err_msg="tpb %d level %d" % (t, lv))

@@ -80,14 +80,26 @@ MIX = [dict(rid=10, kind="uniform", n=48, re=800.0, tstar=1.5, storage="fp16"),
 
 
 def test_server_result_same_alone_and_in_mix():
+    # a uniform solve (batched launches) and an AMR solve (worker thread, own stream) each give the
+    # same result alone and in a mix of six solves that run concurrently
     alone, _ = run_server([R0], tick_steps=16)
+    alone_amr, _ = run_server([MIX[2]], tick_steps=16)
     mixed, peak = run_server([MIX[0], MIX[1], R0] + MIX[2:], tick_steps=16)
-    a, m = alone[1], mixed[1]
-    assert a["status"] == 0 and m["status"] == 0
-    for k in ("steps", "samples", "peak_tstar", "peak_enstrophy", "energy_ratio", "mass_drift", "valid"):
-        assert a[k] == m[k], k
+    for a, m in ((alone[1], mixed[1]), (alone_amr[12], mixed[12])):
+        assert a["status"] == 0 and m["status"] == 0
+        for k in ("steps", "samples", "peak_tstar", "peak_enstrophy", "energy_ratio", "mass_drift", "valid"):
+            assert a[k] == m[k], (a["id"], k)
     assert peak >= 3                                   # solves really ran concurrently
     assert all(r["status"] == 0 for r in mixed.values())
+
+
+def test_server_one_worker_runs_amr_solves_in_turn():
+    # with one worker the AMR solves queue for it while the uniform ones pass them
+    reqs = [dict(MIX[2], rid=40), dict(MIX[4], rid=41), dict(R0, rid=42)]
+    res, _ = run_server(reqs, tick_steps=16, workers=1)
+    assert all(r["status"] == 0 for r in res.values())
+    a, b = res[40], res[41]
+    assert b["t_start"] >= a["t_end"] - 1e-3 or a["t_start"] >= b["t_end"] - 1e-3
 
 
 def test_server_amr_result_matches_program_loop():

@@ -1,6 +1,7 @@
 """The compact ghost-shell numbering of the AMR fine blocks (faces + edges, no corners) is a bijection
-onto [0, 6 MB^2 + 12 MB) and covers every cell a D3Q19 pull can reach.  Host-compiled check of the
-device header (no GPU)."""
+onto [0, 6 MB^2 + 12 MB) and covers every cell a D3Q19 pull can reach; the fine steps' pull
+addressing (neighbour slot + masked cell) equals the global-coordinate pull.  Host-compiled check of
+the device header (no GPU)."""
 import os
 import shutil
 import subprocess
@@ -29,6 +30,16 @@ template <int MB> int check() {
             bool in = li >= 0 && li < MB && lj >= 0 && lj < MB && lk >= 0 && lk < MB;
             int s = jp::amr::shell_index<MB>(li, lj, lk);
             if (!in && (s < 0 || s >= SH)) return 3;
+        }
+    // pull_src against the global coordinates of a block at (1,1,1) in a 3^3 grid of blocks
+    for (int k = 0; k < MB; ++k) for (int j = 0; j < MB; ++j) for (int i = 0; i < MB; ++i)
+        for (int q = 0; q < 19; ++q) {
+            const int gi = MB + i - jp::cx(q), gj = MB + j - jp::cy(q), gk = MB + k - jp::cz(q);
+            const int e_ref = (gk / MB) * 9 + (gj / MB) * 3 + gi / MB;
+            const int sc_ref = ((gk % MB) * MB + gj % MB) * MB + gi % MB;
+            int e, sc;
+            jp::amr::pull_src<MB>(q, i, j, k, e, sc);
+            if (e != e_ref || sc != sc_ref) return 3;
         }
     return 0;
 }
