@@ -168,30 +168,22 @@ __host__ __device__ __forceinline__ void pull_src(int q, int i, int j, int k, in
 }
 
 #ifdef __CUDACC__
-// The pull of the 19 populations of cell (i, j, k) of pool block b in two halves: pull_own loads
-// the values that come from b itself (it needs no table), pull_nbr the rest.  nb[e] is the pool
-// index of the same-level neighbour in slot e (pull_src), or -1 where that neighbour is not on this
-// level; then the value comes from b's ghost shell gh (GHOST = false: every neighbour exists).
-template <int MB>
-__device__ __forceinline__ void pull_own(const float* __restrict__ fa, int b, int i, int j, int k, float (&f)[Q]) {
-    constexpr int MB3 = MB * MB * MB;
+// Pull of the 19 populations of cell (i, j, k) of pool block b.  nbrow[e] (global memory, the
+// block's row of its level's neighbour table) is the pool index of the same-level neighbour in slot
+// e (pull_src), or -1 where that neighbour is not on this level; then the value comes from b's
+// ghost shell gh (GHOST = false: every neighbour exists).  Every thread reads the few table entries
+// its cell needs itself: the row is shared by the whole CTA and stays in L1, and no barrier stands
+// between a thread and its loads.
+template <int MB, bool GHOST>
+__device__ __forceinline__ void pull_cell(const float* __restrict__ fa, const float* __restrict__ gh,
+                                          const int* __restrict__ nbrow, int b, int i, int j, int k,
+                                          float (&f)[Q]) {
+    constexpr int MB3 = MB * MB * MB, SH = Geo<MB>::SH;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         int e, sc;
         pull_src<MB>(q, i, j, k, e, sc);
-        if (e == 13) f[q] = __ldg(fa + ((size_t)b * Q + q) * MB3 + sc);
-    }
-}
-template <int MB, bool GHOST>
-__device__ __forceinline__ void pull_nbr(const float* __restrict__ fa, const float* __restrict__ gh, const int* nb,
-                                         int b, int i, int j, int k, float (&f)[Q]) {
-    constexpr int MB3 = MB * MB * MB, SH = Geo<MB>::SH;
-#pragma unroll
-    for (int q = 1; q < Q; ++q) {
-        int e, sc;
-        pull_src<MB>(q, i, j, k, e, sc);
-        if (e == 13) continue;
-        const int blk = nb[e];
+        const int blk = e == 13 ? b : __ldg(nbrow + e);
         if (!GHOST || blk >= 0) {
             f[q] = __ldg(fa + ((size_t)blk * Q + q) * MB3 + sc);
         } else {

@@ -11,6 +11,7 @@ namespace jp {
 namespace amr {
 
 #define CELL_LOOP(c) for (int c = threadIdx.x; c < G::MB3; c += G::TPB)
+int default_step_tpb(int mb);
 
 // ---- TGV initial state of the coarse grid (src/tgv3d_amr.cu:431-440) ---------------------------
 template <int MB>
@@ -30,32 +31,29 @@ __global__ void __launch_bounds__(Geo<MB>::TPB) k_init(float* __restrict__ f, in
 
 // ---- dense periodic coarse step (src/tgv3d_amr.cu:203-220) ---------------------------------------
 template <int MB, int TPB>
-__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const float* __restrict__ fa, float* __restrict__ fb, int cgx,
-                                                 float om) {
+__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const float* __restrict__ fa, float* __restrict__ fb,
+                                                             int cgx, float om) {
     using G = Geo<MB>;
     const int b = blockIdx.x;
     const int bx = b % cgx, by = (b / cgx) % cgx, bz = b / (cgx * cgx);
-    __shared__ int snb[27];  // periodic neighbour blocks
+    __shared__ int snb[27];  // periodic neighbour blocks (arithmetic only: no loads wait on the barrier)
     if (threadIdx.x < 27) {
         const int dx = threadIdx.x % 3 - 1, dy = (threadIdx.x / 3) % 3 - 1, dz = threadIdx.x / 9 - 1;
         snb[threadIdx.x] = (((bz + dz + cgx) % cgx) * cgx + (by + dy + cgx) % cgx) * cgx + (bx + dx + cgx) % cgx;
     }
-    int cell = threadIdx.x;
-    int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-    float f[Q];
-    pull_own<MB>(fa, b, i, j, k, f);
     __syncthreads();
-    for (;;) {
-        pull_nbr<MB, false>(fa, nullptr, snb, b, i, j, k, f);
+    for (int cell = threadIdx.x; cell < G::MB3; cell += TPB) {
+        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+        float f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            int e, sc;
+            pull_src<MB>(q, i, j, k, e, sc);
+            f[q] = __ldg(fa + ((size_t)snb[e] * Q + q) * G::MB3 + sc);
+        }
         bgk_fast(f, om);
 #pragma unroll
         for (int q = 0; q < Q; ++q) fb[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
-        cell += TPB;
-        if (cell >= G::MB3) break;
-        i = cell % MB;
-        j = (cell / MB) % MB;
-        k = cell / (MB * MB);
-        pull_own<MB>(fa, b, i, j, k, f);
     }
 }
 
@@ -142,9 +140,7 @@ __global__ void __launch_bounds__(256) k_fill_l1(const float* __restrict__ pr, f
                                                 const int* __restrict__ nbtab, int cgx, int N) {
     using G = Geo<MB>;
     const int fb = blockIdx.x;
-    __shared__ int snb[27];
-    if (threadIdx.x < 27) snb[threadIdx.x] = __ldg(nbtab + (size_t)fb * 27 + threadIdx.x);
-    __syncthreads();
+    const int* nbrow = nbtab + (size_t)fb * 27;
     const int cb = pcb[fb], oct = poct[fb];
     const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
     const int ox = cbx * 2 * MB + (oct & 1) * MB, oy = cby * 2 * MB + ((oct >> 1) & 1) * MB, oz = cbz * 2 * MB + (oct >> 2) * MB;
@@ -152,7 +148,7 @@ __global__ void __launch_bounds__(256) k_fill_l1(const float* __restrict__ pr, f
     for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
-        if (snb[shell_slot<MB>(i, j, k)] >= 0) continue;
+        if (__ldg(nbrow + shell_slot<MB>(i, j, k)) >= 0) continue;
         const int gfi = pmod(ox + i, N1), gfj = pmod(oy + j, N1), gfk = pmod(oz + k, N1);
         float out[Q];
         prolong_prep_l0<MB>(pr, cgx, N, gfi, gfj, gfk, out);
@@ -168,9 +164,7 @@ __global__ void __launch_bounds__(256) k_fill_l2(const float* __restrict__ pr, f
                                                 const int* __restrict__ nbtab, int l1gx, int N1) {
     using G = Geo<MB>;
     const int b = blockIdx.x;
-    __shared__ int snb[27];
-    if (threadIdx.x < 27) snb[threadIdx.x] = __ldg(nbtab + (size_t)b * 27 + threadIdx.x);
-    __syncthreads();
+    const int* nbrow = nbtab + (size_t)b * 27;
     const int pl1 = l2pl1[b], oct = l2oct[b];
     const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
     const int ox = px * 2 * MB + (oct & 1) * MB, oy = py * 2 * MB + ((oct >> 1) & 1) * MB, oz = pz * 2 * MB + (oct >> 2) * MB;
@@ -178,7 +172,7 @@ __global__ void __launch_bounds__(256) k_fill_l2(const float* __restrict__ pr, f
     for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
-        if (snb[shell_slot<MB>(i, j, k)] >= 0) continue;
+        if (__ldg(nbrow + shell_slot<MB>(i, j, k)) >= 0) continue;
         const int g2i = pmod(ox + i, N2), g2j = pmod(oy + j, N2), g2k = pmod(oz + k, N2);
         float out[Q];
         prolong_prep_l1<MB>(pr, l1grid, l1gx, N1, g2i, g2j, g2k, out);
@@ -257,41 +251,32 @@ __global__ void k_nbtab_l2(int* __restrict__ nb, const int* __restrict__ l2pl1, 
 
 // ---- fine steps (src/tgv3d_amr.cu:241-274, 331-356) -----------------------------------------------
 // One kernel for both fine levels: the neighbour table says, per offset, which pool block holds the
-// pulled cells or that they come from the ghost shell.  The CTA issues its own-block loads for its
-// first cells while the table is read, then the neighbour loads.  TPB threads share the block's
-// MB^3 cells.  FUSE: this is the last substep before the restriction into the parent level, so the
-// block also restricts itself into its parent octant (`parent`, `poct`), which saves re-reading the
-// level from HBM in a separate restriction kernel.
+// pulled cells or that they come from the ghost shell.  TPB threads share the block's MB^3 cells.
+// FUSE: this is the last substep before the restriction into the parent level, so the block also
+// restricts itself into its parent octant (`parent`, `poct`), which saves re-reading the level from
+// HBM in a separate restriction kernel.
 template <int MB, int TPB, bool FUSE>
 __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_fine(const float* __restrict__ fa, float* __restrict__ fbuf,
-                                                   const float* __restrict__ gh, const int* __restrict__ nbtab,
-                                                   const int* __restrict__ parent, const int* __restrict__ poct,
-                                                   float om, float* __restrict__ parent_pool, float nqi) {
+                                                               const float* __restrict__ gh,
+                                                               const int* __restrict__ nbtab,
+                                                               const int* __restrict__ parent,
+                                                               const int* __restrict__ poct, float om,
+                                                               float* __restrict__ parent_pool, float nqi) {
     static_assert(Geo<MB>::MB3 % TPB == 0, "cells must split evenly over the CTA");
     extern __shared__ float sf[];
     using G = Geo<MB>;
     const int b = blockIdx.x;
-    __shared__ int snb[27];
-    if (threadIdx.x < 27) snb[threadIdx.x] = __ldg(nbtab + (size_t)b * 27 + threadIdx.x);
-    int cell = threadIdx.x;
-    int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-    float f[Q];
-    pull_own<MB>(fa, b, i, j, k, f);
-    __syncthreads();
-    for (;;) {
-        pull_nbr<MB, true>(fa, gh, snb, b, i, j, k, f);
+    const int* nbrow = nbtab + (size_t)b * 27;
+    for (int cell = threadIdx.x; cell < G::MB3; cell += TPB) {
+        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+        float f[Q];
+        pull_cell<MB, true>(fa, gh, nbrow, b, i, j, k, f);
         bgk_fast(f, om);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
             if (FUSE) sf[q * G::MB3 + cell] = f[q];
         }
-        cell += TPB;
-        if (cell >= G::MB3) break;
-        i = cell % MB;
-        j = (cell / MB) % MB;
-        k = cell / (MB * MB);
-        pull_own<MB>(fa, b, i, j, k, f);
     }
     if (FUSE) {
         __syncthreads();
@@ -578,7 +563,7 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
         case OP_STEP_L0:
         case OP_STEP_L1:
         case OP_STEP_L2: {
-            const int tpb = L.tpb ? L.tpb : G::TPB;
+            const int tpb = L.tpb ? L.tpb : default_step_tpb(MB);
             if constexpr (MB == 4) {
                 if (tpb != 64) return cudaErrorInvalidConfiguration;
                 launch_steps<MB, 64>(L, op);
@@ -645,6 +630,9 @@ cudaError_t amr_launch(int mb, int op, const AmrLaunch& L) {
 
 int shell_cells(int mb) { return 6 * mb * mb + 12 * mb; }
 bool can_fuse_restrict(int mb) { return mb <= 8; }
+// measured on the GB300 (static gold N0=64, all levels refined): 256 threads (two cells each) are
+// the fastest split at MB = 8, 512 at MB = 16
+int default_step_tpb(int mb) { return mb == 4 ? 64 : (mb == 8 ? 256 : 512); }
 bool step_tpb_supported(int mb, int tpb) {
     if (mb == 4) return tpb == 64;
     return (mb == 8 || mb == 16) && (tpb == 128 || tpb == 256 || tpb == 512);

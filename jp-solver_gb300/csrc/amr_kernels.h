@@ -36,7 +36,7 @@ struct AmrLaunch {
     const int *t0 = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr, *t6 = nullptr;
     const int* nbt = nullptr;  // same-level neighbour table of the fine level (27 per block)
     int* iout = nullptr;
-    int tpb = 0;               // threads per CTA of the steps (0: min(MB^3, 512))
+    int tpb = 0;               // threads per CTA of the steps (0: default_step_tpb)
     int cgx = 0, n = 0, l1gx = 0, n1 = 0, n2 = 0;
     float omega = 0.f, scale = 0.f;
     double u0 = 0.0, kf = 0.0;
@@ -46,8 +46,9 @@ cudaError_t amr_launch(int mb, int op, const AmrLaunch& L);
 int shell_cells(int mb);
 // the fused restriction stages a block in shared memory: MB <= 8 (38 KiB at MB = 8)
 bool can_fuse_restrict(int mb);
-// threads per CTA a step of block edge mb can run with
+// threads per CTA a step of block edge mb can run with, and the default
 bool step_tpb_supported(int mb, int tpb);
+int default_step_tpb(int mb);
 
 // ---- adaptation pipeline (adapt.cu) ------------------------------------------------------------
 // Device counters shared by the pipeline; the host reads them once per stage.

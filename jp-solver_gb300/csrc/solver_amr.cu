@@ -37,7 +37,7 @@ struct AmrState {
     int *o_ref0 = nullptr, *o_fof0 = nullptr, *o_l1grid = nullptr, *o_ref1 = nullptr, *o_fof1 = nullptr;
     int *rank = nullptr, *deep = nullptr, *flags = nullptr;
     int *nb1 = nullptr, *nb2 = nullptr;  // same-level neighbour tables of the fine levels (27 per block)
-    int tpb = 0;                         // threads per CTA of the steps (0: min(MB^3, 512))
+    int tpb = 0;                         // threads per CTA of the steps (0: default_step_tpb)
     float *sen0 = nullptr, *sen1 = nullptr;
     float *ov_sen0 = nullptr, *ov_sen1pos = nullptr;
     AdaptCounts* cnt_dev = nullptr;
