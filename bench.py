@@ -219,12 +219,13 @@ def c5_requests(J, n_req: int, rate: float, seed: int) -> list:
     return out
 
 
-def serve_run(J, reqs: list, device: int, open_loop: bool, max_active: int = 0, tick: int = 64) -> dict:
+def serve_run(J, reqs: list, device: int, open_loop: bool, max_active: int = 0, tick: int = 64,
+              workers: int = 0) -> dict:
     """Drive the server: open loop submits each request at its arrival time, closed loop submits all
     at once.  Returns throughput and latency percentiles (submit to result)."""
     import numpy as np
 
-    sv = J.Server(device=device, pool_gb=120.0, max_active=max_active, tick_steps=tick)
+    sv = J.Server(device=device, pool_gb=120.0, max_active=max_active, tick_steps=tick, workers=workers)
     t0 = time.perf_counter()
     i, res = 0, {}
     if not open_loop:

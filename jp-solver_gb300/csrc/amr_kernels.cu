@@ -60,8 +60,10 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const float* __rest
 // ---- prolongation sources on a block list (src/tgv3d_amr.cu:160-171) -----------------------------
 template <int MB>
 __global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const float* __restrict__ fin, float* __restrict__ pr,
-                                                      const int* __restrict__ list, float nqs) {
+                                                      const int* __restrict__ list, float nqs,
+                                                      const int* __restrict__ nlim) {
     using G = Geo<MB>;
+    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
     const int b = list[blockIdx.x];
     CELL_LOOP(cell) {
         float f[Q];
@@ -137,8 +139,10 @@ __device__ __forceinline__ void prolong_prep_l1(const float* __restrict__ pr, co
 template <int MB>
 __global__ void __launch_bounds__(256) k_fill_l1(const float* __restrict__ pr, float* __restrict__ gh,
                                                 const int* __restrict__ pcb, const int* __restrict__ poct,
-                                                const int* __restrict__ nbtab, int cgx, int N) {
+                                                const int* __restrict__ nbtab, int cgx, int N,
+                                                const int* __restrict__ nlim) {
     using G = Geo<MB>;
+    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
     const int fb = blockIdx.x;
     const int* nbrow = nbtab + (size_t)fb * 27;
     const int cb = pcb[fb], oct = poct[fb];
@@ -161,8 +165,10 @@ template <int MB>
 __global__ void __launch_bounds__(256) k_fill_l2(const float* __restrict__ pr, float* __restrict__ gh,
                                                 const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
                                                 const int* __restrict__ f1pos, const int* __restrict__ l1grid,
-                                                const int* __restrict__ nbtab, int l1gx, int N1) {
+                                                const int* __restrict__ nbtab, int l1gx, int N1,
+                                                const int* __restrict__ nlim) {
     using G = Geo<MB>;
+    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
     const int b = blockIdx.x;
     const int* nbrow = nbtab + (size_t)b * 27;
     const int pl1 = l2pl1[b], oct = l2oct[b];
@@ -261,10 +267,12 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_fine(const float* __re
                                                                const int* __restrict__ nbtab,
                                                                const int* __restrict__ parent,
                                                                const int* __restrict__ poct, float om,
-                                                               float* __restrict__ parent_pool, float nqi) {
+                                                               float* __restrict__ parent_pool, float nqi,
+                                                               const int* __restrict__ nlim) {
     static_assert(Geo<MB>::MB3 % TPB == 0, "cells must split evenly over the CTA");
     extern __shared__ float sf[];
     using G = Geo<MB>;
+    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;  // whole CTA: the barrier below stays uniform
     const int b = blockIdx.x;
     const int* nbrow = nbtab + (size_t)b * 27;
     for (int cell = threadIdx.x; cell < G::MB3; cell += TPB) {
@@ -290,8 +298,9 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_fine(const float* __re
 template <int MB>
 __global__ void __launch_bounds__(Geo<MB>::TPB) k_restrict(float* __restrict__ cf, const float* __restrict__ ff,
                                                           const int* __restrict__ rl, const int* __restrict__ fof,
-                                                          float nqi) {
+                                                          float nqi, const int* __restrict__ nlim) {
     using G = Geo<MB>;
+    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
     const int cb = rl[blockIdx.x];
     const int fbase = fof[cb];
     CELL_LOOP(cell) {
@@ -543,12 +552,12 @@ static void launch_steps(const AmrLaunch& L, int op) {
     if constexpr (MB <= 8) {
         if (L.out2) {
             k_step_fine<MB, TPB, true><<<L.nblocks, TPB, sizeof(float) * Q * G::MB3, L.st>>>(
-                L.in, L.out, L.aux, L.nbt, parent, L.t1, L.omega, L.out2, L.scale);
+                L.in, L.out, L.aux, L.nbt, parent, L.t1, L.omega, L.out2, L.scale, L.nlim);
             return;
         }
     }
     k_step_fine<MB, TPB, false><<<L.nblocks, TPB, 0, L.st>>>(L.in, L.out, L.aux, L.nbt, parent, L.t1, L.omega,
-                                                             nullptr, 0.f);
+                                                             nullptr, 0.f, L.nlim);
 }
 
 template <int MB>
@@ -584,16 +593,17 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
                                                                                   L.t4, L.t5, L.l1gx, L.nblocks);
             break;
         case OP_PREP:
-            k_prep<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.list, L.scale);
+            k_prep<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.list, L.scale, L.nlim);
             break;
         case OP_FILL_L1:
-            k_fill_l1<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.nbt, L.cgx, L.n);
+            k_fill_l1<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.nbt, L.cgx, L.n, L.nlim);
             break;
         case OP_FILL_L2:
-            k_fill_l2<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.t2, L.t3, L.nbt, L.l1gx, L.n1);
+            k_fill_l2<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.t2, L.t3, L.nbt, L.l1gx, L.n1,
+                                                       L.nlim);
             break;
         case OP_RESTRICT:
-            k_restrict<MB><<<L.nblocks, cta, 0, L.st>>>(L.out, L.in, L.list, L.t0, L.scale);
+            k_restrict<MB><<<L.nblocks, cta, 0, L.st>>>(L.out, L.in, L.list, L.t0, L.scale, L.nlim);
             break;
         case OP_SEED_L1:
             k_seed_l1<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.cgx, L.n, L.scale);

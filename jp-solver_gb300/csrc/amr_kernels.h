@@ -37,6 +37,9 @@ struct AmrLaunch {
     const int* nbt = nullptr;  // same-level neighbour table of the fine level (27 per block)
     int* iout = nullptr;
     int tpb = 0;               // threads per CTA of the steps (0: default_step_tpb)
+    // device count of the blocks to process (prep, fill, fine step, restrict): the grid is sized
+    // for the capacity and CTAs past *nlim return, so a captured step stays valid after a regrid
+    const int* nlim = nullptr;
     int cgx = 0, n = 0, l1gx = 0, n1 = 0, n2 = 0;
     float omega = 0.f, scale = 0.f;
     double u0 = 0.0, kf = 0.0;

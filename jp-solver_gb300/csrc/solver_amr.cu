@@ -45,18 +45,30 @@ struct AmrState {
     int nref0 = 0, nf1 = 0, nref1 = 0, nf2 = 0, n_skin0 = 0, n_skin1 = 0, ndeep = 0;
     float* field = nullptr;
     std::vector<void*> owned;
-    // captured base_step graphs, one per parity of the coarse ping-pong (the fine levels swap an even
-    // number of times per step and return to their buffers); dropped whenever the grid changes
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    float* c0_home = nullptr;
+    // Block counts the step kernels read on the device ({nf1, nf2, n_skin0, n_skin1, nref0, nref1}):
+    // the step launches grids sized for the pool capacities, so one captured step serves every grid
+    // a regrid builds within them.
+    int* step_cnt = nullptr;
+    int* step_cnt_host = nullptr;  // pinned staging of the upload
+    // captured base_step graphs, one per combination of the ping-pong parities of the three levels
+    // (a coarse step swaps level 0 once and the fine levels an even number of times; a regrid's
+    // seeding swaps a fine level once).  Dropped only when buffers move (pool growth, new initial
+    // build) or the launch shape changes.
+    cudaGraphExec_t graph[8] = {};
+    float *c0_home = nullptr, *f1_home = nullptr, *f2_home = nullptr;
 };
+enum { SC_NF1 = 0, SC_NF2, SC_SKIN0, SC_SKIN1, SC_NREF0, SC_NREF1, SC_COUNT };
 
-static void drop_graphs(AmrState* a) {
+// drop the captured steps and take the current buffers as the parity reference
+static void reset_graphs(AmrState* a) {
     for (auto& g : a->graph)
         if (g) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
+    a->c0_home = a->c0a;
+    a->f1_home = a->f1a;
+    a->f2_home = a->f2a;
 }
 
 #define ACK(call, what)                                     \
@@ -142,6 +154,20 @@ static jp_status step_l0(jp_solver* s) {
     return JP_OK;
 }
 
+// the host's block counts of the current grid to the device copy the step kernels read
+static jp_status upload_counts(jp_solver* s) {
+    AmrState* a = s->amr;
+    int* h = a->step_cnt_host;
+    h[SC_NF1] = a->nf1;
+    h[SC_NF2] = a->nf2;
+    h[SC_SKIN0] = a->n_skin0;
+    h[SC_SKIN1] = a->n_skin1;
+    h[SC_NREF0] = a->nref0;
+    h[SC_NREF1] = a->nref1;
+    ACK(cudaMemcpyAsync(a->step_cnt, h, sizeof(int) * SC_COUNT, cudaMemcpyHostToDevice, s->stream), "counts H2D");
+    return JP_OK;
+}
+
 static jp_status skins(jp_solver* s) {
     AmrState* a = s->amr;
     ACK(adapt_skins(a->ref0, a->cnb0, a->cgx, a->ref1, a->f1pos, a->l1grid, a->nf1, a->l1gx, a->flags, a->skin0,
@@ -149,7 +175,7 @@ static jp_status skins(jp_solver* s) {
     TRY(read_counts(s));
     a->n_skin0 = a->cnt_host->n_skin0;
     a->n_skin1 = a->cnt_host->n_skin1;
-    return JP_OK;
+    return upload_counts(s);
 }
 
 static jp_status check_err(jp_solver* s) {
@@ -209,6 +235,7 @@ static jp_status grow_l1(jp_solver* s, int needed) {
     TRY(regrow(s, a->rank, std::max(a->cnb0, cap), 0));
     TRY(regrow(s, a->flags, (size_t)a->cnb0 + cap, 0));
     TRY(regrow(s, a->nb1, (size_t)cap * 27, 0));
+    reset_graphs(a);
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * cap, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * cap, s->stream), "memset");
     a->cap1 = cap;
@@ -229,6 +256,7 @@ static jp_status grow_l2(jp_solver* s, int needed) {
     TRY(regrow(s, a->l2pl1, cap, 0));
     TRY(regrow(s, a->l2oct, cap, 0));
     TRY(regrow(s, a->nb2, (size_t)cap * 27, 0));
+    reset_graphs(a);
     a->cap2 = cap;
     update_bytes(s);
     return JP_OK;
@@ -450,24 +478,27 @@ static jp_status regrid(jp_solver* s) {
 }
 
 // base_step (src/tgv3d_amr.cu:821-837): coarse once, level 1 twice, level 2 four times, restricting
-// level 2 into level 1 after each pair and level 1 into level 0 at the end.
+// level 2 into level 1 after each pair and level 1 into level 0 at the end.  Launch shapes depend on
+// the pool capacities only; the kernels read the block counts of the current grid on the device.
 static jp_status base_step(jp_solver* s) {
     AmrState* a = s->amr;
     const bool skip_prep = s->cfg.flags & JP_FLAG_SKIP_PREP, skip_restrict = s->cfg.flags & JP_FLAG_SKIP_RESTRICT;
     // restrictions fused into the last substep of each fine level (same values, one pass less)
     const bool fuse = !skip_restrict && can_fuse_restrict(a->MB);
+    const int* cnt = a->step_cnt;
     TRY(step_l0(s));
-    if (!a->nf1) return JP_OK;
     if (!skip_prep) {
         AmrLaunch L;
-        L.nblocks = a->n_skin0;
+        L.nblocks = a->cnb0;
+        L.nlim = cnt + SC_SKIN0;
         L.in = a->c0a;
         L.out = a->prep0;
         L.list = a->skin0;
         L.scale = float(a->nqs01);
         TRY(launch(s, OP_PREP, L));
         AmrLaunch F;
-        F.nblocks = a->nf1;
+        F.nblocks = a->cap1;
+        F.nlim = cnt + SC_NF1;
         F.in = a->prep0;
         F.out = a->gh1;
         F.t0 = a->pcb;
@@ -478,16 +509,18 @@ static jp_status base_step(jp_solver* s) {
         TRY(launch(s, OP_FILL_L1, F));
     }
     for (int s1 = 0; s1 < 2; ++s1) {
-        if (a->nf2 && !skip_prep) {
+        if (!skip_prep) {
             AmrLaunch L;
-            L.nblocks = a->n_skin1;
+            L.nblocks = a->cap1;
+            L.nlim = cnt + SC_SKIN1;
             L.in = a->f1a;
             L.out = a->prep1;
             L.list = a->skin1;
             L.scale = float(a->nqs12);
             TRY(launch(s, OP_PREP, L));
             AmrLaunch F;
-            F.nblocks = a->nf2;
+            F.nblocks = a->cap2;
+            F.nlim = cnt + SC_NF2;
             F.in = a->prep1;
             F.out = a->gh2;
             F.t0 = a->l2pl1;
@@ -499,36 +532,39 @@ static jp_status base_step(jp_solver* s) {
             F.n1 = a->N1;
             TRY(launch(s, OP_FILL_L2, F));
         }
-        if (a->nf2) {
-            for (int s2 = 0; s2 < 2; ++s2) {
-                AmrLaunch S;
-                S.nblocks = a->nf2;
-                S.in = a->f2a;
-                S.out = a->f2b;
-                S.aux = a->gh2;
-                S.nbt = a->nb2;
-                S.t0 = a->l2pl1;
-                S.t1 = a->l2oct;
-                S.omega = a->om2;
-                S.tpb = a->tpb;
-                if (s2 == 1 && fuse) {  // last level-2 substep restricts itself into level 1
-                    S.out2 = a->f1a;
-                    S.scale = float(a->nqi21);
-                }
-                TRY(launch(s, OP_STEP_L2, S));
-                std::swap(a->f2a, a->f2b);
+        for (int s2 = 0; s2 < 2; ++s2) {
+            AmrLaunch S;
+            S.nblocks = a->cap2;
+            S.nlim = cnt + SC_NF2;
+            S.in = a->f2a;
+            S.out = a->f2b;
+            S.aux = a->gh2;
+            S.nbt = a->nb2;
+            S.t0 = a->l2pl1;
+            S.t1 = a->l2oct;
+            S.omega = a->om2;
+            S.tpb = a->tpb;
+            if (s2 == 1 && fuse) {  // last level-2 substep restricts itself into level 1
+                S.out2 = a->f1a;
+                S.scale = float(a->nqi21);
             }
+            TRY(launch(s, OP_STEP_L2, S));
+            std::swap(a->f2a, a->f2b);
+        }
+        if (!skip_restrict && !fuse) {
             AmrLaunch R;
-            R.nblocks = a->nref1;
+            R.nblocks = (a->cap2 + 7) / 8;
+            R.nlim = cnt + SC_NREF1;
             R.out = a->f1a;
             R.in = a->f2a;
             R.list = a->rl1;
             R.t0 = a->fof1;
             R.scale = float(a->nqi21);
-            if (!skip_restrict && !fuse) TRY(launch(s, OP_RESTRICT, R));
+            TRY(launch(s, OP_RESTRICT, R));
         }
         AmrLaunch S;
-        S.nblocks = a->nf1;
+        S.nblocks = a->cap1;
+        S.nlim = cnt + SC_NF1;
         S.in = a->f1a;
         S.out = a->f1b;
         S.aux = a->gh1;
@@ -544,41 +580,46 @@ static jp_status base_step(jp_solver* s) {
         TRY(launch(s, OP_STEP_L1, S));
         std::swap(a->f1a, a->f1b);
     }
+    if (skip_restrict || fuse) return JP_OK;
     AmrLaunch R;
-    R.nblocks = a->nref0;
+    R.nblocks = (a->cap1 + 7) / 8;
+    R.nlim = cnt + SC_NREF0;
     R.out = a->c0a;
     R.in = a->f1a;
     R.list = a->rl0;
     R.t0 = a->fof0;
     R.scale = float(a->nqi10);
-    if (skip_restrict || fuse) return JP_OK;
     return launch(s, OP_RESTRICT, R);
 }
 
-// base_step replayed from a captured graph (captured on first use for each coarse parity)
+// base_step replayed from a captured graph (captured on first use for each parity combination)
 static jp_status graph_step(jp_solver* s) {
     AmrState* a = s->amr;
-    const int par = a->c0a == a->c0_home ? 0 : 1;
-    if (!a->graph[par]) {
-        float* c0a = a->c0a;
-        float* c0b = a->c0b;
+    const int key = (a->c0a == a->c0_home ? 0 : 1) | (a->f1a == a->f1_home ? 0 : 2) | (a->f2a == a->f2_home ? 0 : 4);
+    if (!a->graph[key]) {
+        float *c0a = a->c0a, *c0b = a->c0b, *f1a = a->f1a, *f1b = a->f1b, *f2a = a->f2a, *f2b = a->f2b;
         ACK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         jp_status st = base_step(s);
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(s->stream, &g);
-        a->c0a = c0a;  // the capture only recorded the step; the replay below performs it
+        // the capture only recorded the step; the replay below performs it
+        a->c0a = c0a;
         a->c0b = c0b;
+        a->f1a = f1a;
+        a->f1b = f1b;
+        a->f2a = f2a;
+        a->f2b = f2b;
         if (st != JP_OK) {
             if (g) cudaGraphDestroy(g);
             return st;
         }
         if (e != cudaSuccess) return cuda_fail(e, "end capture");
-        e = cudaGraphInstantiate(&a->graph[par], g, 0);
+        e = cudaGraphInstantiate(&a->graph[key], g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
     }
-    ACK(cudaGraphLaunch(a->graph[par], s->stream), "graph launch");
-    std::swap(a->c0a, a->c0b);
+    ACK(cudaGraphLaunch(a->graph[key], s->stream), "graph launch");
+    std::swap(a->c0a, a->c0b);  // the fine levels return to their buffers within the step
     return JP_OK;
 }
 
@@ -652,6 +693,9 @@ jp_status amr_create(jp_solver* s) {
     TRY(dalloc(a, &a->flags, (size_t)a->cnb0 + a->cap1, "cudaMalloc flags"));
     TRY(dalloc(a, &a->sen1, (size_t)a->cap1, "cudaMalloc sen1"));
     TRY(dalloc(a, &a->nb1, (size_t)a->cap1 * 27, "cudaMalloc nb1"));
+    TRY(dalloc(a, &a->step_cnt, SC_COUNT, "cudaMalloc step counts"));
+    a->step_cnt_host = (int*)pinned_slot_alloc();
+    if (!a->step_cnt_host) return fail(JP_ERR_NOMEM, "pinned host slot");
     TRY(dalloc(a, &a->cnt_dev, 1, "cudaMalloc counts"));
     static_assert(sizeof(AdaptCounts) <= 256, "counts exceed a pinned slot");
     a->cnt_host = (AdaptCounts*)pinned_slot_alloc();
@@ -668,9 +712,10 @@ jp_status amr_create(jp_solver* s) {
 void amr_destroy(jp_solver* s) {
     AmrState* a = s->amr;
     if (!a) return;
-    drop_graphs(a);
+    reset_graphs(a);
     for (void* p : a->owned) dev_free(s, p);
     pinned_slot_free(a->cnt_host);
+    pinned_slot_free(a->step_cnt_host);
     dev_free(s, a->field);
     delete a;
     s->amr = nullptr;
@@ -679,7 +724,7 @@ void amr_destroy(jp_solver* s) {
 // TGV state on the coarse grid and the initial build (with the sensor override, if one is set)
 jp_status amr_init(jp_solver* s) {
     AmrState* a = s->amr;
-    drop_graphs(a);
+    reset_graphs(a);
     AmrLaunch L;
     L.nblocks = a->cnb0;
     L.out = a->c0a;
@@ -690,7 +735,7 @@ jp_status amr_init(jp_solver* s) {
     a->hw_nf1 = a->hw_nf2 = 0;
     TRY(initial_build(s));
     ACK(wait_stream(s), "initial build");
-    a->c0_home = a->c0a;
+    reset_graphs(a);  // the level-2 pool was allocated anew
     s->step_count = 0;
     update_bytes(s);
     return JP_OK;
@@ -707,15 +752,14 @@ jp_status amr_step(jp_solver* s, int64_t nsteps) {
 
 jp_status amr_set_step_tpb(jp_solver* s, int tpb) {
     if (tpb && !step_tpb_supported(s->amr->MB, tpb)) return fail(JP_ERR_INVALID, "threads_per_block %d", tpb);
-    drop_graphs(s->amr);
+    reset_graphs(s->amr);
     s->amr->tpb = tpb;
     s->cfg.threads_per_block = tpb;
     return JP_OK;
 }
 
 jp_status amr_regrid(jp_solver* s) {
-    drop_graphs(s->amr);
-    TRY(regrid(s));
+    TRY(regrid(s));  // the captured steps stay valid unless a pool grew (grow_l1/grow_l2 drop them)
     ACK(wait_stream(s), "regrid");
     return JP_OK;
 }
