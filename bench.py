@@ -243,12 +243,15 @@ def serve_run(J, reqs: list, device: int, open_loop: bool, max_active: int = 0, 
         if a == 0 and q == 0 and i < len(reqs):
             time.sleep(min(0.002, max(0.0, reqs[i][0] - (time.perf_counter() - t0))))
     span = time.perf_counter() - t0
+    stats = sv.stats()
     sv.close()
     lat = np.array([r["t_end"] - r["t_submit"] for r in res.values()])
     ok = sum(1 for r in res.values() if r["status"] == 0)
     return {"solves": len(res), "ok": ok, "seconds": span, "solves_per_s": len(res) / span,
             "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-            "valid": sum(1 for r in res.values() if r["valid"])}
+            "valid": sum(1 for r in res.values() if r["valid"]),
+            "host_seconds": {k: round(v, 3) for k, v in stats.items() if k.endswith("_s")},
+            "events": {k: v for k, v in stats.items() if not k.endswith("_s")}}
 
 
 def bench_serve(J, args, device: int) -> dict:

@@ -120,7 +120,7 @@ int32_t jp_abi_version(void);
 const char* jp_build_info(void);
 
 /* sizeof of the ABI structs: 0 jp_config, 1 jp_info, 2 jp_amr_counts, 3 jp_server_config,
- * 4 jp_request, 5 jp_result; else 0.  Lets an FFI binding check its struct mirrors against the
+ * 4 jp_request, 5 jp_result, 6 jp_server_stats; else 0.  Lets an FFI binding check its struct mirrors against the
  * library it loaded. */
 size_t jp_sizeof(int32_t which);
 
@@ -301,6 +301,19 @@ jp_status jp_server_tick(jp_server* sv, int32_t* active, int32_t* queued);
 int32_t jp_server_poll(jp_server* sv, jp_result* out, int32_t max);
 /* Seconds since the server was created (the clock of jp_result timestamps). */
 double jp_server_clock(const jp_server* sv);
+/* Where the server's host time went: cumulative seconds of the calls made for solves, summed over
+ * the tick thread and the AMR workers (so they can exceed the wall clock), and event counts. */
+typedef struct jp_server_stats {
+    double create_s;         /* solver creation: allocation, initial state, initial build */
+    double step_s;           /* issuing lattice steps (uniform batches, AMR steps / graph replays) */
+    double regrid_s;         /* AMR regrids, including their read-backs */
+    double diag_s;           /* diagnostics, including the wait for the result */
+    double destroy_s;        /* retiring solves */
+    double tick_s;           /* inside jp_server_tick */
+    int64_t solves, regrids, diags, coarse_steps;
+    int64_t reserved[8];
+} jp_server_stats;
+jp_status jp_server_get_stats(const jp_server* sv, jp_server_stats* out);
 
 /* ---- autotuning (extension; no counterpart in the reference) ------------------------- */
 

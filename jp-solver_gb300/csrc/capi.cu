@@ -126,6 +126,7 @@ size_t jp_sizeof(int32_t which) {
         case 3: return sizeof(jp_server_config);
         case 4: return sizeof(jp_request);
         case 5: return sizeof(jp_result);
+        case 6: return sizeof(jp_server_stats);
     }
     return 0;
 }

@@ -209,10 +209,23 @@ struct jp_server {
     std::vector<Job*> amr_fin;
     int amr_live = 0;                  // admitted AMR solves not yet retired (tick thread only)
     std::atomic<bool> stop{false};
+    std::mutex stats_mu;
+    jp_server_stats stats{};
+    void add(double jp_server_stats::*field, double seconds, int64_t jp_server_stats::*count = nullptr,
+             int64_t n = 1) {
+        std::lock_guard<std::mutex> lk(stats_mu);
+        stats.*field += seconds;
+        if (count) stats.*count += n;
+    }
     double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 };
 
 namespace {
+
+double seconds_since(std::chrono::steady_clock::time_point t) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t).count();
+}
+using clk = std::chrono::steady_clock;
 
 void finish(jp_server* sv, Job* j, jp_status status) {
     jp_result r;
@@ -232,8 +245,16 @@ void finish(jp_server* sv, Job* j, jp_status status) {
     r.t_end = sv->now();
     r.bytes = j->bytes;
     sv->done.push_back(r);
-    if (j->s) jp_destroy(j->s);
+    if (j->s) {
+        const auto t = clk::now();
+        jp_destroy(j->s);
+        sv->add(&jp_server_stats::destroy_s, seconds_since(t));
+    }
     if (j->admitted) sv->used -= j->bytes;
+    {
+        std::lock_guard<std::mutex> lk(sv->stats_mu);
+        ++sv->stats.solves;
+    }
     delete j;
 }
 
@@ -268,7 +289,9 @@ void run_amr(jp_server* sv, Job* j) {
         j->error = JP_ERR_CUDA;
         return;
     }
+    auto t = clk::now();
     jp_status st = create_solver(&j->req.cfg, sv->pool, &j->s);
+    sv->add(&jp_server_stats::create_s, seconds_since(t));
     if (st != JP_OK) {
         j->s = nullptr;
         if (st == JP_ERR_NOMEM) j->requeue = true;  // the estimate was optimistic: wait for memory
@@ -289,13 +312,21 @@ void run_amr(jp_server* sv, Job* j) {
         }
         const bool rg = j->dynamic && s_ > 0 && s_ % j->adapt == 0, dg = s_ % j->diagK == 0;
         if ((rg || dg) && pending) {
+            t = clk::now();
             st = jp_step(j->s, pending);
+            sv->add(&jp_server_stats::step_s, seconds_since(t), &jp_server_stats::coarse_steps, pending);
             pending = 0;
         }
-        if (st == JP_OK && rg) st = jp_regrid(j->s);
+        if (st == JP_OK && rg) {
+            t = clk::now();
+            st = jp_regrid(j->s);
+            sv->add(&jp_server_stats::regrid_s, seconds_since(t), &jp_server_stats::regrids);
+        }
         if (st == JP_OK && dg) {
             double d[3];
+            t = clk::now();
             st = jp_diag(j->s, d);
+            sv->add(&jp_server_stats::diag_s, seconds_since(t), &jp_server_stats::diags);
             if (st == JP_OK) {
                 j->step = s_;
                 record(j, d);
@@ -303,9 +334,15 @@ void run_amr(jp_server* sv, Job* j) {
         }
         if (s_ < j->steps) pending += sstep;
     }
-    if (st == JP_OK && pending) st = jp_step(j->s, pending);
+    if (st == JP_OK && pending) {
+        t = clk::now();
+        st = jp_step(j->s, pending);
+        sv->add(&jp_server_stats::step_s, seconds_since(t), &jp_server_stats::coarse_steps, pending);
+    }
     j->error = st;
+    t = clk::now();
     jp_destroy(j->s);  // pooled memory returns in stream order behind the last step
+    sv->add(&jp_server_stats::destroy_s, seconds_since(t));
     j->s = nullptr;
 }
 
@@ -418,8 +455,26 @@ jp_status jp_server_submit(jp_server* sv, const jp_request* req) {
     return JP_OK;
 }
 
+static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued);
+
 jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
     if (!sv) return fail(JP_ERR_INVALID, "null server");
+    const auto t = clk::now();
+    const jp_status st = server_tick(sv, n_active, n_queued);
+    sv->add(&jp_server_stats::tick_s, seconds_since(t));
+    return st;
+}
+
+jp_status jp_server_get_stats(const jp_server* sv, jp_server_stats* out) {
+    if (!sv || !out) return fail(JP_ERR_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(const_cast<jp_server*>(sv)->stats_mu);
+    *out = sv->stats;
+    return JP_OK;
+}
+
+}  // extern "C"
+
+static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
     ECK(cudaSetDevice(sv->cfg.device), "cudaSetDevice");
     // 1. retire the AMR solves the workers finished (their memory is back in the pool)
     std::vector<Job*> fin, requeued;
@@ -464,7 +519,9 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
             sv->cv_todo.notify_one();
             continue;
         }
+        const auto tc = clk::now();
         jp_status st = create_solver(&j->req.cfg, sv->pool, &j->s);
+        sv->add(&jp_server_stats::create_s, seconds_since(tc));
         if (st == JP_ERR_NOMEM) {  // the estimate was optimistic: wait for memory to free up
             j->s = nullptr;
             sv->queue.insert(it, j);
@@ -495,6 +552,7 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
     std::vector<Job*> uni_diag;
     for (Job* j : sv->active)
         if (j->error == JP_OK && j->need_diag) uni_diag.push_back(j);
+    const auto td = clk::now();
     if (!uni_diag.empty()) {
         if ((int)uni_diag.size() > sv->diag_cap) {
             ECK(cudaStreamSynchronize(sv->stream), "diag slots");
@@ -516,6 +574,7 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
                             sv->stream), "diag D2H");
         ECK(cudaStreamSynchronize(sv->stream), "diag");
         for (size_t k = 0; k < uni_diag.size(); ++k) record(uni_diag[k], sv->host_diag + 3 * k);
+        sv->add(&jp_server_stats::diag_s, seconds_since(td), &jp_server_stats::diags, (int64_t)uni_diag.size());
     }
     // 4. retire finished uniform solves (after the batched launches that touched them)
     bool any_done = false;
@@ -540,6 +599,7 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
         kmax = std::max(kmax, k);
     }
     std::vector<jp_solver*> members;
+    const auto tsb = clk::now();
     for (long long t = 0; t < kmax; ++t) {
         members.clear();
         for (auto& p : uni)
@@ -547,6 +607,7 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
         jp_status st = batched_step(members, sv->stream);
         if (st != JP_OK) return st;
     }
+    if (kmax) sv->add(&jp_server_stats::step_s, seconds_since(tsb));
     for (auto& p : uni) {
         p.first->step += p.second;
         if (p.first->step % p.first->diagK == 0) p.first->need_diag = true;  // at the new step, next tick
@@ -560,6 +621,8 @@ jp_status jp_server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued) {
     if (n_queued) *n_queued = (int32_t)sv->queue.size();
     return JP_OK;
 }
+
+extern "C" {
 
 int32_t jp_server_poll(jp_server* sv, jp_result* out, int32_t max) {
     if (!sv || !out || max <= 0) return 0;

@@ -72,6 +72,13 @@ class ServerConfig(C.Structure):
                 ("tick_steps", C.c_int32), ("workers", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("create_s", C.c_double), ("step_s", C.c_double), ("regrid_s", C.c_double),
+                ("diag_s", C.c_double), ("destroy_s", C.c_double), ("tick_s", C.c_double),
+                ("solves", C.c_int64), ("regrids", C.c_int64), ("diags", C.c_int64),
+                ("coarse_steps", C.c_int64), ("reserved", C.c_int64 * 8)]
+
+
 class Request(C.Structure):
     _fields_ = [("id", C.c_int64), ("cfg", Config), ("diag_every", C.c_int32), ("reserved", C.c_int32 * 7)]
 
@@ -124,6 +131,7 @@ SIGNATURES = {
     "jp_server_tick": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "jp_server_poll": (C.c_int32, [C.c_void_p, C.POINTER(Result), C.c_int32]),
     "jp_server_clock": (C.c_double, [C.c_void_p]),
+    "jp_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
     "jp_get_output_fields": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                        C.c_int64]),
     "jp_memory_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
@@ -393,6 +401,12 @@ class Server:
 
     def clock(self) -> float:
         return lib().jp_server_clock(self.h)
+
+    def stats(self) -> dict:
+        """Host seconds per phase (summed over threads) and event counts (jp_server_get_stats)."""
+        st = ServerStats()
+        _check(lib().jp_server_get_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_ if k != "reserved"}
 
     def close(self) -> None:
         if self.h:

@@ -44,7 +44,7 @@ def test_abi_version_and_struct_sizes():
     L = jpsolver.lib()
     assert L.jp_abi_version() == 1
     mirrors = [jpsolver.Config, jpsolver.Info, jpsolver.AmrCounts, jpsolver.ServerConfig, jpsolver.Request,
-               jpsolver.Result]
+               jpsolver.Result, jpsolver.ServerStats]
     for i, m in enumerate(mirrors):
         assert L.jp_sizeof(i) == ctypes.sizeof(m), m.__name__
     assert L.jp_sizeof(17) == 0
