@@ -151,6 +151,7 @@ struct Job {
     jp_info info{};
     long long step = 0, steps = 0, diagK = 1, adapt = 0;
     bool dynamic = false, need_diag = true;
+    int inflight = 0;       // diagnostics launched and not yet read back (uniform)
     bool admitted = false;  // holds `bytes` of the pool budget
     bool requeue = false;   // an AMR worker could not get the memory: back to the queue head
     jp_status error = JP_OK;
@@ -197,9 +198,17 @@ struct jp_server {
     double budget = 0;
     long long used = 0;
     std::chrono::steady_clock::time_point t0;
-    double* dev_diag = nullptr;   // 3 doubles per uniform job with a pending diagnostic
-    double* host_diag = nullptr;
-    int diag_cap = 0;
+    // Uniform diagnostics are read back one tick late: tick t launches its diagnostics and steps,
+    // then collects tick t-1's results, so the GPU always has the next tick queued while the host
+    // waits.  Two sets of slots alternate.
+    struct DiagBatch {
+        double* dev = nullptr;    // 3 doubles per entry
+        double* host = nullptr;   // pinned copy
+        int cap = 0;
+        cudaEvent_t done = nullptr;
+        std::vector<std::pair<Job*, long long>> entries;  // job, step the values belong to
+    } diag[2];
+    int diag_cur = 0;
     // AMR solves run whole on worker threads, each on its own stream; the tick thread admits and
     // retires them.  amr_todo and amr_fin are guarded by mu.
     std::vector<std::thread> workers;
@@ -259,9 +268,9 @@ void finish(jp_server* sv, Job* j, jp_status status) {
 }
 
 // diagnostics bookkeeping of the programs' loops (src/tgv3d_uniform.cu:173-188)
-void record(Job* j, const double d[3]) {
+void record(Job* j, const double d[3], long long step) {
     const double E = d[0], ens = d[1], mass = d[2];
-    const double ts = double(j->step) * j->req.cfg.u0 * j->info.kf;
+    const double ts = double(step) * j->req.cfg.u0 * j->info.kf;
     if (j->mass0 < 0) j->mass0 = mass;
     j->drift = std::max(j->drift, std::fabs(mass - j->mass0) / j->mass0);
     if (j->E0 < 0) j->E0 = E;
@@ -329,7 +338,7 @@ void run_amr(jp_server* sv, Job* j) {
             sv->add(&jp_server_stats::diag_s, seconds_since(t), &jp_server_stats::diags);
             if (st == JP_OK) {
                 j->step = s_;
-                record(j, d);
+                record(j, d, s_);
             }
         }
         if (s_ < j->steps) pending += sstep;
@@ -421,8 +430,11 @@ void jp_server_destroy(jp_server* sv) {
     for (Job* j : sv->amr_todo) delete j;
     for (Job* j : sv->amr_fin) delete j;
     for (Job* j : sv->queue) delete j;
-    if (sv->dev_diag) cudaFree(sv->dev_diag);
-    if (sv->host_diag) cudaFreeHost(sv->host_diag);
+    for (auto& b : sv->diag) {
+        if (b.dev) cudaFree(b.dev);
+        if (b.host) cudaFreeHost(b.host);
+        if (b.done) cudaEventDestroy(b.done);
+    }
     if (sv->stream) cudaStreamDestroy(sv->stream);
     if (sv->pool) {
         cudaDeviceSynchronize();
@@ -548,51 +560,42 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         }
         sv->active.push_back(j);
     }
-    // 3. diagnostics due now (uniform), all to one pinned array with one read-back
-    std::vector<Job*> uni_diag;
+    // 3. launch the diagnostics due now (uniform) into this tick's slots, with one read-back
+    auto& cur = sv->diag[sv->diag_cur];
+    cur.entries.clear();
     for (Job* j : sv->active)
-        if (j->error == JP_OK && j->need_diag) uni_diag.push_back(j);
+        if (j->error == JP_OK && j->need_diag) cur.entries.push_back({j, j->step});
     const auto td = clk::now();
-    if (!uni_diag.empty()) {
-        if ((int)uni_diag.size() > sv->diag_cap) {
-            ECK(cudaStreamSynchronize(sv->stream), "diag slots");
-            if (sv->dev_diag) cudaFree(sv->dev_diag);
-            if (sv->host_diag) cudaFreeHost(sv->host_diag);
-            sv->dev_diag = nullptr;
-            sv->host_diag = nullptr;
-            sv->diag_cap = std::max<int>(2 * (int)uni_diag.size(), 64);
-            ECK(cudaMalloc(&sv->dev_diag, sizeof(double) * 3 * sv->diag_cap), "cudaMalloc diag slots");
-            ECK(cudaMallocHost(&sv->host_diag, sizeof(double) * 3 * sv->diag_cap), "cudaMallocHost diag slots");
+    if (!cur.entries.empty()) {
+        if ((int)cur.entries.size() > cur.cap) {  // these slots were read back last tick: free to replace
+            if (cur.dev) cudaFree(cur.dev);
+            if (cur.host) cudaFreeHost(cur.host);
+            cur.dev = nullptr;
+            cur.host = nullptr;
+            cur.cap = std::max<int>(2 * (int)cur.entries.size(), 64);
+            ECK(cudaMalloc(&cur.dev, sizeof(double) * 3 * cur.cap), "cudaMalloc diag slots");
+            ECK(cudaMallocHost(&cur.host, sizeof(double) * 3 * cur.cap), "cudaMallocHost diag slots");
         }
-        for (size_t k = 0; k < uni_diag.size(); ++k) {
-            jp_solver* s = uni_diag[k]->s;
+        if (!cur.done) ECK(cudaEventCreateWithFlags(&cur.done, cudaEventDisableTiming), "diag event");
+        for (size_t k = 0; k < cur.entries.size(); ++k) {
+            Job* j = cur.entries[k].first;
+            jp_solver* s = j->s;
             const bool dbl = s->storage == JP_FP64;
             ECK(launch_macro(s->storage, s->fa, s->field, s->n, sv->stream), "macro");
-            ECK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, sv->dev_diag + 3 * k, sv->stream), "diag");
+            ECK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, cur.dev + 3 * k, sv->stream), "diag");
+            j->need_diag = false;
+            ++j->inflight;
         }
-        ECK(cudaMemcpyAsync(sv->host_diag, sv->dev_diag, sizeof(double) * 3 * uni_diag.size(), cudaMemcpyDeviceToHost,
+        ECK(cudaMemcpyAsync(cur.host, cur.dev, sizeof(double) * 3 * cur.entries.size(), cudaMemcpyDeviceToHost,
                             sv->stream), "diag D2H");
-        ECK(cudaStreamSynchronize(sv->stream), "diag");
-        for (size_t k = 0; k < uni_diag.size(); ++k) record(uni_diag[k], sv->host_diag + 3 * k);
-        sv->add(&jp_server_stats::diag_s, seconds_since(td), &jp_server_stats::diags, (int64_t)uni_diag.size());
+        ECK(cudaEventRecord(cur.done, sv->stream), "diag event");
+        sv->add(&jp_server_stats::diag_s, seconds_since(td), &jp_server_stats::diags, (int64_t)cur.entries.size());
     }
-    // 4. retire finished uniform solves (after the batched launches that touched them)
-    bool any_done = false;
-    for (Job* j : sv->active) any_done |= (j->step >= j->steps && !j->need_diag) || j->error != JP_OK;
-    if (any_done) ECK(cudaStreamSynchronize(sv->stream), "retire");
-    for (size_t i = 0; i < sv->active.size();) {
-        Job* j = sv->active[i];
-        if ((j->step >= j->steps && !j->need_diag) || j->error != JP_OK) {
-            sv->active.erase(sv->active.begin() + i);
-            finish(sv, j, j->error);
-        } else {
-            ++i;
-        }
-    }
-    // 5. advance the uniform solves in batched launches
+    // 4. advance the uniform solves in batched launches (behind this tick's diagnostics)
     std::vector<std::pair<Job*, long long>> uni;
     long long kmax = 0;
     for (Job* j : sv->active) {
+        if (j->error != JP_OK) continue;
         const long long k = std::min(next_event(j) - j->step, (long long)sv->cfg.tick_steps);
         if (k <= 0) continue;
         uni.push_back({j, k});
@@ -611,6 +614,33 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
     for (auto& p : uni) {
         p.first->step += p.second;
         if (p.first->step % p.first->diagK == 0) p.first->need_diag = true;  // at the new step, next tick
+    }
+    // 5. the previous tick's diagnostics (the GPU meanwhile works on this tick's launches)
+    auto& prev = sv->diag[sv->diag_cur ^ 1];
+    if (!prev.entries.empty()) {
+        const auto tw = clk::now();
+        ECK(cudaEventSynchronize(prev.done), "diag");
+        for (size_t k = 0; k < prev.entries.size(); ++k) {
+            record(prev.entries[k].first, prev.host + 3 * k, prev.entries[k].second);
+            --prev.entries[k].first->inflight;
+        }
+        prev.entries.clear();
+        sv->add(&jp_server_stats::diag_s, seconds_since(tw));
+    }
+    sv->diag_cur ^= 1;
+    // retire finished uniform solves: all steps issued, every diagnostic read back.  Their last use
+    // on the server's stream was a diagnostic that has completed (the event above), so their memory
+    // can go back to the pool in their own stream's order.  A solve that failed is retired once
+    // nothing of it is in flight.
+    for (size_t i = 0; i < sv->active.size();) {
+        Job* j = sv->active[i];
+        const bool done = j->step >= j->steps && !j->need_diag && j->inflight == 0;
+        if (done || (j->error != JP_OK && j->inflight == 0)) {
+            sv->active.erase(sv->active.begin() + i);
+            finish(sv, j, j->error);
+        } else {
+            ++i;
+        }
     }
     // 6. nothing to launch here while AMR solves run: wait briefly for one of them to finish
     if (uni.empty() && sv->amr_live > 0) {
