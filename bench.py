@@ -198,7 +198,7 @@ def c5_requests(J, n_req: int, rate: float, seed: int) -> list:
     """The served-ensemble workload: Poisson(rate) arrivals from a seed; each request a uniform solve
     with N in {32,48,64,96,128} or an AMR solve with coarse N in {16,24,32,48} (sensor refinement on
     both levels, frac1 0.3, frac2 0.1, regrid every 20 coarse steps, graph replay); Re log-uniform in
-    [200, 3200]; t* uniform in [2, 10]; FP32 or FP16 storage 50/50 (AMR solves store FP32)."""
+    [200, 3200]; t* uniform in [2, 10]; FP32 or FP16 storage 50/50."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
@@ -210,11 +210,9 @@ def c5_requests(J, n_req: int, rate: float, seed: int) -> list:
         re = float(np.exp(rng.uniform(np.log(200.0), np.log(3200.0))))
         ts = float(rng.uniform(2.0, 10.0))
         half = bool(rng.random() < 0.5)
-        r = dict(rid=i, kind="amr" if amr else "uniform", n=n, re=re, tstar=ts)
+        r = dict(rid=i, kind="amr" if amr else "uniform", n=n, re=re, tstar=ts, storage="fp16" if half else "fp32")
         if amr:
             r.update(l1_mode="sensor", l2_mode="sensor", frac1=0.3, frac2=0.1, adapt_every=20, flags=J.FLAG_GRAPH)
-        else:
-            r.update(storage="fp16" if half else "fp32")
         out.append((float(t[i]), r))
     return out
 

@@ -127,7 +127,11 @@ __device__ __forceinline__ void bgk(float (&f)[Q], float om) {
 // The same BGK collide with the arithmetic of the uniform stream-collide: one reciprocal of rho,
 // out = (1 - omega) f + omega feq with omega*w*rho folded per weight class and
 // feq_pm = w rho (1 - 1.5|u|^2 + 4.5 a^2) +- 3 w rho a for a = c.u over the non-zero terms only.
-// Agrees with bgk() to FP32 round-off (a few ulp per population).
+// Agrees with bgk() to FP32 round-off (a few ulp per population).  SH: the values are the shifts
+// g = f - w_q of a shifted storage format, rho = 1 + sum g, and the result is shifted too
+// (feq_q - w_q = w_q (s + rho (3a + 4.5a^2 - 1.5|u|^2)) with s = sum g), which keeps the round-off at
+// the level of the deviations.
+template <bool SH = false>
 __device__ __forceinline__ void bgk_fast(float (&f)[Q], float om) {
     float sm = f[0];
 #pragma unroll
@@ -135,16 +139,19 @@ __device__ __forceinline__ void bgk_fast(float (&f)[Q], float om) {
     const float jx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
     const float jy = f[3] - f[4] + f[7] - f[8] - f[9] + f[10] + f[15] - f[16] + f[17] - f[18];
     const float jz = f[5] - f[6] + f[11] - f[12] - f[13] + f[14] + f[15] - f[16] - f[17] + f[18];
-    const float inv = 1.f / sm;
+    const float rho = SH ? 1.f + sm : sm;
+    const float inv = 1.f / rho;
     const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-    const float base = 1.f - 1.5f * (ux * ux + uy * uy + uz * uz);
-    const float omc = 1.f - om, orho = om * sm;
+    const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
+    const float base = SH ? -usq : 1.f - usq;
+    const float omc = 1.f - om, orho = om * rho;
     const float owr1 = orho * wf(1), owr2 = orho * wf(7), owr3a = 3.f * owr1, owr3b = 3.f * owr2;
-    f[0] = omc * f[0] + orho * wf(0) * base;
+    const float ows1 = SH ? om * wf(1) * sm : 0.f, ows2 = SH ? om * wf(7) * sm : 0.f;
+    f[0] = omc * f[0] + om * wf(0) * (SH ? sm - rho * usq : rho * base);
 #pragma unroll
     for (int q = 1; q < Q; q += 2) {
         const float a = cdot<float>(q, ux, uy, uz);
-        const float t = (q < 7 ? owr1 : owr2) * (4.5f * a * a + base);
+        const float t = (q < 7 ? owr1 : owr2) * (4.5f * a * a + base) + (q < 7 ? ows1 : ows2);
         const float as = (q < 7 ? owr3a : owr3b) * a;
         f[q] = omc * f[q] + (t + as);
         f[q + 1] = omc * f[q + 1] + (t - as);
@@ -168,14 +175,28 @@ __host__ __device__ __forceinline__ void pull_src(int q, int i, int j, int k, in
 }
 
 #ifdef __CUDACC__
+// Element access of the AMR pools, prolongation sources and ghost shells in a storage format of
+// lattice.cuh.  f(): the unshifted population, the quantity prolongation, restriction, the sensor
+// and the composite work on; n(): the stored number itself, the quantity the collision works on
+// (f for FP32; the shift g = f - w_q for the 16-bit formats).
+template <class ST>
+struct PoolIO {
+    using raw = typename ST::raw;
+    static constexpr bool SH = ST::shifted;
+    __device__ static __forceinline__ float n(const raw* p) { return ST::load(__ldg(p)); }
+    __device__ static __forceinline__ float f(const raw* p, int q) { return SH ? wf(q) + n(p) : n(p); }
+    __device__ static __forceinline__ void put_n(raw* p, float v) { *p = ST::store(v); }
+    __device__ static __forceinline__ void put_f(raw* p, int q, float v) { *p = ST::store(SH ? v - wf(q) : v); }
+};
+
 // Pull of the 19 populations of cell (i, j, k) of pool block b.  nbrow[e] (global memory, the
 // block's row of its level's neighbour table) is the pool index of the same-level neighbour in slot
 // e (pull_src), or -1 where that neighbour is not on this level; then the value comes from b's
 // ghost shell gh (GHOST = false: every neighbour exists).  Every thread reads the few table entries
 // its cell needs itself: the row is shared by the whole CTA and stays in L1, and no barrier stands
 // between a thread and its loads.
-template <int MB, bool GHOST>
-__device__ __forceinline__ void pull_cell(const float* __restrict__ fa, const float* __restrict__ gh,
+template <int MB, class ST, bool GHOST>
+__device__ __forceinline__ void pull_cell(const typename ST::raw* __restrict__ fa, const typename ST::raw* __restrict__ gh,
                                           const int* __restrict__ nbrow, int b, int i, int j, int k,
                                           float (&f)[Q]) {
     constexpr int MB3 = MB * MB * MB, SH = Geo<MB>::SH;
@@ -185,9 +206,9 @@ __device__ __forceinline__ void pull_cell(const float* __restrict__ fa, const fl
         pull_src<MB>(q, i, j, k, e, sc);
         const int blk = e == 13 ? b : __ldg(nbrow + e);
         if (!GHOST || blk >= 0) {
-            f[q] = __ldg(fa + ((size_t)blk * Q + q) * MB3 + sc);
+            f[q] = PoolIO<ST>::n(fa + ((size_t)blk * Q + q) * MB3 + sc);
         } else {
-            f[q] = __ldg(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(i - cx(q), j - cy(q), k - cz(q)));
+            f[q] = PoolIO<ST>::n(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(i - cx(q), j - cy(q), k - cz(q)));
         }
     }
 }

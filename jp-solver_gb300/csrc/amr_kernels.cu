@@ -1,639 +1,20 @@
-// AMR level kernels: coarse step, prolongation sources ("prep"), ghost-shell fill, fine steps,
-// restriction, seeding and migration, sensor and the composite macro field.
-// Reference: src/tgv3d_amr.cu:69-453, 514-536.  One CTA per block; a thread owns one cell (MB<=8)
-// or several (MB=16), and the steps take 128, 256 or 512 threads per CTA at MB = 8 and 16.  Arithmetic follows the reference's expressions so results agree within
-// round-off; loop orders of the trilinear and the 8-child average are the reference's.
-#include "amr_common.cuh"
-#include "amr_kernels.h"
-#include "kernels.h"
+// AMR kernels with FP32 storage, the launch entry point for every storage format, and the launch
+// shape rules of the AMR kernels.  The kernels themselves are in amr_kernels.cuh.
+#include "amr_kernels.cuh"
 
 namespace jp {
 namespace amr {
 
-#define CELL_LOOP(c) for (int c = threadIdx.x; c < G::MB3; c += G::TPB)
-int default_step_tpb(int mb);
+template cudaError_t amr_launch_st<StF32>(int mb, int op, const AmrLaunch& L);
+extern template cudaError_t amr_launch_st<StF16>(int mb, int op, const AmrLaunch& L);
+extern template cudaError_t amr_launch_st<StBF16>(int mb, int op, const AmrLaunch& L);
 
-// ---- TGV initial state of the coarse grid (src/tgv3d_amr.cu:431-440) ---------------------------
-template <int MB>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_init(float* __restrict__ f, int cgx, double u0, double kf) {
-    using G = Geo<MB>;
-    const int b = blockIdx.x;
-    const int bx = b % cgx, by = (b / cgx) % cgx, bz = b / (cgx * cgx);
-    CELL_LOOP(cell) {
-        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-        const double x = (bx * MB + i + 0.5) * kf, y = (by * MB + j + 0.5) * kf, z = (bz * MB + k + 0.5) * kf;
-        const double ux = u0 * sin(x) * cos(y) * cos(z), uy = -u0 * cos(x) * sin(y) * cos(z);
-        const double p = (u0 * u0 / 16.0) * (cos(2 * x) + cos(2 * y)) * (cos(2 * z) + 2.0), rho = 1.0 + 3.0 * p;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) f[((size_t)b * Q + q) * G::MB3 + cell] = feq_ref(q, float(rho), float(ux), float(uy), 0.f);
-    }
-}
-
-// ---- dense periodic coarse step (src/tgv3d_amr.cu:203-220) ---------------------------------------
-template <int MB, int TPB>
-__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const float* __restrict__ fa, float* __restrict__ fb,
-                                                             int cgx, float om) {
-    using G = Geo<MB>;
-    const int b = blockIdx.x;
-    const int bx = b % cgx, by = (b / cgx) % cgx, bz = b / (cgx * cgx);
-    __shared__ int snb[27];  // periodic neighbour blocks (arithmetic only: no loads wait on the barrier)
-    if (threadIdx.x < 27) {
-        const int dx = threadIdx.x % 3 - 1, dy = (threadIdx.x / 3) % 3 - 1, dz = threadIdx.x / 9 - 1;
-        snb[threadIdx.x] = (((bz + dz + cgx) % cgx) * cgx + (by + dy + cgx) % cgx) * cgx + (bx + dx + cgx) % cgx;
-    }
-    __syncthreads();
-    for (int cell = threadIdx.x; cell < G::MB3; cell += TPB) {
-        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-        float f[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            int e, sc;
-            pull_src<MB>(q, i, j, k, e, sc);
-            f[q] = __ldg(fa + ((size_t)snb[e] * Q + q) * G::MB3 + sc);
-        }
-        bgk_fast(f, om);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) fb[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
-    }
-}
-
-// ---- prolongation sources on a block list (src/tgv3d_amr.cu:160-171) -----------------------------
-template <int MB>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const float* __restrict__ fin, float* __restrict__ pr,
-                                                      const int* __restrict__ list, float nqs,
-                                                      const int* __restrict__ nlim) {
-    using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
-    const int b = list[blockIdx.x];
-    CELL_LOOP(cell) {
-        float f[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) f[q] = __ldg(fin + ((size_t)b * Q + q) * G::MB3 + cell);
-        prep_cell(f, nqs);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) pr[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
-    }
-}
-
-// trilinear of a precomputed source on the dense coarse grid (src/tgv3d_amr.cu:122-132)
-template <int MB>
-__device__ __forceinline__ void prolong_prep_l0(const float* __restrict__ pr, int cgx, int N, int gfi, int gfj, int gfk,
-                                                float (&out)[Q]) {
-    constexpr int MB3 = MB * MB * MB;
-    int ib, jb, kb;
-    float tx, ty, tz;
-    tri_axis(gfi, ib, tx);
-    tri_axis(gfj, jb, ty);
-    tri_axis(gfk, kb, tz);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) out[q] = 0.f;
-#pragma unroll 1
-    for (int c = 0; c < 8; ++c) {
-        const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
-        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
-        const int ci = pmod(ib + di, N), cj = pmod(jb + dj, N), ck = pmod(kb + dk, N);
-        const int cb = ((ck / MB) * cgx + cj / MB) * cgx + ci / MB;
-        const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
-        const float* p = pr + (size_t)cb * Q * MB3 + cc;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) out[q] += wgt * __ldg(p + q * MB3);
-    }
-}
-
-// trilinear of a precomputed source on the scattered L1 level, dropping absent corners and
-// renormalising (src/tgv3d_amr.cu:133-144)
-template <int MB>
-__device__ __forceinline__ void prolong_prep_l1(const float* __restrict__ pr, const int* __restrict__ l1grid, int l1gx,
-                                                int N1, int g2i, int g2j, int g2k, float (&out)[Q]) {
-    constexpr int MB3 = MB * MB * MB;
-    int ib, jb, kb;
-    float tx, ty, tz, wsum = 0.f;
-    tri_axis(g2i, ib, tx);
-    tri_axis(g2j, jb, ty);
-    tri_axis(g2k, kb, tz);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) out[q] = 0.f;
-#pragma unroll 1
-    for (int c = 0; c < 8; ++c) {
-        const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
-        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
-        const int ci = pmod(ib + di, N1), cj = pmod(jb + dj, N1), ck = pmod(kb + dk, N1);
-        const int lb = __ldg(l1grid + ((ck / MB) * l1gx + cj / MB) * l1gx + ci / MB);
-        if (lb < 0) continue;
-        const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
-        wsum += wgt;
-        const float* p = pr + (size_t)lb * Q * MB3 + cc;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) out[q] += wgt * __ldg(p + q * MB3);
-    }
-    if (wsum > 0.f && wsum < 0.999f) {
-        const float inv = 1.f / wsum;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) out[q] *= inv;
-    }
-}
-
-// ---- ghost shells (src/tgv3d_amr.cu:173-202) -------------------------------------------------------
-// One CTA per fine block, one thread per shell cell; a shell cell whose same-level neighbour block
-// exists (its parent is refined) is left alone: the step gathers it from that block instead.
-template <int MB>
-__global__ void __launch_bounds__(256) k_fill_l1(const float* __restrict__ pr, float* __restrict__ gh,
-                                                const int* __restrict__ pcb, const int* __restrict__ poct,
-                                                const int* __restrict__ nbtab, int cgx, int N,
-                                                const int* __restrict__ nlim) {
-    using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
-    const int fb = blockIdx.x;
-    const int* nbrow = nbtab + (size_t)fb * 27;
-    const int cb = pcb[fb], oct = poct[fb];
-    const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
-    const int ox = cbx * 2 * MB + (oct & 1) * MB, oy = cby * 2 * MB + ((oct >> 1) & 1) * MB, oz = cbz * 2 * MB + (oct >> 2) * MB;
-    const int N1 = 2 * N;
-    for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
-        int i, j, k;
-        shell_coord<MB>(t, i, j, k);
-        if (__ldg(nbrow + shell_slot<MB>(i, j, k)) >= 0) continue;
-        const int gfi = pmod(ox + i, N1), gfj = pmod(oy + j, N1), gfk = pmod(oz + k, N1);
-        float out[Q];
-        prolong_prep_l0<MB>(pr, cgx, N, gfi, gfj, gfk, out);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) gh[((size_t)fb * Q + q) * G::SH + t] = out[q];
-    }
-}
-
-template <int MB>
-__global__ void __launch_bounds__(256) k_fill_l2(const float* __restrict__ pr, float* __restrict__ gh,
-                                                const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
-                                                const int* __restrict__ f1pos, const int* __restrict__ l1grid,
-                                                const int* __restrict__ nbtab, int l1gx, int N1,
-                                                const int* __restrict__ nlim) {
-    using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
-    const int b = blockIdx.x;
-    const int* nbrow = nbtab + (size_t)b * 27;
-    const int pl1 = l2pl1[b], oct = l2oct[b];
-    const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
-    const int ox = px * 2 * MB + (oct & 1) * MB, oy = py * 2 * MB + ((oct >> 1) & 1) * MB, oz = pz * 2 * MB + (oct >> 2) * MB;
-    const int N2 = 2 * N1;
-    for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
-        int i, j, k;
-        shell_coord<MB>(t, i, j, k);
-        if (__ldg(nbrow + shell_slot<MB>(i, j, k)) >= 0) continue;
-        const int g2i = pmod(ox + i, N2), g2j = pmod(oy + j, N2), g2k = pmod(oz + k, N2);
-        float out[Q];
-        prolong_prep_l1<MB>(pr, l1grid, l1gx, N1, g2i, g2j, g2k, out);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) gh[((size_t)b * Q + q) * G::SH + t] = out[q];
-    }
-}
-
-// Restriction of one fine block, staged in shared memory as sf[q * MB^3 + cell] after its last
-// substep, into the octant `oct` of its parent block: each covered parent cell becomes
-// feq + nqi*regularize(avg - feq) of its 8 children, summed in the reference's dk, dj, di order
-// (k_restrict_L1/L2, src/tgv3d_amr.cu:275-298, 357-381).
-template <int MB>
-__device__ __forceinline__ void restrict_octant(const float* __restrict__ sf, float* __restrict__ parent, int oct,
-                                                float nqi) {
-    constexpr int H = MB / 2, MB3 = MB * MB * MB;
-    for (int t = threadIdx.x; t < H * H * H; t += blockDim.x) {
-        const int i = t % H, j = (t / H) % H, k = t / (H * H);
-        float a[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) a[q] = 0.f;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
-            const int sc = ((2 * k + dk) * MB + (2 * j + dj)) * MB + (2 * i + di);
-#pragma unroll
-            for (int q = 0; q < Q; ++q) a[q] += 0.125f * sf[q * MB3 + sc];
-        }
-        float rho, ux, uy, uz;
-        moments(a, rho, ux, uy, uz);
-        float fe[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            fe[q] = feq_ref(q, rho, ux, uy, uz);
-            a[q] = a[q] - fe[q];
-        }
-        regularize(a);
-        const int pc = (((oct >> 2) * H + k) * MB + (((oct >> 1) & 1) * H + j)) * MB + ((oct & 1) * H + i);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) parent[q * MB3 + pc] = fe[q] + nqi * a[q];
-    }
-}
-
-// ---- same-level neighbour tables -----------------------------------------------------------------
-// nb[b*27 + e] = pool index of the same-level block at offset slot e (pull_src) of fine block b, or
-// -1 where that neighbour is not on the block's level (its cells come from the ghost shell).  Built
-// once per grid change, so the steps and fills read one table instead of walking the block tables.
-__global__ void k_nbtab_l1(int* __restrict__ nb, const int* __restrict__ pcb, const int* __restrict__ poct,
-                           const int* __restrict__ ref0, const int* __restrict__ fof0, int cgx, int nf1) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= 27LL * nf1) return;
-    const int b = int(idx / 27), e = int(idx % 27);
-    const int cb = pcb[b], oct = poct[b], l1gx = 2 * cgx;
-    const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
-    const int dx = e % 3 - 1, dy = (e / 3) % 3 - 1, dz = e / 9 - 1;
-    const int nx = (2 * cbx + (oct & 1) + dx + l1gx) % l1gx, ny = (2 * cby + ((oct >> 1) & 1) + dy + l1gx) % l1gx,
-              nz = (2 * cbz + (oct >> 2) + dz + l1gx) % l1gx;
-    const int ncb = ((nz >> 1) * cgx + (ny >> 1)) * cgx + (nx >> 1);
-    nb[idx] = ref0[ncb] ? fof0[ncb] + ((nz & 1) * 4 + (ny & 1) * 2 + (nx & 1)) : -1;
-}
-
-__global__ void k_nbtab_l2(int* __restrict__ nb, const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
-                           const int* __restrict__ f1pos, const int* __restrict__ l1grid, const int* __restrict__ ref1,
-                           const int* __restrict__ fof1, int l1gx, int nf2) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= 27LL * nf2) return;
-    const int b = int(idx / 27), e = int(idx % 27);
-    const int oct = l2oct[b], p = f1pos[l2pl1[b]], g2 = 2 * l1gx;
-    const int px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
-    const int dx = e % 3 - 1, dy = (e / 3) % 3 - 1, dz = e / 9 - 1;
-    const int nx = (2 * px + (oct & 1) + dx + g2) % g2, ny = (2 * py + ((oct >> 1) & 1) + dy + g2) % g2,
-              nz = (2 * pz + (oct >> 2) + dz + g2) % g2;
-    const int lb = l1grid[((nz >> 1) * l1gx + (ny >> 1)) * l1gx + (nx >> 1)];
-    nb[idx] = (lb >= 0 && ref1[lb]) ? fof1[lb] + ((nz & 1) * 4 + (ny & 1) * 2 + (nx & 1)) : -1;
-}
-
-// ---- fine steps (src/tgv3d_amr.cu:241-274, 331-356) -----------------------------------------------
-// One kernel for both fine levels: the neighbour table says, per offset, which pool block holds the
-// pulled cells or that they come from the ghost shell.  TPB threads share the block's MB^3 cells.
-// FUSE: this is the last substep before the restriction into the parent level, so the block also
-// restricts itself into its parent octant (`parent`, `poct`), which saves re-reading the level from
-// HBM in a separate restriction kernel.
-template <int MB, int TPB, bool FUSE>
-__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_fine(const float* __restrict__ fa, float* __restrict__ fbuf,
-                                                               const float* __restrict__ gh,
-                                                               const int* __restrict__ nbtab,
-                                                               const int* __restrict__ parent,
-                                                               const int* __restrict__ poct, float om,
-                                                               float* __restrict__ parent_pool, float nqi,
-                                                               const int* __restrict__ nlim) {
-    static_assert(Geo<MB>::MB3 % TPB == 0, "cells must split evenly over the CTA");
-    extern __shared__ float sf[];
-    using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;  // whole CTA: the barrier below stays uniform
-    const int b = blockIdx.x;
-    const int* nbrow = nbtab + (size_t)b * 27;
-    for (int cell = threadIdx.x; cell < G::MB3; cell += TPB) {
-        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-        float f[Q];
-        pull_cell<MB, true>(fa, gh, nbrow, b, i, j, k, f);
-        bgk_fast(f, om);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            fbuf[((size_t)b * Q + q) * G::MB3 + cell] = f[q];
-            if (FUSE) sf[q * G::MB3 + cell] = f[q];
-        }
-    }
-    if (FUSE) {
-        __syncthreads();
-        restrict_octant<MB>(sf, parent_pool + (size_t)parent[b] * Q * G::MB3, poct[b], nqi);
-    }
-}
-
-// ---- restriction (src/tgv3d_amr.cu:275-298, 357-381) -------------------------------------------------
-// One CTA per refined parent block; each parent cell becomes feq + nqi*regularize(avg - feq) of the
-// average of its 8 children (summed in the reference's dk, dj, di order).
-template <int MB>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_restrict(float* __restrict__ cf, const float* __restrict__ ff,
-                                                          const int* __restrict__ rl, const int* __restrict__ fof,
-                                                          float nqi, const int* __restrict__ nlim) {
-    using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
-    const int cb = rl[blockIdx.x];
-    const int fbase = fof[cb];
-    CELL_LOOP(cell) {
-        const int lci = cell % MB, lcj = (cell / MB) % MB, lck = cell / (MB * MB);
-        const int oct = (lck / G::HALF) * 4 + (lcj / G::HALF) * 2 + lci / G::HALF;
-        const int fi0 = 2 * (lci % G::HALF), fj0 = 2 * (lcj % G::HALF), fk0 = 2 * (lck % G::HALF);
-        const float* src = ff + (size_t)(fbase + oct) * Q * G::MB3;
-        float a[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) a[q] = 0.f;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
-            const int sc = ((fk0 + dk) * MB + (fj0 + dj)) * MB + (fi0 + di);
-#pragma unroll
-            for (int q = 0; q < Q; ++q) a[q] += 0.125f * __ldg(src + q * G::MB3 + sc);
-        }
-        float rho, ux, uy, uz;
-        moments(a, rho, ux, uy, uz);
-        float fe[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            fe[q] = feq_ref(q, rho, ux, uy, uz);
-            a[q] = a[q] - fe[q];
-        }
-        regularize(a);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) cf[((size_t)cb * Q + q) * G::MB3 + cell] = fe[q] + nqi * a[q];
-    }
-}
-
-// ---- on-the-fly prolongation for seeding and migration (src/tgv3d_amr.cu:70-118) ----------------
-template <int MB>
-__device__ __forceinline__ void prolong_l0(const float* __restrict__ cf, int cgx, int N, int gfi, int gfj, int gfk,
-                                           float nqs, float (&out)[Q]) {
-    constexpr int MB3 = MB * MB * MB;
-    int ib, jb, kb;
-    float tx, ty, tz;
-    tri_axis(gfi, ib, tx);
-    tri_axis(gfj, jb, ty);
-    tri_axis(gfk, kb, tz);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) out[q] = 0.f;
-#pragma unroll 1
-    for (int c = 0; c < 8; ++c) {
-        const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
-        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
-        const int ci = pmod(ib + di, N), cj = pmod(jb + dj, N), ck = pmod(kb + dk, N);
-        const int cb = ((ck / MB) * cgx + cj / MB) * cgx + ci / MB;
-        const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
-        float f[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) f[q] = __ldg(cf + ((size_t)cb * Q + q) * MB3 + cc);
-        prep_cell(f, nqs);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) out[q] += wgt * f[q];
-    }
-}
-template <int MB>
-__device__ __forceinline__ void prolong_l1(const float* __restrict__ f1, const int* __restrict__ l1grid, int l1gx,
-                                           int N1, int g2i, int g2j, int g2k, float nqs, float (&out)[Q]) {
-    constexpr int MB3 = MB * MB * MB;
-    int ib, jb, kb;
-    float tx, ty, tz, wsum = 0.f;
-    tri_axis(g2i, ib, tx);
-    tri_axis(g2j, jb, ty);
-    tri_axis(g2k, kb, tz);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) out[q] = 0.f;
-#pragma unroll 1
-    for (int c = 0; c < 8; ++c) {
-        const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
-        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
-        const int ci = pmod(ib + di, N1), cj = pmod(jb + dj, N1), ck = pmod(kb + dk, N1);
-        const int lb = __ldg(l1grid + ((ck / MB) * l1gx + cj / MB) * l1gx + ci / MB);
-        if (lb < 0) continue;
-        const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
-        float f[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) f[q] = __ldg(f1 + ((size_t)lb * Q + q) * MB3 + cc);
-        prep_cell(f, nqs);
-        wsum += wgt;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) out[q] += wgt * f[q];
-    }
-    if (wsum > 0.f && wsum < 0.999f) {
-        const float inv = 1.f / wsum;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) out[q] *= inv;
-    }
-}
-
-// seed (old_ref == nullptr) or migrate level 1: a block whose parent was refined before copies its old
-// payload, a new one is prolonged from the coarse level (src/tgv3d_amr.cu:299-308, 397-411)
-template <int MB>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_seed_l1(const float* __restrict__ oldf, float* __restrict__ newf,
-                                                         const float* __restrict__ c0, const int* __restrict__ pcb,
-                                                         const int* __restrict__ poct, const int* __restrict__ old_ref0,
-                                                         const int* __restrict__ old_fof0, int cgx, int N, float nqs) {
-    using G = Geo<MB>;
-    const int nfb = blockIdx.x;
-    const int cb = pcb[nfb], oct = poct[nfb];
-    const bool copy = old_ref0 != nullptr && old_ref0[cb];
-    const int ofb = copy ? old_fof0[cb] + oct : 0;
-    const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
-    CELL_LOOP(cell) {
-        if (copy) {
-#pragma unroll
-            for (int q = 0; q < Q; ++q)
-                newf[((size_t)nfb * Q + q) * G::MB3 + cell] = __ldg(oldf + ((size_t)ofb * Q + q) * G::MB3 + cell);
-            continue;
-        }
-        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-        float out[Q];
-        prolong_l0<MB>(c0, cgx, N, cbx * 2 * MB + (oct & 1) * MB + i, cby * 2 * MB + ((oct >> 1) & 1) * MB + j,
-                       cbz * 2 * MB + (oct >> 2) * MB + k, nqs, out);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) newf[((size_t)nfb * Q + q) * G::MB3 + cell] = out[q];
-    }
-}
-
-// seed or migrate level 2, keyed by the level-1 grid position (src/tgv3d_amr.cu:382-393, 414-430)
-template <int MB>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_seed_l2(const float* __restrict__ oldf, float* __restrict__ newf,
-                                                         const float* __restrict__ f1, const int* __restrict__ l2pl1,
-                                                         const int* __restrict__ l2oct, const int* __restrict__ f1pos,
-                                                         const int* __restrict__ old_l1grid, const int* __restrict__ old_ref1,
-                                                         const int* __restrict__ old_fof1, const int* __restrict__ l1grid,
-                                                         int l1gx, int N1, float nqs) {
-    using G = Geo<MB>;
-    const int nfb = blockIdx.x;
-    const int pl1 = l2pl1[nfb], oct = l2oct[nfb], p = f1pos[pl1];
-    bool copy = false;
-    int of2 = 0;
-    if (old_l1grid != nullptr) {
-        const int old_l1b = old_l1grid[p];
-        copy = old_l1b >= 0 && old_ref1[old_l1b];
-        if (copy) of2 = old_fof1[old_l1b] + oct;
-    }
-    const int px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
-    CELL_LOOP(cell) {
-        if (copy) {
-#pragma unroll
-            for (int q = 0; q < Q; ++q)
-                newf[((size_t)nfb * Q + q) * G::MB3 + cell] = __ldg(oldf + ((size_t)of2 * Q + q) * G::MB3 + cell);
-            continue;
-        }
-        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-        float out[Q];
-        prolong_l1<MB>(f1, l1grid, l1gx, N1, px * 2 * MB + (oct & 1) * MB + i, py * 2 * MB + ((oct >> 1) & 1) * MB + j,
-                       pz * 2 * MB + (oct >> 2) * MB + k, nqs, out);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) newf[((size_t)nfb * Q + q) * G::MB3 + cell] = out[q];
-    }
-}
-
-// ---- refinement sensor (src/tgv3d_amr.cu:442-453) -----------------------------------------------
-// Block max over cells of |f - feq|_2 / rho.  With `override_pos` set, block b takes the supplied
-// value of its grid position instead (pos == nullptr: position = block index).
-template <int MB>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_sensor(const float* __restrict__ ff, float* __restrict__ d,
-                                                        const float* __restrict__ override_val,
-                                                        const int* __restrict__ pos) {
-    using G = Geo<MB>;
-    const int b = blockIdx.x;
-    if (override_val) {
-        if (threadIdx.x == 0) d[b] = override_val[pos ? pos[b] : b];
-        return;
-    }
-    float m = -INFINITY;
-    CELL_LOOP(cell) {
-        float f[Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) f[q] = __ldg(ff + ((size_t)b * Q + q) * G::MB3 + cell);
-        float rho, ux, uy, uz;
-        moments(f, rho, ux, uy, uz);
-        float s = 0.f;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            const float d2 = f[q] - feq_ref(q, rho, ux, uy, uz);
-            s += d2 * d2;
-        }
-        m = fmaxf(m, sqrtf(s) / rho);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    __shared__ float sm[32];
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float r = sm[0];
-        for (int w = 1; w < (G::TPB + 31) / 32; ++w) r = fmaxf(r, sm[w]);
-        d[b] = r;
-    }
-}
-
-// ---- composite macro field at 4*N0 (src/tgv3d_amr.cu:514-536) ----------------------------------
-template <int MB>
-__global__ void __launch_bounds__(256) k_composite(const float* __restrict__ c0, const float* __restrict__ f1,
-                                                  const float* __restrict__ f2, const int* __restrict__ ref1,
-                                                  const int* __restrict__ fof1, const int* __restrict__ l1grid, int cgx,
-                                                  int l1gx, int N2, float* __restrict__ F) {
-    constexpr int MB3 = MB * MB * MB;
-    const long long NN = (long long)N2 * N2 * N2;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= NN) return;
-    const int gi = int(idx % N2), gj = int((idx / N2) % N2), gk = int(idx / ((long long)N2 * N2));
-    const int lb = l1grid[((gk / (2 * MB)) * l1gx + gj / (2 * MB)) * l1gx + gi / (2 * MB)];
-    const float* src;
-    size_t blk;
-    int sc;
-    if (lb >= 0 && ref1[lb]) {
-        blk = fof1[lb] + (((gk % (2 * MB)) / MB) * 4 + ((gj % (2 * MB)) / MB) * 2 + (gi % (2 * MB)) / MB);
-        sc = ((gk % MB) * MB + gj % MB) * MB + gi % MB;
-        src = f2;
-    } else if (lb >= 0) {
-        const int g1i = gi / 2, g1j = gj / 2, g1k = gk / 2;
-        blk = lb;
-        sc = ((g1k % MB) * MB + g1j % MB) * MB + g1i % MB;
-        src = f1;
-    } else {
-        const int c0i = gi / 4, c0j = gj / 4, c0k = gk / 4;
-        blk = ((c0k / MB) * cgx + c0j / MB) * cgx + c0i / MB;
-        sc = ((c0k % MB) * MB + c0j % MB) * MB + c0i % MB;
-        src = c0;
-    }
-    float f[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) f[q] = __ldg(src + (blk * Q + q) * MB3 + sc);
-    float rho, ux, uy, uz;
-    moments(f, rho, ux, uy, uz);
-    F[idx * 4 + 0] = rho;
-    F[idx * 4 + 1] = ux;
-    F[idx * 4 + 2] = uy;
-    F[idx * 4 + 3] = uz;
-}
-
-// ---- launchers ------------------------------------------------------------------------------------
-
-// the steps with TPB threads per CTA (the block's MB^3 cells split evenly)
-template <int MB, int TPB>
-static void launch_steps(const AmrLaunch& L, int op) {
-    using G = Geo<MB>;
-    if (op == OP_STEP_L0) {
-        k_step_l0<MB, TPB><<<L.nblocks, TPB, 0, L.st>>>(L.in, L.out, L.cgx, L.omega);
-        return;
-    }
-    const int* parent = L.t0;  // pcb (level 1) or l2pl1 (level 2)
-    if constexpr (MB <= 8) {
-        if (L.out2) {
-            k_step_fine<MB, TPB, true><<<L.nblocks, TPB, sizeof(float) * Q * G::MB3, L.st>>>(
-                L.in, L.out, L.aux, L.nbt, parent, L.t1, L.omega, L.out2, L.scale, L.nlim);
-            return;
-        }
-    }
-    k_step_fine<MB, TPB, false><<<L.nblocks, TPB, 0, L.st>>>(L.in, L.out, L.aux, L.nbt, parent, L.t1, L.omega,
-                                                             nullptr, 0.f, L.nlim);
-}
-
-template <int MB>
-static cudaError_t dispatch(const AmrLaunch& L, int op) {
-    using G = Geo<MB>;
-    const dim3 cta(G::TPB);
-    const dim3 shl(G::SH < 256 ? ((G::SH + 31) / 32) * 32 : 256);
-    switch (op) {
-        case OP_INIT:
-            k_init<MB><<<L.nblocks, cta, 0, L.st>>>(L.out, L.cgx, L.u0, L.kf);
-            break;
-        case OP_STEP_L0:
-        case OP_STEP_L1:
-        case OP_STEP_L2: {
-            const int tpb = L.tpb ? L.tpb : default_step_tpb(MB);
-            if constexpr (MB == 4) {
-                if (tpb != 64) return cudaErrorInvalidConfiguration;
-                launch_steps<MB, 64>(L, op);
-            } else {
-                if (tpb == 128) launch_steps<MB, 128>(L, op);
-                else if (tpb == 256) launch_steps<MB, 256>(L, op);
-                else if (tpb == 512) launch_steps<MB, 512>(L, op);
-                else return cudaErrorInvalidConfiguration;
-            }
-            break;
-        }
-        case OP_NBTAB_L1:
-            k_nbtab_l1<<<(unsigned)((27LL * L.nblocks + 255) / 256), 256, 0, L.st>>>(L.iout, L.t0, L.t1, L.t2, L.t3,
-                                                                                  L.cgx, L.nblocks);
-            break;
-        case OP_NBTAB_L2:
-            k_nbtab_l2<<<(unsigned)((27LL * L.nblocks + 255) / 256), 256, 0, L.st>>>(L.iout, L.t0, L.t1, L.t2, L.t3,
-                                                                                  L.t4, L.t5, L.l1gx, L.nblocks);
-            break;
-        case OP_PREP:
-            k_prep<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.list, L.scale, L.nlim);
-            break;
-        case OP_FILL_L1:
-            k_fill_l1<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.nbt, L.cgx, L.n, L.nlim);
-            break;
-        case OP_FILL_L2:
-            k_fill_l2<MB><<<L.nblocks, shl, 0, L.st>>>(L.in, L.out, L.t0, L.t1, L.t2, L.t3, L.nbt, L.l1gx, L.n1,
-                                                       L.nlim);
-            break;
-        case OP_RESTRICT:
-            k_restrict<MB><<<L.nblocks, cta, 0, L.st>>>(L.out, L.in, L.list, L.t0, L.scale, L.nlim);
-            break;
-        case OP_SEED_L1:
-            k_seed_l1<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.cgx, L.n, L.scale);
-            break;
-        case OP_SEED_L2:
-            k_seed_l2<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0, L.t1, L.t2, L.t3, L.t4, L.t5, L.t6,
-                                                       L.l1gx, L.n1, L.scale);
-            break;
-        case OP_SENSOR:
-            k_sensor<MB><<<L.nblocks, cta, 0, L.st>>>(L.in, L.out, L.aux, L.t0);
-            break;
-        case OP_COMPOSITE: {
-            const long long NN = (long long)L.n2 * L.n2 * L.n2;
-            k_composite<MB><<<(unsigned)((NN + 255) / 256), 256, 0, L.st>>>(L.in, L.aux, L.aux2, L.t0, L.t1, L.t2,
-                                                                          L.cgx, L.l1gx, L.n2, L.out);
-            break;
-        }
-        default:
-            return cudaErrorInvalidValue;
-    }
-    note_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t amr_launch(int mb, int op, const AmrLaunch& L) {
+cudaError_t amr_launch(int storage, int mb, int op, const AmrLaunch& L) {
     if (L.nblocks <= 0 && op != OP_COMPOSITE) return cudaSuccess;
-    switch (mb) {
-        case 4: return dispatch<4>(L, op);
-        case 8: return dispatch<8>(L, op);
-        case 16: return dispatch<16>(L, op);
+    switch (storage) {
+        case 0: return amr_launch_st<StF32>(mb, op, L);
+        case 1: return amr_launch_st<StF16>(mb, op, L);
+        case 2: return amr_launch_st<StBF16>(mb, op, L);
     }
     return cudaErrorInvalidValue;
 }
@@ -647,6 +28,7 @@ bool step_tpb_supported(int mb, int tpb) {
     if (mb == 4) return tpb == 64;
     return (mb == 8 || mb == 16) && (tpb == 128 || tpb == 256 || tpb == 512);
 }
+size_t storage_elem(int storage) { return storage == 0 ? 4 : 2; }
 
 }  // namespace amr
 }  // namespace jp

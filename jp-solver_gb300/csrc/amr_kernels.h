@@ -24,14 +24,16 @@ enum AmrOp {
                        // t3 l1grid, t4 ref1, t5 fof1
 };
 
+// Population arrays (pools, prolongation sources, ghost shells) are in the solver's storage format
+// (FP32, or shifted FP16/BF16); sensor values and the composite field are float.
 struct AmrLaunch {
     cudaStream_t st = nullptr;
     int nblocks = 0;
-    const float* in = nullptr;
-    float* out = nullptr;
-    float* out2 = nullptr;   // fused restriction target of the last fine substep (nullptr: none)
-    const float* aux = nullptr;
-    const float* aux2 = nullptr;
+    const void* in = nullptr;
+    void* out = nullptr;
+    void* out2 = nullptr;    // fused restriction target of the last fine substep (nullptr: none)
+    const void* aux = nullptr;
+    const void* aux2 = nullptr;
     const int* list = nullptr;
     const int *t0 = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr, *t6 = nullptr;
     const int* nbt = nullptr;  // same-level neighbour table of the fine level (27 per block)
@@ -45,7 +47,10 @@ struct AmrLaunch {
     double u0 = 0.0, kf = 0.0;
 };
 
-cudaError_t amr_launch(int mb, int op, const AmrLaunch& L);
+// storage: 0 FP32, 1 shifted FP16, 2 shifted BF16 (jp_storage)
+cudaError_t amr_launch(int storage, int mb, int op, const AmrLaunch& L);
+template <class ST> cudaError_t amr_launch_st(int mb, int op, const AmrLaunch& L);
+size_t storage_elem(int storage);  // bytes per stored population
 int shell_cells(int mb);
 // the fused restriction stages a block in shared memory: MB <= 8 (38 KiB at MB = 8)
 bool can_fuse_restrict(int mb);

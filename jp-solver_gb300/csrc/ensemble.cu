@@ -181,7 +181,8 @@ long long estimate_bytes(const jp_config& c) {
                                     ? cap1
                                     : std::min(cap1, std::max(1LL, (long long)std::ceil(2.5 * c.frac2 * cap1) + 8));
     const long long cap2 = 8 * cap_nref1;
-    const long long blk = Qn * mb3 * 4, gh = Qn * sh * 4;
+    const long long elem = c.storage == JP_FP32 ? 4 : 2;
+    const long long blk = Qn * mb3 * elem, gh = Qn * sh * elem;
     const long long n2 = 4 * n;
     return 3 * cnb0 * blk + cap1 * (3 * blk + gh) + cap2 * (2 * blk + gh) + 16 * n2 * n2 * n2 + (8 << 20);
 }
@@ -282,7 +283,6 @@ void record(Job* j, const double d[3], long long step) {
         j->peak_ts = ts;
     }
     ++j->samples;
-    j->need_diag = false;
 }
 
 long long next_event(const Job* j) {

@@ -20,6 +20,8 @@ using namespace amr;
 
 struct AmrState {
     jp_solver* owner = nullptr;  // allocations go through dev_alloc of the owning solver
+    int storage = 0;             // population format of pools, prolongation sources and ghosts
+    size_t elem = 4;             // bytes per stored population
     int MB = 8, MB3 = 512, SH = 480, N = 0, cgx = 0, cnb0 = 0, l1gx = 0, N1 = 0, N2 = 0, NG1 = 0;
     double tau0 = 0, tau1 = 0, tau2 = 0, nqs01 = 0, nqi10 = 0, nqs12 = 0, nqi21 = 0;
     float om0 = 0, om1 = 0, om2 = 0;
@@ -101,9 +103,13 @@ static void dfree(AmrState* a, T*& p) {
         if (s_ != JP_OK) return s_; \
     } while (0)
 
+// Floats of allocation that hold n populations in the solver's storage format (the population
+// arrays are typed float* and carry 16-bit values for the shifted formats).
+static size_t pf(const AmrState* a, size_t n) { return (n * a->elem + 3) / 4; }
+
 static jp_status launch(jp_solver* s, int op, AmrLaunch L) {
     L.st = s->stream;
-    cudaError_t e = amr_launch(s->amr->MB, op, L);
+    cudaError_t e = amr_launch(s->amr->storage, s->amr->MB, op, L);
     if (e != cudaSuccess) return cuda_fail(e, "AMR kernel launch");
     return JP_OK;
 }
@@ -208,8 +214,8 @@ static jp_status regrow(jp_solver* s, T*& p, size_t count, size_t keep) {
 
 static void update_bytes(jp_solver* s) {
     const AmrState* a = s->amr;
-    s->info.bytes_state = (int64_t)(((size_t)3 * a->cnb0 + 3 * (size_t)a->cap1 + 2 * (size_t)a->cap2) * Q * a->MB3 * 4 +
-                                    ((size_t)a->cap1 + a->cap2) * Q * a->SH * 4);
+    s->info.bytes_state = (int64_t)((((size_t)3 * a->cnb0 + 3 * (size_t)a->cap1 + 2 * (size_t)a->cap2) * Q * a->MB3 +
+                                     ((size_t)a->cap1 + a->cap2) * Q * a->SH) * a->elem);
 }
 
 // Pools grow on overflow instead of being written past their end (the reference sizes them with
@@ -223,10 +229,10 @@ static jp_status grow_l1(jp_solver* s, int needed) {
         return fail(JP_ERR_CAPACITY, "level-1 pool overflow: %d blocks needed, %d held, budget allows no growth", needed,
                     a->cap1);
     const size_t blk = (size_t)Q * a->MB3, old = a->cap1;
-    TRY(regrow(s, a->f1a, cap * blk, old * blk));  // payload the migration reads
-    TRY(regrow(s, a->f1b, cap * blk, 0));
-    TRY(regrow(s, a->gh1, (size_t)cap * Q * a->SH, 0));
-    TRY(regrow(s, a->prep1, cap * blk, 0));
+    TRY(regrow(s, a->f1a, pf(a, cap * blk), pf(a, old * blk)));  // payload the migration reads
+    TRY(regrow(s, a->f1b, pf(a, cap * blk), 0));
+    TRY(regrow(s, a->gh1, pf(a, (size_t)cap * Q * a->SH), 0));
+    TRY(regrow(s, a->prep1, pf(a, cap * blk), 0));
     TRY(regrow(s, a->o_ref1, cap, old));           // snapshots of the previous grid
     TRY(regrow(s, a->o_fof1, cap, old));
     int** scratch[] = {&a->pcb, &a->oct, &a->rl0, &a->f1pos, &a->ref1, &a->fof1, &a->rl1, &a->skin1, &a->deep};
@@ -250,9 +256,9 @@ static jp_status grow_l2(jp_solver* s, int needed) {
         return fail(JP_ERR_CAPACITY, "level-2 pool overflow: %d blocks needed, %d held, budget allows no growth", needed,
                     a->cap2);
     const size_t blk = (size_t)Q * a->MB3, old = a->cap2;
-    TRY(regrow(s, a->f2a, cap * blk, old * blk));  // payload the migration reads
-    TRY(regrow(s, a->f2b, cap * blk, 0));
-    TRY(regrow(s, a->gh2, (size_t)cap * Q * a->SH, 0));
+    TRY(regrow(s, a->f2a, pf(a, cap * blk), pf(a, old * blk)));  // payload the migration reads
+    TRY(regrow(s, a->f2b, pf(a, cap * blk), 0));
+    TRY(regrow(s, a->gh2, pf(a, (size_t)cap * Q * a->SH), 0));
     TRY(regrow(s, a->l2pl1, cap, 0));
     TRY(regrow(s, a->l2oct, cap, 0));
     TRY(regrow(s, a->nb2, (size_t)cap * 27, 0));
@@ -331,7 +337,7 @@ static jp_status initial_build(jp_solver* s) {
     }
     TRY(build_l1(s, false));
     if (a->nf1) {
-        ACK(cudaMemsetAsync(a->gh1, 0, sizeof(float) * (size_t)a->nf1 * Q * a->SH, s->stream), "memset gh1");
+        ACK(cudaMemsetAsync(a->gh1, 0, a->elem * (size_t)a->nf1 * Q * a->SH, s->stream), "memset gh1");
         AmrLaunch L;
         L.nblocks = a->nf1;
         L.out = a->f1a;
@@ -378,16 +384,16 @@ static jp_status initial_build(jp_solver* s) {
     dfree(a, a->nb2);
     const size_t blk = (size_t)Q * a->MB3;
     TRY(dalloc(a, &a->nb2, (size_t)a->cap2 * 27, "cudaMalloc nb2"));
-    TRY(dalloc(a, &a->f2a, (size_t)a->cap2 * blk, "cudaMalloc f2"));
-    TRY(dalloc(a, &a->f2b, (size_t)a->cap2 * blk, "cudaMalloc f2"));
-    TRY(dalloc(a, &a->gh2, (size_t)a->cap2 * Q * a->SH, "cudaMalloc gh2"));
+    TRY(dalloc(a, &a->f2a, pf(a, (size_t)a->cap2 * blk), "cudaMalloc f2"));
+    TRY(dalloc(a, &a->f2b, pf(a, (size_t)a->cap2 * blk), "cudaMalloc f2"));
+    TRY(dalloc(a, &a->gh2, pf(a, (size_t)a->cap2 * Q * a->SH), "cudaMalloc gh2"));
     TRY(dalloc(a, &a->l2pl1, (size_t)a->cap2, "cudaMalloc l2pl1"));
     TRY(dalloc(a, &a->l2oct, (size_t)a->cap2, "cudaMalloc l2oct"));
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset fof1");
     if (a->nf2) {
         ACK(adapt_scatter_l2(a->ref1, a->rank, a->nf1, a->cap2, a->fof1, a->rl1, a->l2pl1, a->l2oct, a->cnt_dev,
                              s->stream), "scatter L2");
-        ACK(cudaMemsetAsync(a->gh2, 0, sizeof(float) * (size_t)a->nf2 * Q * a->SH, s->stream), "memset gh2");
+        ACK(cudaMemsetAsync(a->gh2, 0, a->elem * (size_t)a->nf2 * Q * a->SH, s->stream), "memset gh2");
         AmrLaunch L;
         L.nblocks = a->nf2;
         L.out = a->f2a;
@@ -628,7 +634,8 @@ static jp_status graph_step(jp_solver* s) {
 jp_status amr_create(jp_solver* s) {
     TRY(common_setup(s));
     const jp_config& c = s->cfg;
-    if (c.storage != JP_FP32) return fail(JP_ERR_UNSUPPORTED, "AMR solver: FP32 storage only in this build");
+    if (c.storage != JP_FP32 && c.storage != JP_FP16 && c.storage != JP_BF16)
+        return fail(JP_ERR_UNSUPPORTED, "AMR solver: FP32, FP16 or BF16 storage (FP64 is uniform only)");
     if (c.l1_mode < 0 || c.l1_mode > 2 || c.l2_mode < 0 || c.l2_mode > 2) return fail(JP_ERR_INVALID, "bad refine mode");
     if (c.threads_per_block && !step_tpb_supported(c.mb, c.threads_per_block))
         return fail(JP_ERR_INVALID, "threads_per_block %d does not split a block of edge %d (MB=4: 64; 8, 16: 128, 256, 512)",
@@ -637,6 +644,8 @@ jp_status amr_create(jp_solver* s) {
     if (!a) return fail(JP_ERR_NOMEM, "host allocation");
     s->amr = a;
     a->owner = s;
+    a->storage = c.storage;
+    a->elem = storage_elem(c.storage);
     a->tpb = c.threads_per_block;
     a->MB = c.mb;
     a->MB3 = c.mb * c.mb * c.mb;
@@ -665,8 +674,8 @@ jp_status amr_create(jp_solver* s) {
     s->cells = (long long)a->cnb0 * a->MB3;
     s->n = c.n;
     const size_t blk = (size_t)Q * a->MB3;
-    TRY(dalloc(a, &a->c0a, (size_t)a->cnb0 * blk, "cudaMalloc c0"));
-    TRY(dalloc(a, &a->c0b, (size_t)a->cnb0 * blk, "cudaMalloc c0"));
+    TRY(dalloc(a, &a->c0a, pf(a, (size_t)a->cnb0 * blk), "cudaMalloc c0"));
+    TRY(dalloc(a, &a->c0b, pf(a, (size_t)a->cnb0 * blk), "cudaMalloc c0"));
     TRY(dalloc(a, &a->sen0, (size_t)a->cnb0, "cudaMalloc sen0"));
     // HBM budget for the fine pools: --maxgb, else 75% of free memory (src/tgv3d_amr.cu:684-688)
     size_t freeB = 0, totB = 0;
@@ -677,11 +686,11 @@ jp_status amr_create(jp_solver* s) {
                                                 : std::min(a->cnb0, std::max(1, (int)std::ceil(c.frac1 * a->cnb0 * 1.4)));
     while (a->cap_nref0 > 1 && !pool_fits(a, 8LL * a->cap_nref0, 0)) a->cap_nref0--;
     a->cap1 = 8 * a->cap_nref0;
-    TRY(dalloc(a, &a->f1a, (size_t)a->cap1 * blk, "cudaMalloc f1"));
-    TRY(dalloc(a, &a->f1b, (size_t)a->cap1 * blk, "cudaMalloc f1"));
-    TRY(dalloc(a, &a->gh1, (size_t)a->cap1 * Q * a->SH, "cudaMalloc gh1"));
-    TRY(dalloc(a, &a->prep0, (size_t)a->cnb0 * blk, "cudaMalloc prep0"));
-    TRY(dalloc(a, &a->prep1, (size_t)a->cap1 * blk, "cudaMalloc prep1"));
+    TRY(dalloc(a, &a->f1a, pf(a, (size_t)a->cap1 * blk), "cudaMalloc f1"));
+    TRY(dalloc(a, &a->f1b, pf(a, (size_t)a->cap1 * blk), "cudaMalloc f1"));
+    TRY(dalloc(a, &a->gh1, pf(a, (size_t)a->cap1 * Q * a->SH), "cudaMalloc gh1"));
+    TRY(dalloc(a, &a->prep0, pf(a, (size_t)a->cnb0 * blk), "cudaMalloc prep0"));
+    TRY(dalloc(a, &a->prep1, pf(a, (size_t)a->cap1 * blk), "cudaMalloc prep1"));
     int** cnb_tabs[] = {&a->ref0, &a->fof0, &a->o_ref0, &a->o_fof0, &a->skin0};
     for (int** t : cnb_tabs) TRY(dalloc(a, t, (size_t)a->cnb0, "cudaMalloc table"));
     int** cap_tabs[] = {&a->pcb, &a->oct, &a->rl0, &a->f1pos, &a->ref1, &a->fof1, &a->o_ref1, &a->o_fof1,
@@ -817,6 +826,8 @@ jp_status amr_population_count(const jp_solver* s, int level, int64_t* count) {
     return JP_OK;
 }
 
+// Populations cross the boundary as unshifted values in the blocked layout [blk][q][MB^3]
+// (FP32 storage read as float: the stored bits; shifted formats converted, f = w_q + g).
 jp_status amr_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count) {
     AmrState* a = s->amr;
     long long nb;
@@ -825,15 +836,19 @@ jp_status amr_get_populations(jp_solver* s, int level, int layout, int dtype, vo
     if (layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_UNSUPPORTED, "AMR populations are exported in the blocked layout");
     if (count != nb * Q * a->MB3) return fail(JP_ERR_INVALID, "count %lld != %lld", (long long)count, nb * Q * a->MB3);
     if (count == 0) return JP_OK;
-    if (dtype == JP_F32) {
+    if (dtype == JP_F32 && a->storage == JP_FP32) {
         ACK(cudaMemcpyAsync(host, p, sizeof(float) * count, cudaMemcpyDeviceToHost, s->stream), "D2H");
         ACK(cudaStreamSynchronize(s->stream), "D2H");
         return JP_OK;
     }
-    std::vector<float> tmp((size_t)count);
-    ACK(cudaMemcpyAsync(tmp.data(), p, sizeof(float) * count, cudaMemcpyDeviceToHost, s->stream), "D2H");
+    std::vector<unsigned char> raw((size_t)count * a->elem);
+    ACK(cudaMemcpyAsync(raw.data(), p, raw.size(), cudaMemcpyDeviceToHost, s->stream), "D2H");
     ACK(cudaStreamSynchronize(s->stream), "D2H");
-    for (int64_t i = 0; i < count; ++i) static_cast<double*>(host)[i] = tmp[(size_t)i];
+    for (int64_t i = 0; i < count; ++i) {
+        const double v = stored_to_double(a->storage, raw.data(), (size_t)i, int((i / a->MB3) % Q));
+        if (dtype == JP_F32) static_cast<float*>(host)[i] = float(v);
+        else static_cast<double*>(host)[i] = v;
+    }
     return JP_OK;
 }
 
@@ -845,14 +860,17 @@ jp_status amr_set_populations(jp_solver* s, int level, int layout, int dtype, co
     if (layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_UNSUPPORTED, "AMR populations are imported in the blocked layout");
     if (count != nb * Q * a->MB3) return fail(JP_ERR_INVALID, "count %lld != %lld", (long long)count, nb * Q * a->MB3);
     if (count == 0) return JP_OK;
-    if (dtype == JP_F32) {
+    if (dtype == JP_F32 && a->storage == JP_FP32) {
         ACK(cudaMemcpyAsync(p, host, sizeof(float) * count, cudaMemcpyHostToDevice, s->stream), "H2D");
         ACK(cudaStreamSynchronize(s->stream), "H2D");
         return JP_OK;
     }
-    std::vector<float> tmp((size_t)count);
-    for (int64_t i = 0; i < count; ++i) tmp[(size_t)i] = float(static_cast<const double*>(host)[i]);
-    ACK(cudaMemcpyAsync(p, tmp.data(), sizeof(float) * count, cudaMemcpyHostToDevice, s->stream), "H2D");
+    std::vector<unsigned char> raw((size_t)count * a->elem);
+    for (int64_t i = 0; i < count; ++i) {
+        const double v = dtype == JP_F32 ? double(static_cast<const float*>(host)[i]) : static_cast<const double*>(host)[i];
+        double_to_stored(a->storage, raw.data(), (size_t)i, int((i / a->MB3) % Q), v);
+    }
+    ACK(cudaMemcpyAsync(p, raw.data(), raw.size(), cudaMemcpyHostToDevice, s->stream), "H2D");
     ACK(cudaStreamSynchronize(s->stream), "H2D");
     return JP_OK;
 }

@@ -1,8 +1,9 @@
 // `amr`: drop-in for the reference's three-level AMR Taylor-Green program (src/tgv3d_amr.cu:643-907),
 // driving the GB300 engine through the C ABI.  Same flags and defaults (including --adapt, --maxgb,
 // --graph, --skipprep, --skiprestr, --bench and the parsed-but-unused --buffer), same stdout lines,
-// exit codes and .vti/.vtp frames.  Additions: --mb, --tpb (threads per CTA of the level steps),
-// --develop, --device, --autotune 1 (MB x threads per CTA), --diag-every.
+// exit codes and .vti/.vtp frames.  Additions: --prec fp32|fp16|bf16 (population storage), --mb,
+// --tpb (threads per CTA of the level steps), --develop, --device, --autotune 1 (MB x threads per
+// CTA), --diag-every.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -83,6 +84,7 @@ int main(int argc, char** argv) {
     cfg.develop_steps = argi(argc, argv, "--develop", 300);
     cfg.device = argi(argc, argv, "--device", 0);
     cfg.threads_per_block = argi(argc, argv, "--tpb", 0);
+    cfg.storage = storage_of(args(argc, argv, "--prec", "fp32"));
     cfg.flags = (skipprep ? JP_FLAG_SKIP_PREP : 0) | (skiprestr ? JP_FLAG_SKIP_RESTRICT : 0) | (usegraph ? JP_FLAG_GRAPH : 0);
     if (argd(argc, argv, "--autotune", 0.0) > 0.5) {
         double best = 0.0;

@@ -287,3 +287,50 @@ def test_graph_replay_matches_direct_launches_across_regrids():
     for lv in range(3):
         np.testing.assert_array_equal(runs[J.FLAG_GRAPH][0][lv], runs[0][0][lv], err_msg="level %d" % lv)
     assert runs[0][2] == runs[J.FLAG_GRAPH][2]
+
+
+@pytest.mark.parametrize("storage,atol", [("fp16", 3e-6), ("bf16", 2.5e-5)])
+def test_shifted_storage_one_coarse_step_tracks_oracle(storage, atol):
+    # AMR pools, prolongation sources and ghosts stored as shifted 16-bit values (f - w_q), FP32
+    # arithmetic: from the same (rounded) state, one coarse step stays within the format's rounding
+    # of the FP32 oracle (a few half-ulps of the largest deviations; absolute errors stated here),
+    # and the tables are identical for the same sensor
+    n = 24
+    s0, s1 = O.random_sensor_fields(n, seed=17)
+    with J.Solver("amr", n=n, re=1600.0, l1_mode="sensor", l2_mode="sensor", frac1=0.35, frac2=0.4,
+                  develop_steps=3, max_gb=1024.0, storage=storage) as e:
+        e.set_sensor_override(s0, s1)
+        e.init_tgv()
+        o = oracle(n, 1600.0, "sensor", "sensor", 0.35, 0.4, develop=3, build=False)
+        o.set_sensor_override(s0, s1)
+        o.initial_build()
+        assert_tables_equal(e, o, storage)
+        for lv in range(3):
+            e.set_populations(o.pops(lv), level=lv, layout="blocked")      # rounds to the format
+            o.set_pops(lv, e.get_populations(lv, layout="blocked"))        # the same rounded state
+        e.step(1)
+        o.step(1)
+        for lv in range(3):
+            err = float(np.max(np.abs(e.get_populations(lv, layout="blocked").astype(np.float64) - o.pops(lv))))
+            assert err < atol, "level %d: %.3g" % (lv, err)
+        d, do = e.diag(), o.diag()
+        assert abs(d[2] - do[2]) < 1e-6 and abs(d[0] - do[0]) < 1e-3 * do[0]
+        o.close()
+
+
+@pytest.mark.parametrize("storage", ["fp16", "bf16"])
+def test_shifted_storage_static_gold_holds_mass(storage):
+    # refine-all AMR in shifted storage over 60 coarse steps: the energy decays like the FP32 run's,
+    # mass is held (shifted collision), and the graph replay gives the same bits as direct launches
+    n0, re, steps = 16, 400.0, 60
+    res = {}
+    for st, flags in (("fp32", 0), (storage, 0), (storage, J.FLAG_GRAPH)):
+        with J.Solver("amr", n=n0, re=re, l1_mode="all", l2_mode="all", storage=st, flags=flags) as a:
+            e0, z0, m0 = a.diag()
+            a.step(steps)
+            e1, z1, m1 = a.diag()
+            res[(st, flags)] = (e1 / e0, abs(m1 - m0) / m0, a.get_populations(2, layout="blocked"))
+    r32, r16, r16g = res[("fp32", 0)], res[(storage, 0)], res[(storage, J.FLAG_GRAPH)]
+    assert abs(r16[0] - r32[0]) < (2e-4 if storage == "fp16" else 3e-3)
+    assert r16[1] < 1e-6
+    np.testing.assert_array_equal(r16[2], r16g[2])

@@ -130,6 +130,31 @@ def test_server_amr_result_matches_program_loop():
     assert r["energy_ratio"] == Elast / E0
 
 
+def test_server_uniform_result_matches_program_loop():
+    # the `uniform` program's loop: a diagnostic at every step s % diagK == 0 (diagK = steps/240),
+    # then steps to the next one; the served solve reports the same samples and peak, bit for bit
+    req = dict(rid=21, kind="uniform", n=24, re=300.0, tstar=4.0, storage="fp16")
+    res, _ = run_server([req, dict(R0, rid=22), dict(MIX[0], rid=23)], tick_steps=16)
+    r = res[21]
+    cfg = {k: v for k, v in req.items() if k not in ("rid", "kind")}
+    with J.Solver("uniform", **cfg) as s:
+        steps, kf = s.info["steps"], s.info["kf"]
+        diagK = max(1, steps // 240)
+        E0, peak, peak_ts, samples, Elast = None, -1.0, -1.0, 0, None
+        for step in range(0, steps + 1, diagK):
+            E, ens, mass = s.diag()
+            E0 = E if E0 is None else E0
+            Elast = E
+            samples += 1
+            if ens > peak:
+                peak, peak_ts = ens, step * 0.05 * kf
+            if step + diagK <= steps:
+                s.step(diagK)
+    assert r["steps"] == steps and r["samples"] == samples
+    assert r["peak_enstrophy"] == peak and r["peak_tstar"] == peak_ts
+    assert r["energy_ratio"] == Elast / E0
+
+
 def test_server_admission_respects_budget():
     big = [dict(rid=100 + i, kind="uniform", n=96, re=800.0, tstar=0.3) for i in range(4)]
     one = 2 * 19 * 4 * 96 ** 3 + 16 * 96 ** 3 + (1 << 20)
