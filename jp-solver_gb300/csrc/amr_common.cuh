@@ -146,12 +146,16 @@ __device__ __forceinline__ void bgk_fast(float (&f)[Q], float om) {
     const float base = SH ? -usq : 1.f - usq;
     const float omc = 1.f - om, orho = om * rho;
     const float owr1 = orho * wf(1), owr2 = orho * wf(7), owr3a = 3.f * owr1, owr3b = 3.f * owr2;
-    const float ows1 = SH ? om * wf(1) * sm : 0.f, ows2 = SH ? om * wf(7) * sm : 0.f;
-    f[0] = omc * f[0] + om * wf(0) * (SH ? sm - rho * usq : rho * base);
+    if constexpr (SH) {
+        f[0] = omc * f[0] + om * wf(0) * (sm - rho * usq);
+    } else {
+        f[0] = omc * f[0] + orho * wf(0) * base;
+    }
 #pragma unroll
     for (int q = 1; q < Q; q += 2) {
         const float a = cdot<float>(q, ux, uy, uz);
-        const float t = (q < 7 ? owr1 : owr2) * (4.5f * a * a + base) + (q < 7 ? ows1 : ows2);
+        float t = (q < 7 ? owr1 : owr2) * (4.5f * a * a + base);
+        if constexpr (SH) t += om * wf(q) * sm;  // omega * w * s, the shifted part of the equilibrium
         const float as = (q < 7 ? owr3a : owr3b) * a;
         f[q] = omc * f[q] + (t + as);
         f[q + 1] = omc * f[q + 1] + (t - as);
@@ -200,17 +204,22 @@ __device__ __forceinline__ void pull_cell(const typename ST::raw* __restrict__ f
                                           const int* __restrict__ nbrow, int b, int i, int j, int k,
                                           float (&f)[Q]) {
     constexpr int MB3 = MB * MB * MB, SH = Geo<MB>::SH;
+    // raw values first, conversions after the loop: a conversion inside the branch would wait for
+    // its load before the next population's load is issued
+    typename ST::raw rv[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         int e, sc;
         pull_src<MB>(q, i, j, k, e, sc);
         const int blk = e == 13 ? b : __ldg(nbrow + e);
         if (!GHOST || blk >= 0) {
-            f[q] = PoolIO<ST>::n(fa + ((size_t)blk * Q + q) * MB3 + sc);
+            rv[q] = __ldg(fa + ((size_t)blk * Q + q) * MB3 + sc);
         } else {
-            f[q] = PoolIO<ST>::n(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(i - cx(q), j - cy(q), k - cz(q)));
+            rv[q] = __ldg(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(i - cx(q), j - cy(q), k - cz(q)));
         }
     }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q] = ST::load(rv[q]);
 }
 // Neighbour slot of a ghost-shell cell at block-local (i, j, k), each in [-1, MB].
 template <int MB>
