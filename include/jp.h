@@ -246,13 +246,17 @@ jp_status jp_set_sensor_override(jp_solver* s, const float* sen0, const float* s
 
 /* ---- ensembles and serving (extensions; no counterpart in the reference) ------------- */
 
-/* An ensemble steps many uniform solvers of the same device together: every lattice step is one
- * batched stream-collide launch per storage format (up to 48 cubes of any sizes per launch) on the
- * ensemble's stream, ordered after each member's pending work and before its later work. */
+/* An ensemble steps many solvers of the same device together, on the ensemble's stream, ordered
+ * after each member's pending work and before its later work.  Uniform members: one batched
+ * stream-collide launch per storage format per lattice step (up to 48 cubes of any sizes per
+ * launch).  AMR members: one coarse step (the 1:2:4 subcycle) with one launch per stage over the
+ * blocks of all members of the same block edge, storage and step threads (up to 48 per launch);
+ * jp_ensemble_step(e, k) advances AMR members by k coarse steps.  Regrids and diagnostics stay
+ * per solver (jp_regrid, jp_diag) between ensemble steps. */
 typedef struct jp_ensemble jp_ensemble;
 jp_status jp_ensemble_create(int32_t device, jp_ensemble** out);
 void jp_ensemble_destroy(jp_ensemble* e);
-jp_status jp_ensemble_add(jp_ensemble* e, jp_solver* s);     /* uniform solvers only */
+jp_status jp_ensemble_add(jp_ensemble* e, jp_solver* s);
 jp_status jp_ensemble_remove(jp_ensemble* e, jp_solver* s);
 jp_status jp_ensemble_step(jp_ensemble* e, int64_t nsteps);
 

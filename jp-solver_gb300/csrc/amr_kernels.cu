@@ -6,8 +6,13 @@ namespace jp {
 namespace amr {
 
 template cudaError_t amr_launch_st<StF32>(int mb, int op, const AmrLaunch& L);
+template cudaError_t amr_batch_launch_st<StF32>(int mb, int op, int tpb, bool fuse, const AmrBatch& B, cudaStream_t st);
 extern template cudaError_t amr_launch_st<StF16>(int mb, int op, const AmrLaunch& L);
 extern template cudaError_t amr_launch_st<StBF16>(int mb, int op, const AmrLaunch& L);
+extern template cudaError_t amr_batch_launch_st<StF16>(int mb, int op, int tpb, bool fuse, const AmrBatch& B,
+                                                       cudaStream_t st);
+extern template cudaError_t amr_batch_launch_st<StBF16>(int mb, int op, int tpb, bool fuse, const AmrBatch& B,
+                                                        cudaStream_t st);
 
 cudaError_t amr_launch(int storage, int mb, int op, const AmrLaunch& L) {
     if (L.nblocks <= 0 && op != OP_COMPOSITE) return cudaSuccess;
@@ -15,6 +20,15 @@ cudaError_t amr_launch(int storage, int mb, int op, const AmrLaunch& L) {
         case 0: return amr_launch_st<StF32>(mb, op, L);
         case 1: return amr_launch_st<StF16>(mb, op, L);
         case 2: return amr_launch_st<StBF16>(mb, op, L);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t amr_batch_launch(int storage, int mb, int op, int tpb, bool fuse, const AmrBatch& B, cudaStream_t st) {
+    switch (storage) {
+        case 0: return amr_batch_launch_st<StF32>(mb, op, tpb, fuse, B, st);
+        case 1: return amr_batch_launch_st<StF16>(mb, op, tpb, fuse, B, st);
+        case 2: return amr_batch_launch_st<StBF16>(mb, op, tpb, fuse, B, st);
     }
     return cudaErrorInvalidValue;
 }

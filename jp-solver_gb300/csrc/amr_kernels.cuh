@@ -34,10 +34,10 @@ __global__ void __launch_bounds__(Geo<MB>::TPB) k_init(typename ST::raw* __restr
 
 // ---- dense periodic coarse step (src/tgv3d_amr.cu:203-220) ---------------------------------------
 template <int MB, class ST, int TPB>
-__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const typename ST::raw* __restrict__ fa,
-                                                             typename ST::raw* __restrict__ fb, int cgx, float om) {
+__device__ __forceinline__ void d_step_l0(const typename ST::raw* __restrict__ fa,
+                                                             typename ST::raw* __restrict__ fb, int cgx, float om, int blk) {
     using G = Geo<MB>;
-    const int b = blockIdx.x;
+    const int b = blk;
     const int bx = b % cgx, by = (b / cgx) % cgx, bz = b / (cgx * cgx);
     __shared__ int snb[27];  // periodic neighbour blocks (arithmetic only: no loads wait on the barrier)
     if (threadIdx.x < 27) {
@@ -59,16 +59,21 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const typename ST::
         for (int q = 0; q < Q; ++q) PoolIO<ST>::put_n(fb + ((size_t)b * Q + q) * G::MB3 + cell, f[q]);
     }
 }
+template <int MB, class ST, int TPB>
+__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const typename ST::raw* __restrict__ fa,
+                                                             typename ST::raw* __restrict__ fb, int cgx, float om) {
+    d_step_l0<MB, ST, TPB>(fa, fb, cgx, om, (int)blockIdx.x);
+}
 
 // ---- prolongation sources on a block list (src/tgv3d_amr.cu:160-171) -----------------------------
 template <int MB, class ST>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const typename ST::raw* __restrict__ fin,
+__device__ __forceinline__ void d_prep(const typename ST::raw* __restrict__ fin,
                                                       typename ST::raw* __restrict__ pr,
                                                       const int* __restrict__ list, float nqs,
-                                                      const int* __restrict__ nlim) {
+                                                      const int* __restrict__ nlim, int blk) {
     using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
-    const int b = list[blockIdx.x];
+    if (nlim && (int)blk >= __ldg(nlim)) return;
+    const int b = list[blk];
     CELL_LOOP(cell) {
         float f[Q];
 #pragma unroll
@@ -77,6 +82,13 @@ __global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const typename ST::raw* _
 #pragma unroll
         for (int q = 0; q < Q; ++q) PoolIO<ST>::put_f(pr + ((size_t)b * Q + q) * G::MB3 + cell, q, f[q]);
     }
+}
+template <int MB, class ST>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const typename ST::raw* __restrict__ fin,
+                                                      typename ST::raw* __restrict__ pr,
+                                                      const int* __restrict__ list, float nqs,
+                                                      const int* __restrict__ nlim) {
+    d_prep<MB, ST>(fin, pr, list, nqs, nlim, (int)blockIdx.x);
 }
 
 // trilinear of a precomputed source on the dense coarse grid (src/tgv3d_amr.cu:122-132)
@@ -141,13 +153,13 @@ __device__ __forceinline__ void prolong_prep_l1(const typename ST::raw* __restri
 // One CTA per fine block, one thread per shell cell; a shell cell whose same-level neighbour block
 // exists (its parent is refined) is left alone: the step gathers it from that block instead.
 template <int MB, class ST>
-__global__ void __launch_bounds__(256) k_fill_l1(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
+__device__ __forceinline__ void d_fill_l1(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ pcb, const int* __restrict__ poct,
                                                 const int* __restrict__ nbtab, int cgx, int N,
-                                                const int* __restrict__ nlim) {
+                                                const int* __restrict__ nlim, int blk) {
     using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
-    const int fb = blockIdx.x;
+    if (nlim && (int)blk >= __ldg(nlim)) return;
+    const int fb = blk;
     const int* nbrow = nbtab + (size_t)fb * 27;
     const int cb = pcb[fb], oct = poct[fb];
     const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
@@ -164,16 +176,23 @@ __global__ void __launch_bounds__(256) k_fill_l1(const typename ST::raw* __restr
         for (int q = 0; q < Q; ++q) PoolIO<ST>::put_f(gh + ((size_t)fb * Q + q) * G::SH + t, q, out[q]);
     }
 }
+template <int MB, class ST>
+__global__ void __launch_bounds__(256) k_fill_l1(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
+                                                const int* __restrict__ pcb, const int* __restrict__ poct,
+                                                const int* __restrict__ nbtab, int cgx, int N,
+                                                const int* __restrict__ nlim) {
+    d_fill_l1<MB, ST>(pr, gh, pcb, poct, nbtab, cgx, N, nlim, (int)blockIdx.x);
+}
 
 template <int MB, class ST>
-__global__ void __launch_bounds__(256) k_fill_l2(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
+__device__ __forceinline__ void d_fill_l2(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
                                                 const int* __restrict__ f1pos, const int* __restrict__ l1grid,
                                                 const int* __restrict__ nbtab, int l1gx, int N1,
-                                                const int* __restrict__ nlim) {
+                                                const int* __restrict__ nlim, int blk) {
     using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
-    const int b = blockIdx.x;
+    if (nlim && (int)blk >= __ldg(nlim)) return;
+    const int b = blk;
     const int* nbrow = nbtab + (size_t)b * 27;
     const int pl1 = l2pl1[b], oct = l2oct[b];
     const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
@@ -189,6 +208,14 @@ __global__ void __launch_bounds__(256) k_fill_l2(const typename ST::raw* __restr
 #pragma unroll
         for (int q = 0; q < Q; ++q) PoolIO<ST>::put_f(gh + ((size_t)b * Q + q) * G::SH + t, q, out[q]);
     }
+}
+template <int MB, class ST>
+__global__ void __launch_bounds__(256) k_fill_l2(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
+                                                const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
+                                                const int* __restrict__ f1pos, const int* __restrict__ l1grid,
+                                                const int* __restrict__ nbtab, int l1gx, int N1,
+                                                const int* __restrict__ nlim) {
+    d_fill_l2<MB, ST>(pr, gh, l2pl1, l2oct, f1pos, l1grid, nbtab, l1gx, N1, nlim, (int)blockIdx.x);
 }
 
 // Restriction of one fine block, staged in shared memory as sf[q * MB^3 + cell] after its last
@@ -268,19 +295,19 @@ __global__ void k_nbtab_l2(int* __restrict__ nb, const int* __restrict__ l2pl1, 
 // restricts itself into its parent octant (`parent`, `poct`), which saves re-reading the level from
 // HBM in a separate restriction kernel.
 template <int MB, class ST, int TPB, bool FUSE>
-__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_fine(const typename ST::raw* __restrict__ fa,
+__device__ __forceinline__ void d_step_fine(const typename ST::raw* __restrict__ fa,
                                                                typename ST::raw* __restrict__ fbuf,
                                                                const typename ST::raw* __restrict__ gh,
                                                                const int* __restrict__ nbtab,
                                                                const int* __restrict__ parent,
                                                                const int* __restrict__ poct, float om,
                                                                typename ST::raw* __restrict__ parent_pool, float nqi,
-                                                               const int* __restrict__ nlim) {
+                                                               const int* __restrict__ nlim, int blk) {
     static_assert(Geo<MB>::MB3 % TPB == 0, "cells must split evenly over the CTA");
     extern __shared__ float sf[];
     using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;  // whole CTA: the barrier below stays uniform
-    const int b = blockIdx.x;
+    if (nlim && (int)blk >= __ldg(nlim)) return;  // whole CTA: the barrier below stays uniform
+    const int b = blk;
     const int* nbrow = nbtab + (size_t)b * 27;
     for (int cell = threadIdx.x; cell < G::MB3; cell += TPB) {
         const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
@@ -299,18 +326,29 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_fine(const typename ST
         restrict_octant<MB, ST>(sf, parent_pool + (size_t)parent[b] * Q * G::MB3, poct[b], nqi);
     }
 }
+template <int MB, class ST, int TPB, bool FUSE>
+__global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_fine(const typename ST::raw* __restrict__ fa,
+                                                               typename ST::raw* __restrict__ fbuf,
+                                                               const typename ST::raw* __restrict__ gh,
+                                                               const int* __restrict__ nbtab,
+                                                               const int* __restrict__ parent,
+                                                               const int* __restrict__ poct, float om,
+                                                               typename ST::raw* __restrict__ parent_pool, float nqi,
+                                                               const int* __restrict__ nlim) {
+    d_step_fine<MB, ST, TPB, FUSE>(fa, fbuf, gh, nbtab, parent, poct, om, parent_pool, nqi, nlim, (int)blockIdx.x);
+}
 
 // ---- restriction (src/tgv3d_amr.cu:275-298, 357-381) -------------------------------------------------
 // One CTA per refined parent block; each parent cell becomes feq + nqi*regularize(avg - feq) of the
 // average of its 8 children (summed in the reference's dk, dj, di order).
 template <int MB, class ST>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_restrict(typename ST::raw* __restrict__ cf,
+__device__ __forceinline__ void d_restrict(typename ST::raw* __restrict__ cf,
                                                           const typename ST::raw* __restrict__ ff,
                                                           const int* __restrict__ rl, const int* __restrict__ fof,
-                                                          float nqi, const int* __restrict__ nlim) {
+                                                          float nqi, const int* __restrict__ nlim, int blk) {
     using G = Geo<MB>;
-    if (nlim && (int)blockIdx.x >= __ldg(nlim)) return;
-    const int cb = rl[blockIdx.x];
+    if (nlim && (int)blk >= __ldg(nlim)) return;
+    const int cb = rl[blk];
     const int fbase = fof[cb];
     CELL_LOOP(cell) {
         const int lci = cell % MB, lcj = (cell / MB) % MB, lck = cell / (MB * MB);
@@ -339,6 +377,13 @@ __global__ void __launch_bounds__(Geo<MB>::TPB) k_restrict(typename ST::raw* __r
 #pragma unroll
         for (int q = 0; q < Q; ++q) PoolIO<ST>::put_f(cf + ((size_t)cb * Q + q) * G::MB3 + cell, q, fe[q] + nqi * a[q]);
     }
+}
+template <int MB, class ST>
+__global__ void __launch_bounds__(Geo<MB>::TPB) k_restrict(typename ST::raw* __restrict__ cf,
+                                                          const typename ST::raw* __restrict__ ff,
+                                                          const int* __restrict__ rl, const int* __restrict__ fof,
+                                                          float nqi, const int* __restrict__ nlim) {
+    d_restrict<MB, ST>(cf, ff, rl, fof, nqi, nlim, (int)blockIdx.x);
 }
 
 // ---- on-the-fly prolongation for seeding and migration (src/tgv3d_amr.cu:70-118) ----------------
@@ -644,6 +689,108 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
     }
     note_launch();
     return cudaGetLastError();
+}
+
+// ---- batched launches: one grid over the blocks of many solves ------------------------------------
+// A CTA finds its member by bisection over the members' first CTAs and runs the stage's body on the
+// member's block blockIdx.x - begin.
+__device__ __forceinline__ int batch_member(const AmrBatch& B) {
+    int lo = 0, hi = B.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (B.it[mid].begin <= (int)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int MB, class ST, int TPB, bool FUSE, bool L0>
+__global__ void __launch_bounds__(TPB, 1024 / TPB) kb_step(const __grid_constant__ AmrBatch B) {
+    const AmrItem& it = B.it[batch_member(B)];
+    const int blk = (int)blockIdx.x - it.begin;
+    using raw = typename ST::raw;
+    if constexpr (L0) {
+        d_step_l0<MB, ST, TPB>((const raw*)it.in, (raw*)it.out, it.cgx, it.omega, blk);
+    } else {
+        d_step_fine<MB, ST, TPB, FUSE>((const raw*)it.in, (raw*)it.out, (const raw*)it.aux, it.nbt, it.t0, it.t1,
+                                       it.omega, (raw*)it.out2, it.scale, it.nlim, blk);
+    }
+}
+
+template <int MB, class ST, int OP>
+__global__ void __launch_bounds__(OP == OP_FILL_L1 || OP == OP_FILL_L2 ? 256 : Geo<MB>::TPB)
+    kb_cells(const __grid_constant__ AmrBatch B) {
+    const AmrItem& it = B.it[batch_member(B)];
+    const int blk = (int)blockIdx.x - it.begin;
+    using raw = typename ST::raw;
+    if constexpr (OP == OP_PREP) {
+        d_prep<MB, ST>((const raw*)it.in, (raw*)it.out, it.list, it.scale, it.nlim, blk);
+    } else if constexpr (OP == OP_FILL_L1) {
+        d_fill_l1<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.nbt, it.cgx, it.n, it.nlim, blk);
+    } else if constexpr (OP == OP_FILL_L2) {
+        d_fill_l2<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.t2, it.t3, it.nbt, it.l1gx, it.n1, it.nlim,
+                          blk);
+    } else {
+        d_restrict<MB, ST>((raw*)it.out, (const raw*)it.in, it.list, it.t0, it.scale, it.nlim, blk);
+    }
+}
+
+template <int MB, class ST, int TPB>
+static void batch_steps(int op, bool fuse, const AmrBatch& B, cudaStream_t st) {
+    using G = Geo<MB>;
+    if (op == OP_STEP_L0) {
+        kb_step<MB, ST, TPB, false, true><<<B.total, TPB, 0, st>>>(B);
+        return;
+    }
+    if constexpr (MB <= 8) {
+        if (fuse) {
+            kb_step<MB, ST, TPB, true, false><<<B.total, TPB, sizeof(float) * Q * G::MB3, st>>>(B);
+            return;
+        }
+    }
+    kb_step<MB, ST, TPB, false, false><<<B.total, TPB, 0, st>>>(B);
+}
+
+template <int MB, class ST>
+static cudaError_t batch_dispatch(int op, int tpb, bool fuse, const AmrBatch& B, cudaStream_t st) {
+    using G = Geo<MB>;
+    const dim3 cta(G::TPB);
+    const dim3 shl(G::SH < 256 ? ((G::SH + 31) / 32) * 32 : 256);
+    switch (op) {
+        case OP_STEP_L0:
+        case OP_STEP_L1:
+        case OP_STEP_L2: {
+            const int t = tpb ? tpb : default_step_tpb(MB);
+            if constexpr (MB == 4) {
+                if (t != 64) return cudaErrorInvalidConfiguration;
+                batch_steps<MB, ST, 64>(op, fuse, B, st);
+            } else {
+                if (t == 128) batch_steps<MB, ST, 128>(op, fuse, B, st);
+                else if (t == 256) batch_steps<MB, ST, 256>(op, fuse, B, st);
+                else if (t == 512) batch_steps<MB, ST, 512>(op, fuse, B, st);
+                else return cudaErrorInvalidConfiguration;
+            }
+            break;
+        }
+        case OP_PREP: kb_cells<MB, ST, OP_PREP><<<B.total, cta, 0, st>>>(B); break;
+        case OP_FILL_L1: kb_cells<MB, ST, OP_FILL_L1><<<B.total, shl, 0, st>>>(B); break;
+        case OP_FILL_L2: kb_cells<MB, ST, OP_FILL_L2><<<B.total, shl, 0, st>>>(B); break;
+        case OP_RESTRICT: kb_cells<MB, ST, OP_RESTRICT><<<B.total, cta, 0, st>>>(B); break;
+        default: return cudaErrorInvalidValue;
+    }
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <class ST>
+cudaError_t amr_batch_launch_st(int mb, int op, int tpb, bool fuse, const AmrBatch& B, cudaStream_t st) {
+    if (B.count <= 0 || B.total <= 0) return cudaSuccess;
+    switch (mb) {
+        case 4: return batch_dispatch<4, ST>(op, tpb, fuse, B, st);
+        case 8: return batch_dispatch<8, ST>(op, tpb, fuse, B, st);
+        case 16: return batch_dispatch<16, ST>(op, tpb, fuse, B, st);
+    }
+    return cudaErrorInvalidValue;
 }
 
 // every launch of one storage format (amr_kernels_<format>.cu instantiates it)

@@ -47,8 +47,34 @@ struct AmrLaunch {
     double u0 = 0.0, kf = 0.0;
 };
 
+// One member of a batched launch: the fields of AmrLaunch a per-block stage reads, and the first
+// CTA of the member in the batched grid (members follow each other; a member gets as many CTAs as
+// its single launch would).
+struct AmrItem {
+    const void* in;
+    void* out;
+    const void* aux;
+    void* out2;
+    const int *t0, *t1, *t2, *t3, *nbt, *list, *nlim;
+    int cgx, n, l1gx, n1;
+    float omega, scale;
+    int begin, pad;
+};
+constexpr int kAmrBatchMax = 48;
+// Many solves in one launch per stage: OP_STEP_L0/L1/L2, OP_PREP, OP_FILL_L1/L2, OP_RESTRICT over up
+// to kAmrBatchMax solves of the same block edge, storage and step threads.  Passed by value in kernel
+// parameter space.
+struct AmrBatch {
+    int count = 0, total = 0;  // members, CTAs
+    AmrItem it[kAmrBatchMax];
+};
+
 // storage: 0 FP32, 1 shifted FP16, 2 shifted BF16 (jp_storage)
 cudaError_t amr_launch(int storage, int mb, int op, const AmrLaunch& L);
+// op as in AmrLaunch; tpb: threads per CTA of the steps (0: default); fuse: the fine steps restrict
+// into out2 (every member the same)
+cudaError_t amr_batch_launch(int storage, int mb, int op, int tpb, bool fuse, const AmrBatch& B, cudaStream_t st);
+template <class ST> cudaError_t amr_batch_launch_st(int mb, int op, int tpb, bool fuse, const AmrBatch& B, cudaStream_t st);
 template <class ST> cudaError_t amr_launch_st(int mb, int op, const AmrLaunch& L);
 size_t storage_elem(int storage);  // bytes per stored population
 int shell_cells(int mb);

@@ -5,6 +5,8 @@ namespace jp {
 namespace amr {
 
 template cudaError_t amr_launch_st<StF16>(int mb, int op, const AmrLaunch& L);
+template cudaError_t amr_batch_launch_st<StF16>(int mb, int op, int tpb, bool fuse, const AmrBatch& B,
+                                                 cudaStream_t st);
 
 }  // namespace amr
 }  // namespace jp

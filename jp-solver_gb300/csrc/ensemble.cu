@@ -106,7 +106,6 @@ void jp_ensemble_destroy(jp_ensemble* e) {
 
 jp_status jp_ensemble_add(jp_ensemble* e, jp_solver* s) {
     if (!e || !s) return fail(JP_ERR_INVALID, "null argument");
-    if (s->kind != JP_UNIFORM) return fail(JP_ERR_INVALID, "ensembles hold uniform solvers");
     if (s->device != e->device) return fail(JP_ERR_INVALID, "solver on device %d, ensemble on %d", s->device, e->device);
     if (std::find(e->members.begin(), e->members.end(), s) != e->members.end()) return JP_OK;
     e->members.push_back(s);
@@ -129,9 +128,31 @@ jp_status jp_ensemble_step(jp_ensemble* e, int64_t nsteps) {
         ECK(cudaEventRecord(m->ev1, m->stream), "event");
         ECK(cudaStreamWaitEvent(e->stream, m->ev1, 0), "wait");
     }
+    // uniform members in batched stream-collide launches; AMR members in batched coarse steps, one
+    // group per compatible launch shape (block edge, storage, step threads, skip flags)
+    std::vector<jp_solver*> uni;
+    std::vector<std::vector<jp_solver*>> amr;
+    for (jp_solver* m : e->members) {
+        if (m->kind == JP_UNIFORM) {
+            uni.push_back(m);
+            continue;
+        }
+        bool placed = false;
+        for (auto& g : amr)
+            if (amr_batch_compatible(g[0], m)) {
+                g.push_back(m);
+                placed = true;
+                break;
+            }
+        if (!placed) amr.push_back({m});
+    }
     for (int64_t i = 0; i < nsteps; ++i) {
-        jp_status st = batched_step(e->members, e->stream);
+        jp_status st = batched_step(uni, e->stream);
         if (st != JP_OK) return st;
+        for (auto& g : amr) {
+            st = amr_batch_step(g, e->stream);
+            if (st != JP_OK) return st;
+        }
     }
     ECK(cudaEventRecord(e->done, e->stream), "event");
     for (jp_solver* m : e->members) ECK(cudaStreamWaitEvent(m->stream, e->done, 0), "wait");  // before later work

@@ -598,6 +598,155 @@ static jp_status base_step(jp_solver* s) {
     return launch(s, OP_RESTRICT, R);
 }
 
+// One coarse step of many AMR solves with one launch per stage over all of them (base_step's
+// sequence, each launch an AmrBatch of up to kAmrBatchMax members).  The members share block edge,
+// storage, step threads and skip flags (amr_batch_compatible).
+jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
+    if (ms.empty()) return JP_OK;
+    const AmrState* a0 = ms[0]->amr;
+    const int flags = ms[0]->cfg.flags;
+    const bool skip_prep = flags & JP_FLAG_SKIP_PREP, skip_restrict = flags & JP_FLAG_SKIP_RESTRICT;
+    const bool fuse = !skip_restrict && can_fuse_restrict(a0->MB);
+    // one stage over all members: fill() sets a member's item and returns its CTAs (0: nothing)
+    auto run = [&](int op, bool fused, auto fill) -> jp_status {
+        for (size_t i0 = 0; i0 < ms.size(); i0 += kAmrBatchMax) {
+            AmrBatch B;
+            for (size_t i = i0; i < ms.size() && i < i0 + kAmrBatchMax; ++i) {
+                AmrItem& it = B.it[B.count];
+                std::memset(&it, 0, sizeof it);
+                const int n = fill(ms[i]->amr, it);
+                if (n <= 0) continue;
+                it.begin = B.total;
+                B.total += n;
+                ++B.count;
+            }
+            cudaError_t e = amr_batch_launch(a0->storage, a0->MB, op, a0->tpb, fused, B, st);
+            if (e != cudaSuccess) return cuda_fail(e, "batched AMR launch");
+        }
+        return JP_OK;
+    };
+    TRY(run(OP_STEP_L0, false, [](AmrState* a, AmrItem& it) {
+        it.in = a->c0a;
+        it.out = a->c0b;
+        it.cgx = a->cgx;
+        it.omega = a->om0;
+        return a->cnb0;
+    }));
+    for (jp_solver* m : ms) std::swap(m->amr->c0a, m->amr->c0b);
+    if (!skip_prep) {
+        TRY(run(OP_PREP, false, [](AmrState* a, AmrItem& it) {
+            it.in = a->c0a;
+            it.out = a->prep0;
+            it.list = a->skin0;
+            it.scale = float(a->nqs01);
+            it.nlim = a->step_cnt + SC_SKIN0;
+            return a->cnb0;
+        }));
+        TRY(run(OP_FILL_L1, false, [](AmrState* a, AmrItem& it) {
+            it.in = a->prep0;
+            it.out = a->gh1;
+            it.t0 = a->pcb;
+            it.t1 = a->oct;
+            it.nbt = a->nb1;
+            it.cgx = a->cgx;
+            it.n = a->N;
+            it.nlim = a->step_cnt + SC_NF1;
+            return a->cap1;
+        }));
+    }
+    for (int s1 = 0; s1 < 2; ++s1) {
+        if (!skip_prep) {
+            TRY(run(OP_PREP, false, [](AmrState* a, AmrItem& it) {
+                it.in = a->f1a;
+                it.out = a->prep1;
+                it.list = a->skin1;
+                it.scale = float(a->nqs12);
+                it.nlim = a->step_cnt + SC_SKIN1;
+                return a->cap1;
+            }));
+            TRY(run(OP_FILL_L2, false, [](AmrState* a, AmrItem& it) {
+                it.in = a->prep1;
+                it.out = a->gh2;
+                it.t0 = a->l2pl1;
+                it.t1 = a->l2oct;
+                it.t2 = a->f1pos;
+                it.t3 = a->l1grid;
+                it.nbt = a->nb2;
+                it.l1gx = a->l1gx;
+                it.n1 = a->N1;
+                it.nlim = a->step_cnt + SC_NF2;
+                return a->cap2;
+            }));
+        }
+        for (int s2 = 0; s2 < 2; ++s2) {
+            const bool f = s2 == 1 && fuse;  // last level-2 substep restricts itself into level 1
+            TRY(run(OP_STEP_L2, f, [f](AmrState* a, AmrItem& it) {
+                it.in = a->f2a;
+                it.out = a->f2b;
+                it.aux = a->gh2;
+                it.nbt = a->nb2;
+                it.t0 = a->l2pl1;
+                it.t1 = a->l2oct;
+                it.omega = a->om2;
+                it.nlim = a->step_cnt + SC_NF2;
+                if (f) {
+                    it.out2 = a->f1a;
+                    it.scale = float(a->nqi21);
+                }
+                return a->cap2;
+            }));
+            for (jp_solver* m : ms) std::swap(m->amr->f2a, m->amr->f2b);
+        }
+        if (!skip_restrict && !fuse) {
+            TRY(run(OP_RESTRICT, false, [](AmrState* a, AmrItem& it) {
+                it.out = a->f1a;
+                it.in = a->f2a;
+                it.list = a->rl1;
+                it.t0 = a->fof1;
+                it.scale = float(a->nqi21);
+                it.nlim = a->step_cnt + SC_NREF1;
+                return (a->cap2 + 7) / 8;
+            }));
+        }
+        const bool f = s1 == 1 && fuse;  // last level-1 substep restricts itself into the coarse level
+        TRY(run(OP_STEP_L1, f, [f](AmrState* a, AmrItem& it) {
+            it.in = a->f1a;
+            it.out = a->f1b;
+            it.aux = a->gh1;
+            it.nbt = a->nb1;
+            it.t0 = a->pcb;
+            it.t1 = a->oct;
+            it.omega = a->om1;
+            it.nlim = a->step_cnt + SC_NF1;
+            if (f) {
+                it.out2 = a->c0a;
+                it.scale = float(a->nqi10);
+            }
+            return a->cap1;
+        }));
+        for (jp_solver* m : ms) std::swap(m->amr->f1a, m->amr->f1b);
+    }
+    if (!skip_restrict && !fuse) {
+        TRY(run(OP_RESTRICT, false, [](AmrState* a, AmrItem& it) {
+            it.out = a->c0a;
+            it.in = a->f1a;
+            it.list = a->rl0;
+            it.t0 = a->fof0;
+            it.scale = float(a->nqi10);
+            it.nlim = a->step_cnt + SC_NREF0;
+            return (a->cap1 + 7) / 8;
+        }));
+    }
+    for (jp_solver* m : ms) ++m->step_count;
+    return JP_OK;
+}
+
+bool amr_batch_compatible(const jp_solver* a, const jp_solver* b) {
+    const int skip = JP_FLAG_SKIP_PREP | JP_FLAG_SKIP_RESTRICT;
+    return a->amr->MB == b->amr->MB && a->amr->storage == b->amr->storage && a->amr->tpb == b->amr->tpb &&
+           (a->cfg.flags & skip) == (b->cfg.flags & skip);
+}
+
 // base_step replayed from a captured graph (captured on first use for each parity combination)
 static jp_status graph_step(jp_solver* s) {
     AmrState* a = s->amr;
