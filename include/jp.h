@@ -263,19 +263,20 @@ jp_status jp_ensemble_step(jp_ensemble* e, int64_t nsteps);
 /* A server runs whole Taylor-Green solves (the `uniform` / `amr` programs' runs) for a stream of
  * requests with continuous batching: requests wait in a queue until their HBM estimate fits the
  * pool budget and a slot is free, are admitted between ticks while others run, advance together
- * (uniform solves in batched launches issued by jp_server_tick, AMR solves concurrently on worker
- * threads, each on its own stream), and leave a result with their diagnostics summary and timestamps
- * when they finish.  Device memory of served solves comes from one stream-ordered pool, so solves
- * come and go without synchronising the device.  A process that serves many AMR solves at once
- * should set CUDA_DEVICE_MAX_CONNECTIONS (e.g. 32) before its first CUDA call, so that their
- * streams do not share the default 8 hardware queues. */
+ * in batched launches issued by jp_server_tick (uniform solves: one stream-collide launch over all
+ * cubes; AMR solves: one launch per stage of the coarse step over the blocks of all of them, on a
+ * second stream), and leave a result with their diagnostics summary and timestamps when they
+ * finish.  Diagnostics are launched in the batch and read back one tick late.  AMR creation and
+ * regrids, which need read-backs, run on worker threads on each solve's own stream while the batch
+ * goes on without that solve.  Device memory of served solves comes from one stream-ordered pool,
+ * so solves come and go without synchronising the device. */
 typedef struct jp_server jp_server;
 typedef struct jp_server_config {
     int32_t device;
     int32_t max_active;      /* slots; 0 = unlimited */
     double pool_gb;          /* HBM budget for admitted solves, GiB (0 = 75% of free memory) */
     int32_t tick_steps;      /* lattice steps the uniform solves advance per tick (default 64) */
-    int32_t workers;         /* host threads running AMR solves, one solve each (0 = one per core, 4..32) */
+    int32_t workers;         /* host threads that create and regrid AMR solves (0 = one per core, 4..32) */
     int32_t reserved[6];
 } jp_server_config;
 typedef struct jp_request {

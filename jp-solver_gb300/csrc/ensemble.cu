@@ -1,8 +1,9 @@
 // Ensembles and the solve server: many independent Taylor-Green solves on one GPU.
 //
-// No counterpart in the reference, which runs one solve per process.  An ensemble batches the
-// stream-collide of many uniform cubes into one launch per storage format per lattice step
-// (k_stream_collide takes up to kMaxBatch cubes of any sizes).  The server adds continuous
+// No counterpart in the reference, which runs one solve per process.  An ensemble batches the steps
+// of many solves: uniform cubes in one stream-collide launch per storage format per lattice step
+// (k_stream_collide takes up to kMaxBatch cubes of any sizes), AMR solves in one launch per stage of
+// the coarse step over the blocks of all of them (amr_batch_step).  The server adds continuous
 // batching on top: requests wait until their HBM estimate fits the pool and a slot is free, join
 // between ticks while other solves run, advance together, and leave with a result.  Each solve does
 // exactly what the `uniform` / `amr` programs do for it (same steps, diagnostic cadence, regrid
@@ -19,6 +20,7 @@
 #include <thread>
 #include <vector>
 
+#include "amr_kernels.h"
 #include "jp.h"
 #include "kernels.h"
 #include "solver.h"
@@ -172,9 +174,15 @@ struct Job {
     jp_info info{};
     long long step = 0, steps = 0, diagK = 1, adapt = 0;
     bool dynamic = false, need_diag = true;
-    int inflight = 0;       // diagnostics launched and not yet read back (uniform)
+    int inflight = 0;       // diagnostics launched and not yet read back
     bool admitted = false;  // holds `bytes` of the pool budget
     bool requeue = false;   // an AMR worker could not get the memory: back to the queue head
+    // AMR: `step` is the program loop's s_; events (regrid, diagnostic) of step s_ are handled once
+    // (events_done) before the solve takes its next sstep coarse steps in the batch.  A worker
+    // creates the solve (task 1) or regrids it (task 2, plus the diagnostic of that step when dg).
+    long long sstep = 1;
+    bool events_done = false, dg = false;
+    int task = 0;
     jp_status error = JP_OK;
     int samples = 0;
     double E0 = -1, prevE = 1e30, Elast = 0, peak = -1, peak_ts = -1, mass0 = -1, drift = 0;
@@ -231,8 +239,16 @@ struct jp_server {
         std::vector<std::pair<Job*, long long>> entries;  // job, step the values belong to
     } diag[2];
     int diag_cur = 0;
-    // AMR solves run whole on worker threads, each on its own stream; the tick thread admits and
-    // retires them.  amr_todo and amr_fin are guarded by mu.
+    // AMR solves advance in batched launches (amr_batch_step: one launch per stage over all of them)
+    // on amr_stream, issued by the tick; their diagnostics are launched there too and read back one
+    // tick late.  Creation and regrids, which need read-backs, run on worker threads on each solve's
+    // own stream while the batch goes on without that solve.  amr_todo and amr_fin are guarded by mu.
+    cudaStream_t amr_stream = nullptr;
+    std::vector<Job*> amr_active;      // in the batch (tick thread only)
+    struct AmrDiag {
+        cudaEvent_t done = nullptr;
+        std::vector<std::pair<Job*, long long>> entries;  // job, step; values in the solver's host slot
+    } adiag[2];
     std::vector<std::thread> workers;
     std::mutex mu;
     std::condition_variable cv_todo, cv_fin;
@@ -310,70 +326,50 @@ long long next_event(const Job* j) {
     return std::min(j->steps, (j->step / j->diagK + 1) * j->diagK);
 }
 
-// One AMR solve from creation to destruction, on the calling worker thread: the loop of the `amr`
-// program (regrid every `adapt` coarse steps before the diagnostic of the same step, a diagnostic
-// every steps/160, two coarse steps per iteration with graph replay as the reference's graph holds
-// two), with the steps between two events issued in one call.
-void run_amr(jp_server* sv, Job* j) {
+// A worker's part of an AMR solve, on the solve's own stream: creation with the initial build and
+// the diagnostic of step 0 (task 1), or a regrid and, when due at the same step, the diagnostic
+// (task 2).  Everything else happens in the tick's batched launches.
+void amr_task(jp_server* sv, Job* j) {
     if (cudaSetDevice(sv->cfg.device) != cudaSuccess) {
         j->error = JP_ERR_CUDA;
         return;
     }
-    auto t = clk::now();
-    jp_status st = create_solver(&j->req.cfg, sv->pool, &j->s);
-    sv->add(&jp_server_stats::create_s, seconds_since(t));
-    if (st != JP_OK) {
-        j->s = nullptr;
-        if (st == JP_ERR_NOMEM) j->requeue = true;  // the estimate was optimistic: wait for memory
-        else j->error = st;
-        return;
+    jp_status st = JP_OK;
+    if (j->task == 1) {
+        auto t = clk::now();
+        st = create_solver(&j->req.cfg, sv->pool, &j->s);
+        if (st == JP_OK) st = amr_prepare_diag(j->s);
+        sv->add(&jp_server_stats::create_s, seconds_since(t));
+        if (st != JP_OK) {
+            if (j->s) jp_destroy(j->s);
+            j->s = nullptr;
+            if (st == JP_ERR_NOMEM) j->requeue = true;  // the estimate was optimistic: wait for memory
+            else j->error = st;
+            return;
+        }
+        jp_get_info(j->s, &j->info);
+        j->steps = j->info.steps;
+        j->diagK = j->req.diag_every > 0 ? j->req.diag_every : std::max(1LL, j->steps / 160);
+        j->dynamic = j->req.cfg.l1_mode == JP_REFINE_SENSOR || j->req.cfg.l2_mode == JP_REFINE_SENSOR;
+        j->adapt = j->req.cfg.adapt_every > 0 ? j->req.cfg.adapt_every : 100;
+        j->sstep = (j->req.cfg.flags & JP_FLAG_GRAPH) ? 2 : 1;  // the program steps two at a time then
+        j->step = 0;
+        j->dg = true;  // step 0 has a diagnostic and no regrid
+    } else {
+        auto t = clk::now();
+        st = jp_regrid(j->s);
+        sv->add(&jp_server_stats::regrid_s, seconds_since(t), &jp_server_stats::regrids);
     }
-    jp_get_info(j->s, &j->info);
-    j->steps = j->info.steps;
-    j->diagK = j->req.diag_every > 0 ? j->req.diag_every : std::max(1LL, j->steps / 160);
-    j->dynamic = j->req.cfg.l1_mode == JP_REFINE_SENSOR || j->req.cfg.l2_mode == JP_REFINE_SENSOR;
-    j->adapt = j->req.cfg.adapt_every > 0 ? j->req.cfg.adapt_every : 100;
-    const long long sstep = (j->req.cfg.flags & JP_FLAG_GRAPH) ? 2 : 1;
-    long long pending = 0;
-    for (long long s_ = 0; s_ <= j->steps && st == JP_OK; s_ += sstep) {
-        if (sv->stop.load(std::memory_order_relaxed)) {
-            st = fail(JP_ERR_STATE, "server shut down during the solve");
-            break;
-        }
-        const bool rg = j->dynamic && s_ > 0 && s_ % j->adapt == 0, dg = s_ % j->diagK == 0;
-        if ((rg || dg) && pending) {
-            t = clk::now();
-            st = jp_step(j->s, pending);
-            sv->add(&jp_server_stats::step_s, seconds_since(t), &jp_server_stats::coarse_steps, pending);
-            pending = 0;
-        }
-        if (st == JP_OK && rg) {
-            t = clk::now();
-            st = jp_regrid(j->s);
-            sv->add(&jp_server_stats::regrid_s, seconds_since(t), &jp_server_stats::regrids);
-        }
-        if (st == JP_OK && dg) {
-            double d[3];
-            t = clk::now();
-            st = jp_diag(j->s, d);
-            sv->add(&jp_server_stats::diag_s, seconds_since(t), &jp_server_stats::diags);
-            if (st == JP_OK) {
-                j->step = s_;
-                record(j, d, s_);
-            }
-        }
-        if (s_ < j->steps) pending += sstep;
-    }
-    if (st == JP_OK && pending) {
-        t = clk::now();
-        st = jp_step(j->s, pending);
-        sv->add(&jp_server_stats::step_s, seconds_since(t), &jp_server_stats::coarse_steps, pending);
+    if (st == JP_OK && j->dg) {  // into slot 2 of the solver's pinned read-back area (slots 0, 1: tick)
+        auto t = clk::now();
+        double* d = j->s->diag_host + 6;
+        st = amr_diag_async(j->s, j->s->stream, d);
+        if (st == JP_OK && wait_stream(j->s) != cudaSuccess) st = fail(JP_ERR_CUDA, "diagnostics");
+        sv->add(&jp_server_stats::diag_s, seconds_since(t), &jp_server_stats::diags);
+        if (st == JP_OK) record(j, d, j->step);
     }
     j->error = st;
-    t = clk::now();
-    jp_destroy(j->s);  // pooled memory returns in stream order behind the last step
-    sv->add(&jp_server_stats::destroy_s, seconds_since(t));
-    j->s = nullptr;
+    j->events_done = true;
 }
 
 void worker_main(jp_server* sv) {
@@ -386,13 +382,22 @@ void worker_main(jp_server* sv) {
             j = sv->amr_todo.front();
             sv->amr_todo.pop_front();
         }
-        run_amr(sv, j);
+        amr_task(sv, j);
         {
             std::lock_guard<std::mutex> lk(sv->mu);
             sv->amr_fin.push_back(j);
         }
         sv->cv_fin.notify_all();
     }
+}
+
+void to_worker(jp_server* sv, Job* j, int task) {
+    j->task = task;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->amr_todo.push_back(j);
+    }
+    sv->cv_todo.notify_one();
 }
 
 }  // namespace
@@ -410,6 +415,9 @@ jp_status jp_server_create(const jp_server_config* cfg, jp_server** out) {
     if (sv->cfg.workers <= 0) sv->cfg.workers = (int)std::min(32u, std::max(4u, std::thread::hardware_concurrency()));
     sv->t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->amr_stream, cudaStreamNonBlocking);
+    for (auto& d : sv->adiag)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d.done, cudaEventDisableTiming);
     size_t fr = 0, tot = 0;
     if (e == cudaSuccess) e = cudaMemGetInfo(&fr, &tot);
     if (e == cudaSuccess) {
@@ -442,14 +450,28 @@ void jp_server_destroy(jp_server* sv) {
         sv->stop.store(true);
     }
     sv->cv_todo.notify_all();
-    for (std::thread& t : sv->workers) t.join();  // running solves stop at their next iteration
+    for (std::thread& t : sv->workers) t.join();  // a running task ends first
     if (sv->stream) cudaStreamSynchronize(sv->stream);
+    if (sv->amr_stream) cudaStreamSynchronize(sv->amr_stream);
     for (Job* j : sv->active) {
         if (j->s) jp_destroy(j->s);
         delete j;
     }
-    for (Job* j : sv->amr_todo) delete j;
-    for (Job* j : sv->amr_fin) delete j;
+    for (Job* j : sv->amr_active) {
+        if (j->s) jp_destroy(j->s);
+        delete j;
+    }
+    for (Job* j : sv->amr_todo) {
+        if (j->s) jp_destroy(j->s);
+        delete j;
+    }
+    for (Job* j : sv->amr_fin) {
+        if (j->s) jp_destroy(j->s);
+        delete j;
+    }
+    for (auto& d : sv->adiag)
+        if (d.done) cudaEventDestroy(d.done);
+    if (sv->amr_stream) cudaStreamDestroy(sv->amr_stream);
     for (Job* j : sv->queue) delete j;
     for (auto& b : sv->diag) {
         if (b.dev) cudaFree(b.dev);
@@ -516,15 +538,20 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         fin.swap(sv->amr_fin);
     }
     for (Job* j : fin) {
-        --sv->amr_live;
         if (j->requeue) {
+            --sv->amr_live;
             j->requeue = false;
             j->admitted = false;
             sv->used -= j->bytes;
             sv->queue.push_front(j);
             requeued.push_back(j);
-        } else {
+        } else if (j->error != JP_OK) {
+            --sv->amr_live;
             finish(sv, j, j->error);
+        } else {  // back into the batch, after the worker's work on the solve's own stream
+            ECK(cudaEventRecord(j->s->ev1, j->s->stream), "event");
+            ECK(cudaStreamWaitEvent(sv->amr_stream, j->s->ev1, 0), "wait");
+            sv->amr_active.push_back(j);
         }
     }
     // 2. admission in submission order while the budget and the slots allow.  An AMR solve also
@@ -534,7 +561,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         if (sv->cfg.max_active > 0 && (int)sv->active.size() + sv->amr_live >= sv->cfg.max_active) break;
         Job* j = *it;
         if (std::find(requeued.begin(), requeued.end(), j) != requeued.end()) break;  // no memory: next tick
-        if (j->req.cfg.kind == JP_AMR && sv->amr_live >= sv->cfg.workers) {
+        if (j->req.cfg.kind == JP_AMR && sv->amr_live >= 4 * amr::kAmrBatchMax) {  // enough to fill the batch
             ++it;
             continue;
         }
@@ -545,11 +572,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             j->admitted = true;
             sv->used += j->bytes;
             ++sv->amr_live;
-            {
-                std::lock_guard<std::mutex> lk(sv->mu);
-                sv->amr_todo.push_back(j);
-            }
-            sv->cv_todo.notify_one();
+            to_worker(sv, j, 1);
             continue;
         }
         const auto tc = clk::now();
@@ -612,6 +635,48 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         ECK(cudaEventRecord(cur.done, sv->stream), "diag event");
         sv->add(&jp_server_stats::diag_s, seconds_since(td), &jp_server_stats::diags, (int64_t)cur.entries.size());
     }
+    // 3b. AMR events due at each batched solve's current step: a regrid sends the solve to a worker
+    //     (its stream waits for the batch so far; a diagnostic of the same step goes with it); a
+    //     diagnostic alone is launched here on the batch's stream into this tick's read-back slot.
+    //     A solve with a diagnostic still in flight waits a tick before a regrid, so that its samples
+    //     are recorded in order.
+    auto& acur = sv->adiag[sv->diag_cur];
+    acur.entries.clear();
+    for (size_t i = 0; i < sv->amr_active.size();) {
+        Job* j = sv->amr_active[i];
+        if (j->events_done || j->step > j->steps || j->error != JP_OK) {
+            ++i;
+            continue;
+        }
+        const bool rg = j->dynamic && j->step > 0 && j->step % j->adapt == 0, dg = j->step % j->diagK == 0;
+        if (rg) {
+            if (j->inflight) {
+                ++i;
+                continue;
+            }
+            ECK(cudaEventRecord(j->s->ev0, sv->amr_stream), "event");
+            ECK(cudaStreamWaitEvent(j->s->stream, j->s->ev0, 0), "wait");
+            j->dg = dg;
+            sv->amr_active.erase(sv->amr_active.begin() + i);
+            to_worker(sv, j, 2);
+            continue;
+        }
+        if (dg) {
+            const auto ta = clk::now();
+            jp_status st = amr_diag_async(j->s, sv->amr_stream, j->s->diag_host + 3 * sv->diag_cur);
+            sv->add(&jp_server_stats::diag_s, seconds_since(ta), &jp_server_stats::diags);
+            if (st != JP_OK) {
+                j->error = st;
+                ++i;
+                continue;
+            }
+            acur.entries.push_back({j, j->step});
+            ++j->inflight;
+        }
+        j->events_done = true;
+        ++i;
+    }
+    if (!acur.entries.empty()) ECK(cudaEventRecord(acur.done, sv->amr_stream), "diag event");
     // 4. advance the uniform solves in batched launches (behind this tick's diagnostics)
     std::vector<std::pair<Job*, long long>> uni;
     long long kmax = 0;
@@ -636,6 +701,38 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         p.first->step += p.second;
         if (p.first->step % p.first->diagK == 0) p.first->need_diag = true;  // at the new step, next tick
     }
+    // 4b. advance the batched AMR solves by their sstep coarse steps, one launch per stage per group
+    //     of solves that share a launch shape
+    std::vector<std::vector<Job*>> groups;
+    for (Job* j : sv->amr_active) {
+        if (!j->events_done || j->step >= j->steps || j->error != JP_OK) continue;
+        bool placed = false;
+        for (auto& g : groups)
+            if (amr_batch_compatible(g[0]->s, j->s)) {
+                g.push_back(j);
+                placed = true;
+                break;
+            }
+        if (!placed) groups.push_back({j});
+    }
+    const auto tab = clk::now();
+    long long amr_moved = 0;
+    for (auto& g : groups) {
+        for (long long t = 0; t < 2; ++t) {
+            std::vector<jp_solver*> ms;
+            for (Job* j : g)
+                if (j->sstep > t) ms.push_back(j->s);
+            if (ms.empty()) break;
+            jp_status st = amr_batch_step(ms, sv->amr_stream);
+            if (st != JP_OK) return st;
+            amr_moved += (long long)ms.size();
+        }
+        for (Job* j : g) {
+            j->step += j->sstep;
+            j->events_done = false;
+        }
+    }
+    if (amr_moved) sv->add(&jp_server_stats::step_s, seconds_since(tab), &jp_server_stats::coarse_steps, amr_moved);
     // 5. the previous tick's diagnostics (the GPU meanwhile works on this tick's launches)
     auto& prev = sv->diag[sv->diag_cur ^ 1];
     if (!prev.entries.empty()) {
@@ -647,6 +744,33 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         }
         prev.entries.clear();
         sv->add(&jp_server_stats::diag_s, seconds_since(tw));
+    }
+    // 5b. the previous tick's AMR diagnostics
+    auto& aprev = sv->adiag[sv->diag_cur ^ 1];
+    if (!aprev.entries.empty()) {
+        const auto tw = clk::now();
+        ECK(cudaEventSynchronize(aprev.done), "diag");
+        for (auto& e : aprev.entries) {
+            record(e.first, e.first->s->diag_host + 3 * (sv->diag_cur ^ 1), e.second);
+            --e.first->inflight;
+        }
+        aprev.entries.clear();
+        sv->add(&jp_server_stats::diag_s, seconds_since(tw));
+    }
+    // retire batched AMR solves that take no more steps and have nothing in flight; their frees are
+    // ordered after the batch's last work on them
+    for (size_t i = 0; i < sv->amr_active.size();) {
+        Job* j = sv->amr_active[i];
+        const bool over = j->step > j->steps || (j->step == j->steps && j->events_done) || j->error != JP_OK;
+        if (over && j->inflight == 0) {
+            ECK(cudaEventRecord(j->s->ev0, sv->amr_stream), "event");
+            ECK(cudaStreamWaitEvent(j->s->stream, j->s->ev0, 0), "wait");
+            sv->amr_active.erase(sv->amr_active.begin() + i);
+            --sv->amr_live;
+            finish(sv, j, j->error);
+        } else {
+            ++i;
+        }
     }
     sv->diag_cur ^= 1;
     // retire finished uniform solves: all steps issued, every diagnostic read back.  Their last use
@@ -663,8 +787,8 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             ++i;
         }
     }
-    // 6. nothing to launch here while AMR solves run: wait briefly for one of them to finish
-    if (uni.empty() && sv->amr_live > 0) {
+    // 6. nothing launched while AMR solves are with the workers: wait briefly for one of them
+    if (uni.empty() && !amr_moved && sv->amr_live > 0) {
         std::unique_lock<std::mutex> lk(sv->mu);
         sv->cv_fin.wait_for(lk, std::chrono::milliseconds(1), [sv] { return !sv->amr_fin.empty(); });
     }

@@ -93,6 +93,8 @@ jp_status amr_set_step_tpb(jp_solver* s, int tpb);  // threads per CTA of the le
 // one coarse step of many AMR solvers, one launch per stage over all of them, on `st`
 jp_status amr_batch_step(const std::vector<jp_solver*>& members, cudaStream_t st);
 bool amr_batch_compatible(const jp_solver* a, const jp_solver* b);
+jp_status amr_prepare_diag(jp_solver* s);
+jp_status amr_diag_async(jp_solver* s, cudaStream_t st, double* host_out);
 jp_status amr_get_counts(jp_solver* s, jp_amr_counts* out);
 jp_status amr_get_table(jp_solver* s, int table, int32_t* host, int64_t capacity, int64_t* count);
 jp_status amr_get_sensor(jp_solver* s, int level, float* host, int64_t capacity, int64_t* count);

@@ -922,10 +922,26 @@ jp_status amr_regrid(jp_solver* s) {
     return JP_OK;
 }
 
-static jp_status composite(jp_solver* s) {
+static jp_status composite(jp_solver* s, cudaStream_t st = nullptr) {
     AmrState* a = s->amr;
     if (!a->field) ACK(dev_alloc(s, (void**)&a->field, sizeof(float) * 4 * (size_t)a->N2 * a->N2 * a->N2), "cudaMalloc composite");
     AmrLaunch L;
+    if (st) {  // on another stream: the launch below overrides the solver's own
+        L.in = a->c0a;
+        L.aux = a->f1a;
+        L.aux2 = a->f2a;
+        L.out = a->field;
+        L.t0 = a->ref1;
+        L.t1 = a->fof1;
+        L.t2 = a->l1grid;
+        L.cgx = a->cgx;
+        L.l1gx = a->l1gx;
+        L.n2 = a->N2;
+        L.st = st;
+        cudaError_t e = amr_launch(a->storage, a->MB, OP_COMPOSITE, L);
+        if (e != cudaSuccess) return cuda_fail(e, "AMR kernel launch");
+        return JP_OK;
+    }
     L.in = a->c0a;
     L.aux = a->f1a;
     L.aux2 = a->f2a;
@@ -944,6 +960,25 @@ jp_status amr_get_output_fields(jp_solver* s, float* q, float* speed, float* vel
     if (count != (int64_t)a->N2 * a->N2 * a->N2) return fail(JP_ERR_INVALID, "count %lld != (4 N0)^3", (long long)count);
     TRY(composite(s));
     return output_fields_from(s, a->field, false, false, a->N2, q, speed, vel);
+}
+
+// The composite field the diagnostics need, allocated ahead of an amr_diag_async on another stream.
+jp_status amr_prepare_diag(jp_solver* s) {
+    AmrState* a = s->amr;
+    if (!a->field) ACK(dev_alloc(s, (void**)&a->field, sizeof(float) * 4 * (size_t)a->N2 * a->N2 * a->N2), "cudaMalloc composite");
+    ACK(wait_stream(s), "composite field");
+    return JP_OK;
+}
+
+// Diagnostics of the current state launched on `st` (which must be ordered after the solver's last
+// step) and copied into host_out (pinned, 3 doubles) when the stream gets there.
+jp_status amr_diag_async(jp_solver* s, cudaStream_t st, double* host_out) {
+    AmrState* a = s->amr;
+    if (!a->field) return fail(JP_ERR_STATE, "amr_diag_async: composite field not prepared");
+    TRY(composite(s, st));
+    ACK(launch_diag_field(false, false, a->field, a->N2, s->partials, s->diag_dev, st), "diag");
+    ACK(cudaMemcpyAsync(host_out, s->diag_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, st), "diag D2H");
+    return JP_OK;
 }
 
 jp_status amr_diag(jp_solver* s, double out[3]) {

@@ -93,13 +93,16 @@ def test_server_result_same_alone_and_in_mix():
     assert all(r["status"] == 0 for r in mixed.values())
 
 
-def test_server_one_worker_runs_amr_solves_in_turn():
-    # with one worker the AMR solves queue for it while the uniform ones pass them
+def test_server_one_worker_gives_the_same_results():
+    # one worker thread (creations and regrids one at a time) changes nothing but the timing: the AMR
+    # solves still advance together in the batched launches, with the same results
     reqs = [dict(MIX[2], rid=40), dict(MIX[4], rid=41), dict(R0, rid=42)]
-    res, _ = run_server(reqs, tick_steps=16, workers=1)
-    assert all(r["status"] == 0 for r in res.values())
-    a, b = res[40], res[41]
-    assert b["t_start"] >= a["t_end"] - 1e-3 or a["t_start"] >= b["t_end"] - 1e-3
+    one, _ = run_server(reqs, tick_steps=16, workers=1)
+    many, _ = run_server(reqs, tick_steps=16)
+    for rid in (40, 41, 42):
+        assert one[rid]["status"] == 0
+        for k in ("samples", "peak_tstar", "peak_enstrophy", "energy_ratio", "mass_drift", "valid"):
+            assert one[rid][k] == many[rid][k], (rid, k)
 
 
 def test_server_amr_result_matches_program_loop():
