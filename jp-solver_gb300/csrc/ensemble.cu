@@ -723,7 +723,9 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             for (Job* j : g)
                 if (j->sstep > t) ms.push_back(j->s);
             if (ms.empty()) break;
-            jp_status st = amr_batch_step(ms, sv->amr_stream);
+            // a group of one with graph replay replays its captured step instead (one launch)
+            const bool alone = ms.size() == 1 && (ms[0]->cfg.flags & JP_FLAG_GRAPH);
+            jp_status st = alone ? amr_graph_step_on(ms[0], sv->amr_stream) : amr_batch_step(ms, sv->amr_stream);
             if (st != JP_OK) return st;
             amr_moved += (long long)ms.size();
         }

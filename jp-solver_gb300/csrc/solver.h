@@ -94,6 +94,7 @@ jp_status amr_set_step_tpb(jp_solver* s, int tpb);  // threads per CTA of the le
 jp_status amr_batch_step(const std::vector<jp_solver*>& members, cudaStream_t st);
 bool amr_batch_compatible(const jp_solver* a, const jp_solver* b);
 jp_status amr_prepare_diag(jp_solver* s);
+jp_status amr_graph_step_on(jp_solver* s, cudaStream_t st);
 jp_status amr_diag_async(jp_solver* s, cudaStream_t st, double* host_out);
 jp_status amr_get_counts(jp_solver* s, jp_amr_counts* out);
 jp_status amr_get_table(jp_solver* s, int table, int32_t* host, int64_t capacity, int64_t* count);

@@ -748,7 +748,7 @@ bool amr_batch_compatible(const jp_solver* a, const jp_solver* b) {
 }
 
 // base_step replayed from a captured graph (captured on first use for each parity combination)
-static jp_status graph_step(jp_solver* s) {
+static jp_status graph_step(jp_solver* s, cudaStream_t on = nullptr) {
     AmrState* a = s->amr;
     const int key = (a->c0a == a->c0_home ? 0 : 1) | (a->f1a == a->f1_home ? 0 : 2) | (a->f2a == a->f2_home ? 0 : 4);
     if (!a->graph[key]) {
@@ -773,8 +773,16 @@ static jp_status graph_step(jp_solver* s) {
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
     }
-    ACK(cudaGraphLaunch(a->graph[key], s->stream), "graph launch");
+    ACK(cudaGraphLaunch(a->graph[key], on ? on : s->stream), "graph launch");
     std::swap(a->c0a, a->c0b);  // the fine levels return to their buffers within the step
+    return JP_OK;
+}
+
+// One coarse step replayed from the solver's captured graph on another stream `st` (ordered there
+// like a batched step; the capture itself runs on the solver's idle stream).
+jp_status amr_graph_step_on(jp_solver* s, cudaStream_t st) {
+    TRY(graph_step(s, st));
+    ++s->step_count;
     return JP_OK;
 }
 

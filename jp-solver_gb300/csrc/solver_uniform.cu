@@ -29,7 +29,15 @@ jp_status common_setup(jp_solver* s) {
     JP_CK(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
     if (c.device < 0 || c.device >= ndev) return fail(JP_ERR_INVALID, "device %d out of range (%d devices)", c.device, ndev);
     JP_CK(cudaSetDevice(c.device), "cudaSetDevice");
-    JP_CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (s->pool) {
+        // a served solve: its own stream carries the short latency-bound work (creation, regrids,
+        // read-backs) that the batched launches of the other solves must not hold up
+        int lo = 0, hi = 0;
+        JP_CK(cudaDeviceGetStreamPriorityRange(&lo, &hi), "cudaDeviceGetStreamPriorityRange");
+        JP_CK(cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, hi), "cudaStreamCreate");
+    } else {
+        JP_CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    }
     JP_CK(cudaEventCreate(&s->ev0), "cudaEventCreate");
     JP_CK(cudaEventCreate(&s->ev1), "cudaEventCreate");
     jp_info& in = s->info;
