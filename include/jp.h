@@ -316,7 +316,9 @@ typedef struct jp_server_stats {
     double destroy_s;        /* retiring solves */
     double tick_s;           /* inside jp_server_tick */
     int64_t solves, regrids, diags, coarse_steps;
-    int64_t reserved[8];
+    double uniform_gpu_s;    /* device time of the batched uniform launches (CUDA events) */
+    double amr_gpu_s;        /* device time of the batched AMR launches (CUDA events) */
+    int64_t reserved[6];
 } jp_server_stats;
 jp_status jp_server_get_stats(const jp_server* sv, jp_server_stats* out);
 

@@ -249,6 +249,13 @@ struct jp_server {
         cudaEvent_t done = nullptr;
         std::vector<std::pair<Job*, long long>> entries;  // job, step; values in the solver's host slot
     } adiag[2];
+    // device time of the batched launches: timing events around each tick's launches on both
+    // streams, read once they have completed (two ticks later)
+    struct Span {
+        cudaEvent_t a = nullptr, b = nullptr;
+        bool live = false;
+    } span[2][4];
+    int span_tick = 0;
     std::vector<std::thread> workers;
     std::mutex mu;
     std::condition_variable cv_todo, cv_fin;
@@ -320,6 +327,27 @@ void record(Job* j, const double d[3], long long step) {
         j->peak_ts = ts;
     }
     ++j->samples;
+}
+
+// the device time of stream k's launches of this tick: open before, close after
+cudaError_t span_open(jp_server* sv, int k, cudaStream_t st) {
+    auto& sp = sv->span[k][sv->span_tick & 3];
+    cudaError_t e = cudaSuccess;
+    if (!sp.a) e = cudaEventCreate(&sp.a);
+    if (e == cudaSuccess && !sp.b) e = cudaEventCreate(&sp.b);
+    if (e == cudaSuccess && sp.live) {  // four ticks ago: long done; fold it in before reuse
+        float ms = 0.f;
+        if (cudaEventSynchronize(sp.b) == cudaSuccess && cudaEventElapsedTime(&ms, sp.a, sp.b) == cudaSuccess)
+            sv->add(k == 0 ? &jp_server_stats::uniform_gpu_s : &jp_server_stats::amr_gpu_s, ms * 1e-3);
+        sp.live = false;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(sp.a, st);
+    return e;
+}
+cudaError_t span_close(jp_server* sv, int k, cudaStream_t st) {
+    auto& sp = sv->span[k][sv->span_tick & 3];
+    sp.live = true;
+    return cudaEventRecord(sp.b, st);
 }
 
 long long next_event(const Job* j) {
@@ -471,6 +499,11 @@ void jp_server_destroy(jp_server* sv) {
     }
     for (auto& d : sv->adiag)
         if (d.done) cudaEventDestroy(d.done);
+    for (auto& row : sv->span)
+        for (auto& sp : row) {
+            if (sp.a) cudaEventDestroy(sp.a);
+            if (sp.b) cudaEventDestroy(sp.b);
+        }
     if (sv->amr_stream) cudaStreamDestroy(sv->amr_stream);
     for (Job* j : sv->queue) delete j;
     for (auto& b : sv->diag) {
@@ -689,6 +722,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
     }
     std::vector<jp_solver*> members;
     const auto tsb = clk::now();
+    if (kmax) ECK(span_open(sv, 0, sv->stream), "span");
     for (long long t = 0; t < kmax; ++t) {
         members.clear();
         for (auto& p : uni)
@@ -696,6 +730,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         jp_status st = batched_step(members, sv->stream);
         if (st != JP_OK) return st;
     }
+    if (kmax) ECK(span_close(sv, 0, sv->stream), "span");
     if (kmax) sv->add(&jp_server_stats::step_s, seconds_since(tsb));
     for (auto& p : uni) {
         p.first->step += p.second;
@@ -717,6 +752,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
     }
     const auto tab = clk::now();
     long long amr_moved = 0;
+    if (!groups.empty()) ECK(span_open(sv, 1, sv->amr_stream), "span");
     for (auto& g : groups) {
         for (long long t = 0; t < 2; ++t) {
             std::vector<jp_solver*> ms;
@@ -734,6 +770,8 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             j->events_done = false;
         }
     }
+    if (!groups.empty()) ECK(span_close(sv, 1, sv->amr_stream), "span");
+    ++sv->span_tick;
     if (amr_moved) sv->add(&jp_server_stats::step_s, seconds_since(tab), &jp_server_stats::coarse_steps, amr_moved);
     // 5. the previous tick's diagnostics (the GPU meanwhile works on this tick's launches)
     auto& prev = sv->diag[sv->diag_cur ^ 1];

@@ -76,7 +76,8 @@ class ServerStats(C.Structure):
     _fields_ = [("create_s", C.c_double), ("step_s", C.c_double), ("regrid_s", C.c_double),
                 ("diag_s", C.c_double), ("destroy_s", C.c_double), ("tick_s", C.c_double),
                 ("solves", C.c_int64), ("regrids", C.c_int64), ("diags", C.c_int64),
-                ("coarse_steps", C.c_int64), ("reserved", C.c_int64 * 8)]
+                ("coarse_steps", C.c_int64), ("uniform_gpu_s", C.c_double), ("amr_gpu_s", C.c_double),
+                ("reserved", C.c_int64 * 6)]
 
 
 class Request(C.Structure):
