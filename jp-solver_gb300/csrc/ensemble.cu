@@ -183,6 +183,7 @@ struct Job {
     long long sstep = 1;
     bool events_done = false, dg = false;
     int task = 0;
+    int lane = 0;           // AMR: the batch lane (stream) the solve advances in
     jp_status error = JP_OK;
     int samples = 0;
     double E0 = -1, prevE = 1e30, Elast = 0, peak = -1, peak_ts = -1, mass0 = -1, drift = 0;
@@ -239,22 +240,27 @@ struct jp_server {
         std::vector<std::pair<Job*, long long>> entries;  // job, step the values belong to
     } diag[2];
     int diag_cur = 0;
-    // AMR solves advance in batched launches (amr_batch_step: one launch per stage over all of them)
-    // on amr_stream, issued by the tick; their diagnostics are launched there too and read back one
-    // tick late.  Creation and regrids, which need read-backs, run on worker threads on each solve's
+    // AMR solves advance in batched launches (amr_batch_step: one launch per stage over all of them
+    // in a lane) on the lanes' streams, issued by the tick; their diagnostics are launched there too
+    // and read back one tick late.  Creation and regrids, which need read-backs, run on worker threads on each solve's
     // own stream while the batch goes on without that solve.  amr_todo and amr_fin are guarded by mu.
-    cudaStream_t amr_stream = nullptr;
+    // The batch is split into lanes, each with its own stream and a share of the solves: a solve that
+    // leaves for a regrid waits only for its own lane's queued launches, and the lanes overlap on
+    // the device.
+    static constexpr int kLanes = 8;
+    cudaStream_t amr_stream[kLanes] = {};
+    int lane_load[kLanes] = {};        // admitted AMR solves per lane
     std::vector<Job*> amr_active;      // in the batch (tick thread only)
     struct AmrDiag {
         cudaEvent_t done = nullptr;
         std::vector<std::pair<Job*, long long>> entries;  // job, step; values in the solver's host slot
-    } adiag[2];
+    } adiag[kLanes][2];
     // device time of the batched launches: timing events around each tick's launches on both
     // streams, read once they have completed (two ticks later)
     struct Span {
         cudaEvent_t a = nullptr, b = nullptr;
         bool live = false;
-    } span[2][4];
+    } span[1 + kLanes][4];  // 0: uniform stream, 1 + lane: AMR lanes
     int span_tick = 0;
     std::vector<std::thread> workers;
     std::mutex mu;
@@ -443,9 +449,11 @@ jp_status jp_server_create(const jp_server_config* cfg, jp_server** out) {
     if (sv->cfg.workers <= 0) sv->cfg.workers = (int)std::min(32u, std::max(4u, std::thread::hardware_concurrency()));
     sv->t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->amr_stream, cudaStreamNonBlocking);
-    for (auto& d : sv->adiag)
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d.done, cudaEventDisableTiming);
+    for (int l = 0; l < jp_server::kLanes && e == cudaSuccess; ++l) {
+        e = cudaStreamCreateWithFlags(&sv->amr_stream[l], cudaStreamNonBlocking);
+        for (auto& d : sv->adiag[l])
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d.done, cudaEventDisableTiming);
+    }
     size_t fr = 0, tot = 0;
     if (e == cudaSuccess) e = cudaMemGetInfo(&fr, &tot);
     if (e == cudaSuccess) {
@@ -480,7 +488,8 @@ void jp_server_destroy(jp_server* sv) {
     sv->cv_todo.notify_all();
     for (std::thread& t : sv->workers) t.join();  // a running task ends first
     if (sv->stream) cudaStreamSynchronize(sv->stream);
-    if (sv->amr_stream) cudaStreamSynchronize(sv->amr_stream);
+    for (cudaStream_t st : sv->amr_stream)
+        if (st) cudaStreamSynchronize(st);
     for (Job* j : sv->active) {
         if (j->s) jp_destroy(j->s);
         delete j;
@@ -497,14 +506,16 @@ void jp_server_destroy(jp_server* sv) {
         if (j->s) jp_destroy(j->s);
         delete j;
     }
-    for (auto& d : sv->adiag)
-        if (d.done) cudaEventDestroy(d.done);
+    for (auto& lane : sv->adiag)
+        for (auto& d : lane)
+            if (d.done) cudaEventDestroy(d.done);
     for (auto& row : sv->span)
         for (auto& sp : row) {
             if (sp.a) cudaEventDestroy(sp.a);
             if (sp.b) cudaEventDestroy(sp.b);
         }
-    if (sv->amr_stream) cudaStreamDestroy(sv->amr_stream);
+    for (cudaStream_t st : sv->amr_stream)
+        if (st) cudaStreamDestroy(st);
     for (Job* j : sv->queue) delete j;
     for (auto& b : sv->diag) {
         if (b.dev) cudaFree(b.dev);
@@ -573,6 +584,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
     for (Job* j : fin) {
         if (j->requeue) {
             --sv->amr_live;
+            --sv->lane_load[j->lane];
             j->requeue = false;
             j->admitted = false;
             sv->used -= j->bytes;
@@ -580,10 +592,11 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             requeued.push_back(j);
         } else if (j->error != JP_OK) {
             --sv->amr_live;
+            --sv->lane_load[j->lane];
             finish(sv, j, j->error);
         } else {  // back into the batch, after the worker's work on the solve's own stream
             ECK(cudaEventRecord(j->s->ev1, j->s->stream), "event");
-            ECK(cudaStreamWaitEvent(sv->amr_stream, j->s->ev1, 0), "wait");
+            ECK(cudaStreamWaitEvent(sv->amr_stream[j->lane], j->s->ev1, 0), "wait");
             sv->amr_active.push_back(j);
         }
     }
@@ -605,6 +618,8 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             j->admitted = true;
             sv->used += j->bytes;
             ++sv->amr_live;
+            j->lane = int(std::min_element(sv->lane_load, sv->lane_load + jp_server::kLanes) - sv->lane_load);
+            ++sv->lane_load[j->lane];
             to_worker(sv, j, 1);
             continue;
         }
@@ -673,8 +688,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
     //     diagnostic alone is launched here on the batch's stream into this tick's read-back slot.
     //     A solve with a diagnostic still in flight waits a tick before a regrid, so that its samples
     //     are recorded in order.
-    auto& acur = sv->adiag[sv->diag_cur];
-    acur.entries.clear();
+    for (auto& lane : sv->adiag) lane[sv->diag_cur].entries.clear();
     for (size_t i = 0; i < sv->amr_active.size();) {
         Job* j = sv->amr_active[i];
         if (j->events_done || j->step > j->steps || j->error != JP_OK) {
@@ -687,7 +701,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
                 ++i;
                 continue;
             }
-            ECK(cudaEventRecord(j->s->ev0, sv->amr_stream), "event");
+            ECK(cudaEventRecord(j->s->ev0, sv->amr_stream[j->lane]), "event");
             ECK(cudaStreamWaitEvent(j->s->stream, j->s->ev0, 0), "wait");
             j->dg = dg;
             sv->amr_active.erase(sv->amr_active.begin() + i);
@@ -696,20 +710,23 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         }
         if (dg) {
             const auto ta = clk::now();
-            jp_status st = amr_diag_async(j->s, sv->amr_stream, j->s->diag_host + 3 * sv->diag_cur);
+            jp_status st = amr_diag_async(j->s, sv->amr_stream[j->lane], j->s->diag_host + 3 * sv->diag_cur);
             sv->add(&jp_server_stats::diag_s, seconds_since(ta), &jp_server_stats::diags);
             if (st != JP_OK) {
                 j->error = st;
                 ++i;
                 continue;
             }
-            acur.entries.push_back({j, j->step});
+            sv->adiag[j->lane][sv->diag_cur].entries.push_back({j, j->step});
             ++j->inflight;
         }
         j->events_done = true;
         ++i;
     }
-    if (!acur.entries.empty()) ECK(cudaEventRecord(acur.done, sv->amr_stream), "diag event");
+    for (int l = 0; l < jp_server::kLanes; ++l) {
+        auto& acur = sv->adiag[l][sv->diag_cur];
+        if (!acur.entries.empty()) ECK(cudaEventRecord(acur.done, sv->amr_stream[l]), "diag event");
+    }
     // 4. advance the uniform solves in batched launches (behind this tick's diagnostics)
     std::vector<std::pair<Job*, long long>> uni;
     long long kmax = 0;
@@ -743,7 +760,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         if (!j->events_done || j->step >= j->steps || j->error != JP_OK) continue;
         bool placed = false;
         for (auto& g : groups)
-            if (amr_batch_compatible(g[0]->s, j->s)) {
+            if (g[0]->lane == j->lane && amr_batch_compatible(g[0]->s, j->s)) {
                 g.push_back(j);
                 placed = true;
                 break;
@@ -752,8 +769,12 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
     }
     const auto tab = clk::now();
     long long amr_moved = 0;
-    if (!groups.empty()) ECK(span_open(sv, 1, sv->amr_stream), "span");
+    bool lane_used[jp_server::kLanes] = {};
+    for (auto& g : groups) lane_used[g[0]->lane] = true;
+    for (int l = 0; l < jp_server::kLanes; ++l)
+        if (lane_used[l]) ECK(span_open(sv, 1 + l, sv->amr_stream[l]), "span");
     for (auto& g : groups) {
+        cudaStream_t lst = sv->amr_stream[g[0]->lane];
         for (long long t = 0; t < 2; ++t) {
             std::vector<jp_solver*> ms;
             for (Job* j : g)
@@ -761,7 +782,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             if (ms.empty()) break;
             // a group of one with graph replay replays its captured step instead (one launch)
             const bool alone = ms.size() == 1 && (ms[0]->cfg.flags & JP_FLAG_GRAPH);
-            jp_status st = alone ? amr_graph_step_on(ms[0], sv->amr_stream) : amr_batch_step(ms, sv->amr_stream);
+            jp_status st = alone ? amr_graph_step_on(ms[0], lst) : amr_batch_step(ms, lst);
             if (st != JP_OK) return st;
             amr_moved += (long long)ms.size();
         }
@@ -770,7 +791,8 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             j->events_done = false;
         }
     }
-    if (!groups.empty()) ECK(span_close(sv, 1, sv->amr_stream), "span");
+    for (int l = 0; l < jp_server::kLanes; ++l)
+        if (lane_used[l]) ECK(span_close(sv, 1 + l, sv->amr_stream[l]), "span");
     ++sv->span_tick;
     if (amr_moved) sv->add(&jp_server_stats::step_s, seconds_since(tab), &jp_server_stats::coarse_steps, amr_moved);
     // 5. the previous tick's diagnostics (the GPU meanwhile works on this tick's launches)
@@ -786,8 +808,9 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         sv->add(&jp_server_stats::diag_s, seconds_since(tw));
     }
     // 5b. the previous tick's AMR diagnostics
-    auto& aprev = sv->adiag[sv->diag_cur ^ 1];
-    if (!aprev.entries.empty()) {
+    for (auto& lane : sv->adiag) {
+        auto& aprev = lane[sv->diag_cur ^ 1];
+        if (aprev.entries.empty()) continue;
         const auto tw = clk::now();
         ECK(cudaEventSynchronize(aprev.done), "diag");
         for (auto& e : aprev.entries) {
@@ -803,10 +826,11 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         Job* j = sv->amr_active[i];
         const bool over = j->step > j->steps || (j->step == j->steps && j->events_done) || j->error != JP_OK;
         if (over && j->inflight == 0) {
-            ECK(cudaEventRecord(j->s->ev0, sv->amr_stream), "event");
+            ECK(cudaEventRecord(j->s->ev0, sv->amr_stream[j->lane]), "event");
             ECK(cudaStreamWaitEvent(j->s->stream, j->s->ev0, 0), "wait");
             sv->amr_active.erase(sv->amr_active.begin() + i);
             --sv->amr_live;
+            --sv->lane_load[j->lane];
             finish(sv, j, j->error);
         } else {
             ++i;
