@@ -240,33 +240,43 @@ struct jp_server {
         std::vector<std::pair<Job*, long long>> entries;  // job, step the values belong to
     } diag[2];
     int diag_cur = 0;
-    // AMR solves advance in batched launches (amr_batch_step: one launch per stage over all of them
-    // in a lane) on the lanes' streams, issued by the tick; their diagnostics are launched there too
-    // and read back one tick late.  Creation and regrids, which need read-backs, run on worker threads on each solve's
-    // own stream while the batch goes on without that solve.  amr_todo and amr_fin are guarded by mu.
-    // The batch is split into lanes, each with its own stream and a share of the solves: a solve that
-    // leaves for a regrid waits only for its own lane's queued launches, and the lanes overlap on
-    // the device.
-    static constexpr int kLanes = 8;
-    cudaStream_t amr_stream[kLanes] = {};
-    int lane_load[kLanes] = {};        // admitted AMR solves per lane
-    std::vector<Job*> amr_active;      // in the batch (tick thread only)
-    struct AmrDiag {
-        cudaEvent_t done = nullptr;
-        std::vector<std::pair<Job*, long long>> entries;  // job, step; values in the solver's host slot
-    } adiag[kLanes][2];
-    // device time of the batched launches: timing events around each tick's launches on both
-    // streams, read once they have completed (two ticks later)
+    // device time of batched launches: timing events around a round's launches on a stream, read
+    // once they have completed (four rounds later)
     struct Span {
         cudaEvent_t a = nullptr, b = nullptr;
         bool live = false;
-    } span[1 + kLanes][4];  // 0: uniform stream, 1 + lane: AMR lanes
-    int span_tick = 0;
+    };
+    Span uspan[4];
+    int uspan_tick = 0;
+    // AMR solves advance in lanes, each a thread with its own stream and a share of the solves.  A
+    // lane's rounds launch the diagnostics due, one batched coarse step per stage over the lane's
+    // solves (amr_batch_step), and read the previous round's diagnostics back.  Creation and
+    // regrids, which need read-backs, run on worker threads on each solve's own stream while its
+    // lane goes on without it; a solve that leaves for a regrid waits only for its own lane's queue.
+    struct AmrDiag {
+        cudaEvent_t done = nullptr;
+        std::vector<std::pair<Job*, long long>> entries;  // job, step; values in the solver's host slot
+    };
+    struct Lane {
+        std::thread th;
+        std::mutex mu;
+        std::condition_variable cv;
+        std::deque<Job*> inbox;          // created or regridded solves (re)joining the lane
+        std::vector<Job*> active;        // the lane thread's own
+        cudaStream_t stream = nullptr;
+        AmrDiag adiag[2];
+        int diag_cur = 0;
+        Span span[4];
+        int span_tick = 0;
+    };
+    static constexpr int kLanes = 8;
+    Lane lane[kLanes];
+    int lane_load[kLanes] = {};        // admitted AMR solves per lane (tick thread)
     std::vector<std::thread> workers;
     std::mutex mu;
     std::condition_variable cv_todo, cv_fin;
-    std::deque<Job*> amr_todo;
-    std::vector<Job*> amr_fin;
+    std::deque<Job*> amr_todo;         // worker tasks
+    std::vector<Job*> amr_fin;         // AMR solves to retire (or to requeue) by the tick thread
     int amr_live = 0;                  // admitted AMR solves not yet retired (tick thread only)
     std::atomic<bool> stop{false};
     std::mutex stats_mu;
@@ -335,23 +345,25 @@ void record(Job* j, const double d[3], long long step) {
     ++j->samples;
 }
 
-// the device time of stream k's launches of this tick: open before, close after
-cudaError_t span_open(jp_server* sv, int k, cudaStream_t st) {
-    auto& sp = sv->span[k][sv->span_tick & 3];
+// the device time of a round's launches on a stream: open before, close after; a slot is folded
+// into the statistics when it comes round again
+cudaError_t span_open(jp_server* sv, jp_server::Span (&ring)[4], int tick, double jp_server_stats::*field,
+                      cudaStream_t st) {
+    auto& sp = ring[tick & 3];
     cudaError_t e = cudaSuccess;
     if (!sp.a) e = cudaEventCreate(&sp.a);
     if (e == cudaSuccess && !sp.b) e = cudaEventCreate(&sp.b);
-    if (e == cudaSuccess && sp.live) {  // four ticks ago: long done; fold it in before reuse
+    if (e == cudaSuccess && sp.live) {
         float ms = 0.f;
         if (cudaEventSynchronize(sp.b) == cudaSuccess && cudaEventElapsedTime(&ms, sp.a, sp.b) == cudaSuccess)
-            sv->add(k == 0 ? &jp_server_stats::uniform_gpu_s : &jp_server_stats::amr_gpu_s, ms * 1e-3);
+            sv->add(field, ms * 1e-3);
         sp.live = false;
     }
     if (e == cudaSuccess) e = cudaEventRecord(sp.a, st);
     return e;
 }
-cudaError_t span_close(jp_server* sv, int k, cudaStream_t st) {
-    auto& sp = sv->span[k][sv->span_tick & 3];
+cudaError_t span_close(jp_server::Span (&ring)[4], int tick, cudaStream_t st) {
+    auto& sp = ring[tick & 3];
     sp.live = true;
     return cudaEventRecord(sp.b, st);
 }
@@ -417,11 +429,184 @@ void worker_main(jp_server* sv) {
             sv->amr_todo.pop_front();
         }
         amr_task(sv, j);
+        if (j->requeue || j->error != JP_OK) {  // the tick thread requeues or retires it
+            {
+                std::lock_guard<std::mutex> lk(sv->mu);
+                sv->amr_fin.push_back(j);
+            }
+            sv->cv_fin.notify_all();
+        } else {  // back to its lane
+            auto& L = sv->lane[j->lane];
+            {
+                std::lock_guard<std::mutex> lk(L.mu);
+                L.inbox.push_back(j);
+            }
+            L.cv.notify_one();
+        }
+    }
+}
+
+void to_worker(jp_server* sv, Job* j, int task);
+
+// One round of a lane: the events of each solve's current step (a regrid sends the solve to a
+// worker, its stream ordered after the lane's work so far, and a diagnostic of the same step goes
+// with it; a diagnostic alone is launched on the lane's stream into this round's read-back slot; a
+// solve with a diagnostic in flight waits a round before a regrid, so its samples are recorded in
+// order), the batched coarse steps of the solves that move (sstep of them: two with graph replay, as
+// the program steps), the previous round's read-backs, and the retirement of solves that are over.
+// Returns whether anything was launched or read back.
+bool lane_round(jp_server* sv, jp_server::Lane& L) {
+    bool busy = false;
+    auto fail_all = [&](jp_status st) {
+        for (Job* j : L.active)
+            if (j->error == JP_OK) j->error = st;
+    };
+    auto& cur = L.adiag[L.diag_cur];
+    cur.entries.clear();
+    for (size_t i = 0; i < L.active.size();) {
+        Job* j = L.active[i];
+        if (j->events_done || j->step > j->steps || j->error != JP_OK) {
+            ++i;
+            continue;
+        }
+        const bool rg = j->dynamic && j->step > 0 && j->step % j->adapt == 0, dg = j->step % j->diagK == 0;
+        if (rg) {
+            if (j->inflight) {
+                ++i;
+                continue;
+            }
+            if (cudaEventRecord(j->s->ev0, L.stream) != cudaSuccess ||
+                cudaStreamWaitEvent(j->s->stream, j->s->ev0, 0) != cudaSuccess) {
+                j->error = fail(JP_ERR_CUDA, "lane event");
+                ++i;
+                continue;
+            }
+            j->dg = dg;
+            L.active.erase(L.active.begin() + i);
+            to_worker(sv, j, 2);
+            busy = true;
+            continue;
+        }
+        if (dg) {
+            const auto ta = clk::now();
+            jp_status st = amr_diag_async(j->s, L.stream, j->s->diag_host + 3 * L.diag_cur);
+            sv->add(&jp_server_stats::diag_s, seconds_since(ta), &jp_server_stats::diags);
+            if (st != JP_OK) {
+                j->error = st;
+                ++i;
+                continue;
+            }
+            cur.entries.push_back({j, j->step});
+            ++j->inflight;
+            busy = true;
+        }
+        j->events_done = true;
+        ++i;
+    }
+    if (!cur.entries.empty() && cudaEventRecord(cur.done, L.stream) != cudaSuccess) fail_all(JP_ERR_CUDA);
+    // batched coarse steps, one group per launch shape
+    std::vector<std::vector<Job*>> groups;
+    for (Job* j : L.active) {
+        if (!j->events_done || j->step >= j->steps || j->error != JP_OK) continue;
+        bool placed = false;
+        for (auto& g : groups)
+            if (amr_batch_compatible(g[0]->s, j->s)) {
+                g.push_back(j);
+                placed = true;
+                break;
+            }
+        if (!placed) groups.push_back({j});
+    }
+    if (!groups.empty()) {
+        const auto tab = clk::now();
+        long long moved = 0;
+        if (span_open(sv, L.span, L.span_tick, &jp_server_stats::amr_gpu_s, L.stream) != cudaSuccess)
+            fail_all(JP_ERR_CUDA);
+        for (auto& g : groups) {
+            jp_status st = JP_OK;
+            for (long long t = 0; t < 2 && st == JP_OK; ++t) {
+                std::vector<jp_solver*> ms;
+                for (Job* j : g)
+                    if (j->sstep > t) ms.push_back(j->s);
+                if (ms.empty()) break;
+                // a group of one with graph replay replays its captured step instead (one launch)
+                const bool alone = ms.size() == 1 && (ms[0]->cfg.flags & JP_FLAG_GRAPH);
+                st = alone ? amr_graph_step_on(ms[0], L.stream) : amr_batch_step(ms, L.stream);
+                moved += (long long)ms.size();
+            }
+            for (Job* j : g) {
+                if (st != JP_OK) j->error = st;
+                j->step += j->sstep;
+                j->events_done = false;
+            }
+        }
+        span_close(L.span, L.span_tick, L.stream);
+        ++L.span_tick;
+        sv->add(&jp_server_stats::step_s, seconds_since(tab), &jp_server_stats::coarse_steps, moved);
+        busy = true;
+    }
+    // the previous round's diagnostics
+    auto& prev = L.adiag[L.diag_cur ^ 1];
+    if (!prev.entries.empty()) {
+        const auto tw = clk::now();
+        const cudaError_t e = cudaEventSynchronize(prev.done);
+        for (auto& en : prev.entries) {
+            if (e == cudaSuccess) record(en.first, en.first->s->diag_host + 3 * (L.diag_cur ^ 1), en.second);
+            else if (en.first->error == JP_OK) en.first->error = fail(JP_ERR_CUDA, "diagnostics");
+            --en.first->inflight;
+        }
+        prev.entries.clear();
+        sv->add(&jp_server_stats::diag_s, seconds_since(tw));
+        busy = true;
+    }
+    L.diag_cur ^= 1;
+    // retire solves that take no more steps and have nothing in flight; their frees are ordered
+    // after the lane's last work on them
+    std::vector<Job*> over;
+    for (size_t i = 0; i < L.active.size();) {
+        Job* j = L.active[i];
+        const bool done = j->step > j->steps || (j->step == j->steps && j->events_done) || j->error != JP_OK;
+        if (done && j->inflight == 0) {
+            if (cudaEventRecord(j->s->ev0, L.stream) != cudaSuccess ||
+                cudaStreamWaitEvent(j->s->stream, j->s->ev0, 0) != cudaSuccess)
+                cudaStreamSynchronize(L.stream);
+            L.active.erase(L.active.begin() + i);
+            over.push_back(j);
+        } else {
+            ++i;
+        }
+    }
+    if (!over.empty()) {
         {
             std::lock_guard<std::mutex> lk(sv->mu);
-            sv->amr_fin.push_back(j);
+            for (Job* j : over) sv->amr_fin.push_back(j);
         }
         sv->cv_fin.notify_all();
+        busy = true;
+    }
+    return busy;
+}
+
+void lane_main(jp_server* sv, int l) {
+    jp_server::Lane& L = sv->lane[l];
+    cudaSetDevice(sv->cfg.device);
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(L.mu);
+            if (L.active.empty())
+                L.cv.wait_for(lk, std::chrono::milliseconds(2), [&] { return sv->stop.load() || !L.inbox.empty(); });
+            if (sv->stop.load()) return;
+            while (!L.inbox.empty()) {  // (re)join after the worker's work on the solve's own stream
+                Job* j = L.inbox.front();
+                L.inbox.pop_front();
+                if (cudaEventRecord(j->s->ev1, j->s->stream) != cudaSuccess ||
+                    cudaStreamWaitEvent(L.stream, j->s->ev1, 0) != cudaSuccess)
+                    j->error = fail(JP_ERR_CUDA, "lane event");
+                L.active.push_back(j);
+            }
+        }
+        if (L.active.empty()) continue;
+        if (!lane_round(sv, L)) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
 }
 
@@ -450,8 +635,8 @@ jp_status jp_server_create(const jp_server_config* cfg, jp_server** out) {
     sv->t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
     for (int l = 0; l < jp_server::kLanes && e == cudaSuccess; ++l) {
-        e = cudaStreamCreateWithFlags(&sv->amr_stream[l], cudaStreamNonBlocking);
-        for (auto& d : sv->adiag[l])
+        e = cudaStreamCreateWithFlags(&sv->lane[l].stream, cudaStreamNonBlocking);
+        for (auto& d : sv->lane[l].adiag)
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d.done, cudaEventDisableTiming);
     }
     size_t fr = 0, tot = 0;
@@ -474,6 +659,7 @@ jp_status jp_server_create(const jp_server_config* cfg, jp_server** out) {
     }
     sv->budget = cfg->pool_gb > 0 ? cfg->pool_gb * double(1ull << 30) : 0.75 * double(fr);
     for (int w = 0; w < sv->cfg.workers; ++w) sv->workers.emplace_back(worker_main, sv);
+    for (int l = 0; l < jp_server::kLanes; ++l) sv->lane[l].th = std::thread(lane_main, sv, l);
     *out = sv;
     return JP_OK;
 }
@@ -486,17 +672,29 @@ void jp_server_destroy(jp_server* sv) {
         sv->stop.store(true);
     }
     sv->cv_todo.notify_all();
+    for (auto& L : sv->lane) {
+        { std::lock_guard<std::mutex> lk(L.mu); }
+        L.cv.notify_all();
+    }
     for (std::thread& t : sv->workers) t.join();  // a running task ends first
+    for (auto& L : sv->lane)
+        if (L.th.joinable()) L.th.join();
     if (sv->stream) cudaStreamSynchronize(sv->stream);
-    for (cudaStream_t st : sv->amr_stream)
-        if (st) cudaStreamSynchronize(st);
+    for (auto& L : sv->lane)
+        if (L.stream) cudaStreamSynchronize(L.stream);
     for (Job* j : sv->active) {
         if (j->s) jp_destroy(j->s);
         delete j;
     }
-    for (Job* j : sv->amr_active) {
-        if (j->s) jp_destroy(j->s);
-        delete j;
+    for (auto& L : sv->lane) {
+        for (Job* j : L.active) {
+            if (j->s) jp_destroy(j->s);
+            delete j;
+        }
+        for (Job* j : L.inbox) {
+            if (j->s) jp_destroy(j->s);
+            delete j;
+        }
     }
     for (Job* j : sv->amr_todo) {
         if (j->s) jp_destroy(j->s);
@@ -506,16 +704,20 @@ void jp_server_destroy(jp_server* sv) {
         if (j->s) jp_destroy(j->s);
         delete j;
     }
-    for (auto& lane : sv->adiag)
-        for (auto& d : lane)
-            if (d.done) cudaEventDestroy(d.done);
-    for (auto& row : sv->span)
-        for (auto& sp : row) {
+    auto drop_spans = [](jp_server::Span (&ring)[4]) {
+        for (auto& sp : ring) {
             if (sp.a) cudaEventDestroy(sp.a);
             if (sp.b) cudaEventDestroy(sp.b);
         }
-    for (cudaStream_t st : sv->amr_stream)
-        if (st) cudaStreamDestroy(st);
+    };
+    for (auto& L : sv->lane) {
+        for (auto& d : L.adiag)
+            if (d.done) cudaEventDestroy(d.done);
+        drop_spans(L.span);
+    }
+    drop_spans(sv->uspan);
+    for (auto& L : sv->lane)
+        if (L.stream) cudaStreamDestroy(L.stream);
     for (Job* j : sv->queue) delete j;
     for (auto& b : sv->diag) {
         if (b.dev) cudaFree(b.dev);
@@ -581,23 +783,17 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         std::lock_guard<std::mutex> lk(sv->mu);
         fin.swap(sv->amr_fin);
     }
-    for (Job* j : fin) {
+    for (Job* j : fin) {  // from the lanes (over) and the workers (failed, or no memory yet)
+        --sv->amr_live;
+        --sv->lane_load[j->lane];
         if (j->requeue) {
-            --sv->amr_live;
-            --sv->lane_load[j->lane];
             j->requeue = false;
             j->admitted = false;
             sv->used -= j->bytes;
             sv->queue.push_front(j);
             requeued.push_back(j);
-        } else if (j->error != JP_OK) {
-            --sv->amr_live;
-            --sv->lane_load[j->lane];
+        } else {
             finish(sv, j, j->error);
-        } else {  // back into the batch, after the worker's work on the solve's own stream
-            ECK(cudaEventRecord(j->s->ev1, j->s->stream), "event");
-            ECK(cudaStreamWaitEvent(sv->amr_stream[j->lane], j->s->ev1, 0), "wait");
-            sv->amr_active.push_back(j);
         }
     }
     // 2. admission in submission order while the budget and the slots allow.  An AMR solve also
@@ -683,50 +879,6 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         ECK(cudaEventRecord(cur.done, sv->stream), "diag event");
         sv->add(&jp_server_stats::diag_s, seconds_since(td), &jp_server_stats::diags, (int64_t)cur.entries.size());
     }
-    // 3b. AMR events due at each batched solve's current step: a regrid sends the solve to a worker
-    //     (its stream waits for the batch so far; a diagnostic of the same step goes with it); a
-    //     diagnostic alone is launched here on the batch's stream into this tick's read-back slot.
-    //     A solve with a diagnostic still in flight waits a tick before a regrid, so that its samples
-    //     are recorded in order.
-    for (auto& lane : sv->adiag) lane[sv->diag_cur].entries.clear();
-    for (size_t i = 0; i < sv->amr_active.size();) {
-        Job* j = sv->amr_active[i];
-        if (j->events_done || j->step > j->steps || j->error != JP_OK) {
-            ++i;
-            continue;
-        }
-        const bool rg = j->dynamic && j->step > 0 && j->step % j->adapt == 0, dg = j->step % j->diagK == 0;
-        if (rg) {
-            if (j->inflight) {
-                ++i;
-                continue;
-            }
-            ECK(cudaEventRecord(j->s->ev0, sv->amr_stream[j->lane]), "event");
-            ECK(cudaStreamWaitEvent(j->s->stream, j->s->ev0, 0), "wait");
-            j->dg = dg;
-            sv->amr_active.erase(sv->amr_active.begin() + i);
-            to_worker(sv, j, 2);
-            continue;
-        }
-        if (dg) {
-            const auto ta = clk::now();
-            jp_status st = amr_diag_async(j->s, sv->amr_stream[j->lane], j->s->diag_host + 3 * sv->diag_cur);
-            sv->add(&jp_server_stats::diag_s, seconds_since(ta), &jp_server_stats::diags);
-            if (st != JP_OK) {
-                j->error = st;
-                ++i;
-                continue;
-            }
-            sv->adiag[j->lane][sv->diag_cur].entries.push_back({j, j->step});
-            ++j->inflight;
-        }
-        j->events_done = true;
-        ++i;
-    }
-    for (int l = 0; l < jp_server::kLanes; ++l) {
-        auto& acur = sv->adiag[l][sv->diag_cur];
-        if (!acur.entries.empty()) ECK(cudaEventRecord(acur.done, sv->amr_stream[l]), "diag event");
-    }
     // 4. advance the uniform solves in batched launches (behind this tick's diagnostics)
     std::vector<std::pair<Job*, long long>> uni;
     long long kmax = 0;
@@ -739,7 +891,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
     }
     std::vector<jp_solver*> members;
     const auto tsb = clk::now();
-    if (kmax) ECK(span_open(sv, 0, sv->stream), "span");
+    if (kmax) ECK(span_open(sv, sv->uspan, sv->uspan_tick, &jp_server_stats::uniform_gpu_s, sv->stream), "span");
     for (long long t = 0; t < kmax; ++t) {
         members.clear();
         for (auto& p : uni)
@@ -747,54 +899,15 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         jp_status st = batched_step(members, sv->stream);
         if (st != JP_OK) return st;
     }
-    if (kmax) ECK(span_close(sv, 0, sv->stream), "span");
+    if (kmax) {
+        ECK(span_close(sv->uspan, sv->uspan_tick, sv->stream), "span");
+        ++sv->uspan_tick;
+    }
     if (kmax) sv->add(&jp_server_stats::step_s, seconds_since(tsb));
     for (auto& p : uni) {
         p.first->step += p.second;
         if (p.first->step % p.first->diagK == 0) p.first->need_diag = true;  // at the new step, next tick
     }
-    // 4b. advance the batched AMR solves by their sstep coarse steps, one launch per stage per group
-    //     of solves that share a launch shape
-    std::vector<std::vector<Job*>> groups;
-    for (Job* j : sv->amr_active) {
-        if (!j->events_done || j->step >= j->steps || j->error != JP_OK) continue;
-        bool placed = false;
-        for (auto& g : groups)
-            if (g[0]->lane == j->lane && amr_batch_compatible(g[0]->s, j->s)) {
-                g.push_back(j);
-                placed = true;
-                break;
-            }
-        if (!placed) groups.push_back({j});
-    }
-    const auto tab = clk::now();
-    long long amr_moved = 0;
-    bool lane_used[jp_server::kLanes] = {};
-    for (auto& g : groups) lane_used[g[0]->lane] = true;
-    for (int l = 0; l < jp_server::kLanes; ++l)
-        if (lane_used[l]) ECK(span_open(sv, 1 + l, sv->amr_stream[l]), "span");
-    for (auto& g : groups) {
-        cudaStream_t lst = sv->amr_stream[g[0]->lane];
-        for (long long t = 0; t < 2; ++t) {
-            std::vector<jp_solver*> ms;
-            for (Job* j : g)
-                if (j->sstep > t) ms.push_back(j->s);
-            if (ms.empty()) break;
-            // a group of one with graph replay replays its captured step instead (one launch)
-            const bool alone = ms.size() == 1 && (ms[0]->cfg.flags & JP_FLAG_GRAPH);
-            jp_status st = alone ? amr_graph_step_on(ms[0], lst) : amr_batch_step(ms, lst);
-            if (st != JP_OK) return st;
-            amr_moved += (long long)ms.size();
-        }
-        for (Job* j : g) {
-            j->step += j->sstep;
-            j->events_done = false;
-        }
-    }
-    for (int l = 0; l < jp_server::kLanes; ++l)
-        if (lane_used[l]) ECK(span_close(sv, 1 + l, sv->amr_stream[l]), "span");
-    ++sv->span_tick;
-    if (amr_moved) sv->add(&jp_server_stats::step_s, seconds_since(tab), &jp_server_stats::coarse_steps, amr_moved);
     // 5. the previous tick's diagnostics (the GPU meanwhile works on this tick's launches)
     auto& prev = sv->diag[sv->diag_cur ^ 1];
     if (!prev.entries.empty()) {
@@ -806,35 +919,6 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         }
         prev.entries.clear();
         sv->add(&jp_server_stats::diag_s, seconds_since(tw));
-    }
-    // 5b. the previous tick's AMR diagnostics
-    for (auto& lane : sv->adiag) {
-        auto& aprev = lane[sv->diag_cur ^ 1];
-        if (aprev.entries.empty()) continue;
-        const auto tw = clk::now();
-        ECK(cudaEventSynchronize(aprev.done), "diag");
-        for (auto& e : aprev.entries) {
-            record(e.first, e.first->s->diag_host + 3 * (sv->diag_cur ^ 1), e.second);
-            --e.first->inflight;
-        }
-        aprev.entries.clear();
-        sv->add(&jp_server_stats::diag_s, seconds_since(tw));
-    }
-    // retire batched AMR solves that take no more steps and have nothing in flight; their frees are
-    // ordered after the batch's last work on them
-    for (size_t i = 0; i < sv->amr_active.size();) {
-        Job* j = sv->amr_active[i];
-        const bool over = j->step > j->steps || (j->step == j->steps && j->events_done) || j->error != JP_OK;
-        if (over && j->inflight == 0) {
-            ECK(cudaEventRecord(j->s->ev0, sv->amr_stream[j->lane]), "event");
-            ECK(cudaStreamWaitEvent(j->s->stream, j->s->ev0, 0), "wait");
-            sv->amr_active.erase(sv->amr_active.begin() + i);
-            --sv->amr_live;
-            --sv->lane_load[j->lane];
-            finish(sv, j, j->error);
-        } else {
-            ++i;
-        }
     }
     sv->diag_cur ^= 1;
     // retire finished uniform solves: all steps issued, every diagnostic read back.  Their last use
@@ -851,8 +935,8 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             ++i;
         }
     }
-    // 6. nothing launched while AMR solves are with the workers: wait briefly for one of them
-    if (uni.empty() && !amr_moved && sv->amr_live > 0) {
+    // 6. nothing launched here while AMR solves run in their lanes: wait briefly for one to end
+    if (uni.empty() && sv->amr_live > 0) {
         std::unique_lock<std::mutex> lk(sv->mu);
         sv->cv_fin.wait_for(lk, std::chrono::milliseconds(1), [sv] { return !sv->amr_fin.empty(); });
     }
