@@ -3,8 +3,11 @@
 // ST of lattice.cuh (pools, prolongation sources and ghost shells all in that format; FP32
 // arithmetic).  Instantiated once per format by amr_kernels_<format>.cu.
 // Reference: src/tgv3d_amr.cu:69-453, 514-536.  One CTA per block; a thread owns one cell (MB<=8)
-// or several (MB=16), and the steps take 128, 256 or 512 threads per CTA at MB = 8 and 16.  Arithmetic follows the reference's expressions so results agree within
-// round-off; loop orders of the trilinear and the 8-child average are the reference's.
+// or several (MB=16), and the steps take 128, 256 or 512 threads per CTA at MB = 8 and 16.
+// Arithmetic follows the reference's expressions so results agree within round-off; loop orders of
+// the trilinear and the 8-child average are the reference's.  Per-block kernels keep their body in
+// a d_* device function that takes the block index, shared by the single-solve kernel (k_*) and the
+// batched kernels over many solves (kb_*).
 #pragma once
 #include "amr_common.cuh"
 #include "amr_kernels.h"
@@ -103,7 +106,8 @@ __device__ __forceinline__ void prolong_prep_l0(const typename ST::raw* __restri
     tri_axis(gfk, kb, tz);
 #pragma unroll
     for (int q = 0; q < Q; ++q) out[q] = 0.f;
-#pragma unroll 1
+    // corners unrolled: their loads are in flight together; the sums keep the corner order
+#pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
         const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
@@ -129,7 +133,8 @@ __device__ __forceinline__ void prolong_prep_l1(const typename ST::raw* __restri
     tri_axis(g2k, kb, tz);
 #pragma unroll
     for (int q = 0; q < Q; ++q) out[q] = 0.f;
-#pragma unroll 1
+    // corners unrolled: their loads are in flight together; the sums keep the corner order
+#pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
         const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
