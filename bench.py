@@ -159,6 +159,33 @@ def bench_storage(J, n: int, storage: str, steps: int, warmup: int, device: int,
             "achieved_gbs": BYTES_PER_UPDATE[storage] * cells / per_launch_s / 1e9}
 
 
+def bench_amr(J, device: int, steps: int = 20) -> dict:
+    """The AMR static gold case (coarse N=64, both levels refined everywhere, finest 256^3, MB=8,
+    Re=800, graph replay of the 1:2:4 coarse step): work-normalised GLUPS of the timed coarse steps,
+    work = (cnb0 + 2 nf1 + 4 nf2) MB^3 per coarse step as the reference counts it, against the FP32
+    (152 B) and FP16 (76 B) per-update roofline, in both storages."""
+    peaks = load_peaks()
+    out = {"workload": "AMR static gold: N0=64, --l1 all --l2 all, MB=8, Re=800, CUDA-graph step",
+           "work_per_coarse_step": None}
+    for st in ("fp32", "fp16"):
+        s = J.Solver("amr", n=64, re=800.0, u0=U0, l1_mode="all", l2_mode="all", storage=st, device=device,
+                     flags=J.FLAG_GRAPH)
+        try:
+            c = s.counts()
+            work = (c["cnb0"] + 2 * c["nf1"] + 4 * c["nf2"]) * 512
+            s.step(4)
+            s.sync()
+            ms = s.step_timed(steps)
+        finally:
+            s.close()
+        glups = work * steps / (ms / 1e3) / 1e9
+        gbs = glups * BYTES_PER_UPDATE[st]
+        out["work_per_coarse_step"] = work
+        out[st] = {"glups_work": glups, "ms_per_coarse_step": ms / steps, "achieved_gbs": gbs,
+                   "frac_of_fp32_roofline": glups * 152.0 / peaks["hbm_gbs"], "frac_of_own_roofline": gbs / peaks["hbm_gbs"]}
+    return out
+
+
 def bench_e2e(J, n: int, calls: int, k: int, device: int, pg) -> dict:
     """State in pinned host memory; per call: H2D of the state, k lattice steps, diagnostics D2H."""
     import ctypes as C
@@ -336,6 +363,7 @@ def main() -> int:
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--no-variants", action="store_true", help="skip the FP16/BF16 lines")
+    ap.add_argument("--no-amr", action="store_true", help="skip the AMR static gold line")
     ap.add_argument("--e2e-calls", type=int, default=4)
     ap.add_argument("--cpu-steps", type=int, default=3, help="0 skips the CPU baseline")
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16", "bf16", "fp64"],
@@ -434,6 +462,8 @@ def main() -> int:
         "gpu_launches": main_r["launches"],
         "clocks": main_r["clocks"],
     }
+    if not a.no_amr and rank == 0:
+        line["amr"] = bench_amr(J, local)
     if rank == 0 and world == 1 and a.cpu_steps > 0:
         line["cpu_baseline"] = cpu_baseline(n, a.cpu_steps)
     if rank == 0:

@@ -244,6 +244,17 @@ jp_status jp_get_sensor(jp_solver* s, int32_t level, float* host, int64_t capaci
  * two implementations the same sensor field for bit-exact table comparisons. */
 jp_status jp_set_sensor_override(jp_solver* s, const float* sen0, const float* sen1_by_pos);
 
+/* ---- state files (extension; the reference always starts from the initial state) -------- */
+
+/* Write the whole state of a solve to `path`: a header (kind, n, mb, storage, Re, u0, refinement
+ * modes, step count) and for a uniform cube its stored populations, for an AMR solve its block
+ * counts, capacities, block tables and the populations of the blocks in use.  jp_load_state into a
+ * solver created with the same kind, n, mb, storage, Re, u0 and refinement modes (t*, diagnostic
+ * and regrid cadence may differ) continues bit for bit where the saved solve was, including later
+ * regrids.  JP_ERR_INVALID for a file of another configuration, ABI or a truncated file. */
+jp_status jp_save_state(jp_solver* s, const char* path);
+jp_status jp_load_state(jp_solver* s, const char* path);
+
 /* ---- ensembles and serving (extensions; no counterpart in the reference) ------------- */
 
 /* An ensemble steps many solvers of the same device together, on the ensemble's stream, ordered

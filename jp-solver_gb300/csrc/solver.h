@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstdio>
 #include <vector>
 
 namespace jp {
@@ -95,6 +96,8 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& members, cudaStream_t st
 bool amr_batch_compatible(const jp_solver* a, const jp_solver* b);
 jp_status amr_prepare_diag(jp_solver* s);
 jp_status amr_graph_step_on(jp_solver* s, cudaStream_t st);
+jp_status amr_save_state(jp_solver* s, std::FILE* f);
+jp_status amr_load_state(jp_solver* s, std::FILE* f);
 jp_status amr_diag_async(jp_solver* s, cudaStream_t st, double* host_out);
 jp_status amr_get_counts(jp_solver* s, jp_amr_counts* out);
 jp_status amr_get_table(jp_solver* s, int table, int32_t* host, int64_t capacity, int64_t* count);

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -218,17 +219,11 @@ static void update_bytes(jp_solver* s) {
                                      ((size_t)a->cap1 + a->cap2) * Q * a->SH) * a->elem);
 }
 
-// Pools grow on overflow instead of being written past their end (the reference sizes them with
-// margins and does not check: ties at the threshold over-admit).  The new capacity is at least
-// twice the old one and must fit the HBM budget; payloads and the snapshots of the previous grid
-// that a regrid still reads are kept.
-static jp_status grow_l1(jp_solver* s, int needed) {
+// Reallocate the arrays sized by the level-1 capacity; keep: the payload the migration reads and
+// the snapshots of the previous grid survive (pool growth), else nothing does (state loading).
+static jp_status set_cap1(jp_solver* s, int cap, bool keep) {
     AmrState* a = s->amr;
-    const int cap = ((std::max(needed, 2 * a->cap1) + 7) / 8) * 8;
-    if (!pool_fits(a, cap, a->cap2))
-        return fail(JP_ERR_CAPACITY, "level-1 pool overflow: %d blocks needed, %d held, budget allows no growth", needed,
-                    a->cap1);
-    const size_t blk = (size_t)Q * a->MB3, old = a->cap1;
+    const size_t blk = (size_t)Q * a->MB3, old = keep ? std::min(a->cap1, cap) : 0;
     TRY(regrow(s, a->f1a, pf(a, cap * blk), pf(a, old * blk)));  // payload the migration reads
     TRY(regrow(s, a->f1b, pf(a, cap * blk), 0));
     TRY(regrow(s, a->gh1, pf(a, (size_t)cap * Q * a->SH), 0));
@@ -249,13 +244,9 @@ static jp_status grow_l1(jp_solver* s, int needed) {
     return JP_OK;
 }
 
-static jp_status grow_l2(jp_solver* s, int needed) {
+static jp_status set_cap2(jp_solver* s, int cap, bool keep) {
     AmrState* a = s->amr;
-    const int cap = ((std::max(needed, 2 * a->cap2) + 7) / 8) * 8;
-    if (!pool_fits(a, a->cap1, cap))
-        return fail(JP_ERR_CAPACITY, "level-2 pool overflow: %d blocks needed, %d held, budget allows no growth", needed,
-                    a->cap2);
-    const size_t blk = (size_t)Q * a->MB3, old = a->cap2;
+    const size_t blk = (size_t)Q * a->MB3, old = keep ? std::min(a->cap2, cap) : 0;
     TRY(regrow(s, a->f2a, pf(a, cap * blk), pf(a, old * blk)));  // payload the migration reads
     TRY(regrow(s, a->f2b, pf(a, cap * blk), 0));
     TRY(regrow(s, a->gh2, pf(a, (size_t)cap * Q * a->SH), 0));
@@ -266,6 +257,28 @@ static jp_status grow_l2(jp_solver* s, int needed) {
     a->cap2 = cap;
     update_bytes(s);
     return JP_OK;
+}
+
+// Pools grow on overflow instead of being written past their end (the reference sizes them with
+// margins and does not check: ties at the threshold over-admit).  The new capacity is at least
+// twice the old one and must fit the HBM budget; payloads and the snapshots of the previous grid
+// that a regrid still reads are kept.
+static jp_status grow_l1(jp_solver* s, int needed) {
+    AmrState* a = s->amr;
+    const int cap = ((std::max(needed, 2 * a->cap1) + 7) / 8) * 8;
+    if (!pool_fits(a, cap, a->cap2))
+        return fail(JP_ERR_CAPACITY, "level-1 pool overflow: %d blocks needed, %d held, budget allows no growth", needed,
+                    a->cap1);
+    return set_cap1(s, cap, true);
+}
+
+static jp_status grow_l2(jp_solver* s, int needed) {
+    AmrState* a = s->amr;
+    const int cap = ((std::max(needed, 2 * a->cap2) + 7) / 8) * 8;
+    if (!pool_fits(a, a->cap1, cap))
+        return fail(JP_ERR_CAPACITY, "level-2 pool overflow: %d blocks needed, %d held, budget allows no growth", needed,
+                    a->cap2);
+    return set_cap2(s, cap, true);
 }
 
 // exclusive scan of the marks and the level-1 tables; on overflow of the level-1 pool nothing is
@@ -1064,6 +1077,91 @@ jp_status amr_set_populations(jp_solver* s, int level, int layout, int dtype, co
     }
     ACK(cudaMemcpyAsync(p, raw.data(), raw.size(), cudaMemcpyHostToDevice, s->stream), "H2D");
     ACK(cudaStreamSynchronize(s->stream), "H2D");
+    return JP_OK;
+}
+
+// ---- state files (jp_save_state / jp_load_state) ---------------------------------------------------
+// AMR payload: the host counts and capacities, every block table whole (their sizes follow from the
+// capacities, which a load restores first), then the populations of the blocks in use, as stored.
+// Prolongation sources, ghosts, sensors and regrid snapshots are recomputed before they are read.
+namespace {
+struct TableRef {
+    int* p;
+    size_t n;
+};
+std::vector<TableRef> state_tables(AmrState* a) {
+    const size_t c0 = a->cnb0, c1 = a->cap1, c2 = a->cap2;
+    return {{a->ref0, c0}, {a->fof0, c0}, {a->skin0, c0}, {a->pcb, c1}, {a->oct, c1}, {a->rl0, c1},
+            {a->f1pos, c1}, {a->ref1, c1}, {a->fof1, c1}, {a->rl1, c1}, {a->skin1, c1}, {a->deep, c1},
+            {a->l1grid, (size_t)a->NG1}, {a->l2pl1, c2}, {a->l2oct, c2}, {a->nb1, c1 * 27}, {a->nb2, c2 * 27}};
+}
+bool fwrite_all(std::FILE* f, const void* p, size_t n) { return std::fwrite(p, 1, n, f) == n; }
+bool fread_all(std::FILE* f, void* p, size_t n) { return std::fread(p, 1, n, f) == n; }
+}  // namespace
+
+jp_status amr_save_state(jp_solver* s, std::FILE* f) {
+    AmrState* a = s->amr;
+    ACK(wait_stream(s), "save");
+    const int64_t h[16] = {a->cap1, a->cap2, a->cap_nref0, a->cap_nref1, a->nref0, a->nf1, a->nref1, a->nf2,
+                           a->n_skin0, a->n_skin1, a->ndeep, a->hw_nf1, a->hw_nf2, 0, 0, 0};
+    if (!fwrite_all(f, h, sizeof h)) return fail(JP_ERR_INVALID, "write failed");
+    std::vector<int> buf;
+    for (const TableRef& t : state_tables(a)) {
+        buf.resize(t.n);
+        ACK(cudaMemcpy(buf.data(), t.p, sizeof(int) * t.n, cudaMemcpyDeviceToHost), "table D2H");
+        if (!fwrite_all(f, buf.data(), sizeof(int) * t.n)) return fail(JP_ERR_INVALID, "write failed");
+    }
+    const size_t blk = (size_t)Q * a->MB3 * a->elem;
+    const std::pair<const void*, size_t> pools[3] = {{a->c0a, (size_t)a->cnb0 * blk}, {a->f1a, (size_t)a->nf1 * blk},
+                                                     {a->f2a, (size_t)a->nf2 * blk}};
+    std::vector<unsigned char> raw;
+    for (const auto& pl : pools) {
+        raw.resize(pl.second);
+        if (pl.second) ACK(cudaMemcpy(raw.data(), pl.first, pl.second, cudaMemcpyDeviceToHost), "pool D2H");
+        if (!fwrite_all(f, raw.data(), pl.second)) return fail(JP_ERR_INVALID, "write failed");
+    }
+    return JP_OK;
+}
+
+jp_status amr_load_state(jp_solver* s, std::FILE* f) {
+    AmrState* a = s->amr;
+    int64_t h[16];
+    if (!fread_all(f, h, sizeof h)) return fail(JP_ERR_INVALID, "state file truncated");
+    if (h[0] < 8 || h[1] < 8 || h[5] < 0 || h[5] > h[0] || h[7] < 0 || h[7] > h[1] || h[8] > a->cnb0 || h[9] > h[0])
+        return fail(JP_ERR_INVALID, "state file: inconsistent block counts");
+    ACK(wait_stream(s), "load");
+    if (h[0] != a->cap1) TRY(set_cap1(s, (int)h[0], false));
+    if (h[1] != a->cap2) TRY(set_cap2(s, (int)h[1], false));
+    a->cap_nref0 = (int)h[2];
+    a->cap_nref1 = (int)h[3];
+    a->nref0 = (int)h[4];
+    a->nf1 = (int)h[5];
+    a->nref1 = (int)h[6];
+    a->nf2 = (int)h[7];
+    a->n_skin0 = (int)h[8];
+    a->n_skin1 = (int)h[9];
+    a->ndeep = (int)h[10];
+    a->hw_nf1 = h[11];
+    a->hw_nf2 = h[12];
+    std::vector<int> buf;
+    for (const TableRef& t : state_tables(a)) {
+        buf.resize(t.n);
+        if (!fread_all(f, buf.data(), sizeof(int) * t.n)) return fail(JP_ERR_INVALID, "state file truncated");
+        ACK(cudaMemcpy(t.p, buf.data(), sizeof(int) * t.n, cudaMemcpyHostToDevice), "table H2D");
+    }
+    const size_t blk = (size_t)Q * a->MB3 * a->elem;
+    const std::pair<void*, size_t> pools[3] = {{a->c0a, (size_t)a->cnb0 * blk}, {a->f1a, (size_t)a->nf1 * blk},
+                                               {a->f2a, (size_t)a->nf2 * blk}};
+    std::vector<unsigned char> raw;
+    for (const auto& pl : pools) {
+        raw.resize(pl.second);
+        if (!fread_all(f, raw.data(), pl.second)) return fail(JP_ERR_INVALID, "state file truncated");
+        if (pl.second) ACK(cudaMemcpy(pl.first, raw.data(), pl.second, cudaMemcpyHostToDevice), "pool H2D");
+    }
+    TRY(upload_counts(s));
+    ACK(wait_stream(s), "load");
+    reset_graphs(a);
+    update_bytes(s);
     return JP_OK;
 }
 

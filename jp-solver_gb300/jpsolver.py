@@ -118,6 +118,8 @@ SIGNATURES = {
     "jp_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "jp_host_free": (None, [C.c_void_p]),
     "jp_step_timed": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
+    "jp_save_state": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "jp_load_state": (C.c_int, [C.c_void_p, C.c_char_p]),
     "jp_launch_count": (C.c_int64, []),
     "jp_regrid": (C.c_int, [C.c_void_p]),
     "jp_autotune": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(C.c_double)]),
@@ -228,6 +230,14 @@ class Solver:
 
     def sync(self) -> None:
         _check(lib().jp_sync(self.h))
+
+    def save_state(self, path: str) -> None:
+        """Write the solve's state to a file (jp_save_state)."""
+        _check(lib().jp_save_state(self.h, str(path).encode()))
+
+    def load_state(self, path: str) -> None:
+        """Continue from a state file written by a solver of the same configuration (jp_load_state)."""
+        _check(lib().jp_load_state(self.h, str(path).encode()))
 
     def step_timed(self, n: int) -> float:
         ms = C.c_float()
