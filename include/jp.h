@@ -76,7 +76,9 @@ typedef struct jp_config {
     int32_t threads_per_block; /* 0 = default; uniform: 64..512; AMR steps: 64 (MB=4), 128/256/512 */
     int32_t vec;             /* cells per thread along x in the uniform step; 0 = tuned default */
     int32_t flags;           /* JP_FLAG_* */
-    int32_t reserved[7];
+    int32_t buffer;          /* AMR sensor modes: dilate the refinement marks by this many block layers
+                                (--buffer; parsed but unused by the reference, src/tgv3d_amr.cu:648) */
+    int32_t reserved[6];
 } jp_config;
 
 /* jp_config.flags */

@@ -325,6 +325,38 @@ cudaError_t adapt_skins(const int* ref0, int cnb0, int cgx, const int* ref1, con
     note_launch(2);
     return cudaGetLastError();
 }
+// One layer of refinement-mark dilation (--buffer): out[b] = in[b] or a mark on any of the 26
+// neighbours (periodic).  Level 0 (pos == nullptr): the coarse grid of gx^3 blocks.  Level 1: the
+// neighbours through the level-1 grid map, and only deep blocks take marks (2:1 balance).
+__global__ void k_dilate_marks(const int* __restrict__ in, int* __restrict__ out, int n, int gx,
+                               const int* __restrict__ pos, const int* __restrict__ grid,
+                               const int* __restrict__ deep) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const int p = pos ? pos[b] : b;
+    const int px = p % gx, py = (p / gx) % gx, pz = p / (gx * gx);
+    int f = in[b] != 0;
+    for (int c = 0; c < 27 && !f; ++c) {
+        const int nx = (px + c % 3 - 1 + gx) % gx, ny = (py + (c / 3) % 3 - 1 + gx) % gx, nz = (pz + c / 9 - 1 + gx) % gx;
+        const int q = (nz * gx + ny) * gx + nx;
+        const int nb = grid ? grid[q] : q;
+        f = nb >= 0 && in[nb] != 0;
+    }
+    out[b] = (deep && !deep[b]) ? 0 : f;
+}
+
+cudaError_t adapt_dilate_marks(int* ref, int* tmp, int n, int gx, const int* pos, const int* grid, const int* deep,
+                               int layers, cudaStream_t st) {
+    if (n <= 0 || layers <= 0) return cudaSuccess;
+    for (int l = 0; l < layers; ++l) {
+        k_dilate_marks<<<grid_for(n, 256), 256, 0, st>>>(ref, tmp, n, gx, pos, grid, deep);
+        cudaError_t e = cudaMemcpyAsync(ref, tmp, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
+        note_launch();
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t adapt_fill(int* p, int v, long long n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     const unsigned g = (unsigned)std::min<long long>(grid_for(n, 256), 4096);

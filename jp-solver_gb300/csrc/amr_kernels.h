@@ -117,6 +117,10 @@ cudaError_t adapt_skins(const int* ref0, int cnb0, int cgx, const int* ref1, con
                         int nf1, int l1gx, int* flags, int* skin0, int* skin1, AdaptCounts* counts, cudaStream_t st);
 // set n ints to v
 cudaError_t adapt_fill(int* p, int v, long long n, cudaStream_t st);
+// dilate refinement marks by `layers` block layers (tmp: n ints of scratch); level 1 with the
+// position map pos, the grid map and the deep mask (marks only on deep blocks)
+cudaError_t adapt_dilate_marks(int* ref, int* tmp, int n, int gx, const int* pos, const int* grid, const int* deep,
+                               int layers, cudaStream_t st);
 
 }  // namespace amr
 }  // namespace jp

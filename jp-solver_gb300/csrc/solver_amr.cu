@@ -197,6 +197,17 @@ static jp_status mark_l0_by_sensor(jp_solver* s) {
     TRY(sensor(s, 0));
     ACK(adapt_threshold_mark(a->sen0, nullptr, a->cnb0, s->cfg.frac1, a->cap_nref0, a->ref0, a->cnt_dev, 0, s->stream),
         "threshold L0");
+    // --buffer: a margin of refined blocks around the marked ones (compaction for localised features)
+    ACK(adapt_dilate_marks(a->ref0, a->flags, a->cnb0, a->cgx, nullptr, nullptr, nullptr, s->cfg.buffer, s->stream),
+        "buffer L0");
+    return JP_OK;
+}
+
+// --buffer on level 1: dilate the level-2 marks over the level-1 grid, deep blocks only
+static jp_status buffer_l1(jp_solver* s) {
+    AmrState* a = s->amr;
+    ACK(adapt_dilate_marks(a->ref1, a->flags, a->nf1, a->l1gx, a->f1pos, a->l1grid, a->deep, s->cfg.buffer, s->stream),
+        "buffer L1");
     return JP_OK;
 }
 
@@ -372,6 +383,7 @@ static jp_status initial_build(jp_solver* s) {
         } else {
             ACK(adapt_threshold_mark(a->sen1, a->deep, a->nf1, c.frac2, INT_MAX, a->ref1, a->cnt_dev, 1, s->stream),
                 "threshold L1");
+            TRY(buffer_l1(s));
         }
         ACK(adapt_scan_l2(a->ref1, a->nf1, a->rank, a->cnt_dev, s->stream), "scan L2");
         TRY(read_counts(s));
@@ -460,6 +472,7 @@ static jp_status regrid(jp_solver* s) {
         ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * a->cap1, s->stream), "memset ref1");
         ACK(adapt_threshold_mark(a->sen1, a->deep, a->nf1, c.frac2, a->cap_nref1, a->ref1, a->cnt_dev, 1, s->stream),
             "threshold L1");
+        TRY(buffer_l1(s));
         ACK(adapt_scan_l2(a->ref1, a->nf1, a->rank, a->cnt_dev, s->stream), "scan L2");
         TRY(read_counts(s));
         a->nref1 = a->cnt_host->nref1;

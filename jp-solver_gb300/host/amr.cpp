@@ -1,6 +1,7 @@
 // `amr`: drop-in for the reference's three-level AMR Taylor-Green program (src/tgv3d_amr.cu:643-907),
 // driving the GB300 engine through the C ABI.  Same flags and defaults (including --adapt, --maxgb,
-// --graph, --skipprep, --skiprestr, --bench and the parsed-but-unused --buffer), same stdout lines,
+// --graph, --skipprep, --skiprestr, --bench and --buffer, which the reference parses and this
+// program implements: sensor marks dilated by that many block layers; 0 by default), same stdout lines,
 // exit codes and .vti/.vtp frames.  Additions: --prec fp32|fp16|bf16 (population storage), --mb,
 // --tpb (threads per CTA of the level steps), --develop, --device, --autotune 1 (MB x threads per
 // CTA), --diag-every.
@@ -51,8 +52,7 @@ int main(int argc, char** argv) {
     const double Re = argd(argc, argv, "--re", 800.0), u0 = argd(argc, argv, "--u0", 0.05);
     const double tstar = argd(argc, argv, "--tstar", 12.0);
     const double frac1 = argd(argc, argv, "--frac1", 0.35), frac2 = argd(argc, argv, "--frac2", 0.35);
-    const int buffer = argi(argc, argv, "--buffer", 0);  // parsed, unused (as src/tgv3d_amr.cu:648)
-    (void)buffer;
+    const int buffer = argi(argc, argv, "--buffer", 0);  // mark dilation in block layers (src/tgv3d_amr.cu:648)
     const char* l1mode = args(argc, argv, "--l1", "all");
     const char* l2mode = args(argc, argv, "--l2", "all");
     const char* vtk = args(argc, argv, "--vtk", nullptr);
@@ -82,6 +82,7 @@ int main(int argc, char** argv) {
     cfg.max_gb = argd(argc, argv, "--maxgb", 0.0);
     cfg.mb = MBarg;
     cfg.develop_steps = argi(argc, argv, "--develop", 300);
+    cfg.buffer = buffer;
     cfg.device = argi(argc, argv, "--device", 0);
     cfg.threads_per_block = argi(argc, argv, "--tpb", 0);
     cfg.storage = storage_of(args(argc, argv, "--prec", "fp32"));

@@ -38,7 +38,7 @@ class Config(C.Structure):
         ("adapt_every", C.c_int32), ("develop_steps", C.c_int32),
         ("max_gb", C.c_double),
         ("device", C.c_int32), ("threads_per_block", C.c_int32), ("vec", C.c_int32),
-        ("flags", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("flags", C.c_int32), ("buffer", C.c_int32), ("reserved", C.c_int32 * 6),
     ]
 
 

@@ -338,3 +338,39 @@ def test_shifted_storage_static_gold_holds_mass(storage):
     assert abs(r16[0] - r32[0]) < (2e-4 if storage == "fp16" else 3e-3)
     assert r16[1] < (1e-6 if storage == "fp16" else 1e-5)
     np.testing.assert_array_equal(r16[2], r16g[2])
+
+
+def _dilate(mask, gx):
+    """One 26-neighbour periodic dilation layer of a block mask on a gx^3 grid (x fastest)."""
+    m = mask.reshape(gx, gx, gx).astype(bool)
+    out = m.copy()
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                out |= np.roll(m, (dz, dy, dx), axis=(0, 1, 2))
+    return out.reshape(-1).astype(np.int32)
+
+
+@pytest.mark.parametrize("layers", [1, 2])
+def test_buffer_dilates_the_sensor_marks(layers):
+    # --buffer N (parsed but unused by the reference): the refined coarse blocks are the sensor
+    # marks dilated by N layers; level-2 marks grow only into deep level-1 blocks (2:1 balance)
+    n = 48
+    s0, s1 = O.random_sensor_fields(n, seed=8)
+    res = {}
+    for b in (0, layers):
+        with J.Solver("amr", n=n, re=800.0, l1_mode="sensor", l2_mode="sensor", frac1=0.1, frac2=0.1,
+                      develop_steps=2, max_gb=64.0, buffer=b) as e:
+            e.set_sensor_override(s0, s1)
+            e.init_tgv()
+            res[b] = {t: e.table(t) for t in ("ref0", "ref1", "deep", "f1pos")}
+            res[b]["counts"] = e.counts()
+    ref0, cgx = res[0]["ref0"], n // 8
+    want = ref0
+    for _ in range(layers):
+        want = _dilate(want, cgx)
+    np.testing.assert_array_equal(res[layers]["ref0"], want)
+    assert res[layers]["counts"]["nf1"] > res[0]["counts"]["nf1"]
+    r1, deep = res[layers]["ref1"], res[layers]["deep"]
+    assert np.all(r1[deep == 0] == 0)                  # level-2 marks only on deep blocks
+    assert res[layers]["counts"]["nref1"] >= res[0]["counts"]["nref1"]
