@@ -38,6 +38,9 @@ bool can_fuse_restrict(int mb) { return mb <= 8; }
 // measured on the GB300 (static gold N0=64, all levels refined): 256 threads (two cells each) are
 // the fastest split at MB = 8, 512 at MB = 16
 int default_step_tpb(int mb) { return mb == 4 ? 64 : (mb == 8 ? 256 : 512); }
+// rows of four cells per thread where the block has them (MB >= 8)
+int default_step_vec(int mb) { return mb >= 8 ? 4 : 1; }
+bool step_vec_supported(int mb, int vec) { return vec == 1 || (vec == 4 && mb >= 8); }
 bool step_tpb_supported(int mb, int tpb) {
     if (mb == 4) return tpb == 64;
     return (mb == 8 || mb == 16) && (tpb == 128 || tpb == 256 || tpb == 512);

@@ -343,6 +343,126 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_fine(const typename ST
     d_step_fine<MB, ST, TPB, FUSE>(fa, fbuf, gh, nbtab, parent, poct, om, parent_pool, nqi, nlim, (int)blockIdx.x);
 }
 
+// ---- fine step on rows of four cells -----------------------------------------------------------------
+// The same step as d_step_fine with a thread on four consecutive cells of a block row (MB = 8: two
+// threads per row, 128 per block; MB = 16: four per row, 256 threads looping over the block).  For
+// each population the source row (j - c_y, k - c_z) is read as one vector from the block or the
+// neighbour block that holds it, or from the ghost shell, whose y/z faces and yz edges are contiguous
+// in x.  The value a +-x pull needs from outside the four cells comes from the neighbouring thread of
+// the row by a warp shuffle, or, at the block's x faces, from the x-neighbour block (or its ghost
+// cells).  Per-cell arithmetic is d_step_fine's, so the results are the same bits.
+template <class ST>
+struct Vec4 {  // four stored values, one 16-byte (FP32) or 8-byte (16-bit) access
+    using raw = typename ST::raw;
+    using word = typename std::conditional<sizeof(raw) == 4, uint4, uint2>::type;
+    union {
+        word w;
+        raw v[4];
+    };
+    __device__ __forceinline__ void load(const raw* p) { w = __ldg(reinterpret_cast<const word*>(p)); }
+    __device__ __forceinline__ void store(raw* p) const { __stcs(reinterpret_cast<word*>(p), w); }
+};
+template <class RAW> __device__ __forceinline__ RAW shfl_by(RAW v, int d) {
+    return d > 0 ? __shfl_down_sync(0xffffffffu, v, d) : __shfl_up_sync(0xffffffffu, v, -d);
+}
+template <> __device__ __forceinline__ uint16_t shfl_by<uint16_t>(uint16_t v, int d) {
+    const unsigned u = v;
+    return (uint16_t)(d > 0 ? __shfl_down_sync(0xffffffffu, u, d) : __shfl_up_sync(0xffffffffu, u, -d));
+}
+
+template <int MB>
+struct RowGeo {
+    static constexpr int SPR = MB / 4;                           // threads (segments) per row
+    static constexpr int SEGS = MB * MB * SPR;                   // segments per block
+    static constexpr int TPB = SEGS < 256 ? SEGS : 256;          // threads per CTA
+};
+
+template <int MB, class ST, bool FUSE>
+__device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restrict__ fa,
+                                                 typename ST::raw* __restrict__ fbuf,
+                                                 const typename ST::raw* __restrict__ gh,
+                                                 const int* __restrict__ nbtab, const int* __restrict__ parent,
+                                                 const int* __restrict__ poct, float om,
+                                                 typename ST::raw* __restrict__ parent_pool, float nqi,
+                                                 const int* __restrict__ nlim, int blk) {
+    using G = Geo<MB>;
+    using RG = RowGeo<MB>;
+    using raw = typename ST::raw;
+    constexpr int M = MB - 1, MB3 = G::MB3, SH = G::SH;
+    static_assert(MB % 4 == 0 && 32 % RG::SPR == 0 && RG::SEGS % RG::TPB == 0, "row mapping");
+    extern __shared__ float sf[];
+    if (nlim && (int)blk >= __ldg(nlim)) return;  // whole CTA
+    const int b = blk;
+    const int* nbrow = nbtab + (size_t)b * 27;
+    for (int seg = threadIdx.x; seg < RG::SEGS; seg += RG::TPB) {
+        const int s = seg % RG::SPR, r = seg / RG::SPR, j = r % MB, k = r / MB, i0 = 4 * s;
+        float f[4][Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int lj = j - cy(q), lk = k - cz(q);
+            const int ey = cy(q) > 0 ? (lj < 0 ? 0 : 1) : (cy(q) < 0 ? (lj > M ? 2 : 1) : 1);
+            const int ez = cz(q) > 0 ? (lk < 0 ? 0 : 1) : (cz(q) < 0 ? (lk > M ? 2 : 1) : 1);
+            const int erow = ez * 9 + ey * 3 + 1;
+            const int rb = erow == 13 ? b : __ldg(nbrow + erow);
+            const int rowc = ((lk & M) * MB + (lj & M)) * MB;  // cell of the row's x = 0 in its block
+            Vec4<ST> L;
+            if (rb >= 0) {
+                L.load(fa + ((size_t)rb * Q + q) * MB3 + rowc + i0);
+            } else {  // a y/z face or yz edge of the ghost shell: contiguous in x
+                const int base = (ey != 1 && ez != 1)
+                                     ? 6 * MB * MB + ((lj < 0 ? 0 : 1) + 2 * (lk < 0 ? 0 : 1)) * MB
+                                     : (ey != 1 ? (lj < 0 ? 2 : 3) * MB * MB + lk * MB : (lk < 0 ? 4 : 5) * MB * MB + lj * MB);
+                L.load(gh + ((size_t)b * Q + q) * SH + base + i0);
+            }
+            raw E = raw(0);
+            if (cx(q) != 0) {
+                // the row's neighbouring thread (all lanes take part in the shuffle)
+                const raw nb = cx(q) > 0 ? shfl_by<raw>(L.v[3], -1) : shfl_by<raw>(L.v[0], 1);
+                const bool at_face = cx(q) > 0 ? s == 0 : s == RG::SPR - 1;
+                if (!at_face) {
+                    E = nb;
+                } else {  // x-neighbour block (slot ex = 0 or 2), or the ghost shell
+                    const int e = ez * 9 + ey * 3 + (cx(q) > 0 ? 0 : 2);
+                    const int eb = __ldg(nbrow + e);
+                    const int li = cx(q) > 0 ? -1 : MB;
+                    E = eb >= 0 ? __ldg(fa + ((size_t)eb * Q + q) * MB3 + rowc + (li & M))
+                                : __ldg(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(li, lj, lk));
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const raw x = cx(q) > 0 ? (v == 0 ? E : L.v[v - 1]) : (cx(q) < 0 ? (v == 3 ? E : L.v[v + 1]) : L.v[v]);
+                f[v][q] = ST::load(x);
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < 4; ++v) bgk_fast<ST::shifted>(f[v], om);
+        const int cell0 = (k * MB + j) * MB + i0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            Vec4<ST> o;
+#pragma unroll
+            for (int v = 0; v < 4; ++v) o.v[v] = ST::store(f[v][q]);
+            o.store(fbuf + ((size_t)b * Q + q) * MB3 + cell0);
+            if (FUSE) {  // the restriction works on unshifted populations of the values as stored
+#pragma unroll
+                for (int v = 0; v < 4; ++v) sf[q * MB3 + cell0 + v] = ST::shifted ? wf(q) + ST::load(o.v[v]) : f[v][q];
+            }
+        }
+    }
+    if (FUSE) {
+        __syncthreads();
+        restrict_octant<MB, ST>(sf, parent_pool + (size_t)parent[b] * Q * G::MB3, poct[b], nqi);
+    }
+}
+template <int MB, class ST, bool FUSE>
+__global__ void __launch_bounds__(RowGeo<MB>::TPB, 512 / RowGeo<MB>::TPB) k_step_fine_rows(
+    const typename ST::raw* __restrict__ fa, typename ST::raw* __restrict__ fbuf, const typename ST::raw* __restrict__ gh,
+    const int* __restrict__ nbtab, const int* __restrict__ parent, const int* __restrict__ poct, float om,
+    typename ST::raw* __restrict__ parent_pool, float nqi, const int* __restrict__ nlim) {
+    d_step_fine_rows<MB, ST, FUSE>(fa, fbuf, gh, nbtab, parent, poct, om, parent_pool, nqi, nlim, (int)blockIdx.x);
+}
+
 // ---- restriction (src/tgv3d_amr.cu:275-298, 357-381) -------------------------------------------------
 // One CTA per refined parent block; each parent cell becomes feq + nqi*regularize(avg - feq) of the
 // average of its 8 children (summed in the reference's dk, dj, di order).
@@ -624,6 +744,19 @@ static void launch_steps(const AmrLaunch& L, int op) {
                                                                  parent, L.t1, L.omega, nullptr, 0.f, L.nlim);
 }
 
+// the fine steps on rows of four cells (MB = 8, 16)
+template <int MB, class ST>
+static void launch_rows(const AmrLaunch& L) {
+    using G = Geo<MB>;
+    constexpr int T = RowGeo<MB>::TPB;
+    if (L.out2)
+        k_step_fine_rows<MB, ST, true><<<L.nblocks, T, sizeof(float) * Q * G::MB3, L.st>>>(
+            CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.t0, L.t1, L.omega, POOL(L.out2), L.scale, L.nlim);
+    else
+        k_step_fine_rows<MB, ST, false><<<L.nblocks, T, 0, L.st>>>(CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt,
+                                                                    L.t0, L.t1, L.omega, nullptr, 0.f, L.nlim);
+}
+
 template <int MB, class ST>
 static cudaError_t dispatch(const AmrLaunch& L, int op) {
     using G = Geo<MB>;
@@ -640,6 +773,14 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
             if constexpr (MB == 4) {
                 if (tpb != 64) return cudaErrorInvalidConfiguration;
                 launch_steps<MB, ST, 64>(L, op);
+            } else if (op != OP_STEP_L0 && (L.vec ? L.vec : default_step_vec(MB)) == 4) {
+                // fused restriction with rows: the shared staging is sized for MB <= 8
+                if (L.out2 && MB > 8) return cudaErrorInvalidConfiguration;
+                if constexpr (MB <= 8) launch_rows<MB, ST>(L);
+                else {
+                    if (L.out2) return cudaErrorInvalidConfiguration;
+                    launch_rows<MB, ST>(L);
+                }
             } else {
                 if (tpb == 128) launch_steps<MB, ST, 128>(L, op);
                 else if (tpb == 256) launch_steps<MB, ST, 256>(L, op);
@@ -709,6 +850,15 @@ __device__ __forceinline__ int batch_member(const AmrBatch& B) {
     return lo;
 }
 
+template <int MB, class ST, bool FUSE>
+__global__ void __launch_bounds__(RowGeo<MB>::TPB, 512 / RowGeo<MB>::TPB) kb_step_rows(const __grid_constant__ AmrBatch B) {
+    const AmrItem& it = B.it[batch_member(B)];
+    const int blk = (int)blockIdx.x - it.begin;
+    using raw = typename ST::raw;
+    d_step_fine_rows<MB, ST, FUSE>((const raw*)it.in, (raw*)it.out, (const raw*)it.aux, it.nbt, it.t0, it.t1, it.omega,
+                                   (raw*)it.out2, it.scale, it.nlim, blk);
+}
+
 template <int MB, class ST, int TPB, bool FUSE, bool L0>
 __global__ void __launch_bounds__(TPB, 1024 / TPB) kb_step(const __grid_constant__ AmrBatch B) {
     const AmrItem& it = B.it[batch_member(B)];
@@ -757,6 +907,9 @@ static void batch_steps(int op, bool fuse, const AmrBatch& B, cudaStream_t st) {
 }
 
 template <int MB, class ST>
+static void batch_rows(bool fuse, const AmrBatch& B, cudaStream_t st);
+
+template <int MB, class ST>
 static cudaError_t batch_dispatch(int op, int tpb, bool fuse, const AmrBatch& B, cudaStream_t st) {
     using G = Geo<MB>;
     const dim3 cta(G::TPB);
@@ -769,6 +922,9 @@ static cudaError_t batch_dispatch(int op, int tpb, bool fuse, const AmrBatch& B,
             if constexpr (MB == 4) {
                 if (t != 64) return cudaErrorInvalidConfiguration;
                 batch_steps<MB, ST, 64>(op, fuse, B, st);
+            } else if (op != OP_STEP_L0 && (B.vec ? B.vec : default_step_vec(MB)) == 4) {
+                if (fuse && MB > 8) return cudaErrorInvalidConfiguration;
+                batch_rows<MB, ST>(fuse, B, st);
             } else {
                 if (t == 128) batch_steps<MB, ST, 128>(op, fuse, B, st);
                 else if (t == 256) batch_steps<MB, ST, 256>(op, fuse, B, st);
@@ -785,6 +941,19 @@ static cudaError_t batch_dispatch(int op, int tpb, bool fuse, const AmrBatch& B,
     }
     note_launch();
     return cudaGetLastError();
+}
+
+template <int MB, class ST>
+static void batch_rows(bool fuse, const AmrBatch& B, cudaStream_t st) {
+    using G = Geo<MB>;
+    constexpr int T = RowGeo<MB>::TPB;
+    if constexpr (MB <= 8) {
+        if (fuse) {
+            kb_step_rows<MB, ST, true><<<B.total, T, sizeof(float) * Q * G::MB3, st>>>(B);
+            return;
+        }
+    }
+    kb_step_rows<MB, ST, false><<<B.total, T, 0, st>>>(B);
 }
 
 template <class ST>

@@ -38,7 +38,9 @@ struct AmrLaunch {
     const int *t0 = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr, *t6 = nullptr;
     const int* nbt = nullptr;  // same-level neighbour table of the fine level (27 per block)
     int* iout = nullptr;
-    int tpb = 0;               // threads per CTA of the steps (0: default_step_tpb)
+    int tpb = 0;               // threads per CTA of the per-cell fine steps (0: default_step_tpb)
+    int vec = 0;               // fine steps: 4 = rows of four cells per thread, 1 = a cell per thread
+                               // (0: default_step_vec)
     // device count of the blocks to process (prep, fill, fine step, restrict): the grid is sized
     // for the capacity and CTAs past *nlim return, so a captured step stays valid after a regrid
     const int* nlim = nullptr;
@@ -66,6 +68,7 @@ constexpr int kAmrBatchMax = 48;
 // parameter space.
 struct AmrBatch {
     int count = 0, total = 0;  // members, CTAs
+    int vec = 0, pad = 0;      // fine-step mapping as AmrLaunch::vec
     AmrItem it[kAmrBatchMax];
 };
 
@@ -83,6 +86,9 @@ bool can_fuse_restrict(int mb);
 // threads per CTA a step of block edge mb can run with, and the default
 bool step_tpb_supported(int mb, int tpb);
 int default_step_tpb(int mb);
+// cells per thread of the fine steps: 4 (rows, MB = 8 and 16) or 1
+bool step_vec_supported(int mb, int vec);
+int default_step_vec(int mb);
 
 // ---- adaptation pipeline (adapt.cu) ------------------------------------------------------------
 // Device counters shared by the pipeline; the host reads them once per stage.

@@ -53,12 +53,13 @@ extern "C" jp_status jp_autotune(jp_config* cfg, int32_t steps, double* best) {
     // AMR: block edges that divide n x threads per CTA of the level steps; work-normalised
     // throughput of the 1:2:4 step on the grid each edge builds
     const int mbs[3] = {4, 8, 16};
-    int bmb = cfg->mb, btpb = cfg->threads_per_block;
+    int bmb = cfg->mb, btpb = cfg->threads_per_block, bvec = cfg->vec;
     for (int mb : mbs) {
         if (cfg->n % mb) continue;
         jp_config c = *cfg;
         c.mb = mb;
         c.threads_per_block = 0;
+        c.vec = 0;
         jp_solver* s = nullptr;
         jp_status st = jp_create(&c, &s);
         if (st == JP_ERR_NOMEM || st == JP_ERR_CAPACITY) continue;
@@ -66,10 +67,13 @@ extern "C" jp_status jp_autotune(jp_config* cfg, int32_t steps, double* best) {
         jp_amr_counts k;
         st = jp_amr_get_counts(s, &k);
         const double work = (double(k.cnb0) + 2.0 * k.nf1 + 4.0 * k.nf2) * double(mb) * mb * mb * steps;
-        const int tpbs[3] = {128, 256, 512};
-        for (int t : (mb == 4 ? std::vector<int>{64} : std::vector<int>(tpbs, tpbs + 3))) {
+        // candidates: rows of four cells (vec 4, MB >= 8), then a cell per thread at each CTA size
+        std::vector<std::pair<int, int>> maps;
+        if (mb >= 8) maps.push_back({4, 0});
+        for (int t : (mb == 4 ? std::vector<int>{64} : std::vector<int>{128, 256, 512})) maps.push_back({1, t});
+        for (const auto& m : maps) {
             float ms = 0.f;
-            if (st == JP_OK) st = amr_set_step_tpb(s, t);
+            if (st == JP_OK) st = amr_set_step_map(s, m.first, m.second);
             if (st == JP_OK) st = jp_step(s, 1);
             if (st == JP_OK) st = jp_step_timed(s, steps, &ms);
             if (st != JP_OK) break;
@@ -77,7 +81,8 @@ extern "C" jp_status jp_autotune(jp_config* cfg, int32_t steps, double* best) {
             if (lups > *best) {
                 *best = lups;
                 bmb = mb;
-                btpb = t;
+                btpb = m.second;
+                bvec = m.first;
             }
         }
         jp_destroy(s);
@@ -85,5 +90,6 @@ extern "C" jp_status jp_autotune(jp_config* cfg, int32_t steps, double* best) {
     }
     cfg->mb = bmb;
     cfg->threads_per_block = btpb;
+    cfg->vec = bvec;
     return JP_OK;
 }

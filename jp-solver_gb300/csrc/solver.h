@@ -90,7 +90,8 @@ jp_status amr_population_count(const jp_solver* s, int level, int64_t* count);
 jp_status amr_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count);
 jp_status amr_set_populations(jp_solver* s, int level, int layout, int dtype, const void* host, int64_t count);
 jp_status amr_regrid(jp_solver* s);
-jp_status amr_set_step_tpb(jp_solver* s, int tpb);  // threads per CTA of the level steps (autotuner)
+// the fine steps' mapping: vec 4 (rows) or 1 (a cell per thread, tpb threads per CTA); autotuner
+jp_status amr_set_step_map(jp_solver* s, int vec, int tpb);
 // one coarse step of many AMR solvers, one launch per stage over all of them, on `st`
 jp_status amr_batch_step(const std::vector<jp_solver*>& members, cudaStream_t st);
 bool amr_batch_compatible(const jp_solver* a, const jp_solver* b);

@@ -40,7 +40,8 @@ struct AmrState {
     int *o_ref0 = nullptr, *o_fof0 = nullptr, *o_l1grid = nullptr, *o_ref1 = nullptr, *o_fof1 = nullptr;
     int *rank = nullptr, *deep = nullptr, *flags = nullptr;
     int *nb1 = nullptr, *nb2 = nullptr;  // same-level neighbour tables of the fine levels (27 per block)
-    int tpb = 0;                         // threads per CTA of the steps (0: default_step_tpb)
+    int tpb = 0;                         // threads per CTA of the per-cell steps (0: default_step_tpb)
+    int vec = 0;                         // fine steps: 4 rows of four cells, 1 a cell per thread (0: default)
     float *sen0 = nullptr, *sen1 = nullptr;
     float *ov_sen0 = nullptr, *ov_sen1pos = nullptr;
     AdaptCounts* cnt_dev = nullptr;
@@ -576,6 +577,7 @@ static jp_status base_step(jp_solver* s) {
             S.t1 = a->l2oct;
             S.omega = a->om2;
             S.tpb = a->tpb;
+            S.vec = a->vec;
             if (s2 == 1 && fuse) {  // last level-2 substep restricts itself into level 1
                 S.out2 = a->f1a;
                 S.scale = float(a->nqi21);
@@ -605,6 +607,7 @@ static jp_status base_step(jp_solver* s) {
         S.t1 = a->oct;
         S.omega = a->om1;
         S.tpb = a->tpb;
+        S.vec = a->vec;
         if (s1 == 1 && fuse) {  // last level-1 substep restricts itself into the coarse level
             S.out2 = a->c0a;
             S.scale = float(a->nqi10);
@@ -637,6 +640,7 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
     auto run = [&](int op, bool fused, auto fill) -> jp_status {
         for (size_t i0 = 0; i0 < ms.size(); i0 += kAmrBatchMax) {
             AmrBatch B;
+            B.vec = a0->vec;
             for (size_t i = i0; i < ms.size() && i < i0 + kAmrBatchMax; ++i) {
                 AmrItem& it = B.it[B.count];
                 std::memset(&it, 0, sizeof it);
@@ -770,7 +774,7 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
 bool amr_batch_compatible(const jp_solver* a, const jp_solver* b) {
     const int skip = JP_FLAG_SKIP_PREP | JP_FLAG_SKIP_RESTRICT;
     return a->amr->MB == b->amr->MB && a->amr->storage == b->amr->storage && a->amr->tpb == b->amr->tpb &&
-           (a->cfg.flags & skip) == (b->cfg.flags & skip);
+           a->amr->vec == b->amr->vec && (a->cfg.flags & skip) == (b->cfg.flags & skip);
 }
 
 // base_step replayed from a captured graph (captured on first use for each parity combination)
@@ -823,6 +827,8 @@ jp_status amr_create(jp_solver* s) {
     if (c.threads_per_block && !step_tpb_supported(c.mb, c.threads_per_block))
         return fail(JP_ERR_INVALID, "threads_per_block %d does not split a block of edge %d (MB=4: 64; 8, 16: 128, 256, 512)",
                     c.threads_per_block, c.mb);
+    if (c.vec && !step_vec_supported(c.mb, c.vec))
+        return fail(JP_ERR_INVALID, "vec %d: the AMR fine steps take 1 cell per thread, or 4 (rows) at MB >= 8", c.vec);
     AmrState* a = new (std::nothrow) AmrState();
     if (!a) return fail(JP_ERR_NOMEM, "host allocation");
     s->amr = a;
@@ -830,6 +836,7 @@ jp_status amr_create(jp_solver* s) {
     a->storage = c.storage;
     a->elem = storage_elem(c.storage);
     a->tpb = c.threads_per_block;
+    a->vec = c.vec;
     a->MB = c.mb;
     a->MB3 = c.mb * c.mb * c.mb;
     a->SH = shell_cells(c.mb);
@@ -942,11 +949,14 @@ jp_status amr_step(jp_solver* s, int64_t nsteps) {
     return JP_OK;
 }
 
-jp_status amr_set_step_tpb(jp_solver* s, int tpb) {
+jp_status amr_set_step_map(jp_solver* s, int vec, int tpb) {
     if (tpb && !step_tpb_supported(s->amr->MB, tpb)) return fail(JP_ERR_INVALID, "threads_per_block %d", tpb);
+    if (vec && !step_vec_supported(s->amr->MB, vec)) return fail(JP_ERR_INVALID, "vec %d", vec);
     reset_graphs(s->amr);
     s->amr->tpb = tpb;
+    s->amr->vec = vec;
     s->cfg.threads_per_block = tpb;
+    s->cfg.vec = vec;
     return JP_OK;
 }
 

@@ -374,3 +374,22 @@ def test_buffer_dilates_the_sensor_marks(layers):
     r1, deep = res[layers]["ref1"], res[layers]["deep"]
     assert np.all(r1[deep == 0] == 0)                  # level-2 marks only on deep blocks
     assert res[layers]["counts"]["nref1"] >= res[0]["counts"]["nref1"]
+
+
+@pytest.mark.parametrize("mb,storage", [(8, "fp32"), (8, "fp16"), (16, "fp32"), (16, "bf16")])
+def test_row_steps_bit_exact_with_cell_steps(mb, storage):
+    # the fine steps on rows of four cells per thread (vector loads, shuffles at the row inside, the
+    # x-neighbour block or ghost shell at the faces) compute each cell as the per-cell steps do:
+    # same bits, on a grid with ghost shells on both fine levels and the fused restriction
+    n = 32
+    s0, s1 = O.random_sensor_fields(n, mb=mb, seed=12)
+    out = {}
+    for vec in (1, 4):
+        with J.Solver("amr", n=n, re=1600.0, l1_mode="sensor", l2_mode="sensor", frac1=0.35, frac2=0.4,
+                      develop_steps=2, max_gb=64.0, mb=mb, storage=storage, vec=vec) as e:
+            e.set_sensor_override(s0, s1)
+            e.init_tgv()
+            e.step(3)
+            out[vec] = [e.get_populations(lv, layout="blocked") for lv in range(3)]
+    for lv in range(3):
+        np.testing.assert_array_equal(out[4][lv], out[1][lv], err_msg="level %d" % lv)
