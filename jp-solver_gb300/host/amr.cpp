@@ -3,8 +3,8 @@
 // --graph, --skipprep, --skiprestr, --bench and --buffer, which the reference parses and this
 // program implements: sensor marks dilated by that many block layers; 0 by default), same stdout lines,
 // exit codes and .vti/.vtp frames.  Additions: --prec fp32|fp16|bf16 (population storage), --mb,
-// --tpb (threads per CTA of the level steps), --develop, --device, --autotune 1 (MB x threads per
-// CTA), --diag-every.
+// --vec (fine steps: 4 = rows of four cells per thread, 1 = a cell per thread), --tpb (threads per
+// CTA of the per-cell steps), --develop, --device, --autotune 1 (MB x step mapping), --diag-every.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -85,12 +85,14 @@ int main(int argc, char** argv) {
     cfg.buffer = buffer;
     cfg.device = argi(argc, argv, "--device", 0);
     cfg.threads_per_block = argi(argc, argv, "--tpb", 0);
+    cfg.vec = argi(argc, argv, "--vec", 0);
     cfg.storage = storage_of(args(argc, argv, "--prec", "fp32"));
     cfg.flags = (skipprep ? JP_FLAG_SKIP_PREP : 0) | (skiprestr ? JP_FLAG_SKIP_RESTRICT : 0) | (usegraph ? JP_FLAG_GRAPH : 0);
     if (argd(argc, argv, "--autotune", 0.0) > 0.5) {
         double best = 0.0;
         ck(jp_autotune(&cfg, 4, &best), "autotune");
-        std::printf("[autotune] MB=%d threads/block=%d  %.1f MLUPS(work)\n", cfg.mb, cfg.threads_per_block, best / 1e6);
+        std::printf("[autotune] MB=%d vec=%d threads/block=%d  %.1f MLUPS(work)\n", cfg.mb, cfg.vec, cfg.threads_per_block,
+                    best / 1e6);
     }
     const int MB = cfg.mb;  // the block edge in use (--mb, or the autotuner's pick)
     jp_solver* s = nullptr;
