@@ -396,7 +396,10 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
     const int* nbrow = nbtab + (size_t)b * 27;
     for (int seg = threadIdx.x; seg < RG::SEGS; seg += RG::TPB) {
         const int s = seg % RG::SPR, r = seg / RG::SPR, j = r % MB, k = r / MB, i0 = 4 * s;
-        float f[4][Q];
+        // 1. issue every load: 19 row vectors, and at the block's x faces the one value of each
+        //    +-x population from the x-neighbour block or the ghost shell
+        Vec4<ST> L[Q];
+        raw E[Q];
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const int lj = j - cy(q), lk = k - cz(q);
@@ -405,36 +408,39 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
             const int erow = ez * 9 + ey * 3 + 1;
             const int rb = erow == 13 ? b : __ldg(nbrow + erow);
             const int rowc = ((lk & M) * MB + (lj & M)) * MB;  // cell of the row's x = 0 in its block
-            Vec4<ST> L;
             if (rb >= 0) {
-                L.load(fa + ((size_t)rb * Q + q) * MB3 + rowc + i0);
+                L[q].load(fa + ((size_t)rb * Q + q) * MB3 + rowc + i0);
             } else {  // a y/z face or yz edge of the ghost shell: contiguous in x
                 const int base = (ey != 1 && ez != 1)
                                      ? 6 * MB * MB + ((lj < 0 ? 0 : 1) + 2 * (lk < 0 ? 0 : 1)) * MB
                                      : (ey != 1 ? (lj < 0 ? 2 : 3) * MB * MB + lk * MB : (lk < 0 ? 4 : 5) * MB * MB + lj * MB);
-                L.load(gh + ((size_t)b * Q + q) * SH + base + i0);
+                L[q].load(gh + ((size_t)b * Q + q) * SH + base + i0);
             }
-            raw E = raw(0);
-            if (cx(q) != 0) {
-                // the row's neighbouring thread (all lanes take part in the shuffle)
-                const raw nb = cx(q) > 0 ? shfl_by<raw>(L.v[3], -1) : shfl_by<raw>(L.v[0], 1);
-                const bool at_face = cx(q) > 0 ? s == 0 : s == RG::SPR - 1;
-                if (!at_face) {
-                    E = nb;
-                } else {  // x-neighbour block (slot ex = 0 or 2), or the ghost shell
-                    const int e = ez * 9 + ey * 3 + (cx(q) > 0 ? 0 : 2);
-                    const int eb = __ldg(nbrow + e);
-                    const int li = cx(q) > 0 ? -1 : MB;
-                    E = eb >= 0 ? __ldg(fa + ((size_t)eb * Q + q) * MB3 + rowc + (li & M))
-                                : __ldg(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(li, lj, lk));
-                }
-            }
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                const raw x = cx(q) > 0 ? (v == 0 ? E : L.v[v - 1]) : (cx(q) < 0 ? (v == 3 ? E : L.v[v + 1]) : L.v[v]);
-                f[v][q] = ST::load(x);
+            E[q] = raw(0);
+            if (cx(q) != 0 && (cx(q) > 0 ? s == 0 : s == RG::SPR - 1)) {
+                const int eb = __ldg(nbrow + ez * 9 + ey * 3 + (cx(q) > 0 ? 0 : 2));
+                const int li = cx(q) > 0 ? -1 : MB;
+                E[q] = eb >= 0 ? __ldg(fa + ((size_t)eb * Q + q) * MB3 + rowc + (li & M))
+                               : __ldg(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(li, lj, lk));
             }
         }
+        // 2. inside the row the value comes from the neighbouring thread (all lanes shuffle)
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            if (cx(q) == 0) continue;
+            const raw nb = cx(q) > 0 ? shfl_by<raw>(L[q].v[3], -1) : shfl_by<raw>(L[q].v[0], 1);
+            if (!(cx(q) > 0 ? s == 0 : s == RG::SPR - 1)) E[q] = nb;
+        }
+        // 3. the pulled values of the four cells, converted once
+        float f[4][Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const raw x = cx(q) > 0 ? (v == 0 ? E[q] : L[q].v[v - 1])
+                                        : (cx(q) < 0 ? (v == 3 ? E[q] : L[q].v[v + 1]) : L[q].v[v]);
+                f[v][q] = ST::load(x);
+            }
 #pragma unroll
         for (int v = 0; v < 4; ++v) bgk_fast<ST::shifted>(f[v], om);
         const int cell0 = (k * MB + j) * MB + i0;
@@ -455,8 +461,13 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
         restrict_octant<MB, ST>(sf, parent_pool + (size_t)parent[b] * Q * G::MB3, poct[b], nqi);
     }
 }
+// CTAs per SM the rows kernels are built for: 16-bit rows hold half the bytes in flight per thread,
+// so they trade registers for a fifth CTA
+template <int MB, class ST>
+constexpr int rows_min_blocks() { return (sizeof(typename ST::raw) == 2 ? 640 : 512) / RowGeo<MB>::TPB; }
+
 template <int MB, class ST, bool FUSE>
-__global__ void __launch_bounds__(RowGeo<MB>::TPB, 512 / RowGeo<MB>::TPB) k_step_fine_rows(
+__global__ void __launch_bounds__(RowGeo<MB>::TPB, (rows_min_blocks<MB, ST>())) k_step_fine_rows(
     const typename ST::raw* __restrict__ fa, typename ST::raw* __restrict__ fbuf, const typename ST::raw* __restrict__ gh,
     const int* __restrict__ nbtab, const int* __restrict__ parent, const int* __restrict__ poct, float om,
     typename ST::raw* __restrict__ parent_pool, float nqi, const int* __restrict__ nlim) {
@@ -851,7 +862,7 @@ __device__ __forceinline__ int batch_member(const AmrBatch& B) {
 }
 
 template <int MB, class ST, bool FUSE>
-__global__ void __launch_bounds__(RowGeo<MB>::TPB, 512 / RowGeo<MB>::TPB) kb_step_rows(const __grid_constant__ AmrBatch B) {
+__global__ void __launch_bounds__(RowGeo<MB>::TPB, (rows_min_blocks<MB, ST>())) kb_step_rows(const __grid_constant__ AmrBatch B) {
     const AmrItem& it = B.it[batch_member(B)];
     const int blk = (int)blockIdx.x - it.begin;
     using raw = typename ST::raw;
