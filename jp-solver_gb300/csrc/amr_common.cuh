@@ -128,9 +128,10 @@ __device__ __forceinline__ void bgk(float (&f)[Q], float om) {
 // out = (1 - omega) f + omega feq with omega*w*rho folded per weight class and
 // feq_pm = w rho (1 - 1.5|u|^2 + 4.5 a^2) +- 3 w rho a for a = c.u over the non-zero terms only.
 // Agrees with bgk() to FP32 round-off (a few ulp per population).  SH: the values are the shifts
-// g = f - w_q of a shifted storage format, rho = 1 + sum g, and the result is shifted too
+// g = f - w_q (every AMR step works on them, PoolIO), rho = 1 + sum g, and the result is shifted too
 // (feq_q - w_q = w_q (s + rho (3a + 4.5a^2 - 1.5|u|^2)) with s = sum g), which keeps the round-off at
-// the level of the deviations.
+// the level of the deviations: sum feq - rho then carries no bias of the O(w_q) terms, and mass
+// drifts ~1e3 times less.
 template <bool SH = false>
 __device__ __forceinline__ void bgk_fast(float (&f)[Q], float om) {
     float sm = f[0];
@@ -187,13 +188,22 @@ template <class ST>
 struct PoolIO {
     using raw = typename ST::raw;
     static constexpr bool SH = ST::shifted;
+    // the collision works on shifts g = f - w_q in every format: the 16-bit formats store them, FP32
+    // shifts on load and back on store (its mass then drifts at the deviations' round-off instead of
+    // the O(w_q) totals' biased round-off)
+    static constexpr bool SA = true;
     __device__ static __forceinline__ float n(const raw* p) { return ST::load(__ldg(p)); }
     __device__ static __forceinline__ float f(const raw* p, int q) { return SH ? wf(q) + n(p) : n(p); }
     __device__ static __forceinline__ void put_n(raw* p, float v) { *p = ST::store(v); }
     __device__ static __forceinline__ void put_f(raw* p, int q, float v) { *p = ST::store(SH ? v - wf(q) : v); }
+    // stored value -> the collision's shift, and back; stored value -> unshifted population
+    __device__ static __forceinline__ float g_of(raw x, int q) { return SH ? ST::load(x) : ST::load(x) - wf(q); }
+    __device__ static __forceinline__ raw of_g(float g, int q) { return ST::store(SH ? g : g + wf(q)); }
+    __device__ static __forceinline__ float f_of(raw x, int q) { return SH ? wf(q) + ST::load(x) : ST::load(x); }
 };
 
-// Pull of the 19 populations of cell (i, j, k) of pool block b.  nbrow[e] (global memory, the
+// Pull of the 19 populations of cell (i, j, k) of pool block b, as the collision's shifts
+// (PoolIO::g_of).  nbrow[e] (global memory, the
 // block's row of its level's neighbour table) is the pool index of the same-level neighbour in slot
 // e (pull_src), or -1 where that neighbour is not on this level; then the value comes from b's
 // ghost shell gh (GHOST = false: every neighbour exists).  Every thread reads the few table entries
@@ -219,7 +229,7 @@ __device__ __forceinline__ void pull_cell(const typename ST::raw* __restrict__ f
         }
     }
 #pragma unroll
-    for (int q = 0; q < Q; ++q) f[q] = ST::load(rv[q]);
+    for (int q = 0; q < Q; ++q) f[q] = PoolIO<ST>::g_of(rv[q], q);
 }
 // Neighbour slot of a ghost-shell cell at block-local (i, j, k), each in [-1, MB].
 template <int MB>

@@ -55,11 +55,11 @@ __device__ __forceinline__ void d_step_l0(const typename ST::raw* __restrict__ f
         for (int q = 0; q < Q; ++q) {
             int e, sc;
             pull_src<MB>(q, i, j, k, e, sc);
-            f[q] = PoolIO<ST>::n(fa + ((size_t)snb[e] * Q + q) * G::MB3 + sc);
+            f[q] = PoolIO<ST>::g_of(__ldg(fa + ((size_t)snb[e] * Q + q) * G::MB3 + sc), q);
         }
-        bgk_fast<ST::shifted>(f, om);
+        bgk_fast<true>(f, om);
 #pragma unroll
-        for (int q = 0; q < Q; ++q) PoolIO<ST>::put_n(fb + ((size_t)b * Q + q) * G::MB3 + cell, f[q]);
+        for (int q = 0; q < Q; ++q) fb[((size_t)b * Q + q) * G::MB3 + cell] = PoolIO<ST>::of_g(f[q], q);
     }
 }
 template <int MB, class ST, int TPB>
@@ -318,12 +318,12 @@ __device__ __forceinline__ void d_step_fine(const typename ST::raw* __restrict__
         const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
         float f[Q];
         pull_cell<MB, ST, true>(fa, gh, nbrow, b, i, j, k, f);
-        bgk_fast<ST::shifted>(f, om);
+        bgk_fast<true>(f, om);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-            PoolIO<ST>::put_n(fbuf + ((size_t)b * Q + q) * G::MB3 + cell, f[q]);
-            // the restriction works on unshifted populations of the values as stored
-            if (FUSE) sf[q * G::MB3 + cell] = ST::shifted ? wf(q) + ST::load(ST::store(f[q])) : f[q];
+            const typename ST::raw o = PoolIO<ST>::of_g(f[q], q);
+            fbuf[((size_t)b * Q + q) * G::MB3 + cell] = o;
+            if (FUSE) sf[q * G::MB3 + cell] = PoolIO<ST>::f_of(o, q);  // restriction: unshifted, as stored
         }
     }
     if (FUSE) {
@@ -439,20 +439,20 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
             for (int v = 0; v < 4; ++v) {
                 const raw x = cx(q) > 0 ? (v == 0 ? E[q] : L[q].v[v - 1])
                                         : (cx(q) < 0 ? (v == 3 ? E[q] : L[q].v[v + 1]) : L[q].v[v]);
-                f[v][q] = ST::load(x);
+                f[v][q] = PoolIO<ST>::g_of(x, q);
             }
 #pragma unroll
-        for (int v = 0; v < 4; ++v) bgk_fast<ST::shifted>(f[v], om);
+        for (int v = 0; v < 4; ++v) bgk_fast<true>(f[v], om);
         const int cell0 = (k * MB + j) * MB + i0;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             Vec4<ST> o;
 #pragma unroll
-            for (int v = 0; v < 4; ++v) o.v[v] = ST::store(f[v][q]);
+            for (int v = 0; v < 4; ++v) o.v[v] = PoolIO<ST>::of_g(f[v][q], q);
             o.store(fbuf + ((size_t)b * Q + q) * MB3 + cell0);
             if (FUSE) {  // the restriction works on unshifted populations of the values as stored
 #pragma unroll
-                for (int v = 0; v < 4; ++v) sf[q * MB3 + cell0 + v] = ST::shifted ? wf(q) + ST::load(o.v[v]) : f[v][q];
+                for (int v = 0; v < 4; ++v) sf[q * MB3 + cell0 + v] = PoolIO<ST>::f_of(o.v[v], q);
             }
         }
     }

@@ -76,6 +76,10 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
     using raw = typename ST::raw;
     using R = typename ST::real;
     constexpr bool SH = ST::shifted;
+    // the collision works on the shifts g = f - w_q: the 16-bit formats store them, FP32 shifts on
+    // load and back on store (mass drift at the level of the deviations' round-off, not of the
+    // O(w_q) totals' biased round-off); FP64 works on f
+    constexpr bool SA = SH || sizeof(raw) == 4;
 
     // which cube this CUDA block belongs to (uniform over the block)
     int si = 0;
@@ -137,7 +141,7 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
             if (cx(q) > 0) e = (v == 0) ? E[q] : L[q].v[v - 1];
             else if (cx(q) < 0) e = (v == V - 1) ? E[q] : L[q].v[v + 1];
             else e = L[q].v[v];
-            f[v][q] = ST::load(e);
+            f[v][q] = (SA && !SH) ? ST::load(e) - wgt<R>(q) : ST::load(e);
         }
 
     // 4. moments per cell (one reciprocal of rho instead of three divisions)
@@ -151,7 +155,7 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
         const R jx = g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14];
         const R jy = g[3] - g[4] + g[7] - g[8] - g[9] + g[10] + g[15] - g[16] + g[17] - g[18];
         const R jz = g[5] - g[6] + g[11] - g[12] - g[13] + g[14] + g[15] - g[16] - g[17] + g[18];
-        const R rh = SH ? R(1) + sm : sm;
+        const R rh = SA ? R(1) + sm : sm;
         const R inv = R(1) / rh;
         s[v] = sm;
         rho[v] = rh;
@@ -167,13 +171,13 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
     const R om = sizeof(R) == 8 ? R(d.omega_d) : R(d.omega);
     const R omc = R(1) - om;
     const size_t orow = ((size_t)z * n + y) * n + x0;
-    auto put = [&](Pack<raw, V>& p, const R (&o)[V]) {
+    auto put = [&](Pack<raw, V>& p, const R (&o)[V], int q) {
         if constexpr (SH && V % 2 == 0) {
 #pragma unroll
             for (int v = 0; v < V; v += 2) p.u32[v / 2] = ST::store2(o[v], o[v + 1]);
         } else {
 #pragma unroll
-            for (int v = 0; v < V; ++v) p.v[v] = ST::store(o[v]);
+            for (int v = 0; v < V; ++v) p.v[v] = ST::store((SA && !SH) ? o[v] + wgt<R>(q) : o[v]);
         }
     };
     // per cell: omega*w*rho and (shifted) omega*w*s for the face (1/18) and edge (1/36) classes, and
@@ -184,19 +188,19 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
 #pragma unroll
         for (int v = 0; v < V; ++v) {
             const R w0 = wgt<R>(0);
-            const R feq = SH ? w0 * (s[v] - rho[v] * usq[v]) : w0 * rho[v] * (R(1) - usq[v]);
+            const R feq = SA ? w0 * (s[v] - rho[v] * usq[v]) : w0 * rho[v] * (R(1) - usq[v]);
             o[v] = omc * f[v][0] + om * feq;
             const R orho = om * rho[v];
             owr1[v] = orho * wgt<R>(1);
             owr2[v] = orho * wgt<R>(7);
             owr3a[v] = R(3) * owr1[v];
             owr3b[v] = R(3) * owr2[v];
-            ows1[v] = SH ? om * wgt<R>(1) * s[v] : R(0);
-            ows2[v] = SH ? om * wgt<R>(7) * s[v] : R(0);
-            base[v] = SH ? -usq[v] : R(1) - usq[v];
+            ows1[v] = SA ? om * wgt<R>(1) * s[v] : R(0);
+            ows2[v] = SA ? om * wgt<R>(7) * s[v] : R(0);
+            base[v] = SA ? -usq[v] : R(1) - usq[v];
         }
         Pack<raw, V> p;
-        put(p, o);
+        put(p, o, 0);
         st_pack<raw, V>(dst + orow, p);
     }
 #pragma unroll
@@ -207,14 +211,14 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
             const R a = cdot<R>(q, ux[v], uy[v], uz[v]);
             const R owr = q < 7 ? owr1[v] : owr2[v];
             const R t = owr * (R(4.5) * a * a + base[v]);
-            const R osym = SH ? (q < 7 ? ows1[v] : ows2[v]) + t : t;  // omega * symmetric part
+            const R osym = SA ? (q < 7 ? ows1[v] : ows2[v]) + t : t;  // omega * symmetric part
             const R oasym = (q < 7 ? owr3a[v] : owr3b[v]) * a;           // omega * antisymmetric part
             oa[v] = omc * f[v][q] + (osym + oasym);
             ob[v] = omc * f[v][q + 1] + (osym - oasym);
         }
         Pack<raw, V> pa, pb;
-        put(pa, oa);
-        put(pb, ob);
+        put(pa, oa, q);
+        put(pb, ob, q + 1);
         st_pack<raw, V>(dst + q * qs + orow, pa);
         st_pack<raw, V>(dst + (q + 1) * qs + orow, pb);
     }
