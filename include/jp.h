@@ -85,6 +85,9 @@ typedef struct jp_config {
 #define JP_FLAG_SKIP_PREP 1      /* AMR profiling: skip prep + ghost fill (breaks physics; --skipprep, src/tgv3d_amr.cu:654) */
 #define JP_FLAG_SKIP_RESTRICT 2  /* AMR profiling: skip restriction (breaks physics; --skiprestr, :655) */
 #define JP_FLAG_GRAPH 4          /* replay the step from captured CUDA graphs (--graph, :656) */
+#define JP_FLAG_DEFER_INIT 8     /* jp_create allocates only: set a sensor override (or populations) and
+                                    call jp_init_tgv before the first step, so that even the first
+                                    AMR build uses the supplied sensor */
 
 /* Derived quantities of a solver (src/tgv3d_uniform.cu:151-153, src/tgv3d_amr.cu:658-664). */
 typedef struct jp_info {

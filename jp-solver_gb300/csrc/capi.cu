@@ -191,6 +191,7 @@ jp_status jp_init_tgv(jp_solver* s) {
 jp_status jp_step(jp_solver* s, int64_t nsteps) {
     if (!s) return fail(JP_ERR_INVALID, "null solver");
     if (nsteps < 0) return fail(JP_ERR_INVALID, "negative step count");
+    if (!s->initialized) return fail(JP_ERR_STATE, "solver created with JP_FLAG_DEFER_INIT: call jp_init_tgv first");
     cudaSetDevice(s->device);
     return s->kind == JP_UNIFORM ? uniform_step(s, nsteps) : amr_step(s, nsteps);
 }
@@ -204,6 +205,7 @@ jp_status jp_sync(jp_solver* s) {
 
 jp_status jp_diag(jp_solver* s, double out[3]) {
     if (!s || !out) return fail(JP_ERR_INVALID, "jp_diag: null argument");
+    if (!s->initialized) return fail(JP_ERR_STATE, "solver created with JP_FLAG_DEFER_INIT: call jp_init_tgv first");
     cudaSetDevice(s->device);
     return s->kind == JP_UNIFORM ? uniform_diag(s, out) : amr_diag(s, out);
 }
@@ -268,6 +270,7 @@ static jp_status need_amr(const jp_solver* s) {
 jp_status jp_regrid(jp_solver* s) {
     jp_status st = need_amr(s);
     if (st != JP_OK) return st;
+    if (!s->initialized) return fail(JP_ERR_STATE, "solver created with JP_FLAG_DEFER_INIT: call jp_init_tgv first");
     cudaSetDevice(s->device);
     return amr_regrid(s);
 }

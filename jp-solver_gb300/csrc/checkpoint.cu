@@ -101,6 +101,7 @@ jp_status jp_load_state(jp_solver* s, const char* path) {
         JP_CK(cudaMemcpy(s->fa, raw.data(), bytes, cudaMemcpyHostToDevice), "populations H2D");
     }
     s->step_count = h.step_count;
+    s->initialized = true;
     return JP_OK;
 }
 

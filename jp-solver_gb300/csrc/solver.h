@@ -48,6 +48,7 @@ struct jp_solver {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t ev_wait = nullptr;  // wait_stream of a served solver
     int64_t step_count = 0;
+    bool initialized = false;  // false between jp_create with JP_FLAG_DEFER_INIT and jp_init_tgv
 
     // uniform cube (flat [q][z][y][x])
     int n = 0;

@@ -905,6 +905,7 @@ jp_status amr_create(jp_solver* s) {
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->l1grid, 0xFF, sizeof(int) * a->NG1, s->stream), "memset");
+    if (s->cfg.flags & JP_FLAG_DEFER_INIT) return JP_OK;
     return amr_init(s);
 }
 
@@ -936,6 +937,7 @@ jp_status amr_init(jp_solver* s) {
     ACK(wait_stream(s), "initial build");
     reset_graphs(a);  // the level-2 pool was allocated anew
     s->step_count = 0;
+    s->initialized = true;
     update_bytes(s);
     return JP_OK;
 }

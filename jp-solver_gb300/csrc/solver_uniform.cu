@@ -92,6 +92,7 @@ jp_status uniform_create(jp_solver* s) {
     JP_CK(dev_alloc(s, (void**)&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
     s->diag_host = (double*)pinned_slot_alloc();
     if (!s->diag_host) return fail(JP_ERR_NOMEM, "pinned host slot");
+    if (s->cfg.flags & JP_FLAG_DEFER_INIT) return JP_OK;
     return uniform_init(s);
 }
 
@@ -123,6 +124,7 @@ jp_status uniform_init(jp_solver* s) {
     JP_CK(e, "init_tgv");
     JP_CK(cudaStreamSynchronize(s->stream), "init_tgv");
     s->step_count = 0;
+    s->initialized = true;
     return JP_OK;
 }
 

@@ -77,7 +77,7 @@ def test_engine_matches_reference_amr(n, l1, l2, f1, f2):
     r.set_sensor_override(s0, s1)
     r.initial_build()
     with J.Solver("amr", n=n, re=1600.0, l1_mode=l1, l2_mode=l2, frac1=f1, frac2=f2, develop_steps=3,
-                  max_gb=1024.0) as e:
+                  max_gb=1024.0, flags=J.FLAG_DEFER_INIT) as e:
         e.set_sensor_override(s0, s1)
         e.init_tgv()
         ce, cr = e.counts(), r.counts()

@@ -185,3 +185,20 @@ def test_autotune_picks_a_supported_mapping_that_matches_oracle():
         s.step(2)
         a = s.get_populations(layout="blocked")
     assert rel_err(a, O.step(f0, n, 8, p["omega"], 2)) < 1.1e-5
+
+
+def test_deferred_init_refuses_steps_until_initialised():
+    # JP_FLAG_DEFER_INIT: the solver allocates only; stepping or diagnosing before jp_init_tgv is a
+    # state error, after it the solver is the one jp_create would have made
+    with J.Solver("uniform", n=16, re=400.0, flags=J.FLAG_DEFER_INIT) as s:
+        with pytest.raises(J.JPError) as e:
+            s.step(1)
+        assert e.value.status == 5
+        with pytest.raises(J.JPError):
+            s.diag()
+        s.init_tgv()
+        s.step(3)
+        a = s.get_populations()
+    with J.Solver("uniform", n=16, re=400.0) as r:
+        r.step(3)
+        np.testing.assert_array_equal(a, r.get_populations())
