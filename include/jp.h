@@ -88,6 +88,8 @@ typedef struct jp_config {
 #define JP_FLAG_DEFER_INIT 8     /* jp_create allocates only: set a sensor override (or populations) and
                                     call jp_init_tgv before the first step, so that even the first
                                     AMR build uses the supplied sensor */
+#define JP_FLAG_INPLACE 16       /* uniform: in-place (AA pattern) streaming in one population array,
+                                    half the state's HBM, bit-identical results; no reference counterpart */
 
 /* Derived quantities of a solver (src/tgv3d_uniform.cu:151-153, src/tgv3d_amr.cu:658-664). */
 typedef struct jp_info {
@@ -97,7 +99,7 @@ typedef struct jp_info {
     double nu, tau, omega;   /* level-0 viscosity, relaxation time, 1/tau */
     double tau1, tau2;       /* AMR level 1/2 relaxation times */
     double kf;               /* 2pi/n */
-    int64_t bytes_state;     /* device bytes of the double-buffered populations */
+    int64_t bytes_state;     /* device bytes of the populations (two arrays; one in place) */
     int64_t step_count;      /* time steps taken so far */
     int32_t reserved[8];
 } jp_info;

@@ -2,8 +2,8 @@
 //
 // No counterpart in the reference (its runs start from the initial state every time).  A file holds
 // a header (magic, ABI version, the configuration that fixes the state's shape and physics, the step
-// count) and the kind's payload: for a uniform cube the stored populations [q][z][y][x] as they are
-// in HBM; for an AMR solve its counts, block tables and the populations of the blocks in use
+// count) and the kind's payload: for a uniform cube the stored populations in the flat [q][z][y][x]
+// order of the two-array step (an in-place solver reorders on the host, so files move between the two); for an AMR solve its counts, block tables and the populations of the blocks in use
 // (amr_save_state).  Loading into a solver created with the same kind, n, mb, storage, Re, u0 and
 // refinement modes continues bit for bit where the saved solve was.
 #include <cmath>
@@ -72,6 +72,11 @@ jp_status jp_save_state(jp_solver* s, const char* path) {
     const size_t bytes = (size_t)Q * s->cells * s->elem;
     std::vector<unsigned char> raw(bytes);
     JP_CK(cudaMemcpy(raw.data(), s->fa, bytes, cudaMemcpyDeviceToHost), "populations D2H");
+    if (s->inplace) {
+        std::vector<unsigned char> flat(bytes);
+        uniform_raw_to_flat(s, raw.data(), flat.data());
+        raw.swap(flat);
+    }
     if (std::fwrite(raw.data(), 1, bytes, file.f) != bytes) return fail(JP_ERR_INVALID, "write failed: %s", path);
     return JP_OK;
 }
@@ -97,6 +102,12 @@ jp_status jp_load_state(jp_solver* s, const char* path) {
         const size_t bytes = (size_t)Q * s->cells * s->elem;
         std::vector<unsigned char> raw(bytes);
         if (std::fread(raw.data(), 1, bytes, file.f) != bytes) return fail(JP_ERR_INVALID, "state file truncated");
+        if (s->inplace) {
+            std::vector<unsigned char> st(bytes);
+            s->step_count = h.step_count;  // the in-place layout follows the step count's parity
+            uniform_flat_to_raw(s, raw.data(), st.data());
+            raw.swap(st);
+        }
         JP_CK(cudaStreamSynchronize(s->stream), "load");
         JP_CK(cudaMemcpy(s->fa, raw.data(), bytes, cudaMemcpyHostToDevice), "populations H2D");
     }

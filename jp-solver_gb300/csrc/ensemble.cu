@@ -36,9 +36,11 @@ namespace jp {
 // One batched lattice step of `members` (uniform, same device) on `st`: one launch per
 // (storage, vec, threads) class and per kMaxBatch cubes.  Swaps each member's buffers.
 static jp_status batched_step(const std::vector<jp_solver*>& members, cudaStream_t st) {
+    // in-place cubes group by the parity of their step count too (local or stream step)
     std::map<long long, std::vector<jp_solver*>> groups;
     for (jp_solver* m : members)
-        groups[((long long)m->storage << 32) | ((long long)m->vec << 16) | (long long)m->tpb].push_back(m);
+        groups[((long long)m->inplace << 42) | ((long long)(m->inplace ? m->step_count & 1 : 0) << 40) |
+               ((long long)m->storage << 32) | ((long long)m->vec << 16) | (long long)m->tpb].push_back(m);
     for (auto& g : groups) {
         const std::vector<jp_solver*>& v = g.second;
         for (size_t i = 0; i < v.size(); i += kMaxBatch) {
@@ -48,14 +50,19 @@ static jp_status batched_step(const std::vector<jp_solver*>& members, cudaStream
                 jp_solver* m = v[i + k];
                 std::memset(&us[k], 0, sizeof us[k]);
                 us[k].src = m->fa;
-                us[k].dst = m->fb;
+                us[k].dst = m->inplace ? m->fa : m->fb;
                 us[k].n = m->n;
                 us[k].omega = float(m->info.omega);
                 us[k].omega_d = m->info.omega;
             }
-            ECK(launch_stream_collide(v[i]->storage, us, (int)cnt, v[i]->vec, v[i]->tpb, st), "batched stream_collide");
+            if (v[i]->inplace) {
+                ECK(launch_stream_collide_inplace(v[i]->storage, us, (int)cnt, int(v[i]->step_count & 1), v[i]->vec,
+                                                  v[i]->tpb, st), "batched in-place step");
+            } else {
+                ECK(launch_stream_collide(v[i]->storage, us, (int)cnt, v[i]->vec, v[i]->tpb, st), "batched stream_collide");
+            }
             for (size_t k = 0; k < cnt; ++k) {
-                std::swap(v[i + k]->fa, v[i + k]->fb);
+                if (!v[i + k]->inplace) std::swap(v[i + k]->fa, v[i + k]->fb);
                 ++v[i + k]->step_count;
             }
         }
@@ -869,7 +876,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             Job* j = cur.entries[k].first;
             jp_solver* s = j->s;
             const bool dbl = s->storage == JP_FP64;
-            ECK(launch_macro(s->storage, s->fa, s->field, s->n, sv->stream), "macro");
+            ECK(launch_macro(s->storage, s->fa, s->field, s->n, sv->stream, s->aa_layout()), "macro");
             ECK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, cur.dev + 3 * k, sv->stream), "diag");
             j->need_diag = false;
             ++j->inflight;

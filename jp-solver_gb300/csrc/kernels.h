@@ -34,16 +34,27 @@ struct UniBatch {
 cudaError_t launch_stream_collide(int storage, const UniSolve* solves, int count, int vec, int tpb,
                                   cudaStream_t st);
 
+// In-place (AA) step over `count` cubes, each with src == dst: parity 0 (even step count) runs the
+// local step, 1 the stream step (uniform_aa.cu).  vec must be the storage's default; tpb is a lower
+// bound on the threads per block, which also hold whole x-rows.
+cudaError_t launch_stream_collide_inplace(int storage, const UniSolve* solves, int count, int parity, int vec,
+                                          int tpb, cudaStream_t st);
+// Threads per block the in-place steps use for cubes up to edge max_n (0: not supported).
+int inplace_tpb(int storage, int vec, int tpb, int max_n);
+
 // Largest supported vec for a storage; a valid vec divides n and keeps n^3/vec a multiple of 32.
 int default_vec(int storage);
 bool vec_supported(int storage, int vec);
 
 // TGV initial state (src/tgv3d_uniform.cu:63-77) into flat storage; axis_tab: 3*n doubles of scratch.
-cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, double* axis_tab, cudaStream_t st);
+// aa: in the in-place layout of step 0 (population q of cell x at [q][x + c_q]).
+cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, double* axis_tab, cudaStream_t st,
+                            bool aa = false);
 
 // Macroscopic field (rho, ux, uy, uz) per cell, linear (z*n+y)*n+x.  FP64 storage writes double4,
-// every other storage float4 (k_macro, src/tgv3d_uniform.cu:80-90).
-cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStream_t st);
+// every other storage float4 (k_macro, src/tgv3d_uniform.cu:80-90).  layout: 0 flat [q][x]; 1, 2 the
+// in-place layouts after an even / odd step count (aa_layout()).
+cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStream_t st, int layout = 0);
 
 // Energy, enstrophy, mass of a macro field, reduced deterministically to out_dev[3] (device).
 // partials_dev holds kDiagBlocks*3 doubles.  float_diff=true takes the velocity differences in

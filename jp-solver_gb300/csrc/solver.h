@@ -55,7 +55,8 @@ struct jp_solver {
     long long cells = 0;
     size_t elem = 0;           // bytes per stored population
     void* fa = nullptr;        // state at the current time
-    void* fb = nullptr;        // next state
+    void* fb = nullptr;        // next state (null when in place)
+    bool inplace = false;      // JP_FLAG_INPLACE: one array, AA steps (uniform_aa.cu)
     void* field = nullptr;     // macro field (float4 or double4 per cell), allocated on first use
     double* partials = nullptr;  // diagnostic block partials (kDiagBlocks*3)
     double* diag_dev = nullptr;  // 3 doubles
@@ -64,6 +65,9 @@ struct jp_solver {
     float* outbuf = nullptr;   // device Q / speed / velocity for output frames, allocated on first use
 
     jp::AmrState* amr = nullptr;
+
+    // layout of fa for launch_macro: 0 flat, 1 / 2 in place after an even / odd step count
+    int aa_layout() const { return inplace ? 1 + int(step_count & 1) : 0; }
 };
 
 namespace jp {
@@ -80,6 +84,11 @@ jp_status uniform_get_output_fields(jp_solver* s, float* q, float* speed, float*
 jp_status output_fields_from(jp_solver* s, const void* field, bool field_is_double, bool float_diff, int n, float* q,
                              float* speed, float* vel);
 jp_status common_setup(jp_solver* s);
+// element of fa that holds population q of cell (x, y, z) at the current step count
+size_t uniform_slot(const jp_solver* s, int q, int x, int y, int z);
+// fa as stored <-> the flat [q][z][y][x] order of the two-array step (host copies; identity unless in place)
+void uniform_raw_to_flat(const jp_solver* s, const unsigned char* raw, unsigned char* flat);
+void uniform_flat_to_raw(const jp_solver* s, const unsigned char* flat, unsigned char* raw);
 
 // AMR (solver_amr.cu)
 jp_status amr_create(jp_solver* s);

@@ -823,6 +823,7 @@ jp_status amr_create(jp_solver* s) {
     const jp_config& c = s->cfg;
     if (c.storage != JP_FP32 && c.storage != JP_FP16 && c.storage != JP_BF16)
         return fail(JP_ERR_UNSUPPORTED, "AMR solver: FP32, FP16 or BF16 storage (FP64 is uniform only)");
+    if (c.flags & JP_FLAG_INPLACE) return fail(JP_ERR_UNSUPPORTED, "in-place streaming is for the uniform cube only");
     if (c.l1_mode < 0 || c.l1_mode > 2 || c.l2_mode < 0 || c.l2_mode > 2) return fail(JP_ERR_INVALID, "bad refine mode");
     if (c.threads_per_block && !step_tpb_supported(c.mb, c.threads_per_block))
         return fail(JP_ERR_INVALID, "threads_per_block %d does not split a block of edge %d (MB=4: 64; 8, 16: 128, 256, 512)",

@@ -79,15 +79,25 @@ jp_status uniform_create(jp_solver* s) {
     s->n = c.n;
     s->cells = (long long)c.n * c.n * c.n;
     s->elem = storage_bytes(c.storage);
-    s->vec = pick_vec(c.storage, c.n, c.vec);
-    if (!s->vec) return fail(JP_ERR_INVALID, "no vector width fits n=%d (requested vec=%d)", c.n, c.vec);
+    s->inplace = (c.flags & JP_FLAG_INPLACE) != 0;
     s->tpb = c.threads_per_block ? c.threads_per_block : 128;
     if (s->tpb != 64 && s->tpb != 128 && s->tpb != 256 && s->tpb != 512)
         return fail(JP_ERR_INVALID, "threads_per_block must be 64, 128, 256 or 512");
+    if (s->inplace) {
+        // the in-place steps run the storage's default vector width, whole x-rows per CUDA block
+        s->vec = default_vec(c.storage);
+        if ((c.vec && c.vec != s->vec) || c.n % s->vec)
+            return fail(JP_ERR_INVALID, "in-place streaming needs vec=%d dividing n=%d", s->vec, c.n);
+        if (!inplace_tpb(c.storage, s->vec, s->tpb, c.n))
+            return fail(JP_ERR_INVALID, "in-place streaming: an x-row of n=%d does not fit one CUDA block", c.n);
+    } else {
+        s->vec = pick_vec(c.storage, c.n, c.vec);
+        if (!s->vec) return fail(JP_ERR_INVALID, "no vector width fits n=%d (requested vec=%d)", c.n, c.vec);
+    }
     const size_t bytes = (size_t)Q * s->cells * s->elem;
-    s->info.bytes_state = (int64_t)(2 * bytes);
+    s->info.bytes_state = (int64_t)((s->inplace ? 1 : 2) * bytes);
     JP_CK(dev_alloc(s, &s->fa, bytes), "cudaMalloc populations");
-    JP_CK(dev_alloc(s, &s->fb, bytes), "cudaMalloc populations");
+    if (!s->inplace) JP_CK(dev_alloc(s, &s->fb, bytes), "cudaMalloc populations");
     JP_CK(dev_alloc(s, (void**)&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
     JP_CK(dev_alloc(s, (void**)&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
     s->diag_host = (double*)pinned_slot_alloc();
@@ -118,7 +128,7 @@ jp_status uniform_init(jp_solver* s) {
         JP_CK(dev_alloc(s, (void**)&own, sizeof(double) * 3 * s->n), "cudaMalloc init table");
         tab = own;
     }
-    cudaError_t e = launch_init_tgv(s->storage, s->fa, s->n, s->cfg.u0, s->info.kf, tab, s->stream);
+    cudaError_t e = launch_init_tgv(s->storage, s->fa, s->n, s->cfg.u0, s->info.kf, tab, s->stream, s->inplace);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     dev_free(s, own);
     JP_CK(e, "init_tgv");
@@ -134,6 +144,16 @@ jp_status uniform_step(jp_solver* s, int64_t nsteps) {
     u.n = s->n;
     u.omega = float(s->info.omega);
     u.omega_d = s->info.omega;
+    if (s->inplace) {
+        u.src = u.dst = s->fa;
+        for (int64_t i = 0; i < nsteps; ++i) {
+            cudaError_t e = launch_stream_collide_inplace(s->storage, &u, 1, int(s->step_count & 1), s->vec, s->tpb,
+                                                          s->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "in-place step launch");
+            ++s->step_count;
+        }
+        return JP_OK;
+    }
     for (int64_t i = 0; i < nsteps; ++i) {
         u.src = s->fa;
         u.dst = s->fb;
@@ -155,7 +175,7 @@ static jp_status ensure_field(jp_solver* s) {
 jp_status uniform_diag(jp_solver* s, double out[3]) {
     jp_status st = ensure_field(s);
     if (st != JP_OK) return st;
-    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream), "macro");
+    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream, s->aa_layout()), "macro");
     const bool dbl = s->storage == JP_FP64;
     JP_CK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, s->diag_dev, s->stream), "diag");
     JP_CK(cudaMemcpyAsync(s->diag_host, s->diag_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "diag D2H");
@@ -174,12 +194,56 @@ static inline size_t blocked_index(int n, int mb, int q, int x, int y, int z) {
     return (b * Q + q) * (size_t)mb * mb * mb + cell;
 }
 
+size_t uniform_slot(const jp_solver* s, int q, int x, int y, int z) {
+    const int n = s->n;
+    if (s->inplace) {
+        if (s->step_count & 1) {
+            q = opp(q);
+        } else {
+            x = (x + cx(q) + n) % n;
+            y = (y + cy(q) + n) % n;
+            z = (z + cz(q) + n) % n;
+        }
+    }
+    return (size_t)q * s->cells + ((size_t)z * n + y) * n + x;
+}
+
+void uniform_raw_to_flat(const jp_solver* s, const unsigned char* raw, unsigned char* flat) {
+    const size_t e = s->elem;
+    const int n = s->n;
+    if (!s->inplace) {
+        std::memcpy(flat, raw, (size_t)Q * s->cells * e);
+        return;
+    }
+    for (int q = 0; q < Q; ++q)
+        for (int z = 0; z < n; ++z)
+            for (int y = 0; y < n; ++y)
+                for (int x = 0; x < n; ++x)
+                    std::memcpy(flat + e * ((size_t)q * s->cells + ((size_t)z * n + y) * n + x),
+                                raw + e * uniform_slot(s, q, x, y, z), e);
+}
+
+void uniform_flat_to_raw(const jp_solver* s, const unsigned char* flat, unsigned char* raw) {
+    const size_t e = s->elem;
+    const int n = s->n;
+    if (!s->inplace) {
+        std::memcpy(raw, flat, (size_t)Q * s->cells * e);
+        return;
+    }
+    for (int q = 0; q < Q; ++q)
+        for (int z = 0; z < n; ++z)
+            for (int y = 0; y < n; ++y)
+                for (int x = 0; x < n; ++x)
+                    std::memcpy(raw + e * uniform_slot(s, q, x, y, z),
+                                flat + e * ((size_t)q * s->cells + ((size_t)z * n + y) * n + x), e);
+}
+
 jp_status uniform_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count) {
     if (level != 0) return fail(JP_ERR_INVALID, "uniform solver has only level 0");
     if (count != (int64_t)Q * s->cells) return fail(JP_ERR_INVALID, "count %lld != 19*n^3", (long long)count);
     if (layout != JP_LAYOUT_FLAT && layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_INVALID, "bad layout %d", layout);
     const size_t bytes = (size_t)count * s->elem;
-    const bool native = layout == JP_LAYOUT_FLAT &&
+    const bool native = layout == JP_LAYOUT_FLAT && !s->inplace &&
                         ((dtype == JP_F32 && s->storage == JP_FP32) || (dtype == JP_F64 && s->storage == JP_FP64));
     if (native) {
         JP_CK(cudaMemcpyAsync(host, s->fa, bytes, cudaMemcpyDeviceToHost, s->stream), "populations D2H");
@@ -194,8 +258,9 @@ jp_status uniform_get_populations(jp_solver* s, int level, int layout, int dtype
         for (int z = 0; z < n; ++z)
             for (int y = 0; y < n; ++y)
                 for (int x = 0; x < n; ++x) {
-                    const size_t src = (size_t)q * s->cells + ((size_t)z * n + y) * n + x;
-                    const size_t dst = layout == JP_LAYOUT_FLAT ? src : blocked_index(n, mb, q, x, y, z);
+                    const size_t src = uniform_slot(s, q, x, y, z);
+                    const size_t dst = layout == JP_LAYOUT_FLAT ? (size_t)q * s->cells + ((size_t)z * n + y) * n + x
+                                                                : blocked_index(n, mb, q, x, y, z);
                     const double v = stored_to_double(s->storage, raw.data(), src, q);
                     if (dtype == JP_F32) static_cast<float*>(host)[dst] = float(v);
                     else static_cast<double*>(host)[dst] = v;
@@ -208,7 +273,7 @@ jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype
     if (count != (int64_t)Q * s->cells) return fail(JP_ERR_INVALID, "count %lld != 19*n^3", (long long)count);
     if (layout != JP_LAYOUT_FLAT && layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_INVALID, "bad layout %d", layout);
     const size_t bytes = (size_t)count * s->elem;
-    const bool native = layout == JP_LAYOUT_FLAT &&
+    const bool native = layout == JP_LAYOUT_FLAT && !s->inplace &&
                         ((dtype == JP_F32 && s->storage == JP_FP32) || (dtype == JP_F64 && s->storage == JP_FP64));
     if (native) {
         // asynchronous from pinned memory; stream order puts it before the next step
@@ -221,8 +286,9 @@ jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype
         for (int z = 0; z < n; ++z)
             for (int y = 0; y < n; ++y)
                 for (int x = 0; x < n; ++x) {
-                    const size_t dst = (size_t)q * s->cells + ((size_t)z * n + y) * n + x;
-                    const size_t src = layout == JP_LAYOUT_FLAT ? dst : blocked_index(n, mb, q, x, y, z);
+                    const size_t dst = uniform_slot(s, q, x, y, z);
+                    const size_t src = layout == JP_LAYOUT_FLAT ? (size_t)q * s->cells + ((size_t)z * n + y) * n + x
+                                                                : blocked_index(n, mb, q, x, y, z);
                     const double v = dtype == JP_F32 ? double(static_cast<const float*>(host)[src])
                                                      : static_cast<const double*>(host)[src];
                     double_to_stored(s->storage, raw.data(), dst, q, v);
@@ -252,7 +318,7 @@ jp_status uniform_get_output_fields(jp_solver* s, float* q, float* speed, float*
     if (count != (int64_t)s->cells) return fail(JP_ERR_INVALID, "count %lld != n^3", (long long)count);
     jp_status st = ensure_field(s);
     if (st != JP_OK) return st;
-    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream), "macro");
+    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream, s->aa_layout()), "macro");
     const bool dbl = s->storage == JP_FP64;
     return output_fields_from(s, s->field, dbl, !dbl, s->n, q, speed, vel);
 }
@@ -261,7 +327,7 @@ jp_status uniform_get_macro(jp_solver* s, float* host, int64_t count) {
     if (count != 4 * (int64_t)s->cells) return fail(JP_ERR_INVALID, "count %lld != 4*n^3", (long long)count);
     jp_status st = ensure_field(s);
     if (st != JP_OK) return st;
-    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream), "macro");
+    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream, s->aa_layout()), "macro");
     if (s->storage == JP_FP64) {
         std::vector<double> tmp((size_t)count);
         JP_CK(cudaMemcpyAsync(tmp.data(), s->field, (size_t)count * 8, cudaMemcpyDeviceToHost, s->stream), "macro D2H");

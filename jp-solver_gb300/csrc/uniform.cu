@@ -11,6 +11,7 @@
 // on both sides: 152 B per lattice update in FP32, 76 B in FP16/BF16, 304 B in FP64.
 #include "kernels.h"
 #include "lattice.cuh"
+#include "uniform_common.cuh"
 
 #include <atomic>
 
@@ -19,57 +20,6 @@ namespace jp {
 static std::atomic<long long> g_launches{0};
 void note_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
-
-// ---- vector access helpers ---------------------------------------------------------------------
-
-template <class RAW, int V>
-struct Pack {
-    static constexpr int bytes = int(sizeof(RAW)) * V;
-    using word = typename std::conditional<bytes == 16, uint4,
-                 typename std::conditional<bytes == 8, uint2,
-                 typename std::conditional<bytes == 4, unsigned int, unsigned short>::type>::type>::type;
-    union {
-        word w;
-        RAW v[V];
-        unsigned int u32[(bytes + 3) / 4];
-    };
-};
-
-template <class RAW, int V>
-__device__ __forceinline__ Pack<RAW, V> ld_pack(const RAW* p) {
-    Pack<RAW, V> r;
-    r.w = __ldg(reinterpret_cast<const typename Pack<RAW, V>::word*>(p));
-    return r;
-}
-template <class RAW, int V>
-__device__ __forceinline__ void st_pack(RAW* p, const Pack<RAW, V>& r) {
-    __stcs(reinterpret_cast<typename Pack<RAW, V>::word*>(p), r.w);
-}
-
-template <class RAW> __device__ __forceinline__ RAW ld_one(const RAW* p) { return __ldg(p); }
-template <> __device__ __forceinline__ uint16_t ld_one<uint16_t>(const uint16_t* p) {
-    return __ldg(reinterpret_cast<const unsigned short*>(p));
-}
-
-template <class RAW> __device__ __forceinline__ RAW shfl_up1(RAW v) { return __shfl_up_sync(0xffffffffu, v, 1); }
-template <class RAW> __device__ __forceinline__ RAW shfl_dn1(RAW v) { return __shfl_down_sync(0xffffffffu, v, 1); }
-template <> __device__ __forceinline__ uint16_t shfl_up1<uint16_t>(uint16_t v) {
-    return (uint16_t)__shfl_up_sync(0xffffffffu, (unsigned)v, 1);
-}
-template <> __device__ __forceinline__ uint16_t shfl_dn1<uint16_t>(uint16_t v) {
-    return (uint16_t)__shfl_down_sync(0xffffffffu, (unsigned)v, 1);
-}
-
-// ---- stream-collide ---------------------------------------------------------------------------
-
-// Occupancy floor per SM for a variant: the wide-vector variants need warps (to keep 19 vector
-// loads per thread in flight, and for the issue-bound 16-bit collision) more than registers:
-// FP32 V=4 and 16-bit V=4 to 128 registers, 16-bit V=8 to 168.
-template <class ST, int V, int TPB>
-constexpr int min_blocks() {
-    return (sizeof(typename ST::raw) * V == 16 && sizeof(typename ST::raw) == 2) ? (384 / TPB > 0 ? 384 / TPB : 1)
-         : (sizeof(typename ST::raw) * V >= 8 && sizeof(typename ST::raw) <= 4) ? (512 / TPB > 0 ? 512 / TPB : 1) : 1;
-}
 
 template <class ST, int V, int TPB>
 __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_collide(const __grid_constant__ UniBatch b) {
@@ -144,81 +94,26 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
             f[v][q] = (SA && !SH) ? ST::load(e) - wgt<R>(q) : ST::load(e);
         }
 
-    // 4. moments per cell (one reciprocal of rho instead of three divisions)
-    R rho[V], ux[V], uy[V], uz[V], s[V], usq[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-        const R* g = f[v];
-        R sm = g[0];
-#pragma unroll
-        for (int q = 1; q < Q; ++q) sm += g[q];
-        const R jx = g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14];
-        const R jy = g[3] - g[4] + g[7] - g[8] - g[9] + g[10] + g[15] - g[16] + g[17] - g[18];
-        const R jz = g[5] - g[6] + g[11] - g[12] - g[13] + g[14] + g[15] - g[16] - g[17] + g[18];
-        const R rh = SA ? R(1) + sm : sm;
-        const R inv = R(1) / rh;
-        s[v] = sm;
-        rho[v] = rh;
-        ux[v] = jx * inv;
-        uy[v] = jy * inv;
-        uz[v] = jz * inv;
-        usq[v] = R(1.5) * (ux[v] * ux[v] + uy[v] * uy[v] + uz[v] * uz[v]);
-    }
-
-    // 5. relax and store, one population pair at a time; 16-bit formats convert two cells per
-    //    instruction.  BGK as out = (1 - omega) f + omega feq with omega*w*rho folded per weight
-    //    class: with a = c.u, feq_pm = w rho (1 - 1.5|u|^2 + 4.5 a^2) +- 3 w rho a.
+    // 4. moments, 5. relax and store, one population pair at a time
     const R om = sizeof(R) == 8 ? R(d.omega_d) : R(d.omega);
-    const R omc = R(1) - om;
+    CellBgk<R, V, SA> c(om);
+    c.moments(f);
     const size_t orow = ((size_t)z * n + y) * n + x0;
-    auto put = [&](Pack<raw, V>& p, const R (&o)[V], int q) {
-        if constexpr (SH && V % 2 == 0) {
-#pragma unroll
-            for (int v = 0; v < V; v += 2) p.u32[v / 2] = ST::store2(o[v], o[v + 1]);
-        } else {
-#pragma unroll
-            for (int v = 0; v < V; ++v) p.v[v] = ST::store((SA && !SH) ? o[v] + wgt<R>(q) : o[v]);
-        }
-    };
-    // per cell: omega*w*rho and (shifted) omega*w*s for the face (1/18) and edge (1/36) classes, and
-    // the base term 1 - 1.5|u|^2 (or -1.5|u|^2 shifted)
-    R owr1[V], owr2[V], owr3a[V], owr3b[V], ows1[V], ows2[V], base[V];
     {
         R o[V];
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-            const R w0 = wgt<R>(0);
-            const R feq = SA ? w0 * (s[v] - rho[v] * usq[v]) : w0 * rho[v] * (R(1) - usq[v]);
-            o[v] = omc * f[v][0] + om * feq;
-            const R orho = om * rho[v];
-            owr1[v] = orho * wgt<R>(1);
-            owr2[v] = orho * wgt<R>(7);
-            owr3a[v] = R(3) * owr1[v];
-            owr3b[v] = R(3) * owr2[v];
-            ows1[v] = SA ? om * wgt<R>(1) * s[v] : R(0);
-            ows2[v] = SA ? om * wgt<R>(7) * s[v] : R(0);
-            base[v] = SA ? -usq[v] : R(1) - usq[v];
-        }
+        for (int v = 0; v < V; ++v) o[v] = c.rest(f, v);
         Pack<raw, V> p;
-        put(p, o, 0);
+        put_row<ST, V, SA>(p, o, 0);
         st_pack<raw, V>(dst + orow, p);
     }
 #pragma unroll
     for (int q = 1; q < Q; q += 2) {
         R oa[V], ob[V];
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-            const R a = cdot<R>(q, ux[v], uy[v], uz[v]);
-            const R owr = q < 7 ? owr1[v] : owr2[v];
-            const R t = owr * (R(4.5) * a * a + base[v]);
-            const R osym = SA ? (q < 7 ? ows1[v] : ows2[v]) + t : t;  // omega * symmetric part
-            const R oasym = (q < 7 ? owr3a[v] : owr3b[v]) * a;           // omega * antisymmetric part
-            oa[v] = omc * f[v][q] + (osym + oasym);
-            ob[v] = omc * f[v][q + 1] + (osym - oasym);
-        }
+        c.pair(f, q, oa, ob);
         Pack<raw, V> pa, pb;
-        put(pa, oa, q);
-        put(pb, ob, q + 1);
+        put_row<ST, V, SA>(pa, oa, q);
+        put_row<ST, V, SA>(pb, ob, q + 1);
         st_pack<raw, V>(dst + q * qs + orow, pa);
         st_pack<raw, V>(dst + (q + 1) * qs + orow, pb);
     }
@@ -317,8 +212,11 @@ __global__ void k_tgv_axis(double* __restrict__ tab, int n, double kf) {
     tab[2 * n + i] = cos(2 * x);
 }
 
+// aa: write population q of cell x to x + c_q (the in-place layout of an even step count, in which
+// every population already sits where the next step reads it)
 template <class ST>
-__global__ void k_init_tgv(typename ST::raw* __restrict__ f, int n, double u0, const double* __restrict__ tab) {
+__global__ void k_init_tgv(typename ST::raw* __restrict__ f, int n, double u0, const double* __restrict__ tab,
+                           bool aa) {
     const long long cells = (long long)n * n * n;
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cells) return;
@@ -342,19 +240,25 @@ __global__ void k_init_tgv(typename ST::raw* __restrict__ f, int n, double u0, c
             const double g = wd(q) * (3.0 * p + rho * (cu + 0.5 * cu * cu - 1.5 * (ux * ux + uy * uy)));
             v = ST::store(float(g));
         }
-        f[(size_t)q * cells + c] = v;
+        size_t o = c;
+        if (aa) {
+            const int xi = (i + cx(q) + n) % n, yj = (j + cy(q) + n) % n, zk = (k + cz(q) + n) % n;
+            o = ((size_t)zk * n + yj) * n + xi;
+        }
+        f[(size_t)q * cells + o] = v;
     }
 }
 
-cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, double* axis_tab, cudaStream_t st) {
+cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, double* axis_tab, cudaStream_t st,
+                            bool aa) {
     const long long cells = (long long)n * n * n;
     const unsigned blocks = (unsigned)((cells + 255) / 256);
     k_tgv_axis<<<(n + 255) / 256, 256, 0, st>>>(axis_tab, n, kf);
     switch (storage) {
-        case 0: k_init_tgv<StF32><<<blocks, 256, 0, st>>>((float*)f, n, u0, axis_tab); break;
-        case 1: k_init_tgv<StF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, axis_tab); break;
-        case 2: k_init_tgv<StBF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, axis_tab); break;
-        case 3: k_init_tgv<StF64><<<blocks, 256, 0, st>>>((double*)f, n, u0, axis_tab); break;
+        case 0: k_init_tgv<StF32><<<blocks, 256, 0, st>>>((float*)f, n, u0, axis_tab, aa); break;
+        case 1: k_init_tgv<StF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, axis_tab, aa); break;
+        case 2: k_init_tgv<StBF16><<<blocks, 256, 0, st>>>((uint16_t*)f, n, u0, axis_tab, aa); break;
+        case 3: k_init_tgv<StF64><<<blocks, 256, 0, st>>>((double*)f, n, u0, axis_tab, aa); break;
         default: return cudaErrorInvalidValue;
     }
     note_launch(2);
@@ -362,15 +266,25 @@ cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, d
 }
 
 // ---- macro field ---------------------------------------------------------------------------------
+// layout 0: population q of cell x at [q][x]; the in-place layouts: 1 (even step count) at
+// [q][x + c_q], 2 (odd step count) at [opp q][x]
 template <class ST, class FT>
-__global__ void k_macro(const typename ST::raw* __restrict__ f, FT* __restrict__ out, int n) {
+__global__ void k_macro(const typename ST::raw* __restrict__ f, FT* __restrict__ out, int n, int layout) {
     using R = typename ST::real;
     const long long cells = (long long)n * n * n;
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cells) return;
+    const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
     R v[Q];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) v[q] = ST::load(f[(size_t)q * cells + c]);
+    for (int q = 0; q < Q; ++q) {
+        size_t o = (size_t)q * cells + c;
+        if (layout == 1)
+            o = (size_t)q * cells + ((size_t)((k + cz(q) + n) % n) * n + (j + cy(q) + n) % n) * n + (i + cx(q) + n) % n;
+        else if (layout == 2)
+            o = (size_t)opp(q) * cells + c;
+        v[q] = ST::load(f[o]);
+    }
     R sm = v[0];
 #pragma unroll
     for (int q = 1; q < Q; ++q) sm += v[q];
@@ -385,14 +299,14 @@ __global__ void k_macro(const typename ST::raw* __restrict__ f, FT* __restrict__
     o[3] = FT(jz / rho);
 }
 
-cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStream_t st) {
+cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStream_t st, int layout) {
     const long long cells = (long long)n * n * n;
     const unsigned blocks = (unsigned)((cells + 255) / 256);
     switch (storage) {
-        case 0: k_macro<StF32, float><<<blocks, 256, 0, st>>>((const float*)f, (float*)field, n); break;
-        case 1: k_macro<StF16, float><<<blocks, 256, 0, st>>>((const uint16_t*)f, (float*)field, n); break;
-        case 2: k_macro<StBF16, float><<<blocks, 256, 0, st>>>((const uint16_t*)f, (float*)field, n); break;
-        case 3: k_macro<StF64, double><<<blocks, 256, 0, st>>>((const double*)f, (double*)field, n); break;
+        case 0: k_macro<StF32, float><<<blocks, 256, 0, st>>>((const float*)f, (float*)field, n, layout); break;
+        case 1: k_macro<StF16, float><<<blocks, 256, 0, st>>>((const uint16_t*)f, (float*)field, n, layout); break;
+        case 2: k_macro<StBF16, float><<<blocks, 256, 0, st>>>((const uint16_t*)f, (float*)field, n, layout); break;
+        case 3: k_macro<StF64, double><<<blocks, 256, 0, st>>>((const double*)f, (double*)field, n, layout); break;
         default: return cudaErrorInvalidValue;
     }
     note_launch();

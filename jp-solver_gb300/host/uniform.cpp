@@ -2,7 +2,7 @@
 // driving the GB300 engine through the C ABI.  Same flags and defaults, same stdout lines, same exit
 // codes (0 VALID, 1 CHECK, 2 error or N%MB), same .vti frames.  Additions on top: --prec
 // fp32|fp16|bf16|fp64 storage, --mb, --tpb/--vec thread mapping, --diag-every, --bench 1 (time the
-// step loop without diagnostics), --device.
+// step loop without diagnostics), --device, --inplace 1 (AA streaming in one population array).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -38,6 +38,7 @@ int main(int argc, char** argv) {
     cfg.threads_per_block = argi(argc, argv, "--tpb", 0);
     cfg.vec = argi(argc, argv, "--vec", 0);
     cfg.device = argi(argc, argv, "--device", 0);
+    if (argd(argc, argv, "--inplace", 0.0) > 0.5) cfg.flags |= JP_FLAG_INPLACE;
     if (argd(argc, argv, "--autotune", 0.0) > 0.5) {
         double best = 0.0;
         ck(jp_autotune(&cfg, 10, &best), "autotune");
@@ -60,8 +61,9 @@ int main(int argc, char** argv) {
         ck(jp_step_timed(s, bsteps, &ms), "bench");
         const double cells = double(N) * N * N;
         const double bpu = cfg.storage == JP_FP64 ? 304.0 : (cfg.storage == JP_FP32 ? 152.0 : 76.0);
-        std::printf("[bench] uniform N=%d: %.3f s  %ld steps  %.1f MLUPS  %.1f GB/s (%.0f B/update)\n", N, ms / 1e3,
-                    bsteps, cells * bsteps / (ms * 1e3), cells * bsteps * bpu / (ms * 1e6), bpu);
+        std::printf("[bench] uniform N=%d: %.3f s  %ld steps  %.1f MLUPS  %.1f GB/s (%.0f B/update)  state %.2f GB%s\n",
+                    N, ms / 1e3, bsteps, cells * bsteps / (ms * 1e3), cells * bsteps * bpu / (ms * 1e6), bpu,
+                    double(info.bytes_state) / 1e9, (cfg.flags & JP_FLAG_INPLACE) ? " (in place)" : "");
         jp_destroy(s);
         return 0;
     }

@@ -42,7 +42,7 @@ class Config(C.Structure):
     ]
 
 
-FLAG_SKIP_PREP, FLAG_SKIP_RESTRICT, FLAG_GRAPH, FLAG_DEFER_INIT = 1, 2, 4, 8
+FLAG_SKIP_PREP, FLAG_SKIP_RESTRICT, FLAG_GRAPH, FLAG_DEFER_INIT, FLAG_INPLACE = 1, 2, 4, 8, 16
 
 
 class Info(C.Structure):
