@@ -135,9 +135,11 @@ def load_traffic(key: str):
 
 
 def bench_storage(J, n: int, storage: str, steps: int, warmup: int, device: int, pg, sampler=None, vec: int = 0,
-                  tpb: int = 0) -> dict:
-    s = J.Solver("uniform", n=n, re=RE, u0=U0, storage=storage, device=device, vec=vec, threads_per_block=tpb)
+                  tpb: int = 0, flags: int = 0) -> dict:
+    s = J.Solver("uniform", n=n, re=RE, u0=U0, storage=storage, device=device, vec=vec, threads_per_block=tpb,
+                 flags=flags)
     try:
+        bytes_state = s.info["bytes_state"]
         s.step(warmup)
         s.sync()
         barrier(pg)
@@ -155,7 +157,7 @@ def bench_storage(J, n: int, storage: str, steps: int, warmup: int, device: int,
     cells = n ** 3
     per_launch_s = ms / 1e3 / steps
     return {"ms_per_step": ms / steps, "glups": cells * steps / (ms / 1e3) / 1e9, "launches": launches,
-            "per_launch_s": per_launch_s, "clocks": clocks, "diag": d,
+            "per_launch_s": per_launch_s, "clocks": clocks, "diag": d, "bytes_state": bytes_state,
             "achieved_gbs": BYTES_PER_UPDATE[storage] * cells / per_launch_s / 1e9}
 
 
@@ -323,7 +325,7 @@ def bench_precision(J, args, device: int) -> dict:
     enstrophy curve relative to FP64."""
     import numpy as np
 
-    n, every = args.n, args.every
+    n, every = args.n or 256, args.every
     ref = precision_run(J, n, "fp64", every, device)
     out = {"n": n, "every_steps": every, "dt_star_per_sample": float(ref["t"][1] - ref["t"][0]),
            "fp64": {k: ref[k] for k in ("peak_tstar", "peak_enstrophy", "mass_drift", "energy_monotonic", "seconds")}}
@@ -361,7 +363,7 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--n", type=int, default=None, help="cube edge (default 512; the precision study 256)")
     ap.add_argument("--no-variants", action="store_true", help="skip the FP16/BF16 lines")
     ap.add_argument("--no-amr", action="store_true", help="skip the AMR static gold line")
     ap.add_argument("--e2e-calls", type=int, default=4)
@@ -382,7 +384,7 @@ def main() -> int:
     if a.workload == "serve":  # concurrent AMR solves: one hardware queue per stream (before any CUDA call)
         os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     rank, local, world, pg = dist_setup(a.gpus)
-    n = a.n
+    n = a.n or 512
     config = {"workload": "uniform TGV D3Q19 BGK, N=%d, Re=%g, u0=%g, periodic" % (n, RE, U0),
               "n": n, "re": RE, "storage": a.storage, "cells": n ** 3,
               "l2": "inputs larger than L2 (%.1f GB of populations per step)" % (2 * Q * 4 * n ** 3 / 1e9),
@@ -410,7 +412,7 @@ def main() -> int:
                 "unit": "t*", "n_gpus": world, "steps": pr["fp64"]["seconds"], "warmup": 0, "ms_per_step": None,
                 "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (analytic Taylor-Green initial state)",
-                "config": {"workload": "uniform TGV N=%d Re=%g t*=12, FP64/FP32/FP16/BF16 storage" % (a.n, RE)},
+                "config": {"workload": "uniform TGV N=%d Re=%g t*=12, FP64/FP32/FP16/BF16 storage" % (pr["n"], RE)},
                 "precision": pr}
         if rank == 0:
             print(json.dumps(line))
@@ -441,6 +443,12 @@ def main() -> int:
                             "bytes_per_update": BYTES_PER_UPDATE[st],
                             "achieved_gbs": r["achieved_gbs"], "frac": r["achieved_gbs"] / peaks["hbm_gbs"],
                             "speedup_vs_fp32": r["glups"] / main_r["glups"]}
+        # in-place (AA) streaming: one population array, the same bytes per update
+        for st in ("fp32", "fp16"):
+            r = bench_storage(J, n, st, a.steps, a.warmup, local, pg, flags=J.FLAG_INPLACE)
+            variants[st + "_inplace"] = {"glups": r["glups"], "ms_per_step": r["ms_per_step"],
+                                         "bytes_per_update": BYTES_PER_UPDATE[st], "bytes_state": r["bytes_state"],
+                                         "achieved_gbs": r["achieved_gbs"], "frac": r["achieved_gbs"] / peaks["hbm_gbs"]}
     k = max(1, int(O_diag_every(n)))
     e2e = bench_e2e(J, n, a.e2e_calls, k, local, pg) if a.e2e_calls > 0 else None
     traffic = load_traffic("stream_collide_" + a.storage)

@@ -205,7 +205,8 @@ long long estimate_bytes(const jp_config& c) {
     if (c.kind == JP_UNIFORM) {
         const long long elem = c.storage == JP_FP64 ? 8 : (c.storage == JP_FP32 ? 4 : 2);
         const long long field = (c.storage == JP_FP64 ? 32 : 16) * n * n * n;
-        return 2 * Qn * elem * n * n * n + field + (1 << 20);
+        const long long arrays = (c.flags & JP_FLAG_INPLACE) ? 1 : 2;  // in place: one population array
+        return arrays * Qn * elem * n * n * n + field + (1 << 20);
     }
     // AMR: the pools of amr_create with the level-2 pool at its upper bound
     const long long mb = c.mb, mb3 = mb * mb * mb, sh = 6 * mb * mb + 12 * mb;

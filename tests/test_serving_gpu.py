@@ -171,6 +171,19 @@ def test_server_admission_respects_budget():
     assert starts[2] >= ends[0]
 
 
+def test_server_inplace_requests_fit_twice_as_many_with_the_same_results():
+    base = [dict(rid=200 + i, kind="uniform", n=96, re=800.0, tstar=0.3) for i in range(4)]
+    one = 2 * 19 * 4 * 96 ** 3 + 16 * 96 ** 3 + (1 << 20)
+    budget_gb = 2.5 * one / 2 ** 30                   # two two-array cubes at a time, four in place
+    two, peak2 = run_server(base, pool_gb=budget_gb, tick_steps=32)
+    inp, peak1 = run_server([dict(r, flags=J.FLAG_INPLACE) for r in base], pool_gb=budget_gb, tick_steps=32)
+    assert peak2 == 2 and peak1 == 4
+    for rid in two:
+        assert inp[rid]["status"] == 0
+        for k in ("steps", "samples", "peak_tstar", "peak_enstrophy", "energy_ratio", "mass_drift", "valid"):
+            assert inp[rid][k] == two[rid][k], (rid, k)
+
+
 def test_server_refuses_request_larger_than_pool():
     sv = J.Server(pool_gb=0.001)
     assert sv.submit(rid=7, kind="uniform", n=64, re=400.0, tstar=0.2) == 4     # JP_ERR_NOMEM
