@@ -278,6 +278,28 @@ __global__ void k_fill_int(int* __restrict__ p, int v, long long n) {
         p[i] = v;
 }
 
+// Fill list of a fine level: blocks with a face or edge neighbour slot (the D3Q19 pulls never cross
+// a corner) on another level.  Warp-aggregated append; *count is zero on entry.
+__global__ void k_fill_list(const int* __restrict__ nb, int nf, int* __restrict__ list, int* __restrict__ count) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    bool need = false;
+    if (b < nf) {
+        const int* row = nb + (size_t)b * 27;
+#pragma unroll
+        for (int e = 0; e < 27; ++e) {
+            const int m = (e % 3 != 1) + ((e / 3) % 3 != 1) + (e / 9 != 1);
+            if (m == 1 || m == 2) need |= __ldg(row + e) < 0;
+        }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, need);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (need) list[base + __popc(mask & ((1u << lane) - 1u))] = b;
+}
+
 // ---- host launchers --------------------------------------------------------------------------------
 static inline unsigned grid_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -354,6 +376,14 @@ cudaError_t adapt_dilate_marks(int* ref, int* tmp, int n, int gx, const int* pos
         if (e != cudaSuccess) return e;
         note_launch();
     }
+    return cudaGetLastError();
+}
+
+cudaError_t adapt_fill_list(const int* nb, int nf, int* list, int* count, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
+    if (e != cudaSuccess || nf <= 0) return e;
+    k_fill_list<<<grid_for(nf, 256), 256, 0, st>>>(nb, nf, list, count);
+    note_launch();
     return cudaGetLastError();
 }
 

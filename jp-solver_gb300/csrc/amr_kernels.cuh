@@ -73,9 +73,11 @@ template <int MB, class ST>
 __device__ __forceinline__ void d_prep(const typename ST::raw* __restrict__ fin,
                                                       typename ST::raw* __restrict__ pr,
                                                       const int* __restrict__ list, float nqs,
-                                                      const int* __restrict__ nlim, int blk) {
+                                                      const int* __restrict__ nlim, const int* __restrict__ gate,
+                                                      int blk) {
     using G = Geo<MB>;
     if (nlim && (int)blk >= __ldg(nlim)) return;
+    if (gate && __ldg(gate) == 0) return;  // no fine block of the next level has a ghost to fill
     const int b = list[blk];
     CELL_LOOP(cell) {
         float f[Q];
@@ -90,8 +92,8 @@ template <int MB, class ST>
 __global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const typename ST::raw* __restrict__ fin,
                                                       typename ST::raw* __restrict__ pr,
                                                       const int* __restrict__ list, float nqs,
-                                                      const int* __restrict__ nlim) {
-    d_prep<MB, ST>(fin, pr, list, nqs, nlim, (int)blockIdx.x);
+                                                      const int* __restrict__ nlim, const int* __restrict__ gate) {
+    d_prep<MB, ST>(fin, pr, list, nqs, nlim, gate, (int)blockIdx.x);
 }
 
 // trilinear of a precomputed source on the dense coarse grid (src/tgv3d_amr.cu:122-132)
@@ -155,16 +157,17 @@ __device__ __forceinline__ void prolong_prep_l1(const typename ST::raw* __restri
 }
 
 // ---- ghost shells (src/tgv3d_amr.cu:173-202) -------------------------------------------------------
-// One CTA per fine block, one thread per shell cell; a shell cell whose same-level neighbour block
-// exists (its parent is refined) is left alone: the step gathers it from that block instead.
+// One CTA per fine block that has a neighbour on another level (the fill list, built with the
+// neighbour table), one thread per shell cell; a shell cell whose same-level neighbour block exists
+// (its parent is refined) is left alone: the step gathers it from that block instead.
 template <int MB, class ST>
 __device__ __forceinline__ void d_fill_l1(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ pcb, const int* __restrict__ poct,
                                                 const int* __restrict__ nbtab, int cgx, int N,
-                                                const int* __restrict__ nlim, int blk) {
+                                                const int* __restrict__ list, const int* __restrict__ nlim, int blk) {
     using G = Geo<MB>;
     if (nlim && (int)blk >= __ldg(nlim)) return;
-    const int fb = blk;
+    const int fb = list ? __ldg(list + blk) : blk;
     const int* nbrow = nbtab + (size_t)fb * 27;
     const int cb = pcb[fb], oct = poct[fb];
     const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
@@ -185,8 +188,8 @@ template <int MB, class ST>
 __global__ void __launch_bounds__(256) k_fill_l1(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ pcb, const int* __restrict__ poct,
                                                 const int* __restrict__ nbtab, int cgx, int N,
-                                                const int* __restrict__ nlim) {
-    d_fill_l1<MB, ST>(pr, gh, pcb, poct, nbtab, cgx, N, nlim, (int)blockIdx.x);
+                                                const int* __restrict__ list, const int* __restrict__ nlim) {
+    d_fill_l1<MB, ST>(pr, gh, pcb, poct, nbtab, cgx, N, list, nlim, (int)blockIdx.x);
 }
 
 template <int MB, class ST>
@@ -194,10 +197,10 @@ __device__ __forceinline__ void d_fill_l2(const typename ST::raw* __restrict__ p
                                                 const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
                                                 const int* __restrict__ f1pos, const int* __restrict__ l1grid,
                                                 const int* __restrict__ nbtab, int l1gx, int N1,
-                                                const int* __restrict__ nlim, int blk) {
+                                                const int* __restrict__ list, const int* __restrict__ nlim, int blk) {
     using G = Geo<MB>;
     if (nlim && (int)blk >= __ldg(nlim)) return;
-    const int b = blk;
+    const int b = list ? __ldg(list + blk) : blk;
     const int* nbrow = nbtab + (size_t)b * 27;
     const int pl1 = l2pl1[b], oct = l2oct[b];
     const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
@@ -219,8 +222,8 @@ __global__ void __launch_bounds__(256) k_fill_l2(const typename ST::raw* __restr
                                                 const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
                                                 const int* __restrict__ f1pos, const int* __restrict__ l1grid,
                                                 const int* __restrict__ nbtab, int l1gx, int N1,
-                                                const int* __restrict__ nlim) {
-    d_fill_l2<MB, ST>(pr, gh, l2pl1, l2oct, f1pos, l1grid, nbtab, l1gx, N1, nlim, (int)blockIdx.x);
+                                                const int* __restrict__ list, const int* __restrict__ nlim) {
+    d_fill_l2<MB, ST>(pr, gh, l2pl1, l2oct, f1pos, l1grid, nbtab, l1gx, N1, list, nlim, (int)blockIdx.x);
 }
 
 // Restriction of one fine block, staged in shared memory as sf[q * MB^3 + cell] after its last
@@ -809,15 +812,15 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
                 L.iout, L.t0, L.t1, L.t2, L.t3, L.t4, L.t5, L.l1gx, L.nblocks);
             break;
         case OP_PREP:
-            k_prep<MB, ST><<<L.nblocks, cta, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.list, L.scale, L.nlim);
+            k_prep<MB, ST><<<L.nblocks, cta, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.list, L.scale, L.nlim, L.t0);
             break;
         case OP_FILL_L1:
             k_fill_l1<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.nbt, L.cgx, L.n,
-                                                           L.nlim);
+                                                           L.list, L.nlim);
             break;
         case OP_FILL_L2:
             k_fill_l2<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.t2, L.t3, L.nbt,
-                                                           L.l1gx, L.n1, L.nlim);
+                                                           L.l1gx, L.n1, L.list, L.nlim);
             break;
         case OP_RESTRICT:
             k_restrict<MB, ST><<<L.nblocks, cta, 0, L.st>>>(POOL(L.out), CPOOL(L.in), L.list, L.t0, L.scale, L.nlim);
@@ -890,12 +893,12 @@ __global__ void __launch_bounds__(OP == OP_FILL_L1 || OP == OP_FILL_L2 ? 256 : G
     const int blk = (int)blockIdx.x - it.begin;
     using raw = typename ST::raw;
     if constexpr (OP == OP_PREP) {
-        d_prep<MB, ST>((const raw*)it.in, (raw*)it.out, it.list, it.scale, it.nlim, blk);
+        d_prep<MB, ST>((const raw*)it.in, (raw*)it.out, it.list, it.scale, it.nlim, it.t0, blk);
     } else if constexpr (OP == OP_FILL_L1) {
-        d_fill_l1<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.nbt, it.cgx, it.n, it.nlim, blk);
+        d_fill_l1<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.nbt, it.cgx, it.n, it.list, it.nlim, blk);
     } else if constexpr (OP == OP_FILL_L2) {
-        d_fill_l2<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.t2, it.t3, it.nbt, it.l1gx, it.n1, it.nlim,
-                          blk);
+        d_fill_l2<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.t2, it.t3, it.nbt, it.l1gx, it.n1, it.list,
+                          it.nlim, blk);
     } else {
         d_restrict<MB, ST>((raw*)it.out, (const raw*)it.in, it.list, it.t0, it.scale, it.nlim, blk);
     }

@@ -40,6 +40,7 @@ struct AmrState {
     int *o_ref0 = nullptr, *o_fof0 = nullptr, *o_l1grid = nullptr, *o_ref1 = nullptr, *o_fof1 = nullptr;
     int *rank = nullptr, *deep = nullptr, *flags = nullptr;
     int *nb1 = nullptr, *nb2 = nullptr;  // same-level neighbour tables of the fine levels (27 per block)
+    int *fl1 = nullptr, *fl2 = nullptr;  // fill lists: fine blocks with ghost cells (adapt_fill_list)
     int tpb = 0;                         // threads per CTA of the per-cell steps (0: default_step_tpb)
     int vec = 0;                         // fine steps: 4 rows of four cells, 1 a cell per thread (0: default)
     float *sen0 = nullptr, *sen1 = nullptr;
@@ -61,7 +62,8 @@ struct AmrState {
     cudaGraphExec_t graph[8] = {};
     float *c0_home = nullptr, *f1_home = nullptr, *f2_home = nullptr;
 };
-enum { SC_NF1 = 0, SC_NF2, SC_SKIN0, SC_SKIN1, SC_NREF0, SC_NREF1, SC_COUNT };
+// SC_COUNT entries come from the host (upload_counts); the fill-list lengths are written on the device
+enum { SC_NF1 = 0, SC_NF2, SC_SKIN0, SC_SKIN1, SC_NREF0, SC_NREF1, SC_COUNT, SC_FILL1 = SC_COUNT, SC_FILL2, SC_ALL };
 
 // drop the captured steps and take the current buffers as the parity reference
 static void reset_graphs(AmrState* a) {
@@ -248,6 +250,7 @@ static jp_status set_cap1(jp_solver* s, int cap, bool keep) {
     TRY(regrow(s, a->rank, std::max(a->cnb0, cap), 0));
     TRY(regrow(s, a->flags, (size_t)a->cnb0 + cap, 0));
     TRY(regrow(s, a->nb1, (size_t)cap * 27, 0));
+    TRY(regrow(s, a->fl1, cap, 0));
     reset_graphs(a);
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * cap, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * cap, s->stream), "memset");
@@ -265,6 +268,7 @@ static jp_status set_cap2(jp_solver* s, int cap, bool keep) {
     TRY(regrow(s, a->l2pl1, cap, 0));
     TRY(regrow(s, a->l2oct, cap, 0));
     TRY(regrow(s, a->nb2, (size_t)cap * 27, 0));
+    TRY(regrow(s, a->fl2, cap, 0));
     reset_graphs(a);
     a->cap2 = cap;
     update_bytes(s);
@@ -324,6 +328,14 @@ static jp_status build_l1(jp_solver* s, bool restore_marks) {
     return JP_OK;
 }
 
+// fill lists of both fine levels from their neighbour tables, lengths into the device counts
+static jp_status fill_lists(jp_solver* s) {
+    AmrState* a = s->amr;
+    ACK(adapt_fill_list(a->nb1, a->nf1, a->fl1, a->step_cnt + SC_FILL1, s->stream), "fill list 1");
+    ACK(adapt_fill_list(a->nb2, a->nf2, a->fl2, a->step_cnt + SC_FILL2, s->stream), "fill list 2");
+    return JP_OK;
+}
+
 // same-level neighbour tables of both fine levels for the current grid
 static jp_status neighbour_tables(jp_solver* s) {
     AmrState* a = s->amr;
@@ -346,7 +358,8 @@ static jp_status neighbour_tables(jp_solver* s) {
     M.t4 = a->ref1;
     M.t5 = a->fof1;
     M.l1gx = a->l1gx;
-    return launch(s, OP_NBTAB_L2, M);
+    TRY(launch(s, OP_NBTAB_L2, M));
+    return fill_lists(s);
 }
 
 // gpurce_init (src/tgv3d_amr.cu:776-815)
@@ -408,8 +421,10 @@ static jp_status initial_build(jp_solver* s) {
     dfree(a, a->l2pl1);
     dfree(a, a->l2oct);
     dfree(a, a->nb2);
+    dfree(a, a->fl2);
     const size_t blk = (size_t)Q * a->MB3;
     TRY(dalloc(a, &a->nb2, (size_t)a->cap2 * 27, "cudaMalloc nb2"));
+    TRY(dalloc(a, &a->fl2, (size_t)a->cap2, "cudaMalloc fl2"));
     TRY(dalloc(a, &a->f2a, pf(a, (size_t)a->cap2 * blk), "cudaMalloc f2"));
     TRY(dalloc(a, &a->f2b, pf(a, (size_t)a->cap2 * blk), "cudaMalloc f2"));
     TRY(dalloc(a, &a->gh2, pf(a, (size_t)a->cap2 * Q * a->SH), "cudaMalloc gh2"));
@@ -528,10 +543,12 @@ static jp_status base_step(jp_solver* s) {
         L.out = a->prep0;
         L.list = a->skin0;
         L.scale = float(a->nqs01);
+        L.t0 = cnt + SC_FILL1;
         TRY(launch(s, OP_PREP, L));
         AmrLaunch F;
         F.nblocks = a->cap1;
-        F.nlim = cnt + SC_NF1;
+        F.list = a->fl1;
+        F.nlim = cnt + SC_FILL1;
         F.in = a->prep0;
         F.out = a->gh1;
         F.t0 = a->pcb;
@@ -550,10 +567,12 @@ static jp_status base_step(jp_solver* s) {
             L.out = a->prep1;
             L.list = a->skin1;
             L.scale = float(a->nqs12);
+            L.t0 = cnt + SC_FILL2;
             TRY(launch(s, OP_PREP, L));
             AmrLaunch F;
             F.nblocks = a->cap2;
-            F.nlim = cnt + SC_NF2;
+            F.list = a->fl2;
+            F.nlim = cnt + SC_FILL2;
             F.in = a->prep1;
             F.out = a->gh2;
             F.t0 = a->l2pl1;
@@ -670,6 +689,7 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
             it.list = a->skin0;
             it.scale = float(a->nqs01);
             it.nlim = a->step_cnt + SC_SKIN0;
+            it.t0 = a->step_cnt + SC_FILL1;
             return a->cnb0;
         }));
         TRY(run(OP_FILL_L1, false, [](AmrState* a, AmrItem& it) {
@@ -680,7 +700,8 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
             it.nbt = a->nb1;
             it.cgx = a->cgx;
             it.n = a->N;
-            it.nlim = a->step_cnt + SC_NF1;
+            it.list = a->fl1;
+            it.nlim = a->step_cnt + SC_FILL1;
             return a->cap1;
         }));
     }
@@ -692,6 +713,7 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
                 it.list = a->skin1;
                 it.scale = float(a->nqs12);
                 it.nlim = a->step_cnt + SC_SKIN1;
+                it.t0 = a->step_cnt + SC_FILL2;
                 return a->cap1;
             }));
             TRY(run(OP_FILL_L2, false, [](AmrState* a, AmrItem& it) {
@@ -704,7 +726,8 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
                 it.nbt = a->nb2;
                 it.l1gx = a->l1gx;
                 it.n1 = a->N1;
-                it.nlim = a->step_cnt + SC_NF2;
+                it.list = a->fl2;
+                it.nlim = a->step_cnt + SC_FILL2;
                 return a->cap2;
             }));
         }
@@ -893,7 +916,8 @@ jp_status amr_create(jp_solver* s) {
     TRY(dalloc(a, &a->flags, (size_t)a->cnb0 + a->cap1, "cudaMalloc flags"));
     TRY(dalloc(a, &a->sen1, (size_t)a->cap1, "cudaMalloc sen1"));
     TRY(dalloc(a, &a->nb1, (size_t)a->cap1 * 27, "cudaMalloc nb1"));
-    TRY(dalloc(a, &a->step_cnt, SC_COUNT, "cudaMalloc step counts"));
+    TRY(dalloc(a, &a->fl1, (size_t)a->cap1, "cudaMalloc fl1"));
+    TRY(dalloc(a, &a->step_cnt, SC_ALL, "cudaMalloc step counts"));
     a->step_cnt_host = (int*)pinned_slot_alloc();
     if (!a->step_cnt_host) return fail(JP_ERR_NOMEM, "pinned host slot");
     TRY(dalloc(a, &a->cnt_dev, 1, "cudaMalloc counts"));
@@ -1185,6 +1209,7 @@ jp_status amr_load_state(jp_solver* s, std::FILE* f) {
         if (pl.second) ACK(cudaMemcpy(pl.first, raw.data(), pl.second, cudaMemcpyHostToDevice), "pool H2D");
     }
     TRY(upload_counts(s));
+    TRY(fill_lists(s));
     ACK(wait_stream(s), "load");
     reset_graphs(a);
     update_bytes(s);
