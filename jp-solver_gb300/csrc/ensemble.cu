@@ -929,15 +929,19 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         sv->add(&jp_server_stats::diag_s, seconds_since(tw));
     }
     sv->diag_cur ^= 1;
-    // retire finished uniform solves: all steps issued, every diagnostic read back.  Their last use
-    // on the server's stream was a diagnostic that has completed (the event above), so their memory
-    // can go back to the pool in their own stream's order.  A solve that failed is retired once
-    // nothing of it is in flight.
+    // retire finished uniform solves: all steps issued, every diagnostic read back.  A solve whose
+    // step count is not a multiple of its diagnostic interval ends with steps that no diagnostic
+    // follows, and they may still run on the server's stream: its memory goes back to the pool on
+    // its own stream, ordered after everything the server's stream holds so far.  A solve that
+    // failed is retired the same way once no read-back of it is pending.
     for (size_t i = 0; i < sv->active.size();) {
         Job* j = sv->active[i];
         const bool done = j->step >= j->steps && !j->need_diag && j->inflight == 0;
         if (done || (j->error != JP_OK && j->inflight == 0)) {
             sv->active.erase(sv->active.begin() + i);
+            if (cudaEventRecord(j->s->ev0, sv->stream) != cudaSuccess ||
+                cudaStreamWaitEvent(j->s->stream, j->s->ev0, 0) != cudaSuccess)
+                cudaStreamSynchronize(sv->stream);
             finish(sv, j, j->error);
         } else {
             ++i;
