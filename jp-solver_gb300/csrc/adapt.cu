@@ -8,6 +8,7 @@
 // scans and compactions are single-CTA warp-shuffle scans, and tgt is computed on the device, so a
 // regrid needs no host round trip until the new block counts are read.  All results are integers
 // or selected elements: bit-exact by construction.
+#include "amr_common.cuh"
 #include "amr_kernels.h"
 #include "kernels.h"
 
@@ -278,26 +279,26 @@ __global__ void k_fill_int(int* __restrict__ p, int v, long long n) {
         p[i] = v;
 }
 
-// Fill list of a fine level: blocks with a face or edge neighbour slot (the D3Q19 pulls never cross
-// a corner) on another level.  Warp-aggregated append; *count is zero on entry.
-__global__ void k_fill_list(const int* __restrict__ nb, int nf, int* __restrict__ list, int* __restrict__ count) {
+// Fill list of a fine level: the blocks with a ghost-shell segment (face or edge; the D3Q19 pulls
+// never cross a corner) whose neighbour slot is on another level, as {block, mask of those
+// segments}.  Warp-aggregated append; *count is zero on entry.
+__global__ void k_fill_list(const int* __restrict__ nb, int nf, int2* __restrict__ list, int* __restrict__ count) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    bool need = false;
+    unsigned segs = 0;
     if (b < nf) {
         const int* row = nb + (size_t)b * 27;
 #pragma unroll
-        for (int e = 0; e < 27; ++e) {
-            const int m = (e % 3 != 1) + ((e / 3) % 3 != 1) + (e / 9 != 1);
-            if (m == 1 || m == 2) need |= __ldg(row + e) < 0;
-        }
+        for (int g = 0; g < 18; ++g)
+            if (__ldg(row + seg_slot(g)) < 0) segs |= 1u << g;
     }
+    const bool need = segs != 0;
     const unsigned mask = __ballot_sync(0xffffffffu, need);
     if (!mask) return;
     const int lane = threadIdx.x & 31;
     int base = 0;
     if (lane == 0) base = atomicAdd(count, __popc(mask));
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (need) list[base + __popc(mask & ((1u << lane) - 1u))] = b;
+    if (need) list[base + __popc(mask & ((1u << lane) - 1u))] = make_int2(b, (int)segs);
 }
 
 // ---- host launchers --------------------------------------------------------------------------------
@@ -380,9 +381,10 @@ cudaError_t adapt_dilate_marks(int* ref, int* tmp, int n, int gx, const int* pos
 }
 
 cudaError_t adapt_fill_list(const int* nb, int nf, int* list, int* count, cudaStream_t st) {
+    static_assert(sizeof(int2) == 2 * sizeof(int), "fill list entries are two ints");
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
     if (e != cudaSuccess || nf <= 0) return e;
-    k_fill_list<<<grid_for(nf, 256), 256, 0, st>>>(nb, nf, list, count);
+    k_fill_list<<<grid_for(nf, 256), 256, 0, st>>>(nb, nf, reinterpret_cast<int2*>(list), count);
     note_launch();
     return cudaGetLastError();
 }

@@ -96,10 +96,14 @@ __global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const typename ST::raw* _
     d_prep<MB, ST>(fin, pr, list, nqs, nlim, gate, (int)blockIdx.x);
 }
 
-// trilinear of a precomputed source on the dense coarse grid (src/tgv3d_amr.cu:122-132)
+// Trilinear prolongation from a precomputed source (k_prep), one population at a time: the eight
+// corners (pointer to the corner cell's population 0, weight) are found once per fine cell, then
+// interp() sums q over them in corner order (src/tgv3d_amr.cu:122-144).  On the dense coarse grid
+// every corner exists; on the scattered level 1 an absent corner has a null pointer and is dropped,
+// and the sum is renormalised by the weights present (wsum < 0.999).
 template <int MB, class ST>
-__device__ __forceinline__ void prolong_prep_l0(const typename ST::raw* __restrict__ pr, int cgx, int N, int gfi, int gfj,
-                                                int gfk, float (&out)[Q]) {
+__device__ __forceinline__ void corners_l0(const typename ST::raw* __restrict__ pr, int cgx, int N, int gfi, int gfj,
+                                           int gfk, const typename ST::raw* (&p)[8], float (&w)[8]) {
     constexpr int MB3 = MB * MB * MB;
     int ib, jb, kb;
     float tx, ty, tz;
@@ -107,26 +111,19 @@ __device__ __forceinline__ void prolong_prep_l0(const typename ST::raw* __restri
     tri_axis(gfj, jb, ty);
     tri_axis(gfk, kb, tz);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) out[q] = 0.f;
-    // corners unrolled: their loads are in flight together; the sums keep the corner order
-#pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
-        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
+        w[c] = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
         const int ci = pmod(ib + di, N), cj = pmod(jb + dj, N), ck = pmod(kb + dk, N);
         const int cb = ((ck / MB) * cgx + cj / MB) * cgx + ci / MB;
         const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
-        const typename ST::raw* p = pr + (size_t)cb * Q * MB3 + cc;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) out[q] += wgt * PoolIO<ST>::f(p + q * MB3, q);
+        p[c] = pr + (size_t)cb * Q * MB3 + cc;
     }
 }
-
-// trilinear of a precomputed source on the scattered L1 level, dropping absent corners and
-// renormalising (src/tgv3d_amr.cu:133-144)
 template <int MB, class ST>
-__device__ __forceinline__ void prolong_prep_l1(const typename ST::raw* __restrict__ pr, const int* __restrict__ l1grid, int l1gx,
-                                                int N1, int g2i, int g2j, int g2k, float (&out)[Q]) {
+__device__ __forceinline__ float corners_l1(const typename ST::raw* __restrict__ pr, const int* __restrict__ l1grid,
+                                            int l1gx, int N1, int g2i, int g2j, int g2k,
+                                            const typename ST::raw* (&p)[8], float (&w)[8]) {
     constexpr int MB3 = MB * MB * MB;
     int ib, jb, kb;
     float tx, ty, tz, wsum = 0.f;
@@ -134,96 +131,142 @@ __device__ __forceinline__ void prolong_prep_l1(const typename ST::raw* __restri
     tri_axis(g2j, jb, ty);
     tri_axis(g2k, kb, tz);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) out[q] = 0.f;
-    // corners unrolled: their loads are in flight together; the sums keep the corner order
-#pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
-        const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
+        w[c] = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
         const int ci = pmod(ib + di, N1), cj = pmod(jb + dj, N1), ck = pmod(kb + dk, N1);
         const int lb = __ldg(l1grid + ((ck / MB) * l1gx + cj / MB) * l1gx + ci / MB);
-        if (lb < 0) continue;
         const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
-        wsum += wgt;
-        const typename ST::raw* p = pr + (size_t)lb * Q * MB3 + cc;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) out[q] += wgt * PoolIO<ST>::f(p + q * MB3, q);
+        p[c] = lb < 0 ? nullptr : pr + (size_t)lb * Q * MB3 + cc;
+        if (lb >= 0) wsum += w[c];
     }
-    if (wsum > 0.f && wsum < 0.999f) {
-        const float inv = 1.f / wsum;
+    return wsum;
+}
+template <int MB, class ST, bool SPARSE>
+__device__ __forceinline__ float interp(const typename ST::raw* const (&p)[8], const float (&w)[8], int q) {
+    constexpr int MB3 = MB * MB * MB;
+    float acc = 0.f;
 #pragma unroll
-        for (int q = 0; q < Q; ++q) out[q] *= inv;
-    }
+    for (int c = 0; c < 8; ++c)
+        if (!SPARSE || p[c]) acc += w[c] * PoolIO<ST>::f(p[c] + q * MB3, q);
+    return acc;
+}
+
+// Populations a fine step pulls from the ghost cell at (i, j, k) just outside the block: those whose
+// velocity points from it into the block, c = -d in every direction d in which the cell lies
+// outside (5 for a face cell, 1 for an edge cell).  The fills write only these; the other slots of
+// the shell are never read.
+template <int MB>
+__device__ __forceinline__ unsigned ghost_need(int i, int j, int k) {
+    const int dx = i < 0 ? -1 : (i >= MB ? 1 : 0), dy = j < 0 ? -1 : (j >= MB ? 1 : 0), dz = k < 0 ? -1 : (k >= MB ? 1 : 0);
+    unsigned m = 0;
+#pragma unroll
+    for (int q = 1; q < Q; ++q)
+        if ((dx == 0 || cx(q) == -dx) && (dy == 0 || cy(q) == -dy) && (dz == 0 || cz(q) == -dz)) m |= 1u << q;
+    return m;
+}
+
+// Shell cell of the n-th cell of the segments in `segs` (in shell order), or -1 past their end.
+template <int MB>
+__device__ __forceinline__ int seg_cell(unsigned segs, int n) {
+    int sc = -1;
+#pragma unroll
+    for (int g = 0; g < 18; ++g)
+        if (((segs >> g) & 1u) && sc < 0) {
+            if (n < seg_size<MB>(g)) sc = seg_first<MB>(g) + n;
+            else n -= seg_size<MB>(g);
+        }
+    return sc;
 }
 
 // ---- ghost shells (src/tgv3d_amr.cu:173-202) -------------------------------------------------------
-// One CTA per fine block that has a neighbour on another level (the fill list, built with the
-// neighbour table), one thread per shell cell; a shell cell whose same-level neighbour block exists
-// (its parent is refined) is left alone: the step gathers it from that block instead.
+// One CTA per entry of the fill list {block, segments}: the fine blocks with a face or edge of the
+// shell whose neighbour is on another level (built with the neighbour table).  The CTA's threads
+// cover the cells of those segments only; the shell cells next to a same-level block are left
+// alone (the step gathers them from that block).
 template <int MB, class ST>
 __device__ __forceinline__ void d_fill_l1(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
-                                                const int* __restrict__ pcb, const int* __restrict__ poct,
-                                                const int* __restrict__ nbtab, int cgx, int N,
-                                                const int* __restrict__ list, const int* __restrict__ nlim, int blk) {
+                                                const int* __restrict__ pcb, const int* __restrict__ poct, int cgx, int N,
+                                                const int2* __restrict__ list, const int* __restrict__ nlim, int blk) {
     using G = Geo<MB>;
-    if (nlim && (int)blk >= __ldg(nlim)) return;
-    const int fb = list ? __ldg(list + blk) : blk;
-    const int* nbrow = nbtab + (size_t)fb * 27;
+    if ((int)blk >= __ldg(nlim)) return;
+    const int2 ent = __ldg(list + blk);
+    const int fb = ent.x;
+    const unsigned segs = (unsigned)ent.y;
     const int cb = pcb[fb], oct = poct[fb];
     const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
     const int ox = cbx * 2 * MB + (oct & 1) * MB, oy = cby * 2 * MB + ((oct >> 1) & 1) * MB, oz = cbz * 2 * MB + (oct >> 2) * MB;
     const int N1 = 2 * N;
-    for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
+    for (int n = threadIdx.x;; n += blockDim.x) {
+        const int t = seg_cell<MB>(segs, n);
+        if (t < 0) break;
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
-        if (__ldg(nbrow + shell_slot<MB>(i, j, k)) >= 0) continue;
         const int gfi = pmod(ox + i, N1), gfj = pmod(oy + j, N1), gfk = pmod(oz + k, N1);
-        float out[Q];
-        prolong_prep_l0<MB, ST>(pr, cgx, N, gfi, gfj, gfk, out);
+        const typename ST::raw* p[8];
+        float w[8];
+        corners_l0<MB, ST>(pr, cgx, N, gfi, gfj, gfk, p, w);
+        // only the populations a step pulls from this cell: five on a face, one on an edge
+        unsigned need = ghost_need<MB>(i, j, k);
 #pragma unroll
-        for (int q = 0; q < Q; ++q) PoolIO<ST>::put_f(gh + ((size_t)fb * Q + q) * G::SH + t, q, out[q]);
+        for (int s = 0; s < 5; ++s) {
+            if (!need) break;
+            const int q = __ffs(need) - 1;
+            need &= need - 1;
+            PoolIO<ST>::put_f(gh + ((size_t)fb * Q + q) * G::SH + t, q, interp<MB, ST, false>(p, w, q));
+        }
     }
 }
 template <int MB, class ST>
 __global__ void __launch_bounds__(256) k_fill_l1(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
-                                                const int* __restrict__ pcb, const int* __restrict__ poct,
-                                                const int* __restrict__ nbtab, int cgx, int N,
-                                                const int* __restrict__ list, const int* __restrict__ nlim) {
-    d_fill_l1<MB, ST>(pr, gh, pcb, poct, nbtab, cgx, N, list, nlim, (int)blockIdx.x);
+                                                const int* __restrict__ pcb, const int* __restrict__ poct, int cgx, int N,
+                                                const int2* __restrict__ list, const int* __restrict__ nlim) {
+    d_fill_l1<MB, ST>(pr, gh, pcb, poct, cgx, N, list, nlim, (int)blockIdx.x);
 }
 
 template <int MB, class ST>
 __device__ __forceinline__ void d_fill_l2(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
-                                                const int* __restrict__ f1pos, const int* __restrict__ l1grid,
-                                                const int* __restrict__ nbtab, int l1gx, int N1,
-                                                const int* __restrict__ list, const int* __restrict__ nlim, int blk) {
+                                                const int* __restrict__ f1pos, const int* __restrict__ l1grid, int l1gx, int N1,
+                                                const int2* __restrict__ list, const int* __restrict__ nlim, int blk) {
     using G = Geo<MB>;
-    if (nlim && (int)blk >= __ldg(nlim)) return;
-    const int b = list ? __ldg(list + blk) : blk;
-    const int* nbrow = nbtab + (size_t)b * 27;
+    if ((int)blk >= __ldg(nlim)) return;
+    const int2 ent = __ldg(list + blk);
+    const int b = ent.x;
+    const unsigned segs = (unsigned)ent.y;
     const int pl1 = l2pl1[b], oct = l2oct[b];
     const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
     const int ox = px * 2 * MB + (oct & 1) * MB, oy = py * 2 * MB + ((oct >> 1) & 1) * MB, oz = pz * 2 * MB + (oct >> 2) * MB;
     const int N2 = 2 * N1;
-    for (int t = threadIdx.x; t < G::SH; t += blockDim.x) {
+    for (int n = threadIdx.x;; n += blockDim.x) {
+        const int t = seg_cell<MB>(segs, n);
+        if (t < 0) break;
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
-        if (__ldg(nbrow + shell_slot<MB>(i, j, k)) >= 0) continue;
         const int g2i = pmod(ox + i, N2), g2j = pmod(oy + j, N2), g2k = pmod(oz + k, N2);
-        float out[Q];
-        prolong_prep_l1<MB, ST>(pr, l1grid, l1gx, N1, g2i, g2j, g2k, out);
+        const typename ST::raw* p[8];
+        float w[8];
+        const float wsum = corners_l1<MB, ST>(pr, l1grid, l1gx, N1, g2i, g2j, g2k, p, w);
+        const bool renorm = wsum > 0.f && wsum < 0.999f;
+        const float inv = renorm ? 1.f / wsum : 1.f;
+        unsigned need = ghost_need<MB>(i, j, k);
 #pragma unroll
-        for (int q = 0; q < Q; ++q) PoolIO<ST>::put_f(gh + ((size_t)b * Q + q) * G::SH + t, q, out[q]);
+        for (int s = 0; s < 5; ++s) {
+            if (!need) break;
+            const int q = __ffs(need) - 1;
+            need &= need - 1;
+            float v = interp<MB, ST, true>(p, w, q);
+            if (renorm) v *= inv;
+            PoolIO<ST>::put_f(gh + ((size_t)b * Q + q) * G::SH + t, q, v);
+        }
     }
 }
 template <int MB, class ST>
 __global__ void __launch_bounds__(256) k_fill_l2(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
-                                                const int* __restrict__ f1pos, const int* __restrict__ l1grid,
-                                                const int* __restrict__ nbtab, int l1gx, int N1,
-                                                const int* __restrict__ list, const int* __restrict__ nlim) {
-    d_fill_l2<MB, ST>(pr, gh, l2pl1, l2oct, f1pos, l1grid, nbtab, l1gx, N1, list, nlim, (int)blockIdx.x);
+                                                const int* __restrict__ f1pos, const int* __restrict__ l1grid, int l1gx, int N1,
+                                                const int2* __restrict__ list, const int* __restrict__ nlim) {
+    d_fill_l2<MB, ST>(pr, gh, l2pl1, l2oct, f1pos, l1grid, l1gx, N1, list, nlim, (int)blockIdx.x);
 }
 
 // Restriction of one fine block, staged in shared memory as sf[q * MB^3 + cell] after its last
@@ -815,12 +858,12 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
             k_prep<MB, ST><<<L.nblocks, cta, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.list, L.scale, L.nlim, L.t0);
             break;
         case OP_FILL_L1:
-            k_fill_l1<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.nbt, L.cgx, L.n,
-                                                           L.list, L.nlim);
+            k_fill_l1<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.cgx, L.n,
+                                                           reinterpret_cast<const int2*>(L.list), L.nlim);
             break;
         case OP_FILL_L2:
-            k_fill_l2<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.t2, L.t3, L.nbt,
-                                                           L.l1gx, L.n1, L.list, L.nlim);
+            k_fill_l2<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.t2, L.t3, L.l1gx,
+                                                           L.n1, reinterpret_cast<const int2*>(L.list), L.nlim);
             break;
         case OP_RESTRICT:
             k_restrict<MB, ST><<<L.nblocks, cta, 0, L.st>>>(POOL(L.out), CPOOL(L.in), L.list, L.t0, L.scale, L.nlim);
@@ -895,10 +938,11 @@ __global__ void __launch_bounds__(OP == OP_FILL_L1 || OP == OP_FILL_L2 ? 256 : G
     if constexpr (OP == OP_PREP) {
         d_prep<MB, ST>((const raw*)it.in, (raw*)it.out, it.list, it.scale, it.nlim, it.t0, blk);
     } else if constexpr (OP == OP_FILL_L1) {
-        d_fill_l1<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.nbt, it.cgx, it.n, it.list, it.nlim, blk);
+        d_fill_l1<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.cgx, it.n,
+                          reinterpret_cast<const int2*>(it.list), it.nlim, blk);
     } else if constexpr (OP == OP_FILL_L2) {
-        d_fill_l2<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.t2, it.t3, it.nbt, it.l1gx, it.n1, it.list,
-                          it.nlim, blk);
+        d_fill_l2<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.t2, it.t3, it.l1gx, it.n1,
+                          reinterpret_cast<const int2*>(it.list), it.nlim, blk);
     } else {
         d_restrict<MB, ST>((raw*)it.out, (const raw*)it.in, it.list, it.t0, it.scale, it.nlim, blk);
     }

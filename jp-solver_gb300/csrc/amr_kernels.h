@@ -10,9 +10,8 @@ enum AmrOp {
     OP_STEP_L0,        // in -> out, dense periodic coarse step
     OP_PREP,           // out[list] = prolongation source of in[list]; scale = nqs; t0 = device count of the
                        // next level's fill list (the prep is skipped when it is 0) or null
-    OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, nbt = level-1 neighbour table, list = fill list
-    OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, nbt = level-2 table,
-                       // list = fill list
+    OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, list = fill list ({block, segments} pairs)
+    OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, list = fill list
     OP_STEP_L1,        // in -> out, aux = gh1, nbt = level-1 table; t0 pcb, t1 oct; out2 = c0 restricts (scale nqi)
     OP_STEP_L2,        // in -> out, aux = gh2, nbt = level-2 table; t0 l2pl1, t1 l2oct; out2 = f1 restricts
     OP_RESTRICT,       // out = coarse, in = fine; list = refined coarse blocks, t0 = fof; scale = nqi
@@ -125,9 +124,10 @@ cudaError_t adapt_skins(const int* ref0, int cnb0, int cgx, const int* ref1, con
                         int nf1, int l1gx, int* flags, int* skin0, int* skin1, AdaptCounts* counts, cudaStream_t st);
 // set n ints to v
 cudaError_t adapt_fill(int* p, int v, long long n, cudaStream_t st);
-// fill list of a fine level: the blocks among nf with a face or edge neighbour slot of the
-// neighbour table nb (27 per block) on another level (-1), i.e. with ghost cells to fill; *count is
-// set (the list's order is not fixed: each block's fill is independent of the others)
+// fill list of a fine level: the blocks among nf with a ghost-shell segment (face or edge) whose
+// slot of the neighbour table nb (27 per block) is on another level (-1), as pairs {block, mask of
+// those segments} (list holds 2 ints per entry); *count is set.  The list's order is not fixed:
+// each block's fill is independent of the others.
 cudaError_t adapt_fill_list(const int* nb, int nf, int* list, int* count, cudaStream_t st);
 // dilate refinement marks by `layers` block layers (tmp: n ints of scratch); level 1 with the
 // position map pos, the grid map and the deep mask (marks only on deep blocks)

@@ -40,7 +40,7 @@ struct AmrState {
     int *o_ref0 = nullptr, *o_fof0 = nullptr, *o_l1grid = nullptr, *o_ref1 = nullptr, *o_fof1 = nullptr;
     int *rank = nullptr, *deep = nullptr, *flags = nullptr;
     int *nb1 = nullptr, *nb2 = nullptr;  // same-level neighbour tables of the fine levels (27 per block)
-    int *fl1 = nullptr, *fl2 = nullptr;  // fill lists: fine blocks with ghost cells (adapt_fill_list)
+    int *fl1 = nullptr, *fl2 = nullptr;  // fill lists: {block, shell segments} of the blocks with ghosts
     int tpb = 0;                         // threads per CTA of the per-cell steps (0: default_step_tpb)
     int vec = 0;                         // fine steps: 4 rows of four cells, 1 a cell per thread (0: default)
     float *sen0 = nullptr, *sen1 = nullptr;
@@ -250,7 +250,7 @@ static jp_status set_cap1(jp_solver* s, int cap, bool keep) {
     TRY(regrow(s, a->rank, std::max(a->cnb0, cap), 0));
     TRY(regrow(s, a->flags, (size_t)a->cnb0 + cap, 0));
     TRY(regrow(s, a->nb1, (size_t)cap * 27, 0));
-    TRY(regrow(s, a->fl1, cap, 0));
+    TRY(regrow(s, a->fl1, 2 * (size_t)cap, 0));
     reset_graphs(a);
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * cap, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * cap, s->stream), "memset");
@@ -268,7 +268,7 @@ static jp_status set_cap2(jp_solver* s, int cap, bool keep) {
     TRY(regrow(s, a->l2pl1, cap, 0));
     TRY(regrow(s, a->l2oct, cap, 0));
     TRY(regrow(s, a->nb2, (size_t)cap * 27, 0));
-    TRY(regrow(s, a->fl2, cap, 0));
+    TRY(regrow(s, a->fl2, 2 * (size_t)cap, 0));
     reset_graphs(a);
     a->cap2 = cap;
     update_bytes(s);
@@ -424,7 +424,7 @@ static jp_status initial_build(jp_solver* s) {
     dfree(a, a->fl2);
     const size_t blk = (size_t)Q * a->MB3;
     TRY(dalloc(a, &a->nb2, (size_t)a->cap2 * 27, "cudaMalloc nb2"));
-    TRY(dalloc(a, &a->fl2, (size_t)a->cap2, "cudaMalloc fl2"));
+    TRY(dalloc(a, &a->fl2, 2 * (size_t)a->cap2, "cudaMalloc fl2"));
     TRY(dalloc(a, &a->f2a, pf(a, (size_t)a->cap2 * blk), "cudaMalloc f2"));
     TRY(dalloc(a, &a->f2b, pf(a, (size_t)a->cap2 * blk), "cudaMalloc f2"));
     TRY(dalloc(a, &a->gh2, pf(a, (size_t)a->cap2 * Q * a->SH), "cudaMalloc gh2"));
@@ -553,7 +553,6 @@ static jp_status base_step(jp_solver* s) {
         F.out = a->gh1;
         F.t0 = a->pcb;
         F.t1 = a->oct;
-        F.nbt = a->nb1;
         F.cgx = a->cgx;
         F.n = a->N;
         TRY(launch(s, OP_FILL_L1, F));
@@ -579,7 +578,6 @@ static jp_status base_step(jp_solver* s) {
             F.t1 = a->l2oct;
             F.t2 = a->f1pos;
             F.t3 = a->l1grid;
-            F.nbt = a->nb2;
             F.l1gx = a->l1gx;
             F.n1 = a->N1;
             TRY(launch(s, OP_FILL_L2, F));
@@ -697,7 +695,6 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
             it.out = a->gh1;
             it.t0 = a->pcb;
             it.t1 = a->oct;
-            it.nbt = a->nb1;
             it.cgx = a->cgx;
             it.n = a->N;
             it.list = a->fl1;
@@ -723,7 +720,6 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
                 it.t1 = a->l2oct;
                 it.t2 = a->f1pos;
                 it.t3 = a->l1grid;
-                it.nbt = a->nb2;
                 it.l1gx = a->l1gx;
                 it.n1 = a->N1;
                 it.list = a->fl2;
@@ -916,7 +912,7 @@ jp_status amr_create(jp_solver* s) {
     TRY(dalloc(a, &a->flags, (size_t)a->cnb0 + a->cap1, "cudaMalloc flags"));
     TRY(dalloc(a, &a->sen1, (size_t)a->cap1, "cudaMalloc sen1"));
     TRY(dalloc(a, &a->nb1, (size_t)a->cap1 * 27, "cudaMalloc nb1"));
-    TRY(dalloc(a, &a->fl1, (size_t)a->cap1, "cudaMalloc fl1"));
+    TRY(dalloc(a, &a->fl1, 2 * (size_t)a->cap1, "cudaMalloc fl1"));
     TRY(dalloc(a, &a->step_cnt, SC_ALL, "cudaMalloc step counts"));
     a->step_cnt_host = (int*)pinned_slot_alloc();
     if (!a->step_cnt_host) return fail(JP_ERR_NOMEM, "pinned host slot");
