@@ -301,6 +301,37 @@ __global__ void k_fill_list(const int* __restrict__ nb, int nf, int2* __restrict
     if (need) list[base + __popc(mask & ((1u << lane) - 1u))] = make_int2(b, (int)segs);
 }
 
+// Prep list of a level: the skin blocks with a change of refinement among their 27 neighbour blocks
+// (periodic), as {block, mask of the refined ones}.  Level 0: blocks are positions of the dense grid
+// of edge gx (pos null); level 1: pos[b] in the level-1 grid `grid`, an absent block unrefined.
+__global__ void k_prep_list(const int* __restrict__ skin, int nskin, const int* __restrict__ ref,
+                            const int* __restrict__ pos, const int* __restrict__ grid, int gx,
+                            int2* __restrict__ list, int* __restrict__ count) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned rm = 0;
+    int b = 0;
+    if (s < nskin) {
+        b = skin[s];
+        const int p = pos ? pos[b] : b;
+        const int px = p % gx, py = (p / gx) % gx, pz = p / (gx * gx);
+#pragma unroll 1
+        for (int e = 0; e < 27; ++e) {
+            const int nx = (px + e % 3 - 1 + gx) % gx, ny = (py + (e / 3) % 3 - 1 + gx) % gx, nz = (pz + e / 9 - 1 + gx) % gx;
+            const int np = (nz * gx + ny) * gx + nx;
+            const int nb = pos ? grid[np] : np;
+            if (nb >= 0 && ref[nb] != 0) rm |= 1u << e;
+        }
+    }
+    const bool need = rm != 0u && rm != (1u << 27) - 1u;
+    const unsigned mask = __ballot_sync(0xffffffffu, need);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (need) list[base + __popc(mask & ((1u << lane) - 1u))] = make_int2(b, (int)rm);
+}
+
 // ---- host launchers --------------------------------------------------------------------------------
 static inline unsigned grid_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -385,6 +416,16 @@ cudaError_t adapt_fill_list(const int* nb, int nf, int* list, int* count, cudaSt
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
     if (e != cudaSuccess || nf <= 0) return e;
     k_fill_list<<<grid_for(nf, 256), 256, 0, st>>>(nb, nf, reinterpret_cast<int2*>(list), count);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t adapt_prep_list(const int* skin, int nskin, const int* ref, const int* pos, const int* grid, int gx,
+                            int* list, int* count, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
+    if (e != cudaSuccess || nskin <= 0) return e;
+    k_prep_list<<<grid_for(nskin, 256), 256, 0, st>>>(skin, nskin, ref, pos, grid, gx, reinterpret_cast<int2*>(list),
+                                                       count);
     note_launch();
     return cudaGetLastError();
 }

@@ -69,17 +69,35 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const typename ST::
 }
 
 // ---- prolongation sources on a block list (src/tgv3d_amr.cu:160-171) -----------------------------
+// Only the cells a fill can read are prepared.  A fill interpolates a ghost cell of a fine block
+// from the 2x2x2 parent cells around it; the parent cell U holding the ghost is unrefined, the parent
+// R of the fine cell next to it is refined, and every one of those corners lies within one cell of
+// both (per axis).  So a fill reads only interface cells, whose 3x3x3 neighbourhood holds refined and
+// unrefined cells; other cells of a skin block keep stale values nobody reads.  Refinement is per
+// block, so the prep list (adapt_prep_list) holds the skin blocks with a change of refinement around
+// them and the mask of their refined neighbour blocks, and a cell is an interface cell if the
+// blocks its neighbourhood reaches are mixed.
 template <int MB, class ST>
 __device__ __forceinline__ void d_prep(const typename ST::raw* __restrict__ fin,
                                                       typename ST::raw* __restrict__ pr,
-                                                      const int* __restrict__ list, float nqs,
+                                                      const int2* __restrict__ list, float nqs,
                                                       const int* __restrict__ nlim, const int* __restrict__ gate,
                                                       int blk) {
     using G = Geo<MB>;
-    if (nlim && (int)blk >= __ldg(nlim)) return;
+    if ((int)blk >= __ldg(nlim)) return;
     if (gate && __ldg(gate) == 0) return;  // no fine block of the next level has a ghost to fill
-    const int b = list[blk];
+    const int2 ent = __ldg(list + blk);
+    const int b = ent.x;
+    const unsigned rm = (unsigned)ent.y;
     CELL_LOOP(cell) {
+        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
+        // slots of the blocks the cell's neighbourhood reaches: per axis 0..2 (offset -1..1)
+        const unsigned mx = (i == 0 ? 3u : (i == MB - 1 ? 6u : 2u)), my = (j == 0 ? 3u : (j == MB - 1 ? 6u : 2u)),
+                       mz = (k == 0 ? 3u : (k == MB - 1 ? 6u : 2u));
+        const unsigned plane = ((my & 1u) ? mx : 0u) | ((my & 2u) ? mx << 3 : 0u) | ((my & 4u) ? mx << 6 : 0u);
+        const unsigned span = ((mz & 1u) ? plane : 0u) | ((mz & 2u) ? plane << 9 : 0u) | ((mz & 4u) ? plane << 18 : 0u);
+        const unsigned sel = rm & span;
+        if (sel == 0u || sel == span) continue;
         float f[Q];
 #pragma unroll
         for (int q = 0; q < Q; ++q) f[q] = PoolIO<ST>::f(fin + ((size_t)b * Q + q) * G::MB3 + cell, q);
@@ -91,7 +109,7 @@ __device__ __forceinline__ void d_prep(const typename ST::raw* __restrict__ fin,
 template <int MB, class ST>
 __global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const typename ST::raw* __restrict__ fin,
                                                       typename ST::raw* __restrict__ pr,
-                                                      const int* __restrict__ list, float nqs,
+                                                      const int2* __restrict__ list, float nqs,
                                                       const int* __restrict__ nlim, const int* __restrict__ gate) {
     d_prep<MB, ST>(fin, pr, list, nqs, nlim, gate, (int)blockIdx.x);
 }
@@ -855,7 +873,8 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
                 L.iout, L.t0, L.t1, L.t2, L.t3, L.t4, L.t5, L.l1gx, L.nblocks);
             break;
         case OP_PREP:
-            k_prep<MB, ST><<<L.nblocks, cta, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.list, L.scale, L.nlim, L.t0);
+            k_prep<MB, ST><<<L.nblocks, cta, 0, L.st>>>(CPOOL(L.in), POOL(L.out),
+                                                        reinterpret_cast<const int2*>(L.list), L.scale, L.nlim, L.t0);
             break;
         case OP_FILL_L1:
             k_fill_l1<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.cgx, L.n,
@@ -936,7 +955,8 @@ __global__ void __launch_bounds__(OP == OP_FILL_L1 || OP == OP_FILL_L2 ? 256 : G
     const int blk = (int)blockIdx.x - it.begin;
     using raw = typename ST::raw;
     if constexpr (OP == OP_PREP) {
-        d_prep<MB, ST>((const raw*)it.in, (raw*)it.out, it.list, it.scale, it.nlim, it.t0, blk);
+        d_prep<MB, ST>((const raw*)it.in, (raw*)it.out, reinterpret_cast<const int2*>(it.list), it.scale, it.nlim,
+                       it.t0, blk);
     } else if constexpr (OP == OP_FILL_L1) {
         d_fill_l1<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.cgx, it.n,
                           reinterpret_cast<const int2*>(it.list), it.nlim, blk);

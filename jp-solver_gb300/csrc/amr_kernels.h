@@ -8,8 +8,9 @@ namespace amr {
 enum AmrOp {
     OP_INIT = 0,       // out = TGV state of the coarse grid
     OP_STEP_L0,        // in -> out, dense periodic coarse step
-    OP_PREP,           // out[list] = prolongation source of in[list]; scale = nqs; t0 = device count of the
-                       // next level's fill list (the prep is skipped when it is 0) or null
+    OP_PREP,           // out = prolongation source of in at the cells a fill can read, for the blocks of
+                       // the prep list (list: {block, refined-neighbour mask}); scale = nqs; t0 = device
+                       // count of the next level's fill list (skipped when 0) or null
     OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, list = fill list ({block, segments} pairs)
     OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, list = fill list
     OP_STEP_L1,        // in -> out, aux = gh1, nbt = level-1 table; t0 pcb, t1 oct; out2 = c0 restricts (scale nqi)
@@ -129,6 +130,11 @@ cudaError_t adapt_fill(int* p, int v, long long n, cudaStream_t st);
 // those segments} (list holds 2 ints per entry); *count is set.  The list's order is not fixed:
 // each block's fill is independent of the others.
 cudaError_t adapt_fill_list(const int* nb, int nf, int* list, int* count, cudaStream_t st);
+// prep list of a level: the skin blocks whose 27 neighbour blocks (periodic) mix refined and
+// unrefined, as pairs {block, mask of the refined neighbours (bit = slot)}; level 0: pos null and
+// gx = cgx; level 1: pos = f1pos, grid = l1grid, gx = l1gx (absent blocks unrefined).  *count is set.
+cudaError_t adapt_prep_list(const int* skin, int nskin, const int* ref, const int* pos, const int* grid, int gx,
+                            int* list, int* count, cudaStream_t st);
 // dilate refinement marks by `layers` block layers (tmp: n ints of scratch); level 1 with the
 // position map pos, the grid map and the deep mask (marks only on deep blocks)
 cudaError_t adapt_dilate_marks(int* ref, int* tmp, int n, int gx, const int* pos, const int* grid, const int* deep,

@@ -41,6 +41,7 @@ struct AmrState {
     int *rank = nullptr, *deep = nullptr, *flags = nullptr;
     int *nb1 = nullptr, *nb2 = nullptr;  // same-level neighbour tables of the fine levels (27 per block)
     int *fl1 = nullptr, *fl2 = nullptr;  // fill lists: {block, shell segments} of the blocks with ghosts
+    int *pl0 = nullptr, *pl1 = nullptr;  // prep lists: {skin block, refined neighbours} (adapt_prep_list)
     int tpb = 0;                         // threads per CTA of the per-cell steps (0: default_step_tpb)
     int vec = 0;                         // fine steps: 4 rows of four cells, 1 a cell per thread (0: default)
     float *sen0 = nullptr, *sen1 = nullptr;
@@ -63,7 +64,8 @@ struct AmrState {
     float *c0_home = nullptr, *f1_home = nullptr, *f2_home = nullptr;
 };
 // SC_COUNT entries come from the host (upload_counts); the fill-list lengths are written on the device
-enum { SC_NF1 = 0, SC_NF2, SC_SKIN0, SC_SKIN1, SC_NREF0, SC_NREF1, SC_COUNT, SC_FILL1 = SC_COUNT, SC_FILL2, SC_ALL };
+enum { SC_NF1 = 0, SC_NF2, SC_SKIN0, SC_SKIN1, SC_NREF0, SC_NREF1, SC_COUNT, SC_FILL1 = SC_COUNT, SC_FILL2, SC_PREP0,
+       SC_PREP1, SC_ALL };
 
 // drop the captured steps and take the current buffers as the parity reference
 static void reset_graphs(AmrState* a) {
@@ -178,6 +180,16 @@ static jp_status upload_counts(jp_solver* s) {
     return JP_OK;
 }
 
+// prep lists of both levels from their skin lists and refinement marks, lengths into the device counts
+static jp_status prep_lists(jp_solver* s) {
+    AmrState* a = s->amr;
+    ACK(adapt_prep_list(a->skin0, a->n_skin0, a->ref0, nullptr, nullptr, a->cgx, a->pl0, a->step_cnt + SC_PREP0,
+                        s->stream), "prep list 0");
+    ACK(adapt_prep_list(a->skin1, a->n_skin1, a->ref1, a->f1pos, a->l1grid, a->l1gx, a->pl1, a->step_cnt + SC_PREP1,
+                        s->stream), "prep list 1");
+    return JP_OK;
+}
+
 static jp_status skins(jp_solver* s) {
     AmrState* a = s->amr;
     ACK(adapt_skins(a->ref0, a->cnb0, a->cgx, a->ref1, a->f1pos, a->l1grid, a->nf1, a->l1gx, a->flags, a->skin0,
@@ -185,6 +197,7 @@ static jp_status skins(jp_solver* s) {
     TRY(read_counts(s));
     a->n_skin0 = a->cnt_host->n_skin0;
     a->n_skin1 = a->cnt_host->n_skin1;
+    TRY(prep_lists(s));
     return upload_counts(s);
 }
 
@@ -251,6 +264,7 @@ static jp_status set_cap1(jp_solver* s, int cap, bool keep) {
     TRY(regrow(s, a->flags, (size_t)a->cnb0 + cap, 0));
     TRY(regrow(s, a->nb1, (size_t)cap * 27, 0));
     TRY(regrow(s, a->fl1, 2 * (size_t)cap, 0));
+    TRY(regrow(s, a->pl1, 2 * (size_t)cap, 0));
     reset_graphs(a);
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * cap, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * cap, s->stream), "memset");
@@ -538,10 +552,10 @@ static jp_status base_step(jp_solver* s) {
     if (!skip_prep) {
         AmrLaunch L;
         L.nblocks = a->cnb0;
-        L.nlim = cnt + SC_SKIN0;
+        L.nlim = cnt + SC_PREP0;
         L.in = a->c0a;
         L.out = a->prep0;
-        L.list = a->skin0;
+        L.list = a->pl0;
         L.scale = float(a->nqs01);
         L.t0 = cnt + SC_FILL1;
         TRY(launch(s, OP_PREP, L));
@@ -561,10 +575,10 @@ static jp_status base_step(jp_solver* s) {
         if (!skip_prep) {
             AmrLaunch L;
             L.nblocks = a->cap1;
-            L.nlim = cnt + SC_SKIN1;
+            L.nlim = cnt + SC_PREP1;
             L.in = a->f1a;
             L.out = a->prep1;
-            L.list = a->skin1;
+            L.list = a->pl1;
             L.scale = float(a->nqs12);
             L.t0 = cnt + SC_FILL2;
             TRY(launch(s, OP_PREP, L));
@@ -684,9 +698,9 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
         TRY(run(OP_PREP, false, [](AmrState* a, AmrItem& it) {
             it.in = a->c0a;
             it.out = a->prep0;
-            it.list = a->skin0;
+            it.list = a->pl0;
             it.scale = float(a->nqs01);
-            it.nlim = a->step_cnt + SC_SKIN0;
+            it.nlim = a->step_cnt + SC_PREP0;
             it.t0 = a->step_cnt + SC_FILL1;
             return a->cnb0;
         }));
@@ -707,9 +721,9 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
             TRY(run(OP_PREP, false, [](AmrState* a, AmrItem& it) {
                 it.in = a->f1a;
                 it.out = a->prep1;
-                it.list = a->skin1;
+                it.list = a->pl1;
                 it.scale = float(a->nqs12);
-                it.nlim = a->step_cnt + SC_SKIN1;
+                it.nlim = a->step_cnt + SC_PREP1;
                 it.t0 = a->step_cnt + SC_FILL2;
                 return a->cap1;
             }));
@@ -913,6 +927,8 @@ jp_status amr_create(jp_solver* s) {
     TRY(dalloc(a, &a->sen1, (size_t)a->cap1, "cudaMalloc sen1"));
     TRY(dalloc(a, &a->nb1, (size_t)a->cap1 * 27, "cudaMalloc nb1"));
     TRY(dalloc(a, &a->fl1, 2 * (size_t)a->cap1, "cudaMalloc fl1"));
+    TRY(dalloc(a, &a->pl1, 2 * (size_t)a->cap1, "cudaMalloc pl1"));
+    TRY(dalloc(a, &a->pl0, 2 * (size_t)a->cnb0, "cudaMalloc pl0"));
     TRY(dalloc(a, &a->step_cnt, SC_ALL, "cudaMalloc step counts"));
     a->step_cnt_host = (int*)pinned_slot_alloc();
     if (!a->step_cnt_host) return fail(JP_ERR_NOMEM, "pinned host slot");
@@ -1206,6 +1222,7 @@ jp_status amr_load_state(jp_solver* s, std::FILE* f) {
     }
     TRY(upload_counts(s));
     TRY(fill_lists(s));
+    TRY(prep_lists(s));
     ACK(wait_stream(s), "load");
     reset_graphs(a);
     update_bytes(s);
