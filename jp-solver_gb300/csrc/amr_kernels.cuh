@@ -441,22 +441,25 @@ struct RowGeo {
     static constexpr int TPB = SEGS < 256 ? SEGS : 256;          // threads per CTA
 };
 
-template <int MB, class ST, bool FUSE>
+template <int MB, class ST, bool FUSE, bool WALK>
 __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restrict__ fa,
                                                  typename ST::raw* __restrict__ fbuf,
                                                  const typename ST::raw* __restrict__ gh,
                                                  const int* __restrict__ nbtab, const int* __restrict__ parent,
                                                  const int* __restrict__ poct, float om,
                                                  typename ST::raw* __restrict__ parent_pool, float nqi,
-                                                 const int* __restrict__ nlim, int blk) {
+                                                 const int* __restrict__ nlim, int blk, int stride) {
     using G = Geo<MB>;
     using RG = RowGeo<MB>;
     using raw = typename ST::raw;
     constexpr int M = MB - 1, MB3 = G::MB3, SH = G::SH;
     static_assert(MB % 4 == 0 && 32 % RG::SPR == 0 && RG::SEGS % RG::TPB == 0, "row mapping");
     extern __shared__ float sf[];
-    if (nlim && (int)blk >= __ldg(nlim)) return;  // whole CTA
-    const int b = blk;
+    const int nblk = __ldg(nlim);
+    if (!WALK && blk >= nblk) return;  // whole CTA
+    // WALK: blocks blk, blk + stride, ... (a resident grid walks the level; the loop bound is
+    // CTA-uniform, so the barriers of the fused restriction stay uniform); else the one block blk
+    for (int b = blk; b < nblk; b += stride) {
     const int* nbrow = nbtab + (size_t)b * 27;
     for (int seg = threadIdx.x; seg < RG::SEGS; seg += RG::TPB) {
         const int s = seg % RG::SPR, r = seg / RG::SPR, j = r % MB, k = r / MB, i0 = 4 * s;
@@ -523,6 +526,9 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
     if (FUSE) {
         __syncthreads();
         restrict_octant<MB, ST>(sf, parent_pool + (size_t)parent[b] * Q * G::MB3, poct[b], nqi);
+        if (WALK && b + stride < nblk) __syncthreads();  // the next block stages into sf (CTA-uniform test)
+    }
+    if (!WALK) break;
     }
 }
 // CTAs per SM the rows kernels are built for: 16-bit rows hold half the bytes in flight per thread,
@@ -530,12 +536,29 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
 template <int MB, class ST>
 constexpr int rows_min_blocks() { return (sizeof(typename ST::raw) == 2 ? 640 : 512) / RowGeo<MB>::TPB; }
 
-template <int MB, class ST, bool FUSE>
+template <int MB, class ST, bool FUSE, bool WALK>
 __global__ void __launch_bounds__(RowGeo<MB>::TPB, (rows_min_blocks<MB, ST>())) k_step_fine_rows(
     const typename ST::raw* __restrict__ fa, typename ST::raw* __restrict__ fbuf, const typename ST::raw* __restrict__ gh,
     const int* __restrict__ nbtab, const int* __restrict__ parent, const int* __restrict__ poct, float om,
     typename ST::raw* __restrict__ parent_pool, float nqi, const int* __restrict__ nlim) {
-    d_step_fine_rows<MB, ST, FUSE>(fa, fbuf, gh, nbtab, parent, poct, om, parent_pool, nqi, nlim, (int)blockIdx.x);
+    d_step_fine_rows<MB, ST, FUSE, WALK>(fa, fbuf, gh, nbtab, parent, poct, om, parent_pool, nqi, nlim,
+                                         (int)blockIdx.x, (int)gridDim.x);
+}
+
+// Resident CTAs of a rows kernel on this device (SMs x CTAs per SM), the grid its launches use: each
+// CTA walks the level's blocks, so the start of a CTA (the block count, the first table reads) is
+// paid once per CTA instead of once per block.
+template <int MB, class ST, bool FUSE>
+static int rows_grid_cap() {
+    static const int cap = [] {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step_fine_rows<MB, ST, FUSE, true>, RowGeo<MB>::TPB,
+                                                      FUSE ? sizeof(float) * Q * Geo<MB>::MB3 : 0);
+        return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+    }();
+    return cap;
 }
 
 // ---- restriction (src/tgv3d_amr.cu:275-298, 357-381) -------------------------------------------------
@@ -824,12 +847,20 @@ template <int MB, class ST>
 static void launch_rows(const AmrLaunch& L) {
     using G = Geo<MB>;
     constexpr int T = RowGeo<MB>::TPB;
-    if (L.out2)
-        k_step_fine_rows<MB, ST, true><<<L.nblocks, T, sizeof(float) * Q * G::MB3, L.st>>>(
-            CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.t0, L.t1, L.omega, POOL(L.out2), L.scale, L.nlim);
-    else
-        k_step_fine_rows<MB, ST, false><<<L.nblocks, T, 0, L.st>>>(CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt,
-                                                                    L.t0, L.t1, L.omega, nullptr, 0.f, L.nlim);
+    // FP32 with the fused restriction keeps a CTA per block: walking blocks costs it a barrier per
+    // block (the shared staging is reused) and the loop's registers, more than the CTA starts saved
+    constexpr size_t sm = sizeof(float) * Q * G::MB3;
+    if (L.out2) {
+        if constexpr (sizeof(typename ST::raw) == 4)
+            k_step_fine_rows<MB, ST, true, false><<<L.nblocks, T, sm, L.st>>>(
+                CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.t0, L.t1, L.omega, POOL(L.out2), L.scale, L.nlim);
+        else
+            k_step_fine_rows<MB, ST, true, true><<<std::min(L.nblocks, rows_grid_cap<MB, ST, true>()), T, sm, L.st>>>(
+                CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.t0, L.t1, L.omega, POOL(L.out2), L.scale, L.nlim);
+    } else {
+        k_step_fine_rows<MB, ST, false, true><<<std::min(L.nblocks, rows_grid_cap<MB, ST, false>()), T, 0, L.st>>>(
+            CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.t0, L.t1, L.omega, nullptr, 0.f, L.nlim);
+    }
 }
 
 template <int MB, class ST>
@@ -906,6 +937,12 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
                 reinterpret_cast<float*>(L.out));
             break;
         }
+        case OP_WARM:  // launch shapes of the rows steps, found before any graph capture
+            if constexpr (MB >= 8) {
+                if constexpr (MB <= 8) rows_grid_cap<MB, ST, true>();
+                rows_grid_cap<MB, ST, false>();
+            }
+            return cudaGetLastError();
         default:
             return cudaErrorInvalidValue;
     }
@@ -931,8 +968,8 @@ __global__ void __launch_bounds__(RowGeo<MB>::TPB, (rows_min_blocks<MB, ST>())) 
     const AmrItem& it = B.it[batch_member(B)];
     const int blk = (int)blockIdx.x - it.begin;
     using raw = typename ST::raw;
-    d_step_fine_rows<MB, ST, FUSE>((const raw*)it.in, (raw*)it.out, (const raw*)it.aux, it.nbt, it.t0, it.t1, it.omega,
-                                   (raw*)it.out2, it.scale, it.nlim, blk);
+    d_step_fine_rows<MB, ST, FUSE, false>((const raw*)it.in, (raw*)it.out, (const raw*)it.aux, it.nbt, it.t0, it.t1,
+                                          it.omega, (raw*)it.out2, it.scale, it.nlim, blk, 0);
 }
 
 template <int MB, class ST, int TPB, bool FUSE, bool L0>

@@ -22,8 +22,9 @@ enum AmrOp {
     OP_SENSOR,         // in = level, out = sensor; aux = override values|null, t0 = override position map|null
     OP_COMPOSITE,      // in = c0, aux = f1, aux2 = f2, out = field; t0 ref1, t1 fof1, t2 l1grid
     OP_NBTAB_L1,       // iout = level-1 neighbour table (nblocks = nf1); t0 pcb, t1 oct, t2 ref0, t3 fof0
-    OP_NBTAB_L2        // iout = level-2 neighbour table (nblocks = nf2); t0 l2pl1, t1 l2oct, t2 f1pos,
+    OP_NBTAB_L2,       // iout = level-2 neighbour table (nblocks = nf2); t0 l2pl1, t1 l2oct, t2 f1pos,
                        // t3 l1grid, t4 ref1, t5 fof1
+    OP_WARM            // no launch: find the resident grid of the row steps (before any graph capture)
 };
 
 // Population arrays (pools, prolongation sources, ghost shells) are in the solver's storage format

@@ -942,6 +942,7 @@ jp_status amr_create(jp_solver* s) {
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->l1grid, 0xFF, sizeof(int) * a->NG1, s->stream), "memset");
+    TRY(launch(s, OP_WARM, AmrLaunch()));
     if (s->cfg.flags & JP_FLAG_DEFER_INIT) return JP_OK;
     return amr_init(s);
 }
