@@ -281,6 +281,30 @@ def serve_run(J, reqs: list, device: int, open_loop: bool, max_active: int = 0, 
             "events": {k: v for k, v in stats.items() if not k.endswith("_s")}}
 
 
+def program_args(J, r: dict, device: int) -> list:
+    """The drop-in program and flags that run request r as a solve of its own."""
+    prog = os.path.join(ROOT, "jp-solver_gb300", "bin", "amr" if r["kind"] == "amr" else "uniform")
+    a = [prog, "--n", str(r["n"]), "--re", repr(r["re"]), "--tstar", repr(r["tstar"]), "--prec", r["storage"],
+         "--device", str(device)]
+    if r["kind"] == "amr":
+        a += ["--l1", r["l1_mode"], "--l2", r["l2_mode"], "--frac1", repr(r["frac1"]), "--frac2", repr(r["frac2"]),
+              "--adapt", str(r["adapt_every"]), "--graph", "1" if r.get("flags", 0) & J.FLAG_GRAPH else "0"]
+    return a
+
+
+def programs_one_at_a_time(J, reqs: list, device: int) -> dict:
+    """The reference's way to run an ensemble: one program per solve, one after another (here the
+    drop-in programs, each a process with its own CUDA context)."""
+    import subprocess
+
+    t0 = time.perf_counter()
+    codes = [subprocess.run(program_args(J, r, device), stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL).returncode
+             for _, r in reqs]
+    span = time.perf_counter() - t0
+    return {"solves": len(reqs), "seconds": span, "solves_per_s": len(reqs) / span,
+            "exit_codes": {str(c): codes.count(c) for c in sorted(set(codes))}}
+
+
 def bench_serve(J, args, device: int) -> dict:
     reqs = c5_requests(J, args.requests, args.rate, args.seed)
     open_r = serve_run(J, reqs, device, open_loop=True)
@@ -288,9 +312,14 @@ def bench_serve(J, args, device: int) -> dict:
     sample = reqs[:m]
     batched = serve_run(J, sample, device, open_loop=False)
     single = serve_run(J, sample, device, open_loop=False, max_active=1)
-    return {"open_loop": open_r, "closed_loop": {"sample": m, "batched_solves_per_s": batched["solves_per_s"],
-                                                 "one_at_a_time_solves_per_s": single["solves_per_s"],
-                                                 "speedup": batched["solves_per_s"] / single["solves_per_s"]}}
+    closed = {"sample": m, "batched_solves_per_s": batched["solves_per_s"],
+              "one_at_a_time_solves_per_s": single["solves_per_s"],
+              "speedup": batched["solves_per_s"] / single["solves_per_s"]}
+    if args.programs:
+        pr = programs_one_at_a_time(J, sample, device)
+        closed["programs_one_at_a_time"] = pr
+        closed["speedup_vs_programs"] = batched["solves_per_s"] / pr["solves_per_s"]
+    return {"open_loop": open_r, "closed_loop": closed}
 
 
 def precision_run(J, n: int, storage: str, every: int, device: int, tstar: float = 12.0) -> dict:
@@ -378,6 +407,8 @@ def main() -> int:
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--compare", type=int, default=200, help="requests in the batched vs one-at-a-time comparison")
+    ap.add_argument("--programs", type=int, default=1,
+                    help="serve: also time the comparison sample as one drop-in program per solve (0: skip)")
     a = ap.parse_args()
     if a.warmup < 3:
         a.warmup = 3
