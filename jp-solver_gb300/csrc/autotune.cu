@@ -27,6 +27,7 @@ extern "C" jp_status jp_autotune(jp_config* cfg, int32_t steps, double* best) {
         const double cells = double(s->cells);
         for (int v : vecs) {
             if (!vec_supported(s->storage, v) || s->n % v || ((long long)s->cells / v) % 32) continue;
+            if (s->inplace && v != s->vec) continue;  // the in-place steps run the storage's default width
             for (int t : tpbs) {
                 s->vec = v;
                 s->tpb = t;

@@ -119,6 +119,13 @@ def test_ensemble_of_inplace_members_at_mixed_parity():
         s.close()
 
 
+def test_autotune_of_an_inplace_solve_keeps_its_vector_width():
+    tuned, lups = J.autotune("uniform", steps=3, n=64, re=400.0, flags=IN)
+    assert tuned["vec"] == 4 and tuned["threads_per_block"] in (64, 128, 256, 512) and lups > 0
+    with J.Solver("uniform", n=64, re=400.0, flags=IN, threads_per_block=tuned["threads_per_block"]) as s:
+        s.step(2)
+
+
 def test_inplace_refused_where_unsupported():
     with pytest.raises(J.JPError):
         J.Solver("amr", n=16, flags=IN, l1_mode="all", l2_mode="all")
