@@ -332,6 +332,39 @@ __global__ void k_prep_list(const int* __restrict__ skin, int nskin, const int* 
     if (need) list[base + __popc(mask & ((1u << lane) - 1u))] = make_int2(b, (int)rm);
 }
 
+// Interface cells of the blocks of a prep list {block, refined-neighbour mask}: the cells whose 3x3x3
+// neighbourhood reaches refined and unrefined blocks, as b * mb^3 + cell.  CTA per entry (CTAs past
+// *pcount return); warp-aggregated append, *ncells zero on entry.
+__global__ void k_prep_cells(const int2* __restrict__ plist, const int* __restrict__ pcount, int mb,
+                             int* __restrict__ cells, int* __restrict__ ncells) {
+    if ((int)blockIdx.x >= *pcount) return;
+    const int2 e = plist[blockIdx.x];
+    const int b = e.x;
+    const unsigned rm = (unsigned)e.y;
+    const int mb3 = mb * mb * mb;
+    for (int base = 0; base < mb3; base += blockDim.x) {  // uniform trip count: every lane meets the ballot
+        const int cell = base + threadIdx.x;
+        bool need = false;
+        if (cell < mb3) {
+            const int i = cell % mb, j = (cell / mb) % mb, k = cell / (mb * mb);
+            // slots of the blocks the cell's neighbourhood reaches: per axis 0..2 (offset -1..1)
+            const unsigned mx = (i == 0 ? 3u : (i == mb - 1 ? 6u : 2u)), my = (j == 0 ? 3u : (j == mb - 1 ? 6u : 2u)),
+                           mz = (k == 0 ? 3u : (k == mb - 1 ? 6u : 2u));
+            const unsigned plane = ((my & 1u) ? mx : 0u) | ((my & 2u) ? mx << 3 : 0u) | ((my & 4u) ? mx << 6 : 0u);
+            const unsigned span = ((mz & 1u) ? plane : 0u) | ((mz & 2u) ? plane << 9 : 0u) | ((mz & 4u) ? plane << 18 : 0u);
+            const unsigned sel = rm & span;
+            need = sel != 0u && sel != span;
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, need);
+        if (!mask) continue;
+        const int lane = threadIdx.x & 31;
+        int at = 0;
+        if (lane == 0) at = atomicAdd(ncells, __popc(mask));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (need) cells[at + __popc(mask & ((1u << lane) - 1u))] = b * mb3 + cell;
+    }
+}
+
 // ---- host launchers --------------------------------------------------------------------------------
 static inline unsigned grid_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -426,6 +459,17 @@ cudaError_t adapt_prep_list(const int* skin, int nskin, const int* ref, const in
     if (e != cudaSuccess || nskin <= 0) return e;
     k_prep_list<<<grid_for(nskin, 256), 256, 0, st>>>(skin, nskin, ref, pos, grid, gx, reinterpret_cast<int2*>(list),
                                                        count);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t adapt_prep_cells(const int* plist, const int* pcount, int max_entries, int mb, int* cells, int* ncells,
+                             cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(ncells, 0, sizeof(int), st);
+    if (e != cudaSuccess || max_entries <= 0) return e;
+    const int mb3 = mb * mb * mb;
+    k_prep_cells<<<max_entries, mb3 < 256 ? ((mb3 + 31) / 32) * 32 : 256, 0, st>>>(
+        reinterpret_cast<const int2*>(plist), pcount, mb, cells, ncells);
     note_launch();
     return cudaGetLastError();
 }

@@ -73,31 +73,22 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const typename ST::
 // from the 2x2x2 parent cells around it; the parent cell U holding the ghost is unrefined, the parent
 // R of the fine cell next to it is refined, and every one of those corners lies within one cell of
 // both (per axis).  So a fill reads only interface cells, whose 3x3x3 neighbourhood holds refined and
-// unrefined cells; other cells of a skin block keep stale values nobody reads.  Refinement is per
-// block, so the prep list (adapt_prep_list) holds the skin blocks with a change of refinement around
-// them and the mask of their refined neighbour blocks, and a cell is an interface cell if the
-// blocks its neighbourhood reaches are mixed.
+// unrefined cells; other cells of a skin block keep stale values nobody reads.  The interface cells
+// are listed at each grid change (adapt_prep_list: the skin blocks with a change of refinement among
+// their 27 neighbour blocks; adapt_prep_cells: their interface cells), and a thread prepares one
+// listed cell; the threads tid, tid + nthreads, ... walk the list, whose length stays on the device.
 template <int MB, class ST>
 __device__ __forceinline__ void d_prep(const typename ST::raw* __restrict__ fin,
                                                       typename ST::raw* __restrict__ pr,
-                                                      const int2* __restrict__ list, float nqs,
+                                                      const int* __restrict__ cells, float nqs,
                                                       const int* __restrict__ nlim, const int* __restrict__ gate,
-                                                      int blk) {
+                                                      int tid, int nthreads) {
     using G = Geo<MB>;
-    if ((int)blk >= __ldg(nlim)) return;
     if (gate && __ldg(gate) == 0) return;  // no fine block of the next level has a ghost to fill
-    const int2 ent = __ldg(list + blk);
-    const int b = ent.x;
-    const unsigned rm = (unsigned)ent.y;
-    CELL_LOOP(cell) {
-        const int i = cell % MB, j = (cell / MB) % MB, k = cell / (MB * MB);
-        // slots of the blocks the cell's neighbourhood reaches: per axis 0..2 (offset -1..1)
-        const unsigned mx = (i == 0 ? 3u : (i == MB - 1 ? 6u : 2u)), my = (j == 0 ? 3u : (j == MB - 1 ? 6u : 2u)),
-                       mz = (k == 0 ? 3u : (k == MB - 1 ? 6u : 2u));
-        const unsigned plane = ((my & 1u) ? mx : 0u) | ((my & 2u) ? mx << 3 : 0u) | ((my & 4u) ? mx << 6 : 0u);
-        const unsigned span = ((mz & 1u) ? plane : 0u) | ((mz & 2u) ? plane << 9 : 0u) | ((mz & 4u) ? plane << 18 : 0u);
-        const unsigned sel = rm & span;
-        if (sel == 0u || sel == span) continue;
+    const int n = __ldg(nlim);
+    for (int idx = tid; idx < n; idx += nthreads) {
+        const int v = __ldg(cells + idx);
+        const int b = v / G::MB3, cell = v % G::MB3;
         float f[Q];
 #pragma unroll
         for (int q = 0; q < Q; ++q) f[q] = PoolIO<ST>::f(fin + ((size_t)b * Q + q) * G::MB3 + cell, q);
@@ -107,11 +98,24 @@ __device__ __forceinline__ void d_prep(const typename ST::raw* __restrict__ fin,
     }
 }
 template <int MB, class ST>
-__global__ void __launch_bounds__(Geo<MB>::TPB) k_prep(const typename ST::raw* __restrict__ fin,
-                                                      typename ST::raw* __restrict__ pr,
-                                                      const int2* __restrict__ list, float nqs,
-                                                      const int* __restrict__ nlim, const int* __restrict__ gate) {
-    d_prep<MB, ST>(fin, pr, list, nqs, nlim, gate, (int)blockIdx.x);
+__global__ void __launch_bounds__(256) k_prep(const typename ST::raw* __restrict__ fin,
+                                              typename ST::raw* __restrict__ pr, const int* __restrict__ cells,
+                                              float nqs, const int* __restrict__ nlim, const int* __restrict__ gate) {
+    d_prep<MB, ST>(fin, pr, cells, nqs, nlim, gate, (int)(blockIdx.x * blockDim.x + threadIdx.x),
+                   (int)(gridDim.x * blockDim.x));
+}
+
+// Resident CTAs of the prep kernel on this device (SMs x CTAs per SM): its grid.
+template <int MB, class ST>
+static int prep_grid_cap() {
+    static const int cap = [] {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_prep<MB, ST>, 256, 0);
+        return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+    }();
+    return cap;
 }
 
 // Trilinear prolongation from a precomputed source (k_prep), one population at a time: the eight
@@ -904,8 +908,8 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
                 L.iout, L.t0, L.t1, L.t2, L.t3, L.t4, L.t5, L.l1gx, L.nblocks);
             break;
         case OP_PREP:
-            k_prep<MB, ST><<<L.nblocks, cta, 0, L.st>>>(CPOOL(L.in), POOL(L.out),
-                                                        reinterpret_cast<const int2*>(L.list), L.scale, L.nlim, L.t0);
+            k_prep<MB, ST><<<std::max(1, std::min((L.nblocks + 255) / 256, prep_grid_cap<MB, ST>())), 256, 0, L.st>>>(
+                CPOOL(L.in), POOL(L.out), L.list, L.scale, L.nlim, L.t0);
             break;
         case OP_FILL_L1:
             k_fill_l1<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.cgx, L.n,
@@ -937,7 +941,8 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
                 reinterpret_cast<float*>(L.out));
             break;
         }
-        case OP_WARM:  // launch shapes of the rows steps, found before any graph capture
+        case OP_WARM:  // launch shapes of the rows steps and the prep, found before any graph capture
+            prep_grid_cap<MB, ST>();
             if constexpr (MB >= 8) {
                 if constexpr (MB <= 8) rows_grid_cap<MB, ST, true>();
                 rows_grid_cap<MB, ST, false>();
@@ -986,14 +991,14 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) kb_step(const __grid_constant
 }
 
 template <int MB, class ST, int OP>
-__global__ void __launch_bounds__(OP == OP_FILL_L1 || OP == OP_FILL_L2 ? 256 : Geo<MB>::TPB)
+__global__ void __launch_bounds__(OP == OP_FILL_L1 || OP == OP_FILL_L2 || OP == OP_PREP ? 256 : Geo<MB>::TPB)
     kb_cells(const __grid_constant__ AmrBatch B) {
     const AmrItem& it = B.it[batch_member(B)];
     const int blk = (int)blockIdx.x - it.begin;
     using raw = typename ST::raw;
     if constexpr (OP == OP_PREP) {
-        d_prep<MB, ST>((const raw*)it.in, (raw*)it.out, reinterpret_cast<const int2*>(it.list), it.scale, it.nlim,
-                       it.t0, blk);
+        d_prep<MB, ST>((const raw*)it.in, (raw*)it.out, it.list, it.scale, it.nlim, it.t0,
+                       blk * (int)blockDim.x + (int)threadIdx.x, it.nct * (int)blockDim.x);
     } else if constexpr (OP == OP_FILL_L1) {
         d_fill_l1<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.cgx, it.n,
                           reinterpret_cast<const int2*>(it.list), it.nlim, blk);
@@ -1048,7 +1053,7 @@ static cudaError_t batch_dispatch(int op, int tpb, bool fuse, const AmrBatch& B,
             }
             break;
         }
-        case OP_PREP: kb_cells<MB, ST, OP_PREP><<<B.total, cta, 0, st>>>(B); break;
+        case OP_PREP: kb_cells<MB, ST, OP_PREP><<<B.total, 256, 0, st>>>(B); break;
         case OP_FILL_L1: kb_cells<MB, ST, OP_FILL_L1><<<B.total, shl, 0, st>>>(B); break;
         case OP_FILL_L2: kb_cells<MB, ST, OP_FILL_L2><<<B.total, shl, 0, st>>>(B); break;
         case OP_RESTRICT: kb_cells<MB, ST, OP_RESTRICT><<<B.total, cta, 0, st>>>(B); break;

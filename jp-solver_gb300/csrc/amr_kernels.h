@@ -8,9 +8,10 @@ namespace amr {
 enum AmrOp {
     OP_INIT = 0,       // out = TGV state of the coarse grid
     OP_STEP_L0,        // in -> out, dense periodic coarse step
-    OP_PREP,           // out = prolongation source of in at the cells a fill can read, for the blocks of
-                       // the prep list (list: {block, refined-neighbour mask}); scale = nqs; t0 = device
-                       // count of the next level's fill list (skipped when 0) or null
+    OP_PREP,           // out = prolongation source of in at the cells a fill can read: list = interface
+                       // cells (b * MB^3 + cell, adapt_prep_cells), nlim = their count, nblocks = the
+                       // list's capacity; scale = nqs; t0 = device count of the next level's fill list
+                       // (skipped when 0) or null
     OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, list = fill list ({block, segments} pairs)
     OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, list = fill list
     OP_STEP_L1,        // in -> out, aux = gh1, nbt = level-1 table; t0 pcb, t1 oct; out2 = c0 restricts (scale nqi)
@@ -63,7 +64,8 @@ struct AmrItem {
     const int *t0, *t1, *t2, *t3, *nbt, *list, *nlim;
     int cgx, n, l1gx, n1;
     float omega, scale;
-    int begin, pad;
+    int begin;
+    int nct;  // CTAs of the member (a stage walking a cell list strides with them)
 };
 constexpr int kAmrBatchMax = 48;
 // Many solves in one launch per stage: OP_STEP_L0/L1/L2, OP_PREP, OP_FILL_L1/L2, OP_RESTRICT over up
@@ -136,6 +138,13 @@ cudaError_t adapt_fill_list(const int* nb, int nf, int* list, int* count, cudaSt
 // gx = cgx; level 1: pos = f1pos, grid = l1grid, gx = l1gx (absent blocks unrefined).  *count is set.
 cudaError_t adapt_prep_list(const int* skin, int nskin, const int* ref, const int* pos, const int* grid, int gx,
                             int* list, int* count, cudaStream_t st);
+// interface cells of the (at most max_entries, *pcount) blocks of a prep list: the cells whose 3x3x3
+// neighbourhood reaches refined and unrefined blocks, as b * mb^3 + cell (at most
+// mb^3 - (mb-2)^3 per block); *ncells is set.  The order is not fixed.
+cudaError_t adapt_prep_cells(const int* plist, const int* pcount, int max_entries, int mb, int* cells, int* ncells,
+                             cudaStream_t st);
+// interface cells a block can hold (its cells within one of a face)
+inline int interface_cells(int mb) { return mb * mb * mb - (mb - 2) * (mb - 2) * (mb - 2); }
 // dilate refinement marks by `layers` block layers (tmp: n ints of scratch); level 1 with the
 // position map pos, the grid map and the deep mask (marks only on deep blocks)
 cudaError_t adapt_dilate_marks(int* ref, int* tmp, int n, int gx, const int* pos, const int* grid, const int* deep,

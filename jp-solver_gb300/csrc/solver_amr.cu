@@ -42,6 +42,7 @@ struct AmrState {
     int *nb1 = nullptr, *nb2 = nullptr;  // same-level neighbour tables of the fine levels (27 per block)
     int *fl1 = nullptr, *fl2 = nullptr;  // fill lists: {block, shell segments} of the blocks with ghosts
     int *pl0 = nullptr, *pl1 = nullptr;  // prep lists: {skin block, refined neighbours} (adapt_prep_list)
+    int *pc0 = nullptr, *pc1 = nullptr;  // their interface cells, b * MB^3 + cell (adapt_prep_cells)
     int tpb = 0;                         // threads per CTA of the per-cell steps (0: default_step_tpb)
     int vec = 0;                         // fine steps: 4 rows of four cells, 1 a cell per thread (0: default)
     float *sen0 = nullptr, *sen1 = nullptr;
@@ -64,8 +65,11 @@ struct AmrState {
     float *c0_home = nullptr, *f1_home = nullptr, *f2_home = nullptr;
 };
 // SC_COUNT entries come from the host (upload_counts); the fill-list lengths are written on the device
+// (SC_PREP0/1: interface cells of the prep lists, whose block counts are SC_PBLK0/1)
 enum { SC_NF1 = 0, SC_NF2, SC_SKIN0, SC_SKIN1, SC_NREF0, SC_NREF1, SC_COUNT, SC_FILL1 = SC_COUNT, SC_FILL2, SC_PREP0,
-       SC_PREP1, SC_ALL };
+       SC_PREP1, SC_PBLK0, SC_PBLK1, SC_ALL };
+// CTAs per member of a batched prep (its threads walk the member's interface cells)
+constexpr int kBatchPrepCtas = 64;
 
 // drop the captured steps and take the current buffers as the parity reference
 static void reset_graphs(AmrState* a) {
@@ -183,10 +187,14 @@ static jp_status upload_counts(jp_solver* s) {
 // prep lists of both levels from their skin lists and refinement marks, lengths into the device counts
 static jp_status prep_lists(jp_solver* s) {
     AmrState* a = s->amr;
-    ACK(adapt_prep_list(a->skin0, a->n_skin0, a->ref0, nullptr, nullptr, a->cgx, a->pl0, a->step_cnt + SC_PREP0,
+    ACK(adapt_prep_list(a->skin0, a->n_skin0, a->ref0, nullptr, nullptr, a->cgx, a->pl0, a->step_cnt + SC_PBLK0,
                         s->stream), "prep list 0");
-    ACK(adapt_prep_list(a->skin1, a->n_skin1, a->ref1, a->f1pos, a->l1grid, a->l1gx, a->pl1, a->step_cnt + SC_PREP1,
+    ACK(adapt_prep_list(a->skin1, a->n_skin1, a->ref1, a->f1pos, a->l1grid, a->l1gx, a->pl1, a->step_cnt + SC_PBLK1,
                         s->stream), "prep list 1");
+    ACK(adapt_prep_cells(a->pl0, a->step_cnt + SC_PBLK0, a->n_skin0, a->MB, a->pc0, a->step_cnt + SC_PREP0, s->stream),
+        "prep cells 0");
+    ACK(adapt_prep_cells(a->pl1, a->step_cnt + SC_PBLK1, a->n_skin1, a->MB, a->pc1, a->step_cnt + SC_PREP1, s->stream),
+        "prep cells 1");
     return JP_OK;
 }
 
@@ -265,6 +273,7 @@ static jp_status set_cap1(jp_solver* s, int cap, bool keep) {
     TRY(regrow(s, a->nb1, (size_t)cap * 27, 0));
     TRY(regrow(s, a->fl1, 2 * (size_t)cap, 0));
     TRY(regrow(s, a->pl1, 2 * (size_t)cap, 0));
+    TRY(regrow(s, a->pc1, (size_t)interface_cells(a->MB) * cap, 0));
     reset_graphs(a);
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * cap, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * cap, s->stream), "memset");
@@ -551,11 +560,11 @@ static jp_status base_step(jp_solver* s) {
     TRY(step_l0(s));
     if (!skip_prep) {
         AmrLaunch L;
-        L.nblocks = a->cnb0;
+        L.nblocks = interface_cells(a->MB) * a->cnb0;
         L.nlim = cnt + SC_PREP0;
         L.in = a->c0a;
         L.out = a->prep0;
-        L.list = a->pl0;
+        L.list = a->pc0;
         L.scale = float(a->nqs01);
         L.t0 = cnt + SC_FILL1;
         TRY(launch(s, OP_PREP, L));
@@ -574,11 +583,11 @@ static jp_status base_step(jp_solver* s) {
     for (int s1 = 0; s1 < 2; ++s1) {
         if (!skip_prep) {
             AmrLaunch L;
-            L.nblocks = a->cap1;
+            L.nblocks = interface_cells(a->MB) * a->cap1;
             L.nlim = cnt + SC_PREP1;
             L.in = a->f1a;
             L.out = a->prep1;
-            L.list = a->pl1;
+            L.list = a->pc1;
             L.scale = float(a->nqs12);
             L.t0 = cnt + SC_FILL2;
             TRY(launch(s, OP_PREP, L));
@@ -677,6 +686,7 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
                 std::memset(&it, 0, sizeof it);
                 const int n = fill(ms[i]->amr, it);
                 if (n <= 0) continue;
+                it.nct = n;
                 it.begin = B.total;
                 B.total += n;
                 ++B.count;
@@ -698,11 +708,11 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
         TRY(run(OP_PREP, false, [](AmrState* a, AmrItem& it) {
             it.in = a->c0a;
             it.out = a->prep0;
-            it.list = a->pl0;
+            it.list = a->pc0;
             it.scale = float(a->nqs01);
             it.nlim = a->step_cnt + SC_PREP0;
             it.t0 = a->step_cnt + SC_FILL1;
-            return a->cnb0;
+            return std::min((interface_cells(a->MB) * a->cnb0 + 255) / 256, kBatchPrepCtas);
         }));
         TRY(run(OP_FILL_L1, false, [](AmrState* a, AmrItem& it) {
             it.in = a->prep0;
@@ -721,11 +731,11 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
             TRY(run(OP_PREP, false, [](AmrState* a, AmrItem& it) {
                 it.in = a->f1a;
                 it.out = a->prep1;
-                it.list = a->pl1;
+                it.list = a->pc1;
                 it.scale = float(a->nqs12);
                 it.nlim = a->step_cnt + SC_PREP1;
                 it.t0 = a->step_cnt + SC_FILL2;
-                return a->cap1;
+                return std::min((interface_cells(a->MB) * a->cap1 + 255) / 256, kBatchPrepCtas);
             }));
             TRY(run(OP_FILL_L2, false, [](AmrState* a, AmrItem& it) {
                 it.in = a->prep1;
@@ -929,6 +939,8 @@ jp_status amr_create(jp_solver* s) {
     TRY(dalloc(a, &a->fl1, 2 * (size_t)a->cap1, "cudaMalloc fl1"));
     TRY(dalloc(a, &a->pl1, 2 * (size_t)a->cap1, "cudaMalloc pl1"));
     TRY(dalloc(a, &a->pl0, 2 * (size_t)a->cnb0, "cudaMalloc pl0"));
+    TRY(dalloc(a, &a->pc1, (size_t)interface_cells(a->MB) * a->cap1, "cudaMalloc pc1"));
+    TRY(dalloc(a, &a->pc0, (size_t)interface_cells(a->MB) * a->cnb0, "cudaMalloc pc0"));
     TRY(dalloc(a, &a->step_cnt, SC_ALL, "cudaMalloc step counts"));
     a->step_cnt_host = (int*)pinned_slot_alloc();
     if (!a->step_cnt_host) return fail(JP_ERR_NOMEM, "pinned host slot");
