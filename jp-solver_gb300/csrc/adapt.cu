@@ -279,26 +279,30 @@ __global__ void k_fill_int(int* __restrict__ p, int v, long long n) {
         p[i] = v;
 }
 
-// Fill list of a fine level: the blocks with a ghost-shell segment (face or edge; the D3Q19 pulls
-// never cross a corner) whose neighbour slot is on another level, as {block, mask of those
-// segments}.  Warp-aggregated append; *count is zero on entry.
-__global__ void k_fill_list(const int* __restrict__ nb, int nf, int2* __restrict__ list, int* __restrict__ count) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned segs = 0;
-    if (b < nf) {
-        const int* row = nb + (size_t)b * 27;
-#pragma unroll
-        for (int g = 0; g < 18; ++g)
-            if (__ldg(row + seg_slot(g)) < 0) segs |= 1u << g;
+// Fill list of a fine level: the ghost-shell cells (faces and edges; the D3Q19 pulls never cross a
+// corner) whose neighbour slot is on another level, as b * SH + shell cell.  CTA per block, the
+// threads over its shell; warp-aggregated append, *count zero on entry, order not fixed.
+template <int MB>
+__global__ void k_fill_list(const int* __restrict__ nb, int* __restrict__ list, int* __restrict__ count) {
+    constexpr int SH = Geo<MB>::SH;
+    const int b = blockIdx.x;
+    const int* row = nb + (size_t)b * 27;
+    for (int base = 0; base < SH; base += blockDim.x) {  // uniform trip count: every lane meets the ballot
+        const int t = base + threadIdx.x;
+        bool need = false;
+        if (t < SH) {
+            int i, j, k;
+            shell_coord<MB>(t, i, j, k);
+            need = __ldg(row + shell_slot<MB>(i, j, k)) < 0;
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, need);
+        if (!mask) continue;
+        const int lane = threadIdx.x & 31;
+        int at = 0;
+        if (lane == 0) at = atomicAdd(count, __popc(mask));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (need) list[at + __popc(mask & ((1u << lane) - 1u))] = b * SH + t;
     }
-    const bool need = segs != 0;
-    const unsigned mask = __ballot_sync(0xffffffffu, need);
-    if (!mask) return;
-    const int lane = threadIdx.x & 31;
-    int base = 0;
-    if (lane == 0) base = atomicAdd(count, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (need) list[base + __popc(mask & ((1u << lane) - 1u))] = make_int2(b, (int)segs);
 }
 
 // Prep list of a level: the skin blocks with a change of refinement among their 27 neighbour blocks
@@ -444,11 +448,15 @@ cudaError_t adapt_dilate_marks(int* ref, int* tmp, int n, int gx, const int* pos
     return cudaGetLastError();
 }
 
-cudaError_t adapt_fill_list(const int* nb, int nf, int* list, int* count, cudaStream_t st) {
-    static_assert(sizeof(int2) == 2 * sizeof(int), "fill list entries are two ints");
+cudaError_t adapt_fill_list(const int* nb, int nf, int mb, int* list, int* count, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
     if (e != cudaSuccess || nf <= 0) return e;
-    k_fill_list<<<grid_for(nf, 256), 256, 0, st>>>(nb, nf, reinterpret_cast<int2*>(list), count);
+    switch (mb) {
+        case 4: k_fill_list<4><<<nf, 160, 0, st>>>(nb, list, count); break;
+        case 8: k_fill_list<8><<<nf, 256, 0, st>>>(nb, list, count); break;
+        case 16: k_fill_list<16><<<nf, 256, 0, st>>>(nb, list, count); break;
+        default: return cudaErrorInvalidValue;
+    }
     note_launch();
     return cudaGetLastError();
 }

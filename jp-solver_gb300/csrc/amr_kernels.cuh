@@ -188,40 +188,26 @@ __device__ __forceinline__ unsigned ghost_need(int i, int j, int k) {
     return m;
 }
 
-// Shell cell of the n-th cell of the segments in `segs` (in shell order), or -1 past their end.
-template <int MB>
-__device__ __forceinline__ int seg_cell(unsigned segs, int n) {
-    int sc = -1;
-#pragma unroll
-    for (int g = 0; g < 18; ++g)
-        if (((segs >> g) & 1u) && sc < 0) {
-            if (n < seg_size<MB>(g)) sc = seg_first<MB>(g) + n;
-            else n -= seg_size<MB>(g);
-        }
-    return sc;
-}
-
 // ---- ghost shells (src/tgv3d_amr.cu:173-202) -------------------------------------------------------
-// One CTA per entry of the fill list {block, segments}: the fine blocks with a face or edge of the
-// shell whose neighbour is on another level (built with the neighbour table).  The CTA's threads
-// cover the cells of those segments only; the shell cells next to a same-level block are left
-// alone (the step gathers them from that block).
+// One thread per cell of the fill list: the shell cells (b * SH + t) of fine blocks whose neighbour
+// slot is on another level, listed at each grid change (adapt_fill_list); the threads tid,
+// tid + nthreads, ... walk the list, whose length stays on the device.  Shell cells next to a
+// same-level block are never listed (the step gathers them from that block).
 template <int MB, class ST>
 __device__ __forceinline__ void d_fill_l1(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ pcb, const int* __restrict__ poct, int cgx, int N,
-                                                const int2* __restrict__ list, const int* __restrict__ nlim, int blk) {
+                                                const int* __restrict__ list, const int* __restrict__ nlim, int tid,
+                                                int nthreads) {
     using G = Geo<MB>;
-    if ((int)blk >= __ldg(nlim)) return;
-    const int2 ent = __ldg(list + blk);
-    const int fb = ent.x;
-    const unsigned segs = (unsigned)ent.y;
-    const int cb = pcb[fb], oct = poct[fb];
-    const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
-    const int ox = cbx * 2 * MB + (oct & 1) * MB, oy = cby * 2 * MB + ((oct >> 1) & 1) * MB, oz = cbz * 2 * MB + (oct >> 2) * MB;
+    const int n = __ldg(nlim);
     const int N1 = 2 * N;
-    for (int n = threadIdx.x;; n += blockDim.x) {
-        const int t = seg_cell<MB>(segs, n);
-        if (t < 0) break;
+    for (int idx = tid; idx < n; idx += nthreads) {
+        const int v = __ldg(list + idx);
+        const int fb = v / G::SH, t = v % G::SH;
+        const int cb = __ldg(pcb + fb), oct = __ldg(poct + fb);
+        const int cbx = cb % cgx, cby = (cb / cgx) % cgx, cbz = cb / (cgx * cgx);
+        const int ox = cbx * 2 * MB + (oct & 1) * MB, oy = cby * 2 * MB + ((oct >> 1) & 1) * MB,
+                  oz = cbz * 2 * MB + (oct >> 2) * MB;
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
         const int gfi = pmod(ox + i, N1), gfj = pmod(oy + j, N1), gfk = pmod(oz + k, N1);
@@ -242,27 +228,27 @@ __device__ __forceinline__ void d_fill_l1(const typename ST::raw* __restrict__ p
 template <int MB, class ST>
 __global__ void __launch_bounds__(256) k_fill_l1(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ pcb, const int* __restrict__ poct, int cgx, int N,
-                                                const int2* __restrict__ list, const int* __restrict__ nlim) {
-    d_fill_l1<MB, ST>(pr, gh, pcb, poct, cgx, N, list, nlim, (int)blockIdx.x);
+                                                const int* __restrict__ list, const int* __restrict__ nlim) {
+    d_fill_l1<MB, ST>(pr, gh, pcb, poct, cgx, N, list, nlim, (int)(blockIdx.x * blockDim.x + threadIdx.x),
+                      (int)(gridDim.x * blockDim.x));
 }
 
 template <int MB, class ST>
 __device__ __forceinline__ void d_fill_l2(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
                                                 const int* __restrict__ f1pos, const int* __restrict__ l1grid, int l1gx, int N1,
-                                                const int2* __restrict__ list, const int* __restrict__ nlim, int blk) {
+                                                const int* __restrict__ list, const int* __restrict__ nlim, int tid,
+                                                int nthreads) {
     using G = Geo<MB>;
-    if ((int)blk >= __ldg(nlim)) return;
-    const int2 ent = __ldg(list + blk);
-    const int b = ent.x;
-    const unsigned segs = (unsigned)ent.y;
-    const int pl1 = l2pl1[b], oct = l2oct[b];
-    const int p = f1pos[pl1], px = p % l1gx, py = (p / l1gx) % l1gx, pz = p / (l1gx * l1gx);
-    const int ox = px * 2 * MB + (oct & 1) * MB, oy = py * 2 * MB + ((oct >> 1) & 1) * MB, oz = pz * 2 * MB + (oct >> 2) * MB;
+    const int n = __ldg(nlim);
     const int N2 = 2 * N1;
-    for (int n = threadIdx.x;; n += blockDim.x) {
-        const int t = seg_cell<MB>(segs, n);
-        if (t < 0) break;
+    for (int idx = tid; idx < n; idx += nthreads) {
+        const int v = __ldg(list + idx);
+        const int b = v / G::SH, t = v % G::SH;
+        const int pl1 = __ldg(l2pl1 + b), oct = __ldg(l2oct + b);
+        const int pp = __ldg(f1pos + pl1), px = pp % l1gx, py = (pp / l1gx) % l1gx, pz = pp / (l1gx * l1gx);
+        const int ox = px * 2 * MB + (oct & 1) * MB, oy = py * 2 * MB + ((oct >> 1) & 1) * MB,
+                  oz = pz * 2 * MB + (oct >> 2) * MB;
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
         const int g2i = pmod(ox + i, N2), g2j = pmod(oy + j, N2), g2k = pmod(oz + k, N2);
@@ -277,9 +263,9 @@ __device__ __forceinline__ void d_fill_l2(const typename ST::raw* __restrict__ p
             if (!need) break;
             const int q = __ffs(need) - 1;
             need &= need - 1;
-            float v = interp<MB, ST, true>(p, w, q);
-            if (renorm) v *= inv;
-            PoolIO<ST>::put_f(gh + ((size_t)b * Q + q) * G::SH + t, q, v);
+            float val = interp<MB, ST, true>(p, w, q);
+            if (renorm) val *= inv;
+            PoolIO<ST>::put_f(gh + ((size_t)b * Q + q) * G::SH + t, q, val);
         }
     }
 }
@@ -287,8 +273,23 @@ template <int MB, class ST>
 __global__ void __launch_bounds__(256) k_fill_l2(const typename ST::raw* __restrict__ pr, typename ST::raw* __restrict__ gh,
                                                 const int* __restrict__ l2pl1, const int* __restrict__ l2oct,
                                                 const int* __restrict__ f1pos, const int* __restrict__ l1grid, int l1gx, int N1,
-                                                const int2* __restrict__ list, const int* __restrict__ nlim) {
-    d_fill_l2<MB, ST>(pr, gh, l2pl1, l2oct, f1pos, l1grid, l1gx, N1, list, nlim, (int)blockIdx.x);
+                                                const int* __restrict__ list, const int* __restrict__ nlim) {
+    d_fill_l2<MB, ST>(pr, gh, l2pl1, l2oct, f1pos, l1grid, l1gx, N1, list, nlim,
+                      (int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x));
+}
+
+// Resident CTAs of a fill kernel on this device (SMs x CTAs per SM): the fills' grid.
+template <int MB, class ST, int LEVEL>
+static int fill_grid_cap() {
+    static const int cap = [] {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (LEVEL == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fill_l1<MB, ST>, 256, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fill_l2<MB, ST>, 256, 0);
+        return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+    }();
+    return cap;
 }
 
 // Restriction of one fine block, staged in shared memory as sf[q * MB^3 + cell] after its last
@@ -912,12 +913,12 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
                 CPOOL(L.in), POOL(L.out), L.list, L.scale, L.nlim, L.t0);
             break;
         case OP_FILL_L1:
-            k_fill_l1<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.cgx, L.n,
-                                                           reinterpret_cast<const int2*>(L.list), L.nlim);
+            k_fill_l1<MB, ST><<<std::max(1, std::min((L.nblocks + 255) / 256, fill_grid_cap<MB, ST, 1>())), 256, 0,
+                                L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.cgx, L.n, L.list, L.nlim);
             break;
         case OP_FILL_L2:
-            k_fill_l2<MB, ST><<<L.nblocks, shl, 0, L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.t2, L.t3, L.l1gx,
-                                                           L.n1, reinterpret_cast<const int2*>(L.list), L.nlim);
+            k_fill_l2<MB, ST><<<std::max(1, std::min((L.nblocks + 255) / 256, fill_grid_cap<MB, ST, 2>())), 256, 0,
+                                L.st>>>(CPOOL(L.in), POOL(L.out), L.t0, L.t1, L.t2, L.t3, L.l1gx, L.n1, L.list, L.nlim);
             break;
         case OP_RESTRICT:
             k_restrict<MB, ST><<<L.nblocks, cta, 0, L.st>>>(POOL(L.out), CPOOL(L.in), L.list, L.t0, L.scale, L.nlim);
@@ -941,8 +942,10 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
                 reinterpret_cast<float*>(L.out));
             break;
         }
-        case OP_WARM:  // launch shapes of the rows steps and the prep, found before any graph capture
+        case OP_WARM:  // launch shapes of the rows steps, preps and fills, found before any graph capture
             prep_grid_cap<MB, ST>();
+            fill_grid_cap<MB, ST, 1>();
+            fill_grid_cap<MB, ST, 2>();
             if constexpr (MB >= 8) {
                 if constexpr (MB <= 8) rows_grid_cap<MB, ST, true>();
                 rows_grid_cap<MB, ST, false>();
@@ -1000,11 +1003,11 @@ __global__ void __launch_bounds__(OP == OP_FILL_L1 || OP == OP_FILL_L2 || OP == 
         d_prep<MB, ST>((const raw*)it.in, (raw*)it.out, it.list, it.scale, it.nlim, it.t0,
                        blk * (int)blockDim.x + (int)threadIdx.x, it.nct * (int)blockDim.x);
     } else if constexpr (OP == OP_FILL_L1) {
-        d_fill_l1<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.cgx, it.n,
-                          reinterpret_cast<const int2*>(it.list), it.nlim, blk);
+        d_fill_l1<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.cgx, it.n, it.list, it.nlim,
+                          blk * (int)blockDim.x + (int)threadIdx.x, it.nct * (int)blockDim.x);
     } else if constexpr (OP == OP_FILL_L2) {
-        d_fill_l2<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.t2, it.t3, it.l1gx, it.n1,
-                          reinterpret_cast<const int2*>(it.list), it.nlim, blk);
+        d_fill_l2<MB, ST>((const raw*)it.in, (raw*)it.out, it.t0, it.t1, it.t2, it.t3, it.l1gx, it.n1, it.list, it.nlim,
+                          blk * (int)blockDim.x + (int)threadIdx.x, it.nct * (int)blockDim.x);
     } else {
         d_restrict<MB, ST>((raw*)it.out, (const raw*)it.in, it.list, it.t0, it.scale, it.nlim, blk);
     }
@@ -1054,8 +1057,8 @@ static cudaError_t batch_dispatch(int op, int tpb, bool fuse, const AmrBatch& B,
             break;
         }
         case OP_PREP: kb_cells<MB, ST, OP_PREP><<<B.total, 256, 0, st>>>(B); break;
-        case OP_FILL_L1: kb_cells<MB, ST, OP_FILL_L1><<<B.total, shl, 0, st>>>(B); break;
-        case OP_FILL_L2: kb_cells<MB, ST, OP_FILL_L2><<<B.total, shl, 0, st>>>(B); break;
+        case OP_FILL_L1: kb_cells<MB, ST, OP_FILL_L1><<<B.total, 256, 0, st>>>(B); break;
+        case OP_FILL_L2: kb_cells<MB, ST, OP_FILL_L2><<<B.total, 256, 0, st>>>(B); break;
         case OP_RESTRICT: kb_cells<MB, ST, OP_RESTRICT><<<B.total, cta, 0, st>>>(B); break;
         default: return cudaErrorInvalidValue;
     }

@@ -12,8 +12,10 @@ enum AmrOp {
                        // cells (b * MB^3 + cell, adapt_prep_cells), nlim = their count, nblocks = the
                        // list's capacity; scale = nqs; t0 = device count of the next level's fill list
                        // (skipped when 0) or null
-    OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, list = fill list ({block, segments} pairs)
-    OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid, list = fill list
+    OP_FILL_L1,        // in = prep0, out = gh1; t0 pcb, t1 oct, list = fill list (ghost cells b * SH + t),
+                       // nlim = its length, nblocks = its capacity
+    OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid; list, nlim, nblocks as
+                       // OP_FILL_L1
     OP_STEP_L1,        // in -> out, aux = gh1, nbt = level-1 table; t0 pcb, t1 oct; out2 = c0 restricts (scale nqi)
     OP_STEP_L2,        // in -> out, aux = gh2, nbt = level-2 table; t0 l2pl1, t1 l2oct; out2 = f1 restricts
     OP_RESTRICT,       // out = coarse, in = fine; list = refined coarse blocks, t0 = fof; scale = nqi
@@ -128,11 +130,11 @@ cudaError_t adapt_skins(const int* ref0, int cnb0, int cgx, const int* ref1, con
                         int nf1, int l1gx, int* flags, int* skin0, int* skin1, AdaptCounts* counts, cudaStream_t st);
 // set n ints to v
 cudaError_t adapt_fill(int* p, int v, long long n, cudaStream_t st);
-// fill list of a fine level: the blocks among nf with a ghost-shell segment (face or edge) whose
-// slot of the neighbour table nb (27 per block) is on another level (-1), as pairs {block, mask of
-// those segments} (list holds 2 ints per entry); *count is set.  The list's order is not fixed:
-// each block's fill is independent of the others.
-cudaError_t adapt_fill_list(const int* nb, int nf, int* list, int* count, cudaStream_t st);
+// fill list of a fine level: the ghost-shell cells (faces, edges) of the nf blocks whose slot of the
+// neighbour table nb (27 per block) is on another level (-1), as b * SH + shell cell (SH = shell
+// cells of edge mb; at most SH per block); *count is set.  The list's order is not fixed: each
+// cell is filled independently.
+cudaError_t adapt_fill_list(const int* nb, int nf, int mb, int* list, int* count, cudaStream_t st);
 // prep list of a level: the skin blocks whose 27 neighbour blocks (periodic) mix refined and
 // unrefined, as pairs {block, mask of the refined neighbours (bit = slot)}; level 0: pos null and
 // gx = cgx; level 1: pos = f1pos, grid = l1grid, gx = l1gx (absent blocks unrefined).  *count is set.

@@ -40,7 +40,7 @@ struct AmrState {
     int *o_ref0 = nullptr, *o_fof0 = nullptr, *o_l1grid = nullptr, *o_ref1 = nullptr, *o_fof1 = nullptr;
     int *rank = nullptr, *deep = nullptr, *flags = nullptr;
     int *nb1 = nullptr, *nb2 = nullptr;  // same-level neighbour tables of the fine levels (27 per block)
-    int *fl1 = nullptr, *fl2 = nullptr;  // fill lists: {block, shell segments} of the blocks with ghosts
+    int *fl1 = nullptr, *fl2 = nullptr;  // fill lists: ghost cells b * SH + t to fill (adapt_fill_list)
     int *pl0 = nullptr, *pl1 = nullptr;  // prep lists: {skin block, refined neighbours} (adapt_prep_list)
     int *pc0 = nullptr, *pc1 = nullptr;  // their interface cells, b * MB^3 + cell (adapt_prep_cells)
     int tpb = 0;                         // threads per CTA of the per-cell steps (0: default_step_tpb)
@@ -68,7 +68,7 @@ struct AmrState {
 // (SC_PREP0/1: interface cells of the prep lists, whose block counts are SC_PBLK0/1)
 enum { SC_NF1 = 0, SC_NF2, SC_SKIN0, SC_SKIN1, SC_NREF0, SC_NREF1, SC_COUNT, SC_FILL1 = SC_COUNT, SC_FILL2, SC_PREP0,
        SC_PREP1, SC_PBLK0, SC_PBLK1, SC_ALL };
-// CTAs per member of a batched prep (its threads walk the member's interface cells)
+// CTAs per member of a batched prep or fill (its threads walk the member's cell list)
 constexpr int kBatchPrepCtas = 64;
 
 // drop the captured steps and take the current buffers as the parity reference
@@ -271,7 +271,7 @@ static jp_status set_cap1(jp_solver* s, int cap, bool keep) {
     TRY(regrow(s, a->rank, std::max(a->cnb0, cap), 0));
     TRY(regrow(s, a->flags, (size_t)a->cnb0 + cap, 0));
     TRY(regrow(s, a->nb1, (size_t)cap * 27, 0));
-    TRY(regrow(s, a->fl1, 2 * (size_t)cap, 0));
+    TRY(regrow(s, a->fl1, (size_t)a->SH * cap, 0));
     TRY(regrow(s, a->pl1, 2 * (size_t)cap, 0));
     TRY(regrow(s, a->pc1, (size_t)interface_cells(a->MB) * cap, 0));
     reset_graphs(a);
@@ -291,7 +291,7 @@ static jp_status set_cap2(jp_solver* s, int cap, bool keep) {
     TRY(regrow(s, a->l2pl1, cap, 0));
     TRY(regrow(s, a->l2oct, cap, 0));
     TRY(regrow(s, a->nb2, (size_t)cap * 27, 0));
-    TRY(regrow(s, a->fl2, 2 * (size_t)cap, 0));
+    TRY(regrow(s, a->fl2, (size_t)a->SH * cap, 0));
     reset_graphs(a);
     a->cap2 = cap;
     update_bytes(s);
@@ -354,8 +354,8 @@ static jp_status build_l1(jp_solver* s, bool restore_marks) {
 // fill lists of both fine levels from their neighbour tables, lengths into the device counts
 static jp_status fill_lists(jp_solver* s) {
     AmrState* a = s->amr;
-    ACK(adapt_fill_list(a->nb1, a->nf1, a->fl1, a->step_cnt + SC_FILL1, s->stream), "fill list 1");
-    ACK(adapt_fill_list(a->nb2, a->nf2, a->fl2, a->step_cnt + SC_FILL2, s->stream), "fill list 2");
+    ACK(adapt_fill_list(a->nb1, a->nf1, a->MB, a->fl1, a->step_cnt + SC_FILL1, s->stream), "fill list 1");
+    ACK(adapt_fill_list(a->nb2, a->nf2, a->MB, a->fl2, a->step_cnt + SC_FILL2, s->stream), "fill list 2");
     return JP_OK;
 }
 
@@ -447,7 +447,7 @@ static jp_status initial_build(jp_solver* s) {
     dfree(a, a->fl2);
     const size_t blk = (size_t)Q * a->MB3;
     TRY(dalloc(a, &a->nb2, (size_t)a->cap2 * 27, "cudaMalloc nb2"));
-    TRY(dalloc(a, &a->fl2, 2 * (size_t)a->cap2, "cudaMalloc fl2"));
+    TRY(dalloc(a, &a->fl2, (size_t)a->SH * a->cap2, "cudaMalloc fl2"));
     TRY(dalloc(a, &a->f2a, pf(a, (size_t)a->cap2 * blk), "cudaMalloc f2"));
     TRY(dalloc(a, &a->f2b, pf(a, (size_t)a->cap2 * blk), "cudaMalloc f2"));
     TRY(dalloc(a, &a->gh2, pf(a, (size_t)a->cap2 * Q * a->SH), "cudaMalloc gh2"));
@@ -569,7 +569,7 @@ static jp_status base_step(jp_solver* s) {
         L.t0 = cnt + SC_FILL1;
         TRY(launch(s, OP_PREP, L));
         AmrLaunch F;
-        F.nblocks = a->cap1;
+        F.nblocks = a->SH * a->cap1;
         F.list = a->fl1;
         F.nlim = cnt + SC_FILL1;
         F.in = a->prep0;
@@ -592,7 +592,7 @@ static jp_status base_step(jp_solver* s) {
             L.t0 = cnt + SC_FILL2;
             TRY(launch(s, OP_PREP, L));
             AmrLaunch F;
-            F.nblocks = a->cap2;
+            F.nblocks = a->SH * a->cap2;
             F.list = a->fl2;
             F.nlim = cnt + SC_FILL2;
             F.in = a->prep1;
@@ -723,7 +723,7 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
             it.n = a->N;
             it.list = a->fl1;
             it.nlim = a->step_cnt + SC_FILL1;
-            return a->cap1;
+            return std::min((a->SH * a->cap1 + 255) / 256, kBatchPrepCtas);
         }));
     }
     for (int s1 = 0; s1 < 2; ++s1) {
@@ -748,7 +748,7 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
                 it.n1 = a->N1;
                 it.list = a->fl2;
                 it.nlim = a->step_cnt + SC_FILL2;
-                return a->cap2;
+                return std::min((a->SH * a->cap2 + 255) / 256, kBatchPrepCtas);
             }));
         }
         for (int s2 = 0; s2 < 2; ++s2) {
@@ -936,7 +936,7 @@ jp_status amr_create(jp_solver* s) {
     TRY(dalloc(a, &a->flags, (size_t)a->cnb0 + a->cap1, "cudaMalloc flags"));
     TRY(dalloc(a, &a->sen1, (size_t)a->cap1, "cudaMalloc sen1"));
     TRY(dalloc(a, &a->nb1, (size_t)a->cap1 * 27, "cudaMalloc nb1"));
-    TRY(dalloc(a, &a->fl1, 2 * (size_t)a->cap1, "cudaMalloc fl1"));
+    TRY(dalloc(a, &a->fl1, (size_t)a->SH * a->cap1, "cudaMalloc fl1"));
     TRY(dalloc(a, &a->pl1, 2 * (size_t)a->cap1, "cudaMalloc pl1"));
     TRY(dalloc(a, &a->pl0, 2 * (size_t)a->cnb0, "cudaMalloc pl0"));
     TRY(dalloc(a, &a->pc1, (size_t)interface_cells(a->MB) * a->cap1, "cudaMalloc pc1"));
