@@ -460,11 +460,11 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
     constexpr int M = MB - 1, MB3 = G::MB3, SH = G::SH;
     static_assert(MB % 4 == 0 && 32 % RG::SPR == 0 && RG::SEGS % RG::TPB == 0, "row mapping");
     extern __shared__ float sf[];
-    const int nblk = __ldg(nlim);
-    if (!WALK && blk >= nblk) return;  // whole CTA
-    // WALK: blocks blk, blk + stride, ... (a resident grid walks the level; the loop bound is
-    // CTA-uniform, so the barriers of the fused restriction stay uniform); else the one block blk
-    for (int b = blk; b < nblk; b += stride) {
+    if (!WALK && blk >= __ldg(nlim)) return;  // whole CTA
+    // WALK: blocks blk, blk + gridDim.x, ... (a resident grid walks the level; the loop bound is
+    // CTA-uniform, so the barriers of the fused restriction stay uniform); else the one block blk.
+    // The count is re-read from L1 and the stride is gridDim.x, so the loop holds one register.
+    for (int b = blk; b < __ldg(nlim); b += (WALK ? (int)gridDim.x : stride)) {
     const int* nbrow = nbtab + (size_t)b * 27;
     for (int seg = threadIdx.x; seg < RG::SEGS; seg += RG::TPB) {
         const int s = seg % RG::SPR, r = seg / RG::SPR, j = r % MB, k = r / MB, i0 = 4 * s;
@@ -531,7 +531,7 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
     if (FUSE) {
         __syncthreads();
         restrict_octant<MB, ST>(sf, parent_pool + (size_t)parent[b] * Q * G::MB3, poct[b], nqi);
-        if (WALK && b + stride < nblk) __syncthreads();  // the next block stages into sf (CTA-uniform test)
+        if (WALK && b + (int)gridDim.x < __ldg(nlim)) __syncthreads();  // the next block stages into sf
     }
     if (!WALK) break;
     }
@@ -852,15 +852,17 @@ template <int MB, class ST>
 static void launch_rows(const AmrLaunch& L) {
     using G = Geo<MB>;
     constexpr int T = RowGeo<MB>::TPB;
-    // FP32 with the fused restriction keeps a CTA per block: walking blocks costs it a barrier per
-    // block (the shared staging is reused) and the loop's registers, more than the CTA starts saved
+    // FP32 with the fused restriction walks only levels of up to 16 blocks per resident CTA (by
+    // capacity): there the walk saves CTA starts and evens the tail; on longer levels its barrier per
+    // block (the shared staging is reused) and its registers cost more than a CTA per block
     constexpr size_t sm = sizeof(float) * Q * G::MB3;
     if (L.out2) {
-        if constexpr (sizeof(typename ST::raw) == 4)
+        const int cap = rows_grid_cap<MB, ST, true>();
+        if (sizeof(typename ST::raw) == 4 && L.nblocks > 16 * cap)
             k_step_fine_rows<MB, ST, true, false><<<L.nblocks, T, sm, L.st>>>(
                 CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.t0, L.t1, L.omega, POOL(L.out2), L.scale, L.nlim);
         else
-            k_step_fine_rows<MB, ST, true, true><<<std::min(L.nblocks, rows_grid_cap<MB, ST, true>()), T, sm, L.st>>>(
+            k_step_fine_rows<MB, ST, true, true><<<std::min(L.nblocks, cap), T, sm, L.st>>>(
                 CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.t0, L.t1, L.omega, POOL(L.out2), L.scale, L.nlim);
     } else {
         k_step_fine_rows<MB, ST, false, true><<<std::min(L.nblocks, rows_grid_cap<MB, ST, false>()), T, 0, L.st>>>(
