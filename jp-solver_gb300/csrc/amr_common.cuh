@@ -69,17 +69,6 @@ __host__ __device__ __forceinline__ int shell_slot(int i, int j, int k) {
     return (k < 0 ? 0 : (k >= MB ? 2 : 1)) * 9 + (j < 0 ? 0 : (j >= MB ? 2 : 1)) * 3 + (i < 0 ? 0 : (i >= MB ? 2 : 1));
 }
 
-// The shell as 18 segments in shell order: the six faces (MB^2 cells each), then the twelve edges
-// (MB cells each).  Every cell of segment g borders the same neighbour slot, seg_slot(g).
-template <int MB>
-__host__ __device__ constexpr int seg_first(int g) { return g < 6 ? g * MB * MB : 6 * MB * MB + (g - 6) * MB; }
-template <int MB>
-__host__ __device__ constexpr int seg_size(int g) { return g < 6 ? MB * MB : MB; }
-__host__ __device__ constexpr int seg_slot(int g) {
-    constexpr int t[18] = {12, 14, 10, 16, 4, 22, 1, 7, 19, 25, 3, 5, 21, 23, 9, 11, 15, 17};
-    return t[g];
-}
-
 __device__ __forceinline__ int pmod(int a, int n) {
     const int r = a % n;
     return r < 0 ? r + n : r;

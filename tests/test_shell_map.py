@@ -1,6 +1,6 @@
 """The compact ghost-shell numbering of the AMR fine blocks (faces + edges, no corners) is a bijection
-onto [0, 6 MB^2 + 12 MB), its 18 segments (faces, edges) each border one neighbour slot, and it
-covers every cell a D3Q19 pull can reach; the fine steps' pull
+onto [0, 6 MB^2 + 12 MB), each shell cell maps to the neighbour slot of its offset, and it covers
+every cell a D3Q19 pull can reach; the fine steps' pull
 addressing (neighbour slot + masked cell) equals the global-coordinate pull.  Host-compiled check of
 the device header (no GPU)."""
 import os
@@ -25,18 +25,13 @@ template <int MB> int check() {
         seen.insert(t);
     }
     if ((int)seen.size() != SH) return 2;
-    // the 18 segments tile the shell in order, each on one neighbour slot
-    int next = 0;
-    for (int g = 0; g < 18; ++g) {
-        if (jp::amr::seg_first<MB>(g) != next) return 2;
-        for (int t = next; t < next + jp::amr::seg_size<MB>(g); ++t) {
-            int i, j, k;
-            jp::amr::shell_coord<MB>(t, i, j, k);
-            if (jp::amr::shell_slot<MB>(i, j, k) != jp::amr::seg_slot(g)) return 2;
-        }
-        next += jp::amr::seg_size<MB>(g);
+    // the neighbour slot of every shell cell is the slot of its offset from the block
+    for (int t = 0; t < SH; ++t) {
+        int i, j, k;
+        jp::amr::shell_coord<MB>(t, i, j, k);
+        const int sx = i < 0 ? 0 : (i >= MB ? 2 : 1), sy = j < 0 ? 0 : (j >= MB ? 2 : 1), sz = k < 0 ? 0 : (k >= MB ? 2 : 1);
+        if (jp::amr::shell_slot<MB>(i, j, k) != sz * 9 + sy * 3 + sx || sz * 9 + sy * 3 + sx == 13) return 2;
     }
-    if (next != SH) return 2;
     for (int k = 0; k < MB; ++k) for (int j = 0; j < MB; ++j) for (int i = 0; i < MB; ++i)
         for (int q = 1; q < 19; ++q) {
             int li = i - jp::cx(q), lj = j - jp::cy(q), lk = k - jp::cz(q);
