@@ -136,6 +136,26 @@ def test_pinned_host_round_trip_and_step():
     np.testing.assert_array_equal(a, b)
 
 
+def test_large_state_round_trip_in_stream_order():
+    # 1.27 GB of FP32 populations through pinned memory: the read-back follows the steps before it,
+    # the write precedes the steps after it (asynchronous, in the solver's stream order)
+    n = 256
+    with J.Solver("uniform", n=n, re=1600.0) as a, J.Solver("uniform", n=n, re=1600.0) as b:
+        a.step(3)
+        buf = J.PinnedBuffer(Q * n ** 3)
+        try:
+            assert J.lib().jp_get_populations(a.h, 0, 0, 0, J.C.c_void_p(buf.ptr.value), buf.array.size) == 0
+            ref = buf.array.copy()
+            b.step(1)                          # b's own state, overwritten below in stream order
+            assert J.lib().jp_set_populations(b.h, 0, 0, 0, J.C.c_void_p(buf.ptr.value), buf.array.size) == 0
+            b.step(2)
+            a.step(2)
+            np.testing.assert_array_equal(b.get_populations(), a.get_populations())
+            np.testing.assert_array_equal(ref, buf.array)
+        finally:
+            buf.free()
+
+
 def test_step_counter_and_reinit():
     with J.Solver("uniform", n=16, re=400.0) as s:
         f0 = s.get_populations()
