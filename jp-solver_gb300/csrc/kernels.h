@@ -35,8 +35,8 @@ cudaError_t launch_stream_collide(int storage, const UniSolve* solves, int count
                                   cudaStream_t st);
 
 // In-place (AA) step over `count` cubes, each with src == dst: parity 0 (even step count) runs the
-// local step, 1 the stream step (uniform_aa.cu).  vec must be the storage's default; tpb is a lower
-// bound on the threads per block, which also hold whole x-rows.
+// local step, 1 the stream step (uniform_aa.cu).  vec must be the storage's default; the threads per
+// block are the smallest of 128, 256, 512 that hold a whole x-row (tpb is not followed).
 cudaError_t launch_stream_collide_inplace(int storage, const UniSolve* solves, int count, int parity, int vec,
                                           int tpb, cudaStream_t st);
 // Threads per block the in-place steps use for cubes up to edge max_n (0: not supported).

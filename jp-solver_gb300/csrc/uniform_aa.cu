@@ -272,13 +272,16 @@ static cudaError_t launch_aa_tpb(int tpb, const UniSolve* s, int c, int parity, 
     return cudaErrorInvalidValue;
 }
 
-int inplace_tpb(int storage, int vec, int tpb, int max_n) {
+// The smallest CTA of 128, 256 or 512 threads that holds an x-row: larger CTAs run fewer resident
+// threads per SM (their occupancy floor allows more registers) and measured slower (N=512: 128
+// threads FP16 72.7 GLUPS, 256 threads 51.5), so a larger request is not followed.
+int inplace_tpb(int storage, int vec, int /*tpb*/, int max_n) {
     if (vec == 0) vec = default_vec(storage);
     if (vec <= 0 || max_n % vec) return 0;
     const int nr = max_n / vec;
     const int cap = storage == 3 ? 256 : 512;  // FP64: the exchange buffers of 512 threads exceed 48 KB
     for (int b = 128; b <= cap; b *= 2)
-        if (b >= tpb && b >= nr) return b;
+        if (b >= nr) return b;
     return 0;
 }
 
