@@ -112,6 +112,29 @@ def test_populations_one_coarse_step(n, l1, l2, f1, f2):
         o.close()
 
 
+@pytest.mark.parametrize("n,mb,f1", [(16, 4, 0.35), (64, 16, 0.5)])
+def test_populations_one_coarse_step_other_block_edges(n, mb, f1):
+    # the interface work (fill and prep lists, pulled populations only) at block edges 4 and 16: the
+    # ghost-shell size, the interface cells and the step kernels all depend on MB
+    s0, s1 = O.random_sensor_fields(n, mb=mb, seed=9)
+    with engine(n, 1600.0, "sensor", "sensor", f1, 0.4, develop=3, mb=mb, defer=True) as e:
+        e.set_sensor_override(s0, s1)
+        e.init_tgv()
+        o = oracle(n, 1600.0, "sensor", "sensor", f1, 0.4, develop=3, mb=mb, build=False)
+        o.set_sensor_override(s0, s1)
+        o.initial_build()
+        assert_tables_equal(e, o)
+        counts = e.counts()
+        assert counts["nf1"] > 0 and counts["nf2"] > 0
+        for lv in range(3):
+            e.set_populations(o.pops(lv), level=lv, layout="blocked")
+        e.step(1)
+        o.step(1)
+        for lv in range(3):
+            assert rel_err(e.get_populations(lv, layout="blocked"), o.pops(lv)) < 1e-5, "level %d" % lv
+        o.close()
+
+
 def test_populations_across_regrid_migration():
     n = 32
     s0, s1 = O.random_sensor_fields(n, seed=3)
