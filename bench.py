@@ -185,6 +185,35 @@ def bench_amr(J, device: int, steps: int = 20) -> dict:
         out["work_per_coarse_step"] = work
         out[st] = {"glups_work": glups, "ms_per_coarse_step": ms / steps, "achieved_gbs": gbs,
                    "frac_of_fp32_roofline": glups * 152.0 / peaks["hbm_gbs"], "frac_of_own_roofline": gbs / peaks["hbm_gbs"]}
+    out["dynamic"] = bench_amr_dynamic(J, device)
+    return out
+
+
+def bench_amr_dynamic(J, device: int, steps: int = 200) -> dict:
+    """The dynamic AMR case (coarse N=96, sensor refinement on both levels, frac1 0.3, frac2 0.1,
+    Re=1600, MB=8, a regrid every 20 coarse steps in the warm-up): graph replay of the coarse step,
+    timed without regrids as the reference's bench mode does, work-normalised as above."""
+    peaks = load_peaks()
+    out = {"workload": "AMR dynamic: N0=96, --l1 sensor --l2 sensor, frac1 0.3, frac2 0.1, MB=8, Re=1600, "
+                       "CUDA-graph step"}
+    for st in ("fp32", "fp16"):
+        s = J.Solver("amr", n=96, re=1600.0, u0=U0, l1_mode="sensor", l2_mode="sensor", frac1=0.3, frac2=0.1,
+                     adapt_every=20, storage=st, device=device, flags=J.FLAG_GRAPH)
+        try:
+            for w in range(20):
+                if w % 20 == 0:
+                    s.regrid()
+                s.step(1)
+            s.sync()
+            c = s.counts()
+            work = (c["cnb0"] + 2 * c["nf1"] + 4 * c["nf2"]) * 512
+            ms = s.step_timed(steps)
+        finally:
+            s.close()
+        glups = work * steps / (ms / 1e3) / 1e9
+        out[st] = {"glups_work": glups, "ms_per_coarse_step": ms / steps, "work_per_coarse_step": work,
+                   "frac_of_fp32_roofline": glups * 152.0 / peaks["hbm_gbs"],
+                   "frac_of_own_roofline": glups * BYTES_PER_UPDATE[st] / peaks["hbm_gbs"]}
     return out
 
 
