@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(TPB, 1024 / TPB) k_step_l0(const typename ST::
     d_step_l0<MB, ST, TPB>(fa, fb, cgx, om, (int)blockIdx.x);
 }
 
-// ---- prolongation sources on a block list (src/tgv3d_amr.cu:160-171) -----------------------------
+// ---- prolongation sources on a cell list (src/tgv3d_amr.cu:160-171) ------------------------------
 // Only the cells a fill can read are prepared.  A fill interpolates a ghost cell of a fine block
 // from the 2x2x2 parent cells around it; the parent cell U holding the ghost is unrefined, the parent
 // R of the fine cell next to it is refined, and every one of those corners lies within one cell of
@@ -105,16 +105,21 @@ __global__ void __launch_bounds__(256) k_prep(const typename ST::raw* __restrict
                    (int)(gridDim.x * blockDim.x));
 }
 
-// Resident CTAs of the prep kernel on this device (SMs x CTAs per SM): its grid.
+// SMs x resident CTAs per SM of `kernel` at `threads` threads and `smem` bytes of dynamic shared
+// memory on the current device: the grid of the kernels that walk a list or a level.
+template <class K>
+static int resident_grid(K kernel, int threads, size_t smem) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
+    return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+}
+
+// the prep kernel's grid
 template <int MB, class ST>
 static int prep_grid_cap() {
-    static const int cap = [] {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_prep<MB, ST>, 256, 0);
-        return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
-    }();
+    static const int cap = resident_grid(k_prep<MB, ST>, 256, 0);
     return cap;
 }
 
@@ -278,17 +283,10 @@ __global__ void __launch_bounds__(256) k_fill_l2(const typename ST::raw* __restr
                       (int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x));
 }
 
-// Resident CTAs of a fill kernel on this device (SMs x CTAs per SM): the fills' grid.
+// the fills' grid
 template <int MB, class ST, int LEVEL>
 static int fill_grid_cap() {
-    static const int cap = [] {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (LEVEL == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fill_l1<MB, ST>, 256, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fill_l2<MB, ST>, 256, 0);
-        return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
-    }();
+    static const int cap = LEVEL == 1 ? resident_grid(k_fill_l1<MB, ST>, 256, 0) : resident_grid(k_fill_l2<MB, ST>, 256, 0);
     return cap;
 }
 
@@ -550,19 +548,13 @@ __global__ void __launch_bounds__(RowGeo<MB>::TPB, (rows_min_blocks<MB, ST>())) 
                                          (int)blockIdx.x, (int)gridDim.x);
 }
 
-// Resident CTAs of a rows kernel on this device (SMs x CTAs per SM), the grid its launches use: each
-// CTA walks the level's blocks, so the start of a CTA (the block count, the first table reads) is
-// paid once per CTA instead of once per block.
+// The grid of the walking rows kernels (resident CTAs): each CTA walks the level's blocks, so the
+// start of a CTA (the block count, the first table reads) is paid once per CTA instead of once per
+// block.
 template <int MB, class ST, bool FUSE>
 static int rows_grid_cap() {
-    static const int cap = [] {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step_fine_rows<MB, ST, FUSE, true>, RowGeo<MB>::TPB,
-                                                      FUSE ? sizeof(float) * Q * Geo<MB>::MB3 : 0);
-        return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
-    }();
+    static const int cap = resident_grid(k_step_fine_rows<MB, ST, FUSE, true>, RowGeo<MB>::TPB,
+                                         FUSE ? sizeof(float) * Q * Geo<MB>::MB3 : 0);
     return cap;
 }
 
