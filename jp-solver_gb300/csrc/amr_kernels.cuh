@@ -169,14 +169,34 @@ __device__ __forceinline__ float corners_l1(const typename ST::raw* __restrict__
     }
     return wsum;
 }
+// The pulled populations of one ghost cell (ghost_need: 5 on a face, 1 on an edge), interpolated
+// together: all their corner loads are issued before any sum, each population summed in corner
+// order as one at a time would be.  On an edge the spare slots repeat its one population and are not
+// stored.
 template <int MB, class ST, bool SPARSE>
-__device__ __forceinline__ float interp(const typename ST::raw* const (&p)[8], const float (&w)[8], int q) {
+__device__ __forceinline__ int interp_needed(const typename ST::raw* const (&p)[8], const float (&w)[8], unsigned need,
+                                             int (&qs)[5], float (&v)[5]) {
     constexpr int MB3 = MB * MB * MB;
-    float acc = 0.f;
+    const int nq = __popc(need);
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+        qs[s] = need ? __ffs(need) - 1 : qs[0];
+        need &= need - 1u;
+    }
+    typename ST::raw r[8][5];
 #pragma unroll
     for (int c = 0; c < 8; ++c)
-        if (!SPARSE || p[c]) acc += w[c] * PoolIO<ST>::f(p[c] + q * MB3, q);
-    return acc;
+#pragma unroll
+        for (int s = 0; s < 5; ++s) r[c][s] = (!SPARSE || p[c]) ? __ldg(p[c] + qs[s] * MB3) : typename ST::raw(0);
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+        float acc = 0.f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+            if (!SPARSE || p[c]) acc += w[c] * (ST::shifted ? wf(qs[s]) + ST::load(r[c][s]) : ST::load(r[c][s]));
+        v[s] = acc;
+    }
+    return nq;
 }
 
 // Populations a fine step pulls from the ghost cell at (i, j, k) just outside the block: those whose
@@ -220,14 +240,12 @@ __device__ __forceinline__ void d_fill_l1(const typename ST::raw* __restrict__ p
         float w[8];
         corners_l0<MB, ST>(pr, cgx, N, gfi, gfj, gfk, p, w);
         // only the populations a step pulls from this cell: five on a face, one on an edge
-        unsigned need = ghost_need<MB>(i, j, k);
+        int qs[5];
+        float val[5];
+        const int nq = interp_needed<MB, ST, false>(p, w, ghost_need<MB>(i, j, k), qs, val);
 #pragma unroll
-        for (int s = 0; s < 5; ++s) {
-            if (!need) break;
-            const int q = __ffs(need) - 1;
-            need &= need - 1;
-            PoolIO<ST>::put_f(gh + ((size_t)fb * Q + q) * G::SH + t, q, interp<MB, ST, false>(p, w, q));
-        }
+        for (int s = 0; s < 5; ++s)
+            if (s < nq) PoolIO<ST>::put_f(gh + ((size_t)fb * Q + qs[s]) * G::SH + t, qs[s], val[s]);
     }
 }
 template <int MB, class ST>
@@ -262,16 +280,12 @@ __device__ __forceinline__ void d_fill_l2(const typename ST::raw* __restrict__ p
         const float wsum = corners_l1<MB, ST>(pr, l1grid, l1gx, N1, g2i, g2j, g2k, p, w);
         const bool renorm = wsum > 0.f && wsum < 0.999f;
         const float inv = renorm ? 1.f / wsum : 1.f;
-        unsigned need = ghost_need<MB>(i, j, k);
+        int qs[5];
+        float val[5];
+        const int nq = interp_needed<MB, ST, true>(p, w, ghost_need<MB>(i, j, k), qs, val);
 #pragma unroll
-        for (int s = 0; s < 5; ++s) {
-            if (!need) break;
-            const int q = __ffs(need) - 1;
-            need &= need - 1;
-            float val = interp<MB, ST, true>(p, w, q);
-            if (renorm) val *= inv;
-            PoolIO<ST>::put_f(gh + ((size_t)b * Q + q) * G::SH + t, q, val);
-        }
+        for (int s = 0; s < 5; ++s)
+            if (s < nq) PoolIO<ST>::put_f(gh + ((size_t)b * Q + qs[s]) * G::SH + t, qs[s], renorm ? val[s] * inv : val[s]);
     }
 }
 template <int MB, class ST>
