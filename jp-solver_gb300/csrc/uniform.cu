@@ -50,8 +50,17 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
     const int x0 = xs * V;
     const int lane = threadIdx.x & 31;
     const size_t qs = (size_t)n * n * n;
-    const int ym = y == 0 ? n - 1 : y - 1, yp = y == n - 1 ? 0 : y + 1;
-    const int zm = z == 0 ? n - 1 : z - 1, zp = z == n - 1 ? 0 : z + 1;
+    // the nine x-rows around (y, z) (periodic): offsets of their starts within a population plane,
+    // 32-bit (n^3 < 2^32, checked at launch); row (dy, dz) at roff[(dz + 1) * 3 + dy + 1]
+    unsigned roff[9];
+    {
+        const int ys[3] = {y == 0 ? n - 1 : y - 1, y, y == n - 1 ? 0 : y + 1};
+        const int zs[3] = {z == 0 ? n - 1 : z - 1, z, z == n - 1 ? 0 : z + 1};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) roff[a * 3 + c] = ((unsigned)zs[a] * n + ys[c]) * n;
+    }
     const bool prev_direct = (lane == 0) || (x0 == 0);
     const bool next_direct = (lane == 31) || (x0 + V == n);
     const int xprev = x0 == 0 ? n - 1 : x0 - 1;
@@ -62,9 +71,7 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
     raw E[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const int sy = cy(q) > 0 ? ym : (cy(q) < 0 ? yp : y);   // pull from y - c_y
-        const int sz = cz(q) > 0 ? zm : (cz(q) < 0 ? zp : z);
-        const raw* p = src + q * qs + ((size_t)sz * n + sy) * n;
+        const raw* p = src + q * qs + roff[(1 - cz(q)) * 3 + 1 - cy(q)];  // pull from (y, z) - c_(y,z)
         L[q] = ld_pack<raw, V>(p + x0);
         E[q] = raw(0);
         if (cx(q) > 0 && prev_direct) E[q] = ld_one(p + xprev);
@@ -174,7 +181,8 @@ cudaError_t launch_stream_collide(int storage, const UniSolve* solves, int count
     if (vec == 0) vec = default_vec(storage);
     if (!vec_supported(storage, vec)) return cudaErrorInvalidValue;
     for (int i = 0; i < count; ++i)
-        if (solves[i].n % vec != 0 || ((long long)solves[i].n * solves[i].n * solves[i].n / vec) % 32 != 0)
+        if (solves[i].n % vec != 0 || ((long long)solves[i].n * solves[i].n * solves[i].n / vec) % 32 != 0 ||
+            (long long)solves[i].n * solves[i].n * solves[i].n >= (1LL << 32))
             return cudaErrorInvalidValue;
     switch (storage) {
         case 0:

@@ -126,16 +126,23 @@ __global__ void __launch_bounds__(TPB, (aa_min_blocks<ST, V, TPB>())) k_aa_strea
     const int x0 = X * V;
     raw* __restrict__ A = static_cast<raw*>(d.dst);
     const size_t qs = (size_t)n * n * n;
-    const int ym = y == 0 ? n - 1 : y - 1, yp = y == n - 1 ? 0 : y + 1;
-    const int zm = z == 0 ? n - 1 : z - 1, zp = z == n - 1 ? 0 : z + 1;
+    // the nine x-rows around (y, z) (periodic), this thread's x range: offsets within a population
+    // plane, 32-bit (n^3 < 2^32, checked at launch); row (dy, dz) at roff[(dz + 1) * 3 + dy + 1]
+    unsigned roff[9];
+    {
+        const int ys[3] = {y == 0 ? n - 1 : y - 1, y, y == n - 1 ? 0 : y + 1};
+        const int zs[3] = {z == 0 ? n - 1 : z - 1, z, z == n - 1 ? 0 : z + 1};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) roff[a * 3 + c] = ((unsigned)zs[a] * n + ys[c]) * n + x0;
+    }
 
     // 1. gather: the vector of slot opp(q) in the row at (y, z) - c_(y,z), covering this thread's x range
     Pack<raw, V> L[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const int sy = cy(q) > 0 ? ym : (cy(q) < 0 ? yp : y);
-        const int sz = cz(q) > 0 ? zm : (cz(q) < 0 ? zp : z);
-        if (active) L[q] = ld_pack_cg<raw, V>(A + opp(q) * qs + ((size_t)sz * n + sy) * n + x0);
+        if (active) L[q] = ld_pack_cg<raw, V>(A + opp(q) * qs + roff[(1 - cz(q)) * 3 + 1 - cy(q)]);
         else zero_pack(L[q]);
     }
     // 2. the value from across the vector edge: the left vector's last (c_x > 0) or the right one's first
@@ -208,8 +215,6 @@ __global__ void __launch_bounds__(TPB, (aa_min_blocks<ST, V, TPB>())) k_aa_strea
     }
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const int dy = cy(q) > 0 ? yp : (cy(q) < 0 ? ym : y);
-        const int dz = cz(q) > 0 ? zp : (cz(q) < 0 ? zm : z);
         R e[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) {
@@ -219,7 +224,7 @@ __global__ void __launch_bounds__(TPB, (aa_min_blocks<ST, V, TPB>())) k_aa_strea
         }
         Pack<raw, V> p;
         put_row<ST, V, SA>(p, e, q);
-        st_pack<raw, V>(A + q * qs + ((size_t)dz * n + dy) * n + x0, p);
+        st_pack<raw, V>(A + q * qs + roff[(1 + cz(q)) * 3 + 1 + cy(q)], p);
     }
 }
 
@@ -294,6 +299,7 @@ cudaError_t launch_stream_collide_inplace(int storage, const UniSolve* solves, i
     int max_n = 0;
     for (int i = 0; i < count; ++i) {
         if (solves[i].n <= 0 || solves[i].n % vec != 0 || solves[i].src != solves[i].dst) return cudaErrorInvalidValue;
+        if ((long long)solves[i].n * solves[i].n * solves[i].n >= (1LL << 32)) return cudaErrorInvalidValue;
         max_n = solves[i].n > max_n ? solves[i].n : max_n;
     }
     // the stream step needs whole rows per block; the local step runs at the same width
