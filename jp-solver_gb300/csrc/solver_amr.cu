@@ -63,6 +63,9 @@ struct AmrState {
     // build) or the launch shape changes.
     cudaGraphExec_t graph[8] = {};
     float *c0_home = nullptr, *f1_home = nullptr, *f2_home = nullptr;
+    // a coarse step's level-0 chain runs on `side`, beside the first level-2 pair (base_step)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 // SC_COUNT entries come from the host (upload_counts); the fill-list lengths are written on the device
 // (SC_PREP0/1: interface cells of the prep lists, whose block counts are SC_PBLK0/1)
@@ -117,8 +120,8 @@ static void dfree(AmrState* a, T*& p) {
 // arrays are typed float* and carry 16-bit values for the shifted formats).
 static size_t pf(const AmrState* a, size_t n) { return (n * a->elem + 3) / 4; }
 
-static jp_status launch(jp_solver* s, int op, AmrLaunch L) {
-    L.st = s->stream;
+static jp_status launch(jp_solver* s, int op, AmrLaunch L, cudaStream_t st = nullptr) {
+    L.st = st ? st : s->stream;
     cudaError_t e = amr_launch(s->amr->storage, s->amr->MB, op, L);
     if (e != cudaSuccess) return cuda_fail(e, "AMR kernel launch");
     return JP_OK;
@@ -155,7 +158,7 @@ static jp_status sensor(jp_solver* s, int level) {
     return launch(s, OP_SENSOR, L);
 }
 
-static jp_status step_l0(jp_solver* s) {
+static jp_status step_l0(jp_solver* s, cudaStream_t st = nullptr) {
     AmrState* a = s->amr;
     AmrLaunch L;
     L.nblocks = a->cnb0;
@@ -165,7 +168,7 @@ static jp_status step_l0(jp_solver* s) {
     L.n = a->N;
     L.omega = a->om0;
     L.tpb = a->tpb;
-    TRY(launch(s, OP_STEP_L0, L));
+    TRY(launch(s, OP_STEP_L0, L, st));
     std::swap(a->c0a, a->c0b);
     return JP_OK;
 }
@@ -548,38 +551,65 @@ static jp_status regrid(jp_solver* s) {
     return JP_OK;
 }
 
+// the coarse step and the level-1 ghosts it feeds (prolongation sources of level 0, level-1 fill)
+static jp_status level0_chain(jp_solver* s, cudaStream_t st) {
+    AmrState* a = s->amr;
+    const int* cnt = a->step_cnt;
+    TRY(step_l0(s, st));
+    if (s->cfg.flags & JP_FLAG_SKIP_PREP) return JP_OK;
+    AmrLaunch L;
+    L.nblocks = interface_cells(a->MB) * a->cnb0;
+    L.nlim = cnt + SC_PREP0;
+    L.in = a->c0a;
+    L.out = a->prep0;
+    L.list = a->pc0;
+    L.scale = float(a->nqs01);
+    L.t0 = cnt + SC_FILL1;
+    TRY(launch(s, OP_PREP, L, st));
+    AmrLaunch F;
+    F.nblocks = a->SH * a->cap1;
+    F.list = a->fl1;
+    F.nlim = cnt + SC_FILL1;
+    F.in = a->prep0;
+    F.out = a->gh1;
+    F.t0 = a->pcb;
+    F.t1 = a->oct;
+    F.cgx = a->cgx;
+    F.n = a->N;
+    return launch(s, OP_FILL_L1, F, st);
+}
+
 // base_step (src/tgv3d_amr.cu:821-837): coarse once, level 1 twice, level 2 four times, restricting
 // level 2 into level 1 after each pair and level 1 into level 0 at the end.  Launch shapes depend on
 // the pool capacities only; the kernels read the block counts of the current grid on the device.
+//
+// The level-0 chain (coarse step, its prolongation sources, the level-1 ghost fill) and the first
+// level-2 pair (level-1 sources, level-2 fill, two level-2 substeps restricting into level 1) share
+// no array: 2:1 balance keeps level 2 away from level 0, so level-2 ghosts come from level 1 alone.
+// They meet at the first level-1 substep, which reads the level-1 ghosts and the restricted level 1.
+// The level-0 chain therefore runs on a side stream (a branch of the captured graph), and the short
+// latency-bound fills and preps of one chain overlap the bandwidth-bound steps of the other.  Every
+// kernel sees the same inputs as in one stream: results are unchanged.
 static jp_status base_step(jp_solver* s) {
     AmrState* a = s->amr;
     const bool skip_prep = s->cfg.flags & JP_FLAG_SKIP_PREP, skip_restrict = s->cfg.flags & JP_FLAG_SKIP_RESTRICT;
     // restrictions fused into the last substep of each fine level (same values, one pass less)
     const bool fuse = !skip_restrict && can_fuse_restrict(a->MB);
     const int* cnt = a->step_cnt;
-    TRY(step_l0(s));
-    if (!skip_prep) {
-        AmrLaunch L;
-        L.nblocks = interface_cells(a->MB) * a->cnb0;
-        L.nlim = cnt + SC_PREP0;
-        L.in = a->c0a;
-        L.out = a->prep0;
-        L.list = a->pc0;
-        L.scale = float(a->nqs01);
-        L.t0 = cnt + SC_FILL1;
-        TRY(launch(s, OP_PREP, L));
-        AmrLaunch F;
-        F.nblocks = a->SH * a->cap1;
-        F.list = a->fl1;
-        F.nlim = cnt + SC_FILL1;
-        F.in = a->prep0;
-        F.out = a->gh1;
-        F.t0 = a->pcb;
-        F.t1 = a->oct;
-        F.cgx = a->cgx;
-        F.n = a->N;
-        TRY(launch(s, OP_FILL_L1, F));
-    }
+    ACK(cudaEventRecord(a->fork, s->stream), "fork");
+    ACK(cudaStreamWaitEvent(a->side, a->fork, 0), "fork");
+    const jp_status st0 = level0_chain(s, a->side);
+    ACK(cudaEventRecord(a->join, a->side), "join");
+    // the stream (or the capture) takes the branch back on every return, errors included
+    struct Join {
+        cudaStream_t st;
+        cudaEvent_t ev;
+        bool pending = true;
+        ~Join() {
+            if (pending) cudaStreamWaitEvent(st, ev, 0);
+        }
+    } join{s->stream, a->join};
+    TRY(st0);
     for (int s1 = 0; s1 < 2; ++s1) {
         if (!skip_prep) {
             AmrLaunch L;
@@ -635,6 +665,10 @@ static jp_status base_step(jp_solver* s) {
             R.t0 = a->fof1;
             R.scale = float(a->nqi21);
             TRY(launch(s, OP_RESTRICT, R));
+        }
+        if (s1 == 0) {
+            join.pending = false;
+            ACK(cudaStreamWaitEvent(s->stream, a->join, 0), "join");
         }
         AmrLaunch S;
         S.nblocks = a->cap1;
@@ -951,6 +985,11 @@ jp_status amr_create(jp_solver* s) {
     if (!a->cnt_host || !s->diag_host) return fail(JP_ERR_NOMEM, "pinned host slot");
     ACK(dev_alloc(s, (void**)&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
     ACK(dev_alloc(s, (void**)&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
+    int prio = 0;
+    ACK(cudaStreamGetPriority(s->stream, &prio), "cudaStreamGetPriority");
+    ACK(cudaStreamCreateWithPriority(&a->side, cudaStreamNonBlocking, prio), "cudaStreamCreate");
+    ACK(cudaEventCreateWithFlags(&a->fork, cudaEventDisableTiming), "cudaEventCreate");
+    ACK(cudaEventCreateWithFlags(&a->join, cudaEventDisableTiming), "cudaEventCreate");
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->l1grid, 0xFF, sizeof(int) * a->NG1, s->stream), "memset");
@@ -963,7 +1002,11 @@ void amr_destroy(jp_solver* s) {
     AmrState* a = s->amr;
     if (!a) return;
     reset_graphs(a);
+    if (a->side) cudaStreamSynchronize(a->side);
     for (void* p : a->owned) dev_free(s, p);
+    if (a->fork) cudaEventDestroy(a->fork);
+    if (a->join) cudaEventDestroy(a->join);
+    if (a->side) cudaStreamDestroy(a->side);
     pinned_slot_free(a->cnt_host);
     pinned_slot_free(a->step_cnt_host);
     dev_free(s, a->field);
