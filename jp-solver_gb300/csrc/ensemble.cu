@@ -81,6 +81,7 @@ struct jp_ensemble {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
+    AmrFork fk;  // the level-0 branch of the AMR members' coarse steps
     std::vector<jp_solver*> members;
 };
 
@@ -95,6 +96,7 @@ jp_status jp_ensemble_create(int32_t device, jp_ensemble** out) {
     e->device = device;
     cudaError_t err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = e->fk.create(e->stream);
     if (err != cudaSuccess) {
         jp_ensemble_destroy(e);
         return cuda_fail(err, "ensemble stream");
@@ -109,6 +111,7 @@ void jp_ensemble_destroy(jp_ensemble* e) {
         cudaStreamSynchronize(e->stream);
         cudaStreamDestroy(e->stream);
     }
+    e->fk.destroy();
     if (e->done) cudaEventDestroy(e->done);
     delete e;
 }
@@ -159,7 +162,7 @@ jp_status jp_ensemble_step(jp_ensemble* e, int64_t nsteps) {
         jp_status st = batched_step(uni, e->stream);
         if (st != JP_OK) return st;
         for (auto& g : amr) {
-            st = amr_batch_step(g, e->stream);
+            st = amr_batch_step(g, e->stream, &e->fk);
             if (st != JP_OK) return st;
         }
     }
@@ -272,6 +275,7 @@ struct jp_server {
         std::deque<Job*> inbox;          // created or regridded solves (re)joining the lane
         std::vector<Job*> active;        // the lane thread's own
         cudaStream_t stream = nullptr;
+        AmrFork fk;  // the level-0 branch of the lane's batched coarse steps
         AmrDiag adiag[2];
         int diag_cur = 0;
         Span span[4];
@@ -539,7 +543,7 @@ bool lane_round(jp_server* sv, jp_server::Lane& L) {
                 if (ms.empty()) break;
                 // a group of one with graph replay replays its captured step instead (one launch)
                 const bool alone = ms.size() == 1 && (ms[0]->cfg.flags & JP_FLAG_GRAPH);
-                st = alone ? amr_graph_step_on(ms[0], L.stream) : amr_batch_step(ms, L.stream);
+                st = alone ? amr_graph_step_on(ms[0], L.stream) : amr_batch_step(ms, L.stream, &L.fk);
                 moved += (long long)ms.size();
             }
             for (Job* j : g) {
@@ -644,6 +648,7 @@ jp_status jp_server_create(const jp_server_config* cfg, jp_server** out) {
     cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
     for (int l = 0; l < jp_server::kLanes && e == cudaSuccess; ++l) {
         e = cudaStreamCreateWithFlags(&sv->lane[l].stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = sv->lane[l].fk.create(sv->lane[l].stream);
         for (auto& d : sv->lane[l].adiag)
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d.done, cudaEventDisableTiming);
     }
@@ -724,8 +729,10 @@ void jp_server_destroy(jp_server* sv) {
         drop_spans(L.span);
     }
     drop_spans(sv->uspan);
-    for (auto& L : sv->lane)
+    for (auto& L : sv->lane) {
+        L.fk.destroy();
         if (L.stream) cudaStreamDestroy(L.stream);
+    }
     for (Job* j : sv->queue) delete j;
     for (auto& b : sv->diag) {
         if (b.dev) cudaFree(b.dev);

@@ -102,8 +102,17 @@ jp_status amr_set_populations(jp_solver* s, int level, int layout, int dtype, co
 jp_status amr_regrid(jp_solver* s);
 // the fine steps' mapping: vec 4 (rows) or 1 (a cell per thread, tpb threads per CTA); autotuner
 jp_status amr_set_step_map(jp_solver* s, int vec, int tpb);
-// one coarse step of many AMR solvers, one launch per stage over all of them, on `st`
-jp_status amr_batch_step(const std::vector<jp_solver*>& members, cudaStream_t st);
+// a side stream (at the priority of the stream it branches from) and the two events of the level-0
+// branch of a coarse step
+struct AmrFork {
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaError_t create(cudaStream_t like);
+    void destroy();
+};
+// one coarse step of many AMR solvers, one launch per stage over all of them, on `st` (the level-0
+// stages on fork->side when a fork is given)
+jp_status amr_batch_step(const std::vector<jp_solver*>& members, cudaStream_t st, const AmrFork* fork = nullptr);
 bool amr_batch_compatible(const jp_solver* a, const jp_solver* b);
 jp_status amr_prepare_diag(jp_solver* s);
 jp_status amr_graph_step_on(jp_solver* s, cudaStream_t st);

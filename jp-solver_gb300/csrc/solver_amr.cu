@@ -63,9 +63,7 @@ struct AmrState {
     // build) or the launch shape changes.
     cudaGraphExec_t graph[8] = {};
     float *c0_home = nullptr, *f1_home = nullptr, *f2_home = nullptr;
-    // a coarse step's level-0 chain runs on `side`, beside the first level-2 pair (base_step)
-    cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    AmrFork fk;  // a coarse step's level-0 chain runs on fk.side, beside the first level-2 pair (base_step)
 };
 // SC_COUNT entries come from the host (upload_counts); the fill-list lengths are written on the device
 // (SC_PREP0/1: interface cells of the prep lists, whose block counts are SC_PBLK0/1)
@@ -551,6 +549,40 @@ static jp_status regrid(jp_solver* s) {
     return JP_OK;
 }
 
+cudaError_t AmrFork::create(cudaStream_t like) {
+    int prio = 0;
+    cudaError_t e = cudaStreamGetPriority(like, &prio);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, prio);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    return e;
+}
+
+// the side stream's work is always joined into its main stream, so nothing on it outlives that
+void AmrFork::destroy() {
+    if (side) cudaStreamSynchronize(side);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (side) cudaStreamDestroy(side);
+    side = nullptr;
+    fork = join = nullptr;
+}
+
+// Takes a side branch back into a stream (or a capture) on every return, errors included.
+struct JoinOnExit {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    bool pending = true;
+    jp_status now() {
+        pending = false;
+        ACK(cudaStreamWaitEvent(st, ev, 0), "join");
+        return JP_OK;
+    }
+    ~JoinOnExit() {
+        if (pending) cudaStreamWaitEvent(st, ev, 0);
+    }
+};
+
 // the coarse step and the level-1 ghosts it feeds (prolongation sources of level 0, level-1 fill)
 static jp_status level0_chain(jp_solver* s, cudaStream_t st) {
     AmrState* a = s->amr;
@@ -596,19 +628,11 @@ static jp_status base_step(jp_solver* s) {
     // restrictions fused into the last substep of each fine level (same values, one pass less)
     const bool fuse = !skip_restrict && can_fuse_restrict(a->MB);
     const int* cnt = a->step_cnt;
-    ACK(cudaEventRecord(a->fork, s->stream), "fork");
-    ACK(cudaStreamWaitEvent(a->side, a->fork, 0), "fork");
-    const jp_status st0 = level0_chain(s, a->side);
-    ACK(cudaEventRecord(a->join, a->side), "join");
-    // the stream (or the capture) takes the branch back on every return, errors included
-    struct Join {
-        cudaStream_t st;
-        cudaEvent_t ev;
-        bool pending = true;
-        ~Join() {
-            if (pending) cudaStreamWaitEvent(st, ev, 0);
-        }
-    } join{s->stream, a->join};
+    ACK(cudaEventRecord(a->fk.fork, s->stream), "fork");
+    ACK(cudaStreamWaitEvent(a->fk.side, a->fk.fork, 0), "fork");
+    const jp_status st0 = level0_chain(s, a->fk.side);
+    ACK(cudaEventRecord(a->fk.join, a->fk.side), "join");
+    JoinOnExit join{s->stream, a->fk.join};
     TRY(st0);
     for (int s1 = 0; s1 < 2; ++s1) {
         if (!skip_prep) {
@@ -666,10 +690,7 @@ static jp_status base_step(jp_solver* s) {
             R.scale = float(a->nqi21);
             TRY(launch(s, OP_RESTRICT, R));
         }
-        if (s1 == 0) {
-            join.pending = false;
-            ACK(cudaStreamWaitEvent(s->stream, a->join, 0), "join");
-        }
+        if (s1 == 0) TRY(join.now());
         AmrLaunch S;
         S.nblocks = a->cap1;
         S.nlim = cnt + SC_NF1;
@@ -704,14 +725,15 @@ static jp_status base_step(jp_solver* s) {
 // One coarse step of many AMR solves with one launch per stage over all of them (base_step's
 // sequence, each launch an AmrBatch of up to kAmrBatchMax members).  The members share block edge,
 // storage, step threads and skip flags (amr_batch_compatible).
-jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
+jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st, const AmrFork* fk) {
     if (ms.empty()) return JP_OK;
     const AmrState* a0 = ms[0]->amr;
     const int flags = ms[0]->cfg.flags;
     const bool skip_prep = flags & JP_FLAG_SKIP_PREP, skip_restrict = flags & JP_FLAG_SKIP_RESTRICT;
     const bool fuse = !skip_restrict && can_fuse_restrict(a0->MB);
-    // one stage over all members: fill() sets a member's item and returns its CTAs (0: nothing)
-    auto run = [&](int op, bool fused, auto fill) -> jp_status {
+    // one stage over all members on stream `on`: fill() sets a member's item and returns its CTAs
+    // (0: nothing)
+    auto run_on = [&](cudaStream_t on, int op, bool fused, auto fill) -> jp_status {
         for (size_t i0 = 0; i0 < ms.size(); i0 += kAmrBatchMax) {
             AmrBatch B;
             B.vec = a0->vec;
@@ -725,21 +747,30 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
                 B.total += n;
                 ++B.count;
             }
-            cudaError_t e = amr_batch_launch(a0->storage, a0->MB, op, a0->tpb, fused, B, st);
+            cudaError_t e = amr_batch_launch(a0->storage, a0->MB, op, a0->tpb, fused, B, on);
             if (e != cudaSuccess) return cuda_fail(e, "batched AMR launch");
         }
         return JP_OK;
     };
-    TRY(run(OP_STEP_L0, false, [](AmrState* a, AmrItem& it) {
-        it.in = a->c0a;
-        it.out = a->c0b;
-        it.cgx = a->cgx;
-        it.omega = a->om0;
-        return a->cnb0;
-    }));
-    for (jp_solver* m : ms) std::swap(m->amr->c0a, m->amr->c0b);
-    if (!skip_prep) {
-        TRY(run(OP_PREP, false, [](AmrState* a, AmrItem& it) {
+    auto run = [&](int op, bool fused, auto fill) { return run_on(st, op, fused, fill); };
+    // the level-0 chain, on the side stream when there is one (base_step: it shares no array with
+    // the first level-2 pair and joins before the first level-1 substep)
+    const cudaStream_t s0 = fk ? fk->side : st;
+    if (fk) {
+        ACK(cudaEventRecord(fk->fork, st), "fork");
+        ACK(cudaStreamWaitEvent(fk->side, fk->fork, 0), "fork");
+    }
+    auto level0 = [&]() -> jp_status {
+        TRY(run_on(s0, OP_STEP_L0, false, [](AmrState* a, AmrItem& it) {
+            it.in = a->c0a;
+            it.out = a->c0b;
+            it.cgx = a->cgx;
+            it.omega = a->om0;
+            return a->cnb0;
+        }));
+        for (jp_solver* m : ms) std::swap(m->amr->c0a, m->amr->c0b);
+        if (skip_prep) return JP_OK;
+        TRY(run_on(s0, OP_PREP, false, [](AmrState* a, AmrItem& it) {
             it.in = a->c0a;
             it.out = a->prep0;
             it.list = a->pc0;
@@ -748,7 +779,7 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
             it.t0 = a->step_cnt + SC_FILL1;
             return std::min((interface_cells(a->MB) * a->cnb0 + 255) / 256, kBatchPrepCtas);
         }));
-        TRY(run(OP_FILL_L1, false, [](AmrState* a, AmrItem& it) {
+        return run_on(s0, OP_FILL_L1, false, [](AmrState* a, AmrItem& it) {
             it.in = a->prep0;
             it.out = a->gh1;
             it.t0 = a->pcb;
@@ -758,8 +789,12 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
             it.list = a->fl1;
             it.nlim = a->step_cnt + SC_FILL1;
             return std::min((a->SH * a->cap1 + 255) / 256, kBatchPrepCtas);
-        }));
-    }
+        });
+    };
+    const jp_status st0 = level0();
+    if (fk) ACK(cudaEventRecord(fk->join, fk->side), "join");
+    JoinOnExit join{st, fk ? fk->join : nullptr, fk != nullptr};
+    TRY(st0);
     for (int s1 = 0; s1 < 2; ++s1) {
         if (!skip_prep) {
             TRY(run(OP_PREP, false, [](AmrState* a, AmrItem& it) {
@@ -815,6 +850,7 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st) {
                 return (a->cap2 + 7) / 8;
             }));
         }
+        if (s1 == 0 && join.pending) TRY(join.now());
         const bool f = s1 == 1 && fuse;  // last level-1 substep restricts itself into the coarse level
         TRY(run(OP_STEP_L1, f, [f](AmrState* a, AmrItem& it) {
             it.in = a->f1a;
@@ -985,11 +1021,7 @@ jp_status amr_create(jp_solver* s) {
     if (!a->cnt_host || !s->diag_host) return fail(JP_ERR_NOMEM, "pinned host slot");
     ACK(dev_alloc(s, (void**)&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
     ACK(dev_alloc(s, (void**)&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
-    int prio = 0;
-    ACK(cudaStreamGetPriority(s->stream, &prio), "cudaStreamGetPriority");
-    ACK(cudaStreamCreateWithPriority(&a->side, cudaStreamNonBlocking, prio), "cudaStreamCreate");
-    ACK(cudaEventCreateWithFlags(&a->fork, cudaEventDisableTiming), "cudaEventCreate");
-    ACK(cudaEventCreateWithFlags(&a->join, cudaEventDisableTiming), "cudaEventCreate");
+    ACK(a->fk.create(s->stream), "side stream");
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->ref1, 0, sizeof(int) * a->cap1, s->stream), "memset");
     ACK(cudaMemsetAsync(a->l1grid, 0xFF, sizeof(int) * a->NG1, s->stream), "memset");
@@ -1002,11 +1034,8 @@ void amr_destroy(jp_solver* s) {
     AmrState* a = s->amr;
     if (!a) return;
     reset_graphs(a);
-    if (a->side) cudaStreamSynchronize(a->side);
     for (void* p : a->owned) dev_free(s, p);
-    if (a->fork) cudaEventDestroy(a->fork);
-    if (a->join) cudaEventDestroy(a->join);
-    if (a->side) cudaStreamDestroy(a->side);
+    a->fk.destroy();
     pinned_slot_free(a->cnt_host);
     pinned_slot_free(a->step_cnt_host);
     dev_free(s, a->field);
