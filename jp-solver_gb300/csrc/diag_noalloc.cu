@@ -23,6 +23,7 @@
 
 #include <mutex>
 
+#include "diag_terms.cuh"
 #include "jp.h"
 #include "solver.h"
 
@@ -46,32 +47,24 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // One partial (E, enstrophy, mass sums) per chunk of kChunk cells.  Per cell: 1/2|u|^2,
-// 1/2|curl u|^2 from central differences with periodic wrap, rho; FP64 accumulation.  float_diff
-// takes each velocity difference in float before widening (the uniform solver's convention).
+// 1/2|curl u|^2 from central differences with periodic wrap, rho, in double-float
+// (diag_terms.cuh); FP64 accumulation.  float_diff takes each velocity difference in float before
+// halving (the uniform solver's convention).
 __global__ void __launch_bounds__(kThreads) k_noalloc_partials(const float* __restrict__ F, int n, int float_diff,
                                                               double* __restrict__ partials) {
     const long long cells = (long long)n * n * n;
     const long long begin = (long long)blockIdx.x * kChunk;
     const long long end = begin + kChunk < cells ? begin + kChunk : cells;
-    double e = 0.0, ens = 0.0, mass = 0.0;
+    dterm::Acc acc;
     for (long long c = begin + threadIdx.x; c < end; c += kThreads) {
-        const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
-        const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
-        const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
-        const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
-        auto at = [&](int a, int b, int cc, int comp) { return F[(((size_t)cc * n + b) * n + a) * 4 + comp]; };
-        auto dif = [&](float a, float b) -> double {
-            return float_diff ? double(a - b) * 0.5 : (double(a) - double(b)) * 0.5;
-        };
-        const double u = F[c * 4 + 1], v = F[c * 4 + 2], w = F[c * 4 + 3];
-        const double dudy = dif(at(i, jp, k, 1), at(i, jm, k, 1)), dudz = dif(at(i, j, kp, 1), at(i, j, km, 1));
-        const double dvdx = dif(at(ip, j, k, 2), at(im, j, k, 2)), dvdz = dif(at(i, j, kp, 2), at(i, j, km, 2));
-        const double dwdx = dif(at(ip, j, k, 3), at(im, j, k, 3)), dwdy = dif(at(i, jp, k, 3), at(i, jm, k, 3));
-        const double ox = dwdy - dvdz, oy = dudz - dwdx, oz = dvdx - dudy;
-        e += 0.5 * (u * u + v * v + w * w);
-        ens += 0.5 * (ox * ox + oy * oy + oz * oz);
-        mass += double(F[c * 4 + 0]);
+        dterm::FF ce, cens;
+        float rho;
+        if (float_diff) dterm::cell_terms<true>(F, n, c, ce, cens, rho);
+        else dterm::cell_terms<false>(F, n, c, ce, cens, rho);
+        acc.add_cell(ce, cens, rho);
     }
+    acc.flush();
+    double e = acc.de, ens = acc.dens, mass = acc.dmass;
     __shared__ double sh[3][kThreads / 32];
     e = warp_sum(e);
     ens = warp_sum(ens);

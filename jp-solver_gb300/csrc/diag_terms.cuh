@@ -1,0 +1,128 @@
+// Per-cell diagnostic terms of a float macro field (rho, ux, uy, uz per cell) without FP64 arithmetic
+// in the per-cell work.
+//
+// The reference forms 1/2|u|^2, 1/2|curl u|^2 (central differences, periodic) and rho per cell in
+// FP64 and sums them in FP64 (src/tgv3d_amr.cu:538-549; the uniform program's host loop,
+// src/tgv3d_uniform.cu:172-181).  GB300 issues FP64 at a small fraction of its FP32 rate, so those
+// ~45 FP64 instructions per cell made a diagnostic cost more than the steps it reports on (an N=128
+// field: ~150 us, against ~50 us for an FP32 step of the cube).
+//
+// Here each per-cell term is an unevaluated sum of two floats (hi + lo, "double-float") built from
+// error-free transformations: TwoProd (hi = a*b, lo = fma(a, b, -hi)) makes the product of two floats
+// exact, TwoSum (Knuth) the sum of two floats.  The velocity differences are therefore exact (in FP64
+// they are exact for floats of similar magnitude), the squares and sums carry about 2^-47 relative
+// error, and the three terms are non-negative, so every sum of them keeps that relative error
+// (~1e-14), well below the summation-order differences of FP64 sums (the diagnostics are checked to
+// 1e-12 relative).  A thread keeps its running sums in double-float over kFlush cells and then adds
+// them to FP64 accumulators: a few FP64 instructions per kFlush cells.  All arithmetic goes through
+// the _rn intrinsics, which the compiler never contracts or reorders.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace jp {
+namespace dterm {
+
+struct FF {
+    float hi, lo;
+};
+
+// a + b exactly (Knuth's TwoSum)
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+// a + b exactly when |a| >= |b| or a == 0 (Dekker's Fast2Sum)
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// a * b exactly (barring underflow of the error term)
+__device__ __forceinline__ FF two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+// x + y for x, y of the same sign: relative error below 2^-46
+__device__ __forceinline__ FF add_same_sign(FF x, FF y) {
+    const FF s = two_sum(x.hi, y.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+
+// x + y of any signs (Joldes, Muller, Popescu 2017, "AccurateDWPlusDW"): relative error below
+// 3 * 2^-48 even under cancellation
+__device__ __forceinline__ FF add(FF x, FF y) {
+    const FF s = two_sum(x.hi, y.hi);
+    const FF t = two_sum(x.lo, y.lo);
+    const FF v = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+    return fast_two_sum(v.hi, __fadd_rn(t.lo, v.lo));
+}
+
+__device__ __forceinline__ FF sq(FF x) {
+    const FF p = two_prod(x.hi, x.hi);
+    return fast_two_sum(p.hi, __fmaf_rn(__fmul_rn(2.f, x.hi), x.lo, p.lo));
+}
+
+__device__ __forceinline__ FF half(FF x) { return {__fmul_rn(x.hi, 0.5f), __fmul_rn(x.lo, 0.5f)}; }
+
+__device__ __forceinline__ double to_double(FF x) { return double(x.hi) + double(x.lo); }
+
+// 1/2|u|^2, 1/2|curl u|^2 and rho of cell c (i fastest) of an n^3 field F[cell][4].  FLOAT_DIFF takes
+// each velocity difference in float (rounded) before halving, as the uniform program's host loop
+// does; otherwise the difference of the two floats is exact, as in the AMR diagnostic kernel.
+template <bool FLOAT_DIFF>
+__device__ __forceinline__ void cell_terms(const float* __restrict__ F, int n, long long c, FF& e, FF& ens,
+                                           float& rho) {
+    const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
+    const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
+    const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
+    const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
+    auto at = [&](int a, int b, int cc, int comp) { return F[(((size_t)cc * n + b) * n + a) * 4 + comp]; };
+    auto dif = [&](float a, float b) -> FF {
+        if (FLOAT_DIFF) return {__fmul_rn(__fsub_rn(a, b), 0.5f), 0.f};
+        return half(two_sum(a, -b));
+    };
+    rho = F[c * 4 + 0];
+    const float u = F[c * 4 + 1], v = F[c * 4 + 2], w = F[c * 4 + 3];
+    e = half(add_same_sign(add_same_sign(two_prod(u, u), two_prod(v, v)), two_prod(w, w)));
+    const FF dudy = dif(at(i, jp, k, 1), at(i, jm, k, 1)), dudz = dif(at(i, j, kp, 1), at(i, j, km, 1));
+    const FF dvdx = dif(at(ip, j, k, 2), at(im, j, k, 2)), dvdz = dif(at(i, j, kp, 2), at(i, j, km, 2));
+    const FF dwdx = dif(at(ip, j, k, 3), at(im, j, k, 3)), dwdy = dif(at(i, jp, k, 3), at(i, jm, k, 3));
+    FF ox, oy, oz;
+    if (FLOAT_DIFF) {  // differences of single floats: exact
+        ox = two_sum(dwdy.hi, -dvdz.hi);
+        oy = two_sum(dudz.hi, -dwdx.hi);
+        oz = two_sum(dvdx.hi, -dudy.hi);
+    } else {
+        ox = add(dwdy, {-dvdz.hi, -dvdz.lo});
+        oy = add(dudz, {-dwdx.hi, -dwdx.lo});
+        oz = add(dvdx, {-dudy.hi, -dudy.lo});
+    }
+    ens = half(add_same_sign(add_same_sign(sq(ox), sq(oy)), sq(oz)));
+}
+
+// A thread's sums: double-float over kFlush cells, then into FP64.
+struct Acc {
+    static constexpr int kFlush = 8;
+    FF e{0.f, 0.f}, ens{0.f, 0.f}, mass{0.f, 0.f};
+    double de = 0.0, dens = 0.0, dmass = 0.0;
+    int k = 0;
+    __device__ __forceinline__ void add_cell(FF ce, FF cens, float rho) {
+        e = add_same_sign(e, ce);
+        ens = add_same_sign(ens, cens);
+        mass = add(mass, {rho, 0.f});  // rho of any sign (a field under test need not be physical)
+        if (++k == kFlush) flush();
+    }
+    __device__ __forceinline__ void flush() {
+        de += to_double(e);
+        dens += to_double(ens);
+        dmass += to_double(mass);
+        e = ens = mass = FF{0.f, 0.f};
+        k = 0;
+    }
+};
+
+}  // namespace dterm
+}  // namespace jp

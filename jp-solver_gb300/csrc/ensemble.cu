@@ -188,7 +188,7 @@ struct Job {
     bool admitted = false;  // holds `bytes` of the pool budget
     bool requeue = false;   // an AMR worker could not get the memory: back to the queue head
     // AMR: `step` is the program loop's s_; events (regrid, diagnostic) of step s_ are handled once
-    // (events_done) before the solve takes its next sstep coarse steps in the batch.  A worker
+    // (events_done) before the solve takes its next coarse steps in the batch (round_steps).  A worker
     // creates the solve (task 1) or regrids it (task 2, plus the diagnostic of that step when dg).
     long long sstep = 1;
     bool events_done = false, dg = false;
@@ -260,8 +260,8 @@ struct jp_server {
     Span uspan[4];
     int uspan_tick = 0;
     // AMR solves advance in lanes, each a thread with its own stream and a share of the solves.  A
-    // lane's rounds launch the diagnostics due, one batched coarse step per stage over the lane's
-    // solves (amr_batch_step), and read the previous round's diagnostics back.  Creation and
+    // lane's rounds launch the diagnostics due, batched coarse steps with one launch per stage over
+    // the lane's solves (amr_batch_step), and read the previous round's diagnostics back.  Creation and
     // regrids, which need read-backs, run on worker threads on each solve's own stream while its
     // lane goes on without it; a solve that leaves for a regrid waits only for its own lane's queue.
     struct AmrDiag {
@@ -367,7 +367,7 @@ cudaError_t span_open(jp_server* sv, jp_server::Span (&ring)[4], int tick, doubl
     if (e == cudaSuccess && !sp.b) e = cudaEventCreate(&sp.b);
     if (e == cudaSuccess && sp.live) {
         float ms = 0.f;
-        if (cudaEventSynchronize(sp.b) == cudaSuccess && cudaEventElapsedTime(&ms, sp.a, sp.b) == cudaSuccess)
+        if (wait_event(sp.b) == cudaSuccess && cudaEventElapsedTime(&ms, sp.a, sp.b) == cudaSuccess)
             sv->add(field, ms * 1e-3);
         sp.live = false;
     }
@@ -460,12 +460,27 @@ void worker_main(jp_server* sv) {
 
 void to_worker(jp_server* sv, Job* j, int task);
 
+// Coarse steps of an AMR solve in one lane round: up to the next step the program would visit
+// (steps sstep apart) at which the solve has an event (a regrid, a diagnostic, the end), at most
+// kRoundSteps.  Fewer, longer rounds leave less of a solve's time to the lane's per-round host work
+// and read-back; the events still fall on the program's steps.
+constexpr long long kRoundSteps = 8;
+long long round_steps(const Job* j) {
+    const long long cap = std::max(j->sstep, (kRoundSteps / j->sstep) * j->sstep);
+    long long e = j->step;
+    do {
+        e += j->sstep;
+    } while (e - j->step < cap && e < j->steps && !(j->dynamic && e % j->adapt == 0) && e % j->diagK != 0);
+    return e - j->step;
+}
+
 // One round of a lane: the events of each solve's current step (a regrid sends the solve to a
 // worker, its stream ordered after the lane's work so far, and a diagnostic of the same step goes
 // with it; a diagnostic alone is launched on the lane's stream into this round's read-back slot; a
 // solve with a diagnostic in flight waits a round before a regrid, so its samples are recorded in
-// order), the batched coarse steps of the solves that move (sstep of them: two with graph replay, as
-// the program steps), the previous round's read-backs, and the retirement of solves that are over.
+// order), the batched coarse steps of the solves that move (each up to its next event, round_steps:
+// the program's steps, two at a time with graph replay), the previous round's read-backs, and the
+// retirement of solves that are over.
 // Returns whether anything was launched or read back.
 bool lane_round(jp_server* sv, jp_server::Lane& L) {
     bool busy = false;
@@ -536,20 +551,22 @@ bool lane_round(jp_server* sv, jp_server::Lane& L) {
             fail_all(JP_ERR_CUDA);
         for (auto& g : groups) {
             jp_status st = JP_OK;
-            for (long long t = 0; t < 2 && st == JP_OK; ++t) {
+            std::vector<long long> ks(g.size());
+            long long kmax = 0;
+            for (size_t i = 0; i < g.size(); ++i) kmax = std::max(kmax, ks[i] = round_steps(g[i]));
+            for (long long t = 0; t < kmax && st == JP_OK; ++t) {
                 std::vector<jp_solver*> ms;
-                for (Job* j : g)
-                    if (j->sstep > t) ms.push_back(j->s);
-                if (ms.empty()) break;
+                for (size_t i = 0; i < g.size(); ++i)
+                    if (ks[i] > t) ms.push_back(g[i]->s);
                 // a group of one with graph replay replays its captured step instead (one launch)
                 const bool alone = ms.size() == 1 && (ms[0]->cfg.flags & JP_FLAG_GRAPH);
                 st = alone ? amr_graph_step_on(ms[0], L.stream) : amr_batch_step(ms, L.stream, &L.fk);
                 moved += (long long)ms.size();
             }
-            for (Job* j : g) {
-                if (st != JP_OK) j->error = st;
-                j->step += j->sstep;
-                j->events_done = false;
+            for (size_t i = 0; i < g.size(); ++i) {
+                if (st != JP_OK) g[i]->error = st;
+                g[i]->step += ks[i];
+                g[i]->events_done = false;
             }
         }
         span_close(L.span, L.span_tick, L.stream);
@@ -561,7 +578,7 @@ bool lane_round(jp_server* sv, jp_server::Lane& L) {
     auto& prev = L.adiag[L.diag_cur ^ 1];
     if (!prev.entries.empty()) {
         const auto tw = clk::now();
-        const cudaError_t e = cudaEventSynchronize(prev.done);
+        const cudaError_t e = wait_event(prev.done);
         for (auto& en : prev.entries) {
             if (e == cudaSuccess) record(en.first, en.first->s->diag_host + 3 * (L.diag_cur ^ 1), en.second);
             else if (en.first->error == JP_OK) en.first->error = fail(JP_ERR_CUDA, "diagnostics");
@@ -927,7 +944,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
     auto& prev = sv->diag[sv->diag_cur ^ 1];
     if (!prev.entries.empty()) {
         const auto tw = clk::now();
-        ECK(cudaEventSynchronize(prev.done), "diag");
+        ECK(wait_event(prev.done), "diag");
         for (size_t k = 0; k < prev.entries.size(); ++k) {
             record(prev.entries[k].first, prev.host + 3 * k, prev.entries[k].second);
             --prev.entries[k].first->inflight;

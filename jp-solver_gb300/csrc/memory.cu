@@ -38,9 +38,16 @@ cudaError_t wait_stream(jp_solver* s) {
     }
     cudaError_t e = cudaEventRecord(s->ev_wait, s->stream);
     if (e != cudaSuccess) return e;
+    return wait_event(s->ev_wait);
+}
+
+// The server's threads (tick, lanes, workers) outnumber the host cores; a spinning
+// cudaEventSynchronize in each would keep them all runnable.  This wait polls, yielding the core for
+// the first 200 us and sleeping between polls after that.
+cudaError_t wait_event(cudaEvent_t ev) {
     const auto t0 = std::chrono::steady_clock::now();
     for (;;) {
-        e = cudaEventQuery(s->ev_wait);
+        const cudaError_t e = cudaEventQuery(ev);
         if (e != cudaErrorNotReady) return e;
         if (std::chrono::steady_clock::now() - t0 < std::chrono::microseconds(200)) {
             std::this_thread::yield();

@@ -33,6 +33,8 @@ jp_status create_solver(const jp_config* cfg, cudaMemPool_t pool, jp_solver** ou
 // then sleeping in short slices, so that many solves waiting at once leave the host cores to the
 // threads that issue work; otherwise cudaStreamSynchronize.
 cudaError_t wait_stream(jp_solver* s);
+// wait for an event without spinning on a core (yield, then sleep between polls)
+cudaError_t wait_event(cudaEvent_t ev);
 double stored_to_double(int storage, const void* base, size_t idx, int q);
 void double_to_stored(int storage, void* base, size_t idx, int q, double v);
 }  // namespace jp

@@ -11,6 +11,7 @@
 // on both sides: 152 B per lattice update in FP32, 76 B in FP16/BF16, 304 B in FP64.
 #include "kernels.h"
 #include "lattice.cuh"
+#include "diag_terms.cuh"
 #include "uniform_common.cuh"
 
 #include <atomic>
@@ -322,9 +323,10 @@ cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStr
 }
 
 // ---- energy / enstrophy / mass ---------------------------------------------------------------------
-// Per cell: 1/2|u|^2, 1/2|curl u|^2 with central differences (periodic), rho; all in FP64.  Each
-// thread walks a fixed grid-stride sequence of cells, blocks reduce in a fixed tree, and one block
-// sums the block partials in a fixed order, so the result is the same on every run.
+// Per cell: 1/2|u|^2, 1/2|curl u|^2 with central differences (periodic), rho; a float field's terms
+// in double-float (diag_terms.cuh), an FP64 field's in FP64; sums in FP64.  Each thread walks a fixed
+// grid-stride sequence of cells, blocks reduce in a fixed tree, and one block sums the block partials
+// in a fixed order, so the result is the same on every run.
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -337,28 +339,39 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_field(const FT* __restric
                                                              double* __restrict__ partials) {
     const long long cells = (long long)n * n * n;
     double e = 0.0, ens = 0.0, mass = 0.0;
-    for (long long c = (long long)blockIdx.x * kDiagThreads + threadIdx.x; c < cells;
-         c += (long long)gridDim.x * kDiagThreads) {
-        const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
-        const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
-        const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
-        const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
-        auto at = [&](int a, int b, int cc, int comp) -> FT {
-            return F[(((size_t)cc * n + b) * n + a) * 4 + comp];
-        };
-        auto dif = [&](FT a, FT b) -> double {
-            if (FLOAT_DIFF) return double(FT(a - b)) * 0.5;
-            return (double(a) - double(b)) * 0.5;
-        };
-        const double rho = double(F[c * 4 + 0]);
-        const double u = double(F[c * 4 + 1]), v = double(F[c * 4 + 2]), w = double(F[c * 4 + 3]);
-        const double dudy = dif(at(i, jp, k, 1), at(i, jm, k, 1)), dudz = dif(at(i, j, kp, 1), at(i, j, km, 1));
-        const double dvdx = dif(at(ip, j, k, 2), at(im, j, k, 2)), dvdz = dif(at(i, j, kp, 2), at(i, j, km, 2));
-        const double dwdx = dif(at(ip, j, k, 3), at(im, j, k, 3)), dwdy = dif(at(i, jp, k, 3), at(i, jm, k, 3));
-        const double ox = dwdy - dvdz, oy = dudz - dwdx, oz = dvdx - dudy;
-        e += 0.5 * (u * u + v * v + w * w);
-        ens += 0.5 * (ox * ox + oy * oy + oz * oz);
-        mass += rho;
+    if constexpr (sizeof(FT) == 4) {  // float fields: per-cell terms in double-float (diag_terms.cuh)
+        dterm::Acc acc;
+        for (long long c = (long long)blockIdx.x * kDiagThreads + threadIdx.x; c < cells;
+             c += (long long)gridDim.x * kDiagThreads) {
+            dterm::FF ce, cens;
+            float rho;
+            dterm::cell_terms<FLOAT_DIFF>(F, n, c, ce, cens, rho);
+            acc.add_cell(ce, cens, rho);
+        }
+        acc.flush();
+        e = acc.de;
+        ens = acc.dens;
+        mass = acc.dmass;
+    } else {  // FP64 fields (FP64 storage): per-cell terms in FP64
+        for (long long c = (long long)blockIdx.x * kDiagThreads + threadIdx.x; c < cells;
+             c += (long long)gridDim.x * kDiagThreads) {
+            const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
+            const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
+            const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
+            const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
+            auto at = [&](int a, int b, int cc, int comp) -> double {
+                return double(F[(((size_t)cc * n + b) * n + a) * 4 + comp]);
+            };
+            const double rho = double(F[c * 4 + 0]);
+            const double u = double(F[c * 4 + 1]), v = double(F[c * 4 + 2]), w = double(F[c * 4 + 3]);
+            const double dudy = (at(i, jp, k, 1) - at(i, jm, k, 1)) * 0.5, dudz = (at(i, j, kp, 1) - at(i, j, km, 1)) * 0.5;
+            const double dvdx = (at(ip, j, k, 2) - at(im, j, k, 2)) * 0.5, dvdz = (at(i, j, kp, 2) - at(i, j, km, 2)) * 0.5;
+            const double dwdx = (at(ip, j, k, 3) - at(im, j, k, 3)) * 0.5, dwdy = (at(i, jp, k, 3) - at(i, jm, k, 3)) * 0.5;
+            const double ox = dwdy - dvdz, oy = dudz - dwdx, oz = dvdx - dudy;
+            e += 0.5 * (u * u + v * v + w * w);
+            ens += 0.5 * (ox * ox + oy * oy + oz * oz);
+            mass += rho;
+        }
     }
     __shared__ double sh[3][kDiagThreads / 32];
     e = warp_sum(e);
