@@ -380,10 +380,6 @@ cudaError_t span_close(jp_server::Span (&ring)[4], int tick, cudaStream_t st) {
     return cudaEventRecord(sp.b, st);
 }
 
-long long next_event(const Job* j) {
-    return std::min(j->steps, (j->step / j->diagK + 1) * j->diagK);
-}
-
 // A worker's part of an AMR solve, on the solve's own stream: creation with the initial build and
 // the diagnostic of step 0 (task 1), or a regrid and, when due at the same step, the diagnostic
 // (task 2).  Everything else happens in the tick's batched launches.
@@ -880,65 +876,82 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         }
         sv->active.push_back(j);
     }
-    // 3. launch the diagnostics due now (uniform) into this tick's slots, with one read-back
+    // 3. the tick's uniform work on the server's stream: up to tick_steps batched steps, and each
+    // diagnostic at the step it belongs to (macro field and reduction of that solve, into its own
+    // slot of this tick's batch), so a solve sampled every step still advances tick_steps steps per
+    // tick.  One read-back of all slots at the end.
     auto& cur = sv->diag[sv->diag_cur];
     cur.entries.clear();
+    const long long T = sv->cfg.tick_steps;
+    int slots = 0;  // diagnostics this tick can reach: the one due now and those at multiples of diagK
     for (Job* j : sv->active)
-        if (j->error == JP_OK && j->need_diag) cur.entries.push_back({j, j->step});
-    const auto td = clk::now();
-    if (!cur.entries.empty()) {
-        if ((int)cur.entries.size() > cur.cap) {  // these slots were read back last tick: free to replace
-            if (cur.dev) cudaFree(cur.dev);
-            if (cur.host) cudaFreeHost(cur.host);
-            cur.dev = nullptr;
-            cur.host = nullptr;
-            cur.cap = std::max<int>(2 * (int)cur.entries.size(), 64);
-            ECK(cudaMalloc(&cur.dev, sizeof(double) * 3 * cur.cap), "cudaMalloc diag slots");
-            ECK(cudaMallocHost(&cur.host, sizeof(double) * 3 * cur.cap), "cudaMallocHost diag slots");
+        if (j->error == JP_OK) {
+            const long long last = std::min(j->steps, j->step + T);
+            slots += (j->need_diag ? 1 : 0) + int(last / j->diagK - j->step / j->diagK);
         }
-        if (!cur.done) ECK(cudaEventCreateWithFlags(&cur.done, cudaEventDisableTiming), "diag event");
-        for (size_t k = 0; k < cur.entries.size(); ++k) {
-            Job* j = cur.entries[k].first;
+    if (slots > cur.cap) {  // these slots were read back last tick: free to replace
+        if (cur.dev) cudaFree(cur.dev);
+        if (cur.host) cudaFreeHost(cur.host);
+        cur.dev = nullptr;
+        cur.host = nullptr;
+        cur.cap = std::max(2 * slots, 64);
+        ECK(cudaMalloc(&cur.dev, sizeof(double) * 3 * cur.cap), "cudaMalloc diag slots");
+        ECK(cudaMallocHost(&cur.host, sizeof(double) * 3 * cur.cap), "cudaMallocHost diag slots");
+    }
+    if (!cur.done) ECK(cudaEventCreateWithFlags(&cur.done, cudaEventDisableTiming), "diag event");
+    double diag_host_s = 0.0;
+    auto launch_diags = [&]() -> jp_status {  // the diagnostics due at the solves' current steps
+        const auto td = clk::now();
+        for (Job* j : sv->active) {
+            if (j->error != JP_OK || !j->need_diag) continue;
+            if ((int)cur.entries.size() >= cur.cap) return fail(JP_ERR_CAPACITY, "diagnostic slots exhausted");
             jp_solver* s = j->s;
             const bool dbl = s->storage == JP_FP64;
+            double* slot = cur.dev + 3 * cur.entries.size();
             ECK(launch_macro(s->storage, s->fa, s->field, s->n, sv->stream, s->aa_layout()), "macro");
-            ECK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, cur.dev + 3 * k, sv->stream), "diag");
+            ECK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, slot, sv->stream), "diag");
+            cur.entries.push_back({j, j->step});
             j->need_diag = false;
             ++j->inflight;
         }
+        diag_host_s += seconds_since(td);
+        return JP_OK;
+    };
+    std::vector<Job*> moving;
+    std::vector<jp_solver*> members;
+    const auto tsb = clk::now();
+    bool spanned = false;
+    for (long long t = 0;; ++t) {
+        const jp_status dst = launch_diags();
+        if (dst != JP_OK) return dst;
+        if (t == T) break;
+        moving.clear();
+        members.clear();
+        for (Job* j : sv->active)
+            if (j->error == JP_OK && j->step < j->steps) {
+                moving.push_back(j);
+                members.push_back(j->s);
+            }
+        if (members.empty()) break;
+        if (!spanned) {
+            ECK(span_open(sv, sv->uspan, sv->uspan_tick, &jp_server_stats::uniform_gpu_s, sv->stream), "span");
+            spanned = true;
+        }
+        jp_status st = batched_step(members, sv->stream);
+        if (st != JP_OK) return st;
+        for (Job* j : moving)
+            if (++j->step % j->diagK == 0) j->need_diag = true;  // launched before the next step
+    }
+    if (spanned) {
+        ECK(span_close(sv->uspan, sv->uspan_tick, sv->stream), "span");
+        ++sv->uspan_tick;
+        sv->add(&jp_server_stats::step_s, seconds_since(tsb) - diag_host_s);
+    }
+    if (!cur.entries.empty()) {
         ECK(cudaMemcpyAsync(cur.host, cur.dev, sizeof(double) * 3 * cur.entries.size(), cudaMemcpyDeviceToHost,
                             sv->stream), "diag D2H");
         ECK(cudaEventRecord(cur.done, sv->stream), "diag event");
-        sv->add(&jp_server_stats::diag_s, seconds_since(td), &jp_server_stats::diags, (int64_t)cur.entries.size());
-    }
-    // 4. advance the uniform solves in batched launches (behind this tick's diagnostics)
-    std::vector<std::pair<Job*, long long>> uni;
-    long long kmax = 0;
-    for (Job* j : sv->active) {
-        if (j->error != JP_OK) continue;
-        const long long k = std::min(next_event(j) - j->step, (long long)sv->cfg.tick_steps);
-        if (k <= 0) continue;
-        uni.push_back({j, k});
-        kmax = std::max(kmax, k);
-    }
-    std::vector<jp_solver*> members;
-    const auto tsb = clk::now();
-    if (kmax) ECK(span_open(sv, sv->uspan, sv->uspan_tick, &jp_server_stats::uniform_gpu_s, sv->stream), "span");
-    for (long long t = 0; t < kmax; ++t) {
-        members.clear();
-        for (auto& p : uni)
-            if (p.second > t) members.push_back(p.first->s);
-        jp_status st = batched_step(members, sv->stream);
-        if (st != JP_OK) return st;
-    }
-    if (kmax) {
-        ECK(span_close(sv->uspan, sv->uspan_tick, sv->stream), "span");
-        ++sv->uspan_tick;
-    }
-    if (kmax) sv->add(&jp_server_stats::step_s, seconds_since(tsb));
-    for (auto& p : uni) {
-        p.first->step += p.second;
-        if (p.first->step % p.first->diagK == 0) p.first->need_diag = true;  // at the new step, next tick
+        sv->add(&jp_server_stats::diag_s, diag_host_s, &jp_server_stats::diags, (int64_t)cur.entries.size());
     }
     // 5. the previous tick's diagnostics (the GPU meanwhile works on this tick's launches)
     auto& prev = sv->diag[sv->diag_cur ^ 1];
@@ -972,7 +985,7 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         }
     }
     // 6. nothing launched here while AMR solves run in their lanes: wait briefly for one to end
-    if (uni.empty() && sv->amr_live > 0) {
+    if (!spanned && sv->amr_live > 0) {
         std::unique_lock<std::mutex> lk(sv->mu);
         sv->cv_fin.wait_for(lk, std::chrono::milliseconds(1), [sv] { return !sv->amr_fin.empty(); });
     }
