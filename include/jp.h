@@ -149,7 +149,8 @@ jp_status jp_step(jp_solver* s, int64_t nsteps);
 jp_status jp_sync(jp_solver* s);
 
 /* Mean kinetic energy 1/2|u|^2, mean enstrophy 1/2|omega|^2 (central differences, periodic) and
- * mean density of the current state, computed on the device in FP64 with a deterministic reduction.
+ * mean density of the current state, computed on the device with a deterministic reduction: per-cell
+ * terms of a float field in double-float (within ~1e-14 relative of FP64), sums in FP64.
  * out[0]=E, out[1]=enstrophy, out[2]=mass.  Replaces k_macro + the host loop of
  * src/tgv3d_uniform.cu:169-189 and k_composite + k_diag_reduce of src/tgv3d_amr.cu:882-888. */
 jp_status jp_diag(jp_solver* s, double out[3]);
@@ -189,7 +190,7 @@ jp_status jp_memory_info(jp_solver* s, int64_t* free_bytes, int64_t* total_bytes
  * start-up, work recorded into a CUDA graph).  `field_dev` holds n^3 float4 (rho, ux, uy, uz) in the
  * order of jp_get_macro; `out_dev` receives 3 doubles (mean E, mean enstrophy, mean rho), written on
  * `stream` (a cudaStream_t; NULL = default stream) without host synchronisation.  float_diff = 1 takes
- * velocity differences in float (the uniform solver's jp_diag), 0 in double (the AMR composite).
+ * velocity differences in float (the uniform solver's jp_diag), 0 exactly (the AMR composite).
  * Scratch lives in a fixed 384 KiB device array inside the library, so fields above 268,435,456 cells
  * (n > 645) are rejected with JP_ERR_CAPACITY.  The first call on each device looks up that array's
  * address and should come before any stream capture.  Calls share the array: calls that overlap on
