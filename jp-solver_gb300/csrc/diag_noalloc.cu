@@ -21,6 +21,7 @@
 // capture.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 
 #include "diag_terms.cuh"
@@ -50,6 +51,7 @@ __device__ __forceinline__ double warp_sum(double v) {
 // 1/2|curl u|^2 from central differences with periodic wrap, rho, in double-float
 // (diag_terms.cuh); FP64 accumulation.  float_diff takes each velocity difference in float before
 // halving (the uniform solver's convention).
+template <bool VEC>
 __global__ void __launch_bounds__(kThreads) k_noalloc_partials(const float* __restrict__ F, int n, int float_diff,
                                                               double* __restrict__ partials) {
     const long long cells = (long long)n * n * n;
@@ -59,8 +61,8 @@ __global__ void __launch_bounds__(kThreads) k_noalloc_partials(const float* __re
     for (long long c = begin + threadIdx.x; c < end; c += kThreads) {
         dterm::FF ce, cens;
         float rho;
-        if (float_diff) dterm::cell_terms<true>(F, n, c, ce, cens, rho);
-        else dterm::cell_terms<false>(F, n, c, ce, cens, rho);
+        if (float_diff) dterm::cell_terms<true, VEC>(F, n, c, ce, cens, rho);
+        else dterm::cell_terms<false, VEC>(F, n, c, ce, cens, rho);
         acc.add_cell(ce, cens, rho);
     }
     acc.flush();
@@ -140,7 +142,11 @@ extern "C" jp_status jp_diag_field_noalloc(const float* field_dev, int32_t n, in
     jp_status st = scratch_address(&partials);
     if (st != JP_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    k_noalloc_partials<<<(unsigned)chunks, kThreads, 0, s>>>(field_dev, n, float_diff ? 1 : 0, partials);
+    // a caller's field may start anywhere a float can: 16-byte record loads only where aligned
+    if (reinterpret_cast<uintptr_t>(field_dev) % 16 == 0)
+        k_noalloc_partials<true><<<(unsigned)chunks, kThreads, 0, s>>>(field_dev, n, float_diff ? 1 : 0, partials);
+    else
+        k_noalloc_partials<false><<<(unsigned)chunks, kThreads, 0, s>>>(field_dev, n, float_diff ? 1 : 0, partials);
     k_noalloc_finish<<<1, kThreads, 0, s>>>(partials, (int)chunks, 1.0 / double(cells), out_dev);
     note_launch(2);
     cudaError_t e = cudaGetLastError();

@@ -71,25 +71,33 @@ __device__ __forceinline__ double to_double(FF x) { return double(x.hi) + double
 
 // 1/2|u|^2, 1/2|curl u|^2 and rho of cell c (i fastest) of an n^3 field F[cell][4].  FLOAT_DIFF takes
 // each velocity difference in float (rounded) before halving, as the uniform program's host loop
-// does; otherwise the difference of the two floats is exact, as in the AMR diagnostic kernel.
-template <bool FLOAT_DIFF>
+// does; otherwise the difference of the two floats is exact, as in the AMR diagnostic kernel.  VEC
+// reads each cell record (rho, ux, uy, uz) with one 16-byte load (F 16-byte aligned), else per float.
+template <bool FLOAT_DIFF, bool VEC>
 __device__ __forceinline__ void cell_terms(const float* __restrict__ F, int n, long long c, FF& e, FF& ens,
                                            float& rho) {
     const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
     const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
     const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
     const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
-    auto at = [&](int a, int b, int cc, int comp) { return F[(((size_t)cc * n + b) * n + a) * 4 + comp]; };
+    auto rec = [&](int a, int b, int cc) -> float4 {
+        const float* p = F + (((size_t)cc * n + b) * n + a) * 4;
+        if (VEC) return __ldg(reinterpret_cast<const float4*>(p));
+        return make_float4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
+    };
     auto dif = [&](float a, float b) -> FF {
         if (FLOAT_DIFF) return {__fmul_rn(__fsub_rn(a, b), 0.5f), 0.f};
         return half(two_sum(a, -b));
     };
-    rho = F[c * 4 + 0];
-    const float u = F[c * 4 + 1], v = F[c * 4 + 2], w = F[c * 4 + 3];
+    const float4 me = rec(i, j, k);
+    const float4 xp = rec(ip, j, k), xm = rec(im, j, k), yp = rec(i, jp, k), ym = rec(i, jm, k);
+    const float4 zp = rec(i, j, kp), zm = rec(i, j, km);
+    rho = me.x;
+    const float u = me.y, v = me.z, w = me.w;
     e = half(add_same_sign(add_same_sign(two_prod(u, u), two_prod(v, v)), two_prod(w, w)));
-    const FF dudy = dif(at(i, jp, k, 1), at(i, jm, k, 1)), dudz = dif(at(i, j, kp, 1), at(i, j, km, 1));
-    const FF dvdx = dif(at(ip, j, k, 2), at(im, j, k, 2)), dvdz = dif(at(i, j, kp, 2), at(i, j, km, 2));
-    const FF dwdx = dif(at(ip, j, k, 3), at(im, j, k, 3)), dwdy = dif(at(i, jp, k, 3), at(i, jm, k, 3));
+    const FF dudy = dif(yp.y, ym.y), dudz = dif(zp.y, zm.y);
+    const FF dvdx = dif(xp.z, xm.z), dvdz = dif(zp.z, zm.z);
+    const FF dwdx = dif(xp.w, xm.w), dwdy = dif(yp.w, ym.w);
     FF ox, oy, oz;
     if (FLOAT_DIFF) {  // differences of single floats: exact
         ox = two_sum(dwdy.hi, -dvdz.hi);

@@ -58,8 +58,9 @@ cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStr
 
 // Energy, enstrophy, mass of a macro field, reduced deterministically to out_dev[3] (device).
 // partials_dev holds kDiagBlocks*3 doubles.  float_diff=true takes the velocity differences in
-// float before widening (the uniform host loop, src/tgv3d_uniform.cu:103-105); false in double
-// (k_diag_reduce, src/tgv3d_amr.cu:542-546).
+// float before widening (the uniform host loop, src/tgv3d_uniform.cu:103-105); false exactly
+// (k_diag_reduce, src/tgv3d_amr.cu:542-546).  A float field is read in 16-byte cell records and must
+// be 16-byte aligned (every solver's own field is).
 constexpr int kDiagBlocks = 1216;   // 152 SMs x 8
 constexpr int kDiagThreads = 256;
 cudaError_t launch_diag_field(bool field_is_double, bool float_diff, const void* field, int n,

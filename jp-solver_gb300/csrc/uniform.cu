@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_field(const FT* __restric
              c += (long long)gridDim.x * kDiagThreads) {
             dterm::FF ce, cens;
             float rho;
-            dterm::cell_terms<FLOAT_DIFF>(F, n, c, ce, cens, rho);
+            dterm::cell_terms<FLOAT_DIFF, true>(F, n, c, ce, cens, rho);  // fields from cudaMalloc
             acc.add_cell(ce, cens, rho);
         }
         acc.flush();

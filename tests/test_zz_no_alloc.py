@@ -45,3 +45,53 @@ def test_noalloc_diag_rejects_field_beyond_scratch():
     assert call(field, 646, 1, out) == 3                   # JP_ERR_CAPACITY, checked before any launch
     assert b"645" in J.lib().jp_last_error()
     torch.cuda.synchronize()
+
+
+def fp64_diag(F, n, float_diff):
+    """The reference's per-cell arithmetic in FP64 (numpy): 1/2|u|^2, 1/2|curl u|^2 with central
+    differences (periodic), rho; float_diff rounds each velocity difference to float first."""
+    G = F.reshape(n, n, n, 4)                                   # [k][j][i][comp]
+
+    def dif(comp, axis):                                        # (f(x+1) - f(x-1)) / 2 along axis
+        a, b = np.roll(G[..., comp], -1, axis), np.roll(G[..., comp], 1, axis)
+        if float_diff:
+            return (a - b).astype(np.float64) * 0.5             # float32 subtraction, then widened
+        return (a.astype(np.float64) - b.astype(np.float64)) * 0.5
+
+    u, v, w = (G[..., c].astype(np.float64) for c in (1, 2, 3))
+    ox = dif(3, 1) - dif(2, 0)                                  # dw/dy - dv/dz
+    oy = dif(1, 0) - dif(3, 2)                                  # du/dz - dw/dx
+    oz = dif(2, 2) - dif(1, 1)                                  # dv/dx - du/dy
+    cells = float(n) ** 3
+    return (float(np.sum(0.5 * (u * u + v * v + w * w))) / cells,
+            float(np.sum(0.5 * (ox * ox + oy * oy + oz * oz))) / cells,
+            float(np.sum(G[..., 0].astype(np.float64))) / cells)
+
+
+def adversarial_field(kind, n, rng):
+    F = np.empty((n ** 3, 4), dtype=np.float32)
+    F[:, 0] = 1.0 + 0.01 * rng.standard_normal(n ** 3)
+    if kind == "wide":          # signs mixed, magnitudes over six decades from cell to cell
+        F[:, 1:] = rng.uniform(-1, 1, (n ** 3, 3)) * 10.0 ** rng.uniform(-6, 0, (n ** 3, 3))
+    elif kind == "cancel":      # nearly equal neighbours: differences lose most leading bits
+        F[:, 1:] = 0.7 + 1e-6 * rng.standard_normal((n ** 3, 3))
+    else:                       # large and small blocks of cells side by side
+        F[:, 1:] = np.where(rng.random((n ** 3, 1)) < 0.5, 1e3, 1e-3) * rng.standard_normal((n ** 3, 3))
+    return F.reshape(-1)
+
+
+@pytest.mark.parametrize("kind", ["wide", "cancel", "mixed"])
+@pytest.mark.parametrize("float_diff", [1, 0])
+def test_double_float_terms_match_fp64_on_adversarial_fields(kind, float_diff):
+    # the per-cell terms are carried in double-float (error-free products and sums), the sums in
+    # FP64: within 1e-13 relative of the FP64 computation on fields chosen to stress it
+    n = 24
+    F = adversarial_field(kind, n, np.random.default_rng(5))
+    field = torch.from_numpy(F.copy()).cuda()
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    assert call(field, n, float_diff, out) == 0, J.lib().jp_last_error().decode()
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    want = fp64_diag(F, n, float_diff)
+    for g, w in zip(got, want):
+        assert abs(g - w) <= 1e-13 * abs(w), (kind, float_diff, g, w)
