@@ -58,11 +58,12 @@ __global__ void __launch_bounds__(kThreads) k_noalloc_partials(const float* __re
     const long long begin = (long long)blockIdx.x * kChunk;
     const long long end = begin + kChunk < cells ? begin + kChunk : cells;
     dterm::Acc acc;
-    for (long long c = begin + threadIdx.x; c < end; c += kThreads) {
+    dterm::CellWalk w(begin + threadIdx.x, kThreads, n);
+    for (long long c = begin + threadIdx.x; c < end; c += kThreads, w.next()) {
         dterm::FF ce, cens;
         float rho;
-        if (float_diff) dterm::cell_terms<true, VEC>(F, n, c, ce, cens, rho);
-        else dterm::cell_terms<false, VEC>(F, n, c, ce, cens, rho);
+        if (float_diff) dterm::cell_terms<true, VEC>(F, n, w.i, w.j, w.k, ce, cens, rho);
+        else dterm::cell_terms<false, VEC>(F, n, w.i, w.j, w.k, ce, cens, rho);
         acc.add_cell(ce, cens, rho);
     }
     acc.flush();

@@ -74,9 +74,8 @@ __device__ __forceinline__ double to_double(FF x) { return double(x.hi) + double
 // does; otherwise the difference of the two floats is exact, as in the AMR diagnostic kernel.  VEC
 // reads each cell record (rho, ux, uy, uz) with one 16-byte load (F 16-byte aligned), else per float.
 template <bool FLOAT_DIFF, bool VEC>
-__device__ __forceinline__ void cell_terms(const float* __restrict__ F, int n, long long c, FF& e, FF& ens,
+__device__ __forceinline__ void cell_terms(const float* __restrict__ F, int n, int i, int j, int k, FF& e, FF& ens,
                                            float& rho) {
-    const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
     const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
     const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
     const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
@@ -110,6 +109,36 @@ __device__ __forceinline__ void cell_terms(const float* __restrict__ F, int n, l
     }
     ens = half(add_same_sign(add_same_sign(sq(ox), sq(oy)), sq(oz)));
 }
+
+// The cells c0, c0 + S, c0 + 2S, ... of an n^3 grid (i fastest) as (i, j, k), advanced by adding the
+// stride's own (i, j, k) with carries: no division per cell (a 64-bit division by a runtime n is a
+// long instruction sequence).  Valid while k < n.
+struct CellWalk {
+    int i, j, k, si, sj, sk, n;
+    __device__ __forceinline__ CellWalk(long long c0, long long S, int n_) : n(n_) {
+        const long long plane = (long long)n * n;
+        k = int(c0 / plane);
+        j = int((c0 - (long long)k * plane) / n);
+        i = int(c0 - (long long)k * plane - (long long)j * n);
+        sk = int(S / plane);
+        sj = int((S - (long long)sk * plane) / n);
+        si = int(S - (long long)sk * plane - (long long)sj * n);
+    }
+    __device__ __forceinline__ bool valid() const { return k < n; }
+    __device__ __forceinline__ void next() {
+        i += si;
+        if (i >= n) {
+            i -= n;
+            ++j;
+        }
+        j += sj;
+        if (j >= n) {
+            j -= n;
+            ++k;
+        }
+        k += sk;
+    }
+};
 
 // A thread's sums: double-float over kFlush cells, then into FP64.
 struct Acc {

@@ -341,11 +341,11 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_field(const FT* __restric
     double e = 0.0, ens = 0.0, mass = 0.0;
     if constexpr (sizeof(FT) == 4) {  // float fields: per-cell terms in double-float (diag_terms.cuh)
         dterm::Acc acc;
-        for (long long c = (long long)blockIdx.x * kDiagThreads + threadIdx.x; c < cells;
-             c += (long long)gridDim.x * kDiagThreads) {
+        for (dterm::CellWalk w((long long)blockIdx.x * kDiagThreads + threadIdx.x, (long long)gridDim.x * kDiagThreads, n);
+             w.valid(); w.next()) {
             dterm::FF ce, cens;
             float rho;
-            dterm::cell_terms<FLOAT_DIFF, true>(F, n, c, ce, cens, rho);  // fields from cudaMalloc
+            dterm::cell_terms<FLOAT_DIFF, true>(F, n, w.i, w.j, w.k, ce, cens, rho);  // fields from cudaMalloc
             acc.add_cell(ce, cens, rho);
         }
         acc.flush();
