@@ -798,7 +798,17 @@ __global__ void __launch_bounds__(256) k_composite(const typename ST::raw* __res
     const long long NN = (long long)N2 * N2 * N2;
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= NN) return;
-    const int gi = int(idx % N2), gj = int((idx / N2) % N2), gk = int(idx / ((long long)N2 * N2));
+    int gi, gj, gk;
+    if (NN <= 0xffffffffLL) {  // 32-bit division: a 64-bit one by a runtime N2 is a long sequence
+        const unsigned u = unsigned(idx), n2 = unsigned(N2);
+        gi = int(u % n2);
+        gj = int((u / n2) % n2);
+        gk = int(u / (n2 * n2));
+    } else {
+        gi = int(idx % N2);
+        gj = int((idx / N2) % N2);
+        gk = int(idx / ((long long)N2 * N2));
+    }
     const int lb = l1grid[((gk / (2 * MB)) * l1gx + gj / (2 * MB)) * l1gx + gi / (2 * MB)];
     const typename ST::raw* src;
     size_t blk;
