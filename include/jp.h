@@ -170,6 +170,18 @@ jp_status jp_get_populations(jp_solver* s, int32_t level, int32_t layout, int32_
 jp_status jp_set_populations(jp_solver* s, int32_t level, int32_t layout, int32_t dtype,
                              const void* host, int64_t count);
 
+/* Upload the populations for the solver's next step while the work already queued runs: the copy
+ * goes on a copy stream into a second state buffer (allocated by the first call, counted in
+ * bytes_state), and the next jp_step (or ensemble step) waits for it on the device and takes it as
+ * the state before its first step.  Calls in between (jp_diag, jp_get_populations, ...) still see the
+ * current state, so a caller can stage call i+1's input right after call i's jp_step and overlap the
+ * upload with those steps and their diagnostics.  Uniform solvers without JP_FLAG_INPLACE, flat
+ * layout in the storage's own type (JP_F32 for FP32, JP_F64 for FP64; else JP_ERR_UNSUPPORTED).
+ * `host` (pinned, for an asynchronous copy) must stay valid and unchanged until the step that takes
+ * it has been synchronised (jp_sync, jp_diag).  JP_ERR_STATE if populations are already staged.  No
+ * reference counterpart: the reference uploads nothing after its initial state. */
+jp_status jp_stage_populations(jp_solver* s, int32_t layout, int32_t dtype, const void* host, int64_t count);
+
 /* Macroscopic field of the current uniform state: `host` receives n^3 float4 (rho, ux, uy, uz) in
  * the linear order (z*n+y)*n+x, as k_macro writes it (src/tgv3d_uniform.cu:80-90). */
 jp_status jp_get_macro(jp_solver* s, float* host, int64_t count);

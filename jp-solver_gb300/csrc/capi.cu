@@ -236,6 +236,13 @@ jp_status jp_set_populations(jp_solver* s, int32_t level, int32_t layout, int32_
     return amr_set_populations(s, level, layout, dtype, host, count);
 }
 
+jp_status jp_stage_populations(jp_solver* s, int32_t layout, int32_t dtype, const void* host, int64_t count) {
+    if (!s || !host) return fail(JP_ERR_INVALID, "null argument");
+    if (s->kind != JP_UNIFORM) return fail(JP_ERR_UNSUPPORTED, "jp_stage_populations: uniform solvers only");
+    cudaSetDevice(s->device);
+    return uniform_stage_populations(s, layout, dtype, host, count);
+}
+
 jp_status jp_get_macro(jp_solver* s, float* host, int64_t count) {
     if (!s || !host) return fail(JP_ERR_INVALID, "null argument");
     if (s->kind != JP_UNIFORM) return fail(JP_ERR_UNSUPPORTED, "jp_get_macro: uniform solvers only");

@@ -137,6 +137,10 @@ jp_status jp_ensemble_step(jp_ensemble* e, int64_t nsteps) {
     if (nsteps < 0) return fail(JP_ERR_INVALID, "negative step count");
     ECK(cudaSetDevice(e->device), "cudaSetDevice");
     for (jp_solver* m : e->members) {  // after each member's pending work
+        if (m->kind == JP_UNIFORM && nsteps > 0) {  // populations staged for the next step
+            const jp_status taken = uniform_take_staged(m);
+            if (taken != JP_OK) return taken;
+        }
         ECK(cudaEventRecord(m->ev1, m->stream), "event");
         ECK(cudaStreamWaitEvent(e->stream, m->ev1, 0), "wait");
     }

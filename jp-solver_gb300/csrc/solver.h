@@ -65,6 +65,13 @@ struct jp_solver {
     double* diag_host = nullptr; // 3 doubles, pinned
     int vec = 0, tpb = 0;
     float* outbuf = nullptr;   // device Q / speed / velocity for output frames, allocated on first use
+    // populations staged for the next step (jp_stage_populations): uploaded into `staging` on
+    // copy_stream while the solver's stream works, swapped in as fa by the next step
+    void* staging = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_staged = nullptr;        // the upload has landed
+    cudaEvent_t ev_staging_free = nullptr;  // the work that used the buffer before it was swapped out is done
+    bool staged = false;
 
     jp::AmrState* amr = nullptr;
 
@@ -78,6 +85,10 @@ jp_status uniform_create(jp_solver* s);
 void uniform_free(jp_solver* s);
 jp_status uniform_init(jp_solver* s);
 jp_status uniform_step(jp_solver* s, int64_t nsteps);
+// upload populations for the next step on the copy stream (jp_stage_populations)
+jp_status uniform_stage_populations(jp_solver* s, int layout, int dtype, const void* host, int64_t count);
+// take staged populations as the state (the next step's first action); no-op when none are staged
+jp_status uniform_take_staged(jp_solver* s);
 jp_status uniform_diag(jp_solver* s, double out[3]);
 jp_status uniform_get_populations(jp_solver* s, int level, int layout, int dtype, void* host, int64_t count);
 jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype, const void* host, int64_t count);

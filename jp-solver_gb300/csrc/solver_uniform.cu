@@ -107,6 +107,15 @@ jp_status uniform_create(jp_solver* s) {
 }
 
 void uniform_free(jp_solver* s) {
+    if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);  // an upload in flight ends first
+    dev_free(s, s->staging);
+    if (s->ev_staged) cudaEventDestroy(s->ev_staged);
+    if (s->ev_staging_free) cudaEventDestroy(s->ev_staging_free);
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    s->staging = nullptr;
+    s->ev_staged = s->ev_staging_free = nullptr;
+    s->copy_stream = nullptr;
+    s->staged = false;
     dev_free(s, s->fa);
     dev_free(s, s->fb);
     dev_free(s, s->field);
@@ -138,7 +147,48 @@ jp_status uniform_init(jp_solver* s) {
     return JP_OK;
 }
 
+// The state for the next step, uploaded while the solver's stream still works on the current one.
+// The copy runs on copy_stream into a second state buffer; the next step waits for it on the device
+// and swaps the buffers, and the buffer swapped out takes the upload after that, once the work queued
+// before the swap (which may still read or write it) is done.  An uploading call overlaps the
+// previous call's steps: at N=512 FP32 the 10.2 GB upload (~49 ms at the box's ~210 GB/s) hides
+// behind 81 steps (~240 ms).
+jp_status uniform_stage_populations(jp_solver* s, int layout, int dtype, const void* host, int64_t count) {
+    if (s->inplace) return fail(JP_ERR_UNSUPPORTED, "jp_stage_populations: not for in-place solvers");
+    if (count != (int64_t)Q * s->cells) return fail(JP_ERR_INVALID, "count %lld != 19*n^3", (long long)count);
+    const bool native = layout == JP_LAYOUT_FLAT &&
+                        ((dtype == JP_F32 && s->storage == JP_FP32) || (dtype == JP_F64 && s->storage == JP_FP64));
+    if (!native)
+        return fail(JP_ERR_UNSUPPORTED, "jp_stage_populations: flat layout in the storage's own type (FP32 or FP64)");
+    if (s->staged) return fail(JP_ERR_STATE, "jp_stage_populations: populations are already staged for the next step");
+    const size_t bytes = (size_t)count * s->elem;
+    if (!s->staging) {
+        JP_CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking), "copy stream");
+        JP_CK(cudaEventCreateWithFlags(&s->ev_staged, cudaEventDisableTiming), "cudaEventCreate");
+        JP_CK(cudaEventCreateWithFlags(&s->ev_staging_free, cudaEventDisableTiming), "cudaEventCreate");
+        JP_CK(dev_alloc(s, &s->staging, bytes), "cudaMalloc staging populations");
+        JP_CK(cudaEventRecord(s->ev_staging_free, s->stream), "cudaEventRecord");  // after a pooled allocation
+        s->info.bytes_state += (int64_t)bytes;
+    }
+    JP_CK(cudaStreamWaitEvent(s->copy_stream, s->ev_staging_free, 0), "cudaStreamWaitEvent");
+    JP_CK(cudaMemcpyAsync(s->staging, host, bytes, cudaMemcpyHostToDevice, s->copy_stream), "staged populations H2D");
+    JP_CK(cudaEventRecord(s->ev_staged, s->copy_stream), "cudaEventRecord");
+    s->staged = true;
+    return JP_OK;
+}
+
+jp_status uniform_take_staged(jp_solver* s) {
+    if (!s->staged) return JP_OK;
+    JP_CK(cudaStreamWaitEvent(s->stream, s->ev_staged, 0), "cudaStreamWaitEvent");
+    std::swap(s->fa, s->staging);
+    JP_CK(cudaEventRecord(s->ev_staging_free, s->stream), "cudaEventRecord");
+    s->staged = false;
+    return JP_OK;
+}
+
 jp_status uniform_step(jp_solver* s, int64_t nsteps) {
+    const jp_status taken = uniform_take_staged(s);
+    if (taken != JP_OK) return taken;
     UniSolve u;
     std::memset(&u, 0, sizeof u);
     u.n = s->n;

@@ -114,6 +114,7 @@ SIGNATURES = {
     "jp_population_count": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
     "jp_get_populations": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]),
     "jp_set_populations": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]),
+    "jp_stage_populations": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64]),
     "jp_get_macro": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
     "jp_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "jp_host_free": (None, [C.c_void_p]),
@@ -270,6 +271,13 @@ class Solver:
         dt = 0 if a.dtype == np.float32 else 1
         _check(lib().jp_set_populations(self.h, level, LAYOUT[layout], dt, a.ctypes.data_as(C.c_void_p), a.size))
         self.sync()
+
+    def stage_populations(self, buf: "PinnedBuffer") -> None:
+        """Upload populations (flat layout, the storage's own type) from pinned memory for the next
+        step, overlapping the work already queued (jp_stage_populations); the next step takes them.
+        `buf` must stay unchanged until that step has been synchronised."""
+        dt = 0 if buf.dtype == np.float32 else 1
+        _check(lib().jp_stage_populations(self.h, LAYOUT["flat"], dt, C.c_void_p(buf.ptr.value), buf.array.size))
 
     # ---- AMR ----
     def regrid(self) -> None:
