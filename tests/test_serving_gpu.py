@@ -133,16 +133,22 @@ def test_server_amr_result_matches_program_loop():
     assert r["energy_ratio"] == Elast / E0
 
 
-def test_server_uniform_result_matches_program_loop():
-    # the `uniform` program's loop: a diagnostic at every step s % diagK == 0 (diagK = steps/240),
-    # then steps to the next one; the served solve reports the same samples and peak, bit for bit
+@pytest.mark.parametrize("diag_every", [0, 3, 7])
+def test_server_uniform_result_matches_program_loop(diag_every):
+    # the `uniform` program's loop: a diagnostic at every step s % diagK == 0 (diagK = steps/240,
+    # here 1: 305 steps), then steps to the next one; the served solve reports the same samples and
+    # peak, bit for bit.  The server interleaves a solve's diagnostics with its batched steps inside
+    # a tick (16 steps here), so intervals of 1, 3 and 7 steps put several samples in one tick, and
+    # 305 steps leave a last interval that no sample follows
     req = dict(rid=21, kind="uniform", n=24, re=300.0, tstar=4.0, storage="fp16")
+    if diag_every:
+        req["diag_every"] = diag_every
     res, _ = run_server([req, dict(R0, rid=22), dict(MIX[0], rid=23)], tick_steps=16)
     r = res[21]
-    cfg = {k: v for k, v in req.items() if k not in ("rid", "kind")}
+    cfg = {k: v for k, v in req.items() if k not in ("rid", "kind", "diag_every")}
     with J.Solver("uniform", **cfg) as s:
         steps, kf = s.info["steps"], s.info["kf"]
-        diagK = max(1, steps // 240)
+        diagK = diag_every or max(1, steps // 240)
         E0, peak, peak_ts, samples, Elast = None, -1.0, -1.0, 0, None
         for step in range(0, steps + 1, diagK):
             E, ens, mass = s.diag()
