@@ -178,8 +178,10 @@ jp_status jp_set_populations(jp_solver* s, int32_t level, int32_t layout, int32_
  * upload with those steps and their diagnostics.  Uniform solvers without JP_FLAG_INPLACE, flat
  * layout in the storage's own type (JP_F32 for FP32, JP_F64 for FP64; else JP_ERR_UNSUPPORTED).
  * `host` (pinned, for an asynchronous copy) must stay valid and unchanged until the step that takes
- * it has been synchronised (jp_sync, jp_diag).  JP_ERR_STATE if populations are already staged.  No
- * reference counterpart: the reference uploads nothing after its initial state. */
+ * it has been synchronised (jp_sync, jp_diag).  JP_ERR_STATE if populations are already staged.
+ * jp_init_tgv, jp_set_populations and jp_load_state set the state explicitly and discard populations
+ * staged before them.  No reference counterpart: the reference uploads nothing after its initial
+ * state. */
 jp_status jp_stage_populations(jp_solver* s, int32_t layout, int32_t dtype, const void* host, int64_t count);
 
 /* Macroscopic field of the current uniform state: `host` receives n^3 float4 (rho, ux, uy, uz) in

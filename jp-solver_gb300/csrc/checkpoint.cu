@@ -110,6 +110,7 @@ jp_status jp_load_state(jp_solver* s, const char* path) {
         }
         JP_CK(cudaStreamSynchronize(s->stream), "load");
         JP_CK(cudaMemcpy(s->fa, raw.data(), bytes, cudaMemcpyHostToDevice), "populations H2D");
+        s->staged = false;  // the loaded state replaces any populations staged before it
     }
     s->step_count = h.step_count;
     s->initialized = true;

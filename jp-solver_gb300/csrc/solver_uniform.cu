@@ -129,6 +129,7 @@ void uniform_free(jp_solver* s) {
 }
 
 jp_status uniform_init(jp_solver* s) {
+    s->staged = false;  // an explicit new state discards populations staged before it
     // the per-axis trigonometry table of the initial state lives in the diagnostic partials buffer
     // (3n <= 3 * kDiagBlocks doubles for n <= kDiagBlocks), which is free between diagnostics
     double* tab = s->partials;
@@ -323,6 +324,7 @@ jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype
     if (count != (int64_t)Q * s->cells) return fail(JP_ERR_INVALID, "count %lld != 19*n^3", (long long)count);
     if (layout != JP_LAYOUT_FLAT && layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_INVALID, "bad layout %d", layout);
     const size_t bytes = (size_t)count * s->elem;
+    s->staged = false;  // an explicit new state discards populations staged before it
     const bool native = layout == JP_LAYOUT_FLAT && !s->inplace &&
                         ((dtype == JP_F32 && s->storage == JP_FP32) || (dtype == JP_F64 && s->storage == JP_FP64));
     if (native) {

@@ -60,6 +60,31 @@ def test_calls_between_stage_and_step_see_the_current_state():
             buf.free()
 
 
+def test_explicit_state_discards_staged_populations():
+    # init_tgv, set_populations and load_state set the state; an upload staged before them is dropped
+    n = 16
+    with J.Solver("uniform", n=n, re=800.0) as s, J.Solver("uniform", n=n, re=800.0) as r:
+        f0 = s.get_populations()
+        g = perturbed(f0, 4)
+        buf = J.PinnedBuffer(f0.size)
+        try:
+            buf.array[:] = perturbed(f0, 5)
+            s.stage_populations(buf)
+            s.set_populations(g)
+            s.step(2)
+            r.set_populations(g)
+            r.step(2)
+            np.testing.assert_array_equal(s.get_populations(), r.get_populations())
+            s.stage_populations(buf)
+            s.init_tgv()
+            s.step(1)
+            r.init_tgv()
+            r.step(1)
+            np.testing.assert_array_equal(s.get_populations(), r.get_populations())
+        finally:
+            buf.free()
+
+
 def test_pipelined_calls_match_sequential_calls():
     # per call: the state comes from the host, k steps, diagnostics; pipelined, call i+1's upload is
     # staged right after call i's steps are queued
