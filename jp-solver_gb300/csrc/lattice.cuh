@@ -29,6 +29,21 @@ __host__ __device__ constexpr int cz(int q) {
     return t[q];
 }
 // opposite direction of q
+// (i, j, k) of cell c of an n^3 grid, i fastest: 32-bit division while the grid has fewer than 2^32
+// cells (a 64-bit division by a runtime n is a long instruction sequence)
+__device__ __forceinline__ void cell_ijk(long long c, int n, int& i, int& j, int& k) {
+    if ((long long)n * n * n <= 0xffffffffLL) {
+        const unsigned u = unsigned(c), un = unsigned(n);
+        i = int(u % un);
+        j = int((u / un) % un);
+        k = int(u / (un * un));
+    } else {
+        i = int(c % n);
+        j = int((c / n) % n);
+        k = int(c / ((long long)n * n));
+    }
+}
+
 __host__ __device__ constexpr int opp(int q) { return q == 0 ? 0 : ((q & 1) ? q + 1 : q - 1); }
 
 // Weights as the reference rounds them to float (1.f/3, 1.f/18, 1.f/36).

@@ -229,7 +229,8 @@ __global__ void k_init_tgv(typename ST::raw* __restrict__ f, int n, double u0, c
     const long long cells = (long long)n * n * n;
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cells) return;
-    const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
+    int i, j, k;
+    cell_ijk(c, n, i, j, k);
     const double sx = tab[i], cxv = tab[n + i], c2x = tab[2 * n + i];
     const double sy = tab[j], cyv = tab[n + j], c2y = tab[2 * n + j];
     const double czv = tab[n + k], c2z = tab[2 * n + k];
@@ -283,7 +284,8 @@ __global__ void k_macro(const typename ST::raw* __restrict__ f, FT* __restrict__
     const long long cells = (long long)n * n * n;
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cells) return;
-    const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
+    int i, j, k;
+    cell_ijk(c, n, i, j, k);
     R v[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -355,7 +357,8 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_field(const FT* __restric
     } else {  // FP64 fields (FP64 storage): per-cell terms in FP64
         for (long long c = (long long)blockIdx.x * kDiagThreads + threadIdx.x; c < cells;
              c += (long long)gridDim.x * kDiagThreads) {
-            const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
+            int i, j, k;
+            cell_ijk(c, n, i, j, k);
             const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
             const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
             const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
@@ -425,7 +428,8 @@ __global__ void __launch_bounds__(256) k_qspeed(const FT* __restrict__ F, int n,
     const long long cells = (long long)n * n * n;
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cells) return;
-    const int i = int(c % n), j = int((c / n) % n), k = int(c / ((long long)n * n));
+    int i, j, k;
+    cell_ijk(c, n, i, j, k);
     const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
     const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
     const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
