@@ -308,10 +308,11 @@ __global__ void k_fill_list(const int* __restrict__ nb, int* __restrict__ list, 
 // Prep list of a level: the skin blocks with a change of refinement among their 27 neighbour blocks
 // (periodic), as {block, mask of the refined ones}.  Level 0: blocks are positions of the dense grid
 // of edge gx (pos null); level 1: pos[b] in the level-1 grid `grid`, an absent block unrefined.
-__global__ void k_prep_list(const int* __restrict__ skin, int nskin, const int* __restrict__ ref,
+__global__ void k_prep_list(const int* __restrict__ skin, const int* __restrict__ nskin_dev, const int* __restrict__ ref,
                             const int* __restrict__ pos, const int* __restrict__ grid, int gx,
                             int2* __restrict__ list, int* __restrict__ count) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nskin = __ldg(nskin_dev);  // the skin count as the device holds it (grid: capacity)
     unsigned rm = 0;
     int b = 0;
     if (s < nskin) {
@@ -461,12 +462,12 @@ cudaError_t adapt_fill_list(const int* nb, int nf, int mb, int* list, int* count
     return cudaGetLastError();
 }
 
-cudaError_t adapt_prep_list(const int* skin, int nskin, const int* ref, const int* pos, const int* grid, int gx,
-                            int* list, int* count, cudaStream_t st) {
+cudaError_t adapt_prep_list(const int* skin, const int* nskin_dev, int cap, const int* ref, const int* pos,
+                            const int* grid, int gx, int* list, int* count, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), st);
-    if (e != cudaSuccess || nskin <= 0) return e;
-    k_prep_list<<<grid_for(nskin, 256), 256, 0, st>>>(skin, nskin, ref, pos, grid, gx, reinterpret_cast<int2*>(list),
-                                                       count);
+    if (e != cudaSuccess || cap <= 0) return e;
+    k_prep_list<<<grid_for(cap, 256), 256, 0, st>>>(skin, nskin_dev, ref, pos, grid, gx, reinterpret_cast<int2*>(list),
+                                                     count);
     note_launch();
     return cudaGetLastError();
 }

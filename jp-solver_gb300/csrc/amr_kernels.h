@@ -137,9 +137,11 @@ cudaError_t adapt_fill(int* p, int v, long long n, cudaStream_t st);
 cudaError_t adapt_fill_list(const int* nb, int nf, int mb, int* list, int* count, cudaStream_t st);
 // prep list of a level: the skin blocks whose 27 neighbour blocks (periodic) mix refined and
 // unrefined, as pairs {block, mask of the refined neighbours (bit = slot)}; level 0: pos null and
-// gx = cgx; level 1: pos = f1pos, grid = l1grid, gx = l1gx (absent blocks unrefined).  *count is set.
-cudaError_t adapt_prep_list(const int* skin, int nskin, const int* ref, const int* pos, const int* grid, int gx,
-                            int* list, int* count, cudaStream_t st);
+// gx = cgx; level 1: pos = f1pos, grid = l1grid, gx = l1gx (absent blocks unrefined).  The skin
+// count is read on the device (*nskin_dev, at most cap: the grid), so no read-back precedes the
+// list.  *count is set.
+cudaError_t adapt_prep_list(const int* skin, const int* nskin_dev, int cap, const int* ref, const int* pos,
+                            const int* grid, int gx, int* list, int* count, cudaStream_t st);
 // interface cells of the (at most max_entries, *pcount) blocks of a prep list: the cells whose 3x3x3
 // neighbourhood reaches refined and unrefined blocks, as b * mb^3 + cell (at most
 // mb^3 - (mb-2)^3 per block); *ncells is set.  The order is not fixed.

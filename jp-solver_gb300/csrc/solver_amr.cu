@@ -10,6 +10,7 @@
 #include "solver.h"
 
 #include <algorithm>
+#include <cstddef>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -50,6 +51,7 @@ struct AmrState {
     AdaptCounts* cnt_dev = nullptr;
     AdaptCounts* cnt_host = nullptr;
     int nref0 = 0, nf1 = 0, nref1 = 0, nf2 = 0, n_skin0 = 0, n_skin1 = 0, ndeep = 0;
+    bool skins_pending = false;  // n_skin0/1 arrive with the read-back skins() queued (skins_landed)
     float* field = nullptr;
     std::vector<void*> owned;
     // Block counts the step kernels read on the device ({nf1, nf2, n_skin0, n_skin1, nref0, nref1}):
@@ -185,29 +187,49 @@ static jp_status upload_counts(jp_solver* s) {
     return JP_OK;
 }
 
-// prep lists of both levels from their skin lists and refinement marks, lengths into the device counts
+// prep lists of both levels from their skin lists and refinement marks, lengths into the device counts;
+// the skin counts are read on the device (step_cnt[SC_SKIN0/1]), the grids sized by capacity
 static jp_status prep_lists(jp_solver* s) {
     AmrState* a = s->amr;
-    ACK(adapt_prep_list(a->skin0, a->n_skin0, a->ref0, nullptr, nullptr, a->cgx, a->pl0, a->step_cnt + SC_PBLK0,
-                        s->stream), "prep list 0");
-    ACK(adapt_prep_list(a->skin1, a->n_skin1, a->ref1, a->f1pos, a->l1grid, a->l1gx, a->pl1, a->step_cnt + SC_PBLK1,
-                        s->stream), "prep list 1");
-    ACK(adapt_prep_cells(a->pl0, a->step_cnt + SC_PBLK0, a->n_skin0, a->MB, a->pc0, a->step_cnt + SC_PREP0, s->stream),
+    ACK(adapt_prep_list(a->skin0, a->step_cnt + SC_SKIN0, a->cnb0, a->ref0, nullptr, nullptr, a->cgx, a->pl0,
+                        a->step_cnt + SC_PBLK0, s->stream), "prep list 0");
+    ACK(adapt_prep_list(a->skin1, a->step_cnt + SC_SKIN1, a->cap1, a->ref1, a->f1pos, a->l1grid, a->l1gx, a->pl1,
+                        a->step_cnt + SC_PBLK1, s->stream), "prep list 1");
+    ACK(adapt_prep_cells(a->pl0, a->step_cnt + SC_PBLK0, a->cnb0, a->MB, a->pc0, a->step_cnt + SC_PREP0, s->stream),
         "prep cells 0");
-    ACK(adapt_prep_cells(a->pl1, a->step_cnt + SC_PBLK1, a->n_skin1, a->MB, a->pc1, a->step_cnt + SC_PREP1, s->stream),
+    ACK(adapt_prep_cells(a->pl1, a->step_cnt + SC_PBLK1, a->cap1, a->MB, a->pc1, a->step_cnt + SC_PREP1, s->stream),
         "prep cells 1");
     return JP_OK;
 }
 
+static_assert(offsetof(AdaptCounts, n_skin1) == offsetof(AdaptCounts, n_skin0) + sizeof(int) &&
+                  SC_SKIN1 == SC_SKIN0 + 1,
+              "the two skin counts are copied as one pair");
+
+// Skin lists of the current grid and the prep lists built from them.  Their lengths stay on the
+// device: the host's block counts go up first, then the two skin counts are copied over theirs
+// from the adaptation counts, and the prep lists read them there.  The host's copy of the skin
+// counts arrives with a read-back queued here and is taken after the caller's wait (skins_landed):
+// a regrid needs no read-back for its skins.
 static jp_status skins(jp_solver* s) {
     AmrState* a = s->amr;
     ACK(adapt_skins(a->ref0, a->cnb0, a->cgx, a->ref1, a->f1pos, a->l1grid, a->nf1, a->l1gx, a->flags, a->skin0,
                     a->skin1, a->cnt_dev, s->stream), "skins");
-    TRY(read_counts(s));
+    TRY(upload_counts(s));
+    ACK(cudaMemcpyAsync(a->step_cnt + SC_SKIN0, &a->cnt_dev->n_skin0, 2 * sizeof(int), cudaMemcpyDeviceToDevice,
+                        s->stream), "skin counts");
+    TRY(prep_lists(s));
+    ACK(cudaMemcpyAsync(a->cnt_host, a->cnt_dev, sizeof(AdaptCounts), cudaMemcpyDeviceToHost, s->stream), "counts D2H");
+    a->skins_pending = true;
+    return JP_OK;
+}
+
+// the host's skin counts, once the stream has passed the read-back skins() queued
+static void skins_landed(AmrState* a) {
+    if (!a->skins_pending) return;
     a->n_skin0 = a->cnt_host->n_skin0;
     a->n_skin1 = a->cnt_host->n_skin1;
-    TRY(prep_lists(s));
-    return upload_counts(s);
+    a->skins_pending = false;
 }
 
 static jp_status check_err(jp_solver* s) {
@@ -1057,6 +1079,7 @@ jp_status amr_init(jp_solver* s) {
     a->hw_nf1 = a->hw_nf2 = 0;
     TRY(initial_build(s));
     ACK(wait_stream(s), "initial build");
+    skins_landed(a);
     reset_graphs(a);  // the level-2 pool was allocated anew
     s->step_count = 0;
     s->initialized = true;
@@ -1087,6 +1110,7 @@ jp_status amr_set_step_map(jp_solver* s, int vec, int tpb) {
 jp_status amr_regrid(jp_solver* s) {
     TRY(regrid(s));  // the captured steps stay valid unless a pool grew (grow_l1/grow_l2 drop them)
     ACK(wait_stream(s), "regrid");
+    skins_landed(s->amr);
     return JP_OK;
 }
 
