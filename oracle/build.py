@@ -6,7 +6,11 @@
                              checkout (only when that checkout is present; the cubins then travel
                              with the repository copy, the sources never do)
 
-    python oracle/build.py [--reference /root/reference]
+    python oracle/build.py [--reference DIR]
+
+The reference checkout is taken from --reference, else from the JP_REFERENCE environment variable,
+else from the location this recipe was written for (DEFAULT_REFERENCE); without a checkout the
+cubins are left as they are.
 """
 from __future__ import annotations
 
@@ -20,6 +24,14 @@ CUDA = "/usr/local/cuda"
 NVCC = os.path.join(CUDA, "bin", "nvcc") if os.path.exists(os.path.join(CUDA, "bin", "nvcc")) else "nvcc"
 CXX = os.environ.get("CXX", "g++")
 DEFAULT_REFERENCE = "/root/reference"
+
+
+def reference_dir(argv: list[str] | None = None) -> str:
+    """--reference DIR, else $JP_REFERENCE, else DEFAULT_REFERENCE."""
+    argv = sys.argv if argv is None else argv
+    if "--reference" in argv:
+        return argv[argv.index("--reference") + 1]
+    return os.environ.get("JP_REFERENCE") or DEFAULT_REFERENCE
 
 
 def _stale(target: str, deps: list[str]) -> bool:
@@ -55,10 +67,10 @@ def build_refrun() -> str | None:
     return out
 
 
-def build_reference_cubins(reference: str = DEFAULT_REFERENCE) -> list[str]:
+def build_reference_cubins(reference: str | None = None) -> list[str]:
     """Compile the reference's .cu files, in place in its checkout, to device-only cubins (MB=8, the
     reference's default; AMR with its Makefile's -maxrregcount=128)."""
-    src_dir = os.path.join(reference, "src")
+    src_dir = os.path.join(reference or reference_dir([]), "src")
     if not os.path.isdir(src_dir):
         return []
     os.makedirs(REF_OUT, exist_ok=True)
@@ -78,14 +90,11 @@ def build_reference_cubins(reference: str = DEFAULT_REFERENCE) -> list[str]:
     return outs
 
 
-def build(reference: str = DEFAULT_REFERENCE) -> None:
+def build(reference: str | None = None) -> None:
     build_oracle()
     build_refrun()
     build_reference_cubins(reference)
 
 
 if __name__ == "__main__":
-    ref = DEFAULT_REFERENCE
-    if "--reference" in sys.argv:
-        ref = sys.argv[sys.argv.index("--reference") + 1]
-    build(ref)
+    build(reference_dir())

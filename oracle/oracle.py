@@ -47,6 +47,7 @@ def orc() -> C.CDLL:
         L.orc_diag_f64.argtypes = [_D, C.c_int, _D]
         L.orc_run_f32.argtypes = [_F, _F, C.c_int, C.c_int, C.c_float, C.c_long]
         L.orc_run_f32.restype = C.c_int
+        L.orc_qspeed_f32.argtypes = [_F, C.c_int, _F, _F, _F]
         _orc = L
     return _orc
 
@@ -120,6 +121,16 @@ def diag_field(F: np.ndarray, n: int) -> tuple:
 
 def diag(f: np.ndarray, n: int, mb: int) -> tuple:
     return diag_field(macro(f, n, mb), n)
+
+
+def qspeed(F: np.ndarray, n: int) -> tuple:
+    """(Q, speed, velocity) of a float macro field [cell][rho,u,v,w] as the uniform program's VTK
+    writer forms them (src/tgv3d_uniform.cu:112-121)."""
+    F = np.ascontiguousarray(F, dtype=np.float32).reshape(-1)
+    q, sp, v = (np.empty(n ** 3, dtype=np.float32), np.empty(n ** 3, dtype=np.float32),
+                np.empty(3 * n ** 3, dtype=np.float32))
+    orc().orc_qspeed_f32(_fp(F), n, _fp(q), _fp(sp), _fp(v))
+    return q, sp, v
 
 
 # ---- the reference's own kernels on the GPU ------------------------------------------------------
@@ -306,6 +317,15 @@ class AmrBackend:
             raise RuntimeError("pops: %d" % n)
         return a[:n].copy()
 
+    def qspeed(self) -> tuple:
+        """(Q, speed) on the (4 n)^3 composite: the reference's k_composite + k_qspeed."""
+        nn = (4 * self.n) ** 3
+        q, sp = np.empty(nn, dtype=np.float32), np.empty(nn, dtype=np.float32)
+        rc = self.L.ref_amr_qspeed(C.c_void_p(self.h), _fp(q), _fp(sp))
+        if rc:
+            raise RuntimeError("reference qspeed failed (%d): %s" % (rc, self.L.refrun_last_error().decode()))
+        return q, sp
+
     def set_pops(self, level: int, arr: np.ndarray):
         a = np.ascontiguousarray(arr, dtype=np.float32)
         n = self._f("set_pops")(C.c_void_p(self.h), level, _fp(a), a.size)
@@ -333,6 +353,7 @@ def ref_amr() -> C.CDLL:
                                      C.c_double, C.c_int, C.c_double]
         L.ref_amr_initial_build.argtypes = [C.c_void_p]
         L.ref_amr_time.argtypes = [C.c_void_p, C.c_long, C.c_long, _F]
+        L.ref_amr_qspeed.argtypes = [C.c_void_p, _F, _F]
         _amr_sigs(L, "ref_amr")
         _ref_amr_ready = True
     return L

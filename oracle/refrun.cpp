@@ -175,7 +175,7 @@ namespace {
 cudaLibrary_t g_amr = nullptr;
 struct AmrK {
     cudaKernel_t init, step0, prep_list, fill1p, fill2p, step1, step2, restr1, restr2, seed1, seed2, mig1, mig2, sensor,
-        mark_thr, mark_ref1, deepmask, scat1, scat2, setall, slab, ref1all, dil0, dil1, composite, diag;
+        mark_thr, mark_ref1, deepmask, scat1, scat2, setall, slab, ref1all, dil0, dil1, composite, diag, qspeed;
 } K;
 const int EB = 10, EB3 = 1000, HALF = 4;
 
@@ -470,6 +470,7 @@ int refrun_load_amr(const char* path) {
         {&K.slab, "_Z11k_mark_slabPiii"}, {&K.ref1all, "_Z15k_mark_ref1_allPKiiPi"},
         {&K.dil0, "_Z11k_dilate_L0PKiiiPi"}, {&K.dil1, "_Z11k_dilate_L1PKiS0_S0_iiPi"},
         {&K.composite, "_Z11k_compositePKfS0_S0_PKiS2_S2_iiiPf"}, {&K.diag, "_Z13k_diag_reducePKfiPd"},
+        {&K.qspeed, "_Z8k_qspeedPKfiPfS1_S1_i"},
     };
     for (auto& t : tab) RK(cudaLibraryGetKernel(t.k, g_amr, t.n), t.n);
     return 0;
@@ -557,6 +558,30 @@ int ref_amr_diag(void* h, double* out) {
     cudaFree(acc);
     double inv = 1.0 / double(NN);
     for (int i = 0; i < 3; ++i) out[i] = h3[i] * inv;
+    return rc;
+}
+// reference k_composite + k_qspeed (src/tgv3d_amr.cu:523-536,553-564): Q-criterion and speed at 4N0
+int ref_amr_qspeed(void* h, float* q_out, float* speed_out) {
+    RefAmr* a = static_cast<RefAmr*>(h);
+    long NN = (long)a->N2 * a->N2 * a->N2;
+    float *F = nullptr, *Qd = nullptr, *Sd = nullptr, *nov = nullptr;
+    int zero = 0;
+    RK(cudaMalloc(&F, sizeof(float) * 4 * NN), "cudaMalloc");
+    cudaError_t e = cudaMalloc(&Qd, sizeof(float) * NN);
+    if (e == cudaSuccess) e = cudaMalloc(&Sd, sizeof(float) * NN);
+    int rc = e == cudaSuccess ? 0 : seterr("cudaMalloc", e);
+    unsigned g = (unsigned)((NN + 255) / 256);
+    if (!rc)
+        rc = L(K.composite, g, 256, {&a->c0a, &a->f1a, &a->f2a, &a->ref1, &a->fof1, &a->l1grid, &a->cgx, &a->l1gx, &a->N2, &F});
+    if (!rc) rc = L(K.qspeed, g, 256, {&F, &a->N2, &Qd, &Sd, &nov, &zero});
+    if (!rc) {
+        e = cudaMemcpy(q_out, Qd, sizeof(float) * NN, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(speed_out, Sd, sizeof(float) * NN, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = seterr("qspeed", e);
+    }
+    cudaFree(F);
+    cudaFree(Qd);
+    cudaFree(Sd);
     return rc;
 }
 void ref_amr_counts(void* h, long* out) {

@@ -164,6 +164,30 @@ void diag(const R* F, int N, double out[3]) {
     out[2] = mass * invn;
 }
 
+// src/tgv3d_uniform.cu:112-121 (write_vti): speed |u| and velocity from the field's float values
+// widened to double; Q = -1/2 sum_ab g_ab g_ba of grad_at's gradient, in double, rounded to float.
+void qspeed(const float* F, int N, float* Qo, float* spd, float* vel) {
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < N; ++k)
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                size_t p = idx3(i, j, k, N);
+                double u = F[p * 4 + 1], v = F[p * 4 + 2], w = F[p * 4 + 3];
+                spd[p] = float(std::sqrt(u * u + v * v + w * w));
+                if (vel) {
+                    vel[p * 3 + 0] = float(u);
+                    vel[p * 3 + 1] = float(v);
+                    vel[p * 3 + 2] = float(w);
+                }
+                double g[3][3];
+                grad_at<float>(F, N, i, j, k, g);
+                double Qc = 0;
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) Qc -= 0.5 * g[a][b] * g[b][a];
+                Qo[p] = float(Qc);
+            }
+}
+
 }  // namespace
 
 extern "C" {
@@ -178,6 +202,7 @@ void orc_macro_f32(const float* f, int N, int MB, float* out) { macro<float>(f, 
 void orc_macro_f64(const double* f, int N, int MB, double* out) { macro<double>(f, N, MB, out); }
 void orc_diag_f32(const float* F, int N, double out[3]) { diag<float>(F, N, out); }
 void orc_diag_f64(const double* F, int N, double out[3]) { diag<double>(F, N, out); }
+void orc_qspeed_f32(const float* F, int N, float* Q, float* speed, float* vel) { qspeed(F, N, Q, speed, vel); }
 
 // nsteps FP32 steps in place (ping-pong through a scratch buffer of the same size); returns the
 // buffer that holds the final state (0 = f, 1 = scratch).
