@@ -201,14 +201,15 @@ jp_status jp_memory_info(jp_solver* s, int64_t* free_bytes, int64_t* total_bytes
 /* Diagnostics of a caller-owned macro field with no device allocation.  No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc when they need the numbers (a host
  * framework that owns all device memory through its own pool, a loop that must not allocate after
- * start-up, work recorded into a CUDA graph).  `field_dev` holds n^3 float4 (rho, ux, uy, uz) in the
- * order of jp_get_macro; `out_dev` receives 3 doubles (mean E, mean enstrophy, mean rho), written on
- * `stream` (a cudaStream_t; NULL = default stream) without host synchronisation.  float_diff = 1 takes
- * velocity differences in float (the uniform solver's jp_diag), 0 exactly (the AMR composite).
- * Scratch lives in a fixed 384 KiB device array inside the library, so fields above 268,435,456 cells
- * (n > 645) are rejected with JP_ERR_CAPACITY.  The first call on each device looks up that array's
- * address and should come before any stream capture.  Calls share the array: calls that overlap on
- * the GPU race and must be serialised by the caller. */
+ * start-up).  `field_dev` holds n^3 float4 (rho, ux, uy, uz) in the order of jp_get_macro; `out_dev`
+ * receives 3 doubles (mean E, mean enstrophy, mean rho), written on `stream` (a cudaStream_t; NULL =
+ * default stream) without host synchronisation.  Both must be device (or managed) memory of the
+ * current device, else JP_ERR_INVALID.  float_diff = 1 takes velocity differences in float (the
+ * uniform solver's jp_diag), 0 exactly (the AMR composite).  Scratch lives in a fixed 384 KiB device
+ * array inside the library, so fields above 268,435,456 cells (n > 645) are rejected with
+ * JP_ERR_CAPACITY.  The first call on each device looks up that array's address (again after the
+ * device's context was replaced, e.g. by cudaDeviceReset) and should come before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race and must be serialised by the caller. */
 jp_status jp_diag_field_noalloc(const float* field_dev, int32_t n, int32_t float_diff, double* out_dev,
                                 void* stream);
 

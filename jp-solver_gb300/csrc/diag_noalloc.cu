@@ -2,10 +2,10 @@
 //
 // Some callers cannot allocate device memory at the moment they need the diagnostics: a host
 // framework that owns all device memory through its own pool (and forbids cudaMalloc behind its
-// back), a real-time loop that must not allocate after start-up, or code that records work into a
-// CUDA graph.  jp_diag() keeps its reduction partials in memory the solver allocated; this variant
-// keeps them in a fixed array compiled into the library instead, so it only needs the caller's input
-// field and output buffer.
+// back), or a real-time loop that must not allocate after start-up.  jp_diag() keeps its reduction
+// partials in memory the solver allocated; this variant keeps them in a fixed array compiled into
+// the library instead, so it only needs the caller's input field and output buffer, both in device
+// memory of the current device (checked before any work is queued).
 //
 // The scratch is a file-scope __device__ array of kMaxChunks partial triples (384 KiB).  Every GPU
 // that loads this library holds it until the process exits.  Each CTA reduces one chunk of kChunk
@@ -16,9 +16,12 @@
 // every partial it reads, so nothing has to be cleared between calls.
 //
 // Host code cannot use the array's name as a device address (it names a host-side stand-in); the
-// device address is looked up once per device with cudaGetSymbolAddress, on the first call made with
-// that device current.  That first call may load the module, so it should come before any stream
+// device address is looked up with cudaGetSymbolAddress on the first call made with a device's
+// context current, and looked up again when that context has been replaced (cudaDeviceReset tears
+// the primary context down and the next one loads the module anew, possibly elsewhere).  The
+// lookup may load the module, so the first call on each device should come before any stream
 // capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -38,8 +41,18 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_partials[kMaxChunks * 3];
 
+// per device: the context the address was looked up in (its process-unique id) and the address
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    double* addr;
+};
 std::mutex g_setup_mutex;
-double* g_partials_addr[kMaxDevices] = {};
+ScratchSlot g_slots[kMaxDevices] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -108,20 +121,62 @@ __global__ void __launch_bounds__(kThreads) k_noalloc_finish(const double* __res
     }
 }
 
-// Device address of the scratch array on the current device, looked up once per device.
-jp_status scratch_address(double** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+// Id of the calling thread's current context (0: none yet).  The two driver calls are reached
+// through the runtime's entry-point table, so the library needs no link against the driver.
+jp_status current_context_id(unsigned long long* id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void* f0 = nullptr;
+        void* f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = q0;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetDriverEntryPointByVersion");
+        if (q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+            return fail(JP_ERR_CUDA, "jp_diag_field_noalloc: driver lacks cuCtxGetCurrent / cuCtxGetId");
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f1);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return fail(JP_ERR_CUDA, "cuCtxGetCurrent failed");
+    *id = 0;
+    if (ctx && g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return fail(JP_ERR_CUDA, "cuCtxGetId failed");
+    return JP_OK;
+}
+
+// Device address of the scratch array in the current device's current context: looked up once per
+// device and context, again after the context was replaced.
+jp_status scratch_address(int dev, double** out) {
     if (dev < 0 || dev >= kMaxDevices) return fail(JP_ERR_INVALID, "device ordinal %d out of range", dev);
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_partials_addr[dev]) {
+    unsigned long long id = 0;
+    jp_status st = current_context_id(&id);
+    if (st != JP_OK) return st;
+    ScratchSlot& slot = g_slots[dev];
+    if (id == 0 || !slot.addr || slot.ctx_id != id) {
         double* p = nullptr;
-        e = cudaGetSymbolAddress((void**)&p, g_noalloc_partials);
+        cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_partials);  // makes the context current
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
-        g_partials_addr[dev] = p;
+        st = current_context_id(&id);
+        if (st != JP_OK) return st;
+        slot.ctx_id = id;
+        slot.addr = p;
     }
-    *out = g_partials_addr[dev];
+    *out = slot.addr;
+    return JP_OK;
+}
+
+// The caller's buffer must be device (or managed) memory reachable on device `dev`: a host pointer
+// or another GPU's memory would fault in the kernel, so it is refused here.
+jp_status check_on_device(const void* p, int dev, const char* what) {
+    cudaPointerAttributes at{};
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaPointerGetAttributes");
+    if (at.type == cudaMemoryTypeManaged) return JP_OK;
+    if (at.type != cudaMemoryTypeDevice)
+        return fail(JP_ERR_INVALID, "jp_diag_field_noalloc: %s is not device memory", what);
+    if (at.device != dev)
+        return fail(JP_ERR_INVALID, "jp_diag_field_noalloc: %s lives on device %d, device %d is current", what,
+                    at.device, dev);
     return JP_OK;
 }
 
@@ -139,8 +194,13 @@ extern "C" jp_status jp_diag_field_noalloc(const float* field_dev, int32_t n, in
         return fail(JP_ERR_CAPACITY,
                     "jp_diag_field_noalloc: %lld cells exceed the fixed scratch (at most %lld cells, n <= 645)", cells,
                     (long long)kMaxChunks * kChunk);
+    int dev = 0;
+    cudaError_t de = cudaGetDevice(&dev);
+    if (de != cudaSuccess) return cuda_fail(de, "cudaGetDevice");
     double* partials = nullptr;
-    jp_status st = scratch_address(&partials);
+    jp_status st = scratch_address(dev, &partials);
+    if (st == JP_OK) st = check_on_device(field_dev, dev, "the field");
+    if (st == JP_OK) st = check_on_device(out_dev, dev, "the output");
     if (st != JP_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // a caller's field may start anywhere a float can: 16-byte record loads only where aligned

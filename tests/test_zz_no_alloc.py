@@ -1,8 +1,9 @@
 """jp_diag_field_noalloc: the diagnostics entry point for callers that cannot allocate device memory
-(a framework that owns all device memory, a loop that must not allocate after start-up, graph
-capture).  Through the C ABI it must give the same energy, enstrophy and mass as the solver's own
-jp_diag, on two calls in a row (the fixed scratch array keeps the previous call's contents), and
-reject a field larger than its scratch can reduce.
+(a framework that owns all device memory through its own pool, a loop that must not allocate after
+start-up).  Through the C ABI it must give the same energy, enstrophy and mass as the solver's own
+jp_diag, on two calls in a row (the fixed scratch array keeps the previous call's contents), refuse
+buffers that are not device memory and a field larger than its scratch can reduce, and keep working
+after the device's context was replaced.
 
 The caller's buffers come from PyTorch here: the entry point itself allocates nothing.  Collected
 last (file name) so that a failure here does not hide the other tests."""
@@ -45,6 +46,67 @@ def test_noalloc_diag_rejects_field_beyond_scratch():
     assert call(field, 646, 1, out) == 3                   # JP_ERR_CAPACITY, checked before any launch
     assert b"645" in J.lib().jp_last_error()
     torch.cuda.synchronize()
+
+
+def test_noalloc_diag_rejects_host_buffers():
+    # a host pointer would fault in the kernel: refused before any launch, nothing written
+    host_field = np.zeros(4 * 16 ** 3, dtype=np.float32)
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    st = J.lib().jp_diag_field_noalloc(ctypes.c_void_p(host_field.ctypes.data), 16, 1, ctypes.c_void_p(out.data_ptr()),
+                                       None)
+    assert st == 1 and b"not device memory" in J.lib().jp_last_error()
+    field = torch.zeros(4 * 16 ** 3, dtype=torch.float32, device="cuda")
+    host_out = np.zeros(3)
+    st = J.lib().jp_diag_field_noalloc(ctypes.c_void_p(field.data_ptr()), 16, 1, ctypes.c_void_p(host_out.ctypes.data),
+                                       None)
+    assert st == 1 and b"not device memory" in J.lib().jp_last_error()
+    torch.cuda.synchronize()
+
+
+RESET_SCRIPT = r"""
+import ctypes, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import jpsolver as J
+L = J.lib()
+rt = ctypes.CDLL("libcudart.so.13")
+n = 16
+rng = np.random.default_rng(3)
+F = np.empty((n ** 3, 4), dtype=np.float32)
+F[:, 0] = 1.0 + 0.01 * rng.standard_normal(n ** 3)
+F[:, 1:] = 0.05 * rng.standard_normal((n ** 3, 3))
+res = []
+for rnd in range(2):
+    f, o = ctypes.c_void_p(), ctypes.c_void_p()
+    assert rt.cudaMalloc(ctypes.byref(f), ctypes.c_size_t(F.nbytes)) == 0
+    assert rt.cudaMalloc(ctypes.byref(o), ctypes.c_size_t(24)) == 0
+    assert rt.cudaMemcpy(f, F.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(F.nbytes), 1) == 0
+    assert L.jp_diag_field_noalloc(f, n, 1, o, None) == 0, L.jp_last_error()
+    out = np.zeros(3)
+    assert rt.cudaMemcpy(out.ctypes.data_as(ctypes.c_void_p), o, ctypes.c_size_t(24), 2) == 0
+    res.append(out)
+    rt.cudaFree(f)
+    rt.cudaFree(o)
+    if rnd == 0:
+        assert rt.cudaDeviceReset() == 0   # the next call runs in a new primary context
+assert np.array_equal(res[0], res[1]), res
+print("reset ok", res[1])
+"""
+
+
+def test_noalloc_diag_after_context_reset(tmp_path):
+    # in a process of its own (no torch): a call, cudaDeviceReset, a call in the new context; the
+    # scratch address is looked up again and both calls give the same bits
+    import os
+    import subprocess
+    import sys
+
+    pkg = os.path.dirname(J.__file__)
+    script = tmp_path / "reset.py"
+    script.write_text(RESET_SCRIPT)
+    r = subprocess.run([sys.executable, str(script), pkg], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "reset ok" in r.stdout
 
 
 def fp64_diag(F, n, float_diff):
