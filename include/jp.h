@@ -293,6 +293,19 @@ void jp_ensemble_destroy(jp_ensemble* e);
 jp_status jp_ensemble_add(jp_ensemble* e, jp_solver* s);
 jp_status jp_ensemble_remove(jp_ensemble* e, jp_solver* s);
 jp_status jp_ensemble_step(jp_ensemble* e, int64_t nsteps);
+/* Persistent AMR coarse steps (no counterpart in the reference; its base_step issues 18 launches per
+ * coarse step, src/tgv3d_amr.cu:821-837).  mode 1: jp_ensemble_step(e, k) runs the k coarse steps of
+ * up to 48 AMR members (block edge 8, rows of four cells, restrictions fused; others keep the
+ * per-stage launches) in ONE cooperative launch that walks every member's per-level block and
+ * cell lists stage by stage, with grid barriers between dependent stages; mode 0 (the default):
+ * one launch per stage and coarse step.  Results are the same bits either way.  wait_limit_ns
+ * bounds each barrier wait (0: 2 s); past it the launch stops and the next jp_ensemble_sync
+ * returns JP_ERR_TIMEOUT (the members' states are then undefined).  grid: CTAs of the launch (0:
+ * every CTA that can be resident). */
+jp_status jp_ensemble_set_persistent(jp_ensemble* e, int32_t mode, int64_t wait_limit_ns, int32_t grid);
+/* Wait for the ensemble's queued steps; JP_ERR_TIMEOUT if a persistent launch gave up at a grid
+ * barrier since the last jp_ensemble_sync (the message names the phase and coarse step). */
+jp_status jp_ensemble_sync(jp_ensemble* e);
 
 /* A server runs whole Taylor-Green solves (the `uniform` / `amr` programs' runs) for a stream of
  * requests with continuous batching: requests wait in a queue until their HBM estimate fits the

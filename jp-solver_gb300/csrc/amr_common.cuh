@@ -10,6 +10,18 @@
 
 #include "lattice.cuh"
 
+// Loads of population arrays (pools, prolongation sources, ghost shells).  Separate kernel launches
+// read them through the read-only path (__ldg).  A kernel that writes these arrays in one phase and
+// reads them in a later phase of the same launch (the persistent coarse step, amr_persist.cuh)
+// defines JP_COHERENT_POOLS before including this header: its loads are then ordinary weak loads
+// (ld.global.ca), which the memory model orders after the acquire of the grid barrier between the
+// phases; the read-only path carries no such guarantee for data written during the launch.
+#ifdef JP_COHERENT_POOLS
+#define JP_LDP(p) __ldca(p)
+#else
+#define JP_LDP(p) __ldg(p)
+#endif
+
 namespace jp {
 namespace amr {
 
@@ -198,7 +210,7 @@ struct PoolIO {
     // shifts on load and back on store (its mass then drifts at the deviations' round-off instead of
     // the O(w_q) totals' biased round-off)
     static constexpr bool SA = true;
-    __device__ static __forceinline__ float n(const raw* p) { return ST::load(__ldg(p)); }
+    __device__ static __forceinline__ float n(const raw* p) { return ST::load(JP_LDP(p)); }
     __device__ static __forceinline__ float f(const raw* p, int q) { return SH ? wf(q) + n(p) : n(p); }
     __device__ static __forceinline__ void put_n(raw* p, float v) { *p = ST::store(v); }
     __device__ static __forceinline__ void put_f(raw* p, int q, float v) { *p = ST::store(SH ? v - wf(q) : v); }
@@ -229,9 +241,9 @@ __device__ __forceinline__ void pull_cell(const typename ST::raw* __restrict__ f
         pull_src<MB>(q, i, j, k, e, sc);
         const int blk = e == 13 ? b : __ldg(nbrow + e);
         if (!GHOST || blk >= 0) {
-            rv[q] = __ldg(fa + ((size_t)blk * Q + q) * MB3 + sc);
+            rv[q] = JP_LDP(fa + ((size_t)blk * Q + q) * MB3 + sc);
         } else {
-            rv[q] = __ldg(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(i - cx(q), j - cy(q), k - cz(q)));
+            rv[q] = JP_LDP(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(i - cx(q), j - cy(q), k - cz(q)));
         }
     }
 #pragma unroll

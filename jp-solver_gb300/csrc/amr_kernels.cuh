@@ -55,7 +55,7 @@ __device__ __forceinline__ void d_step_l0(const typename ST::raw* __restrict__ f
         for (int q = 0; q < Q; ++q) {
             int e, sc;
             pull_src<MB>(q, i, j, k, e, sc);
-            f[q] = PoolIO<ST>::g_of(__ldg(fa + ((size_t)snb[e] * Q + q) * G::MB3 + sc), q);
+            f[q] = PoolIO<ST>::g_of(JP_LDP(fa + ((size_t)snb[e] * Q + q) * G::MB3 + sc), q);
         }
         bgk_fast<true>(f, om);
 #pragma unroll
@@ -187,7 +187,7 @@ __device__ __forceinline__ int interp_needed(const typename ST::raw* const (&p)[
 #pragma unroll
     for (int c = 0; c < 8; ++c)
 #pragma unroll
-        for (int s = 0; s < 5; ++s) r[c][s] = (!SPARSE || p[c]) ? __ldg(p[c] + qs[s] * MB3) : typename ST::raw(0);
+        for (int s = 0; s < 5; ++s) r[c][s] = (!SPARSE || p[c]) ? JP_LDP(p[c] + qs[s] * MB3) : typename ST::raw(0);
 #pragma unroll
     for (int s = 0; s < 5; ++s) {
         float acc = 0.f;
@@ -440,7 +440,7 @@ struct Vec4 {  // four stored values, one 16-byte (FP32) or 8-byte (16-bit) acce
         word w;
         raw v[4];
     };
-    __device__ __forceinline__ void load(const raw* p) { w = __ldg(reinterpret_cast<const word*>(p)); }
+    __device__ __forceinline__ void load(const raw* p) { w = JP_LDP(reinterpret_cast<const word*>(p)); }
     __device__ __forceinline__ void store(raw* p) const { __stcs(reinterpret_cast<word*>(p), w); }
 };
 template <class RAW> __device__ __forceinline__ RAW shfl_by(RAW v, int d) {
@@ -504,8 +504,8 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
             if (cx(q) != 0 && (cx(q) > 0 ? s == 0 : s == RG::SPR - 1)) {
                 const int eb = __ldg(nbrow + ez * 9 + ey * 3 + (cx(q) > 0 ? 0 : 2));
                 const int li = cx(q) > 0 ? -1 : MB;
-                E[q] = eb >= 0 ? __ldg(fa + ((size_t)eb * Q + q) * MB3 + rowc + (li & M))
-                               : __ldg(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(li, lj, lk));
+                E[q] = eb >= 0 ? JP_LDP(fa + ((size_t)eb * Q + q) * MB3 + rowc + (li & M))
+                               : JP_LDP(gh + ((size_t)b * Q + q) * SH + shell_index<MB>(li, lj, lk));
             }
         }
         // 2. inside the row the value comes from the neighbouring thread (all lanes shuffle)

@@ -79,6 +79,46 @@ struct AmrBatch {
     AmrItem it[kAmrBatchMax];
 };
 
+// ---- persistent coarse steps: many solves, several coarse steps, one launch ---------------------
+// One member of a persistent launch: the arrays and device counts of one solve's coarse step
+// (base_step's sequence).  c0[0] holds the coarse state when the launch starts; after `steps`
+// coarse steps it is in c0[steps & 1].  The fine levels end in f1a / f2a as they started.
+struct PersistMember {
+    void* c0[2];
+    void *prep0, *gh1, *f1a, *f1b, *prep1, *gh2, *f2a, *f2b;
+    const int *pc0, *pc1, *fl1, *fl2;                  // interface-cell and fill lists
+    const int *pcb, *oct, *l2pl1, *l2oct, *f1pos, *l1grid, *nb1, *nb2;
+    const int *n_prep0, *n_fill1, *n_prep1, *n_fill2;  // list lengths on the device
+    const int *n_f1, *n_f2;                            // fine block counts on the device
+    int cgx, n, l1gx, n1, cnb0, steps;
+    float om0, om1, om2, nqs01, nqs12, nqi21, nqi10;
+};
+// Grid barrier state of a persistent launch: arrivals (zeroed before each launch), and the first
+// error (a barrier wait that ran past the limit: 1), the phase and the coarse step where it happened
+// (kept until the owner reads and clears them).
+struct PersistSync {
+    unsigned int arrived;
+    int err, phase, step;
+};
+constexpr size_t kPersistResetBytes = sizeof(unsigned int);  // arrived
+constexpr int kPersistPhases = 10;  // grid-wide phases of one coarse step
+// Up to kAmrBatchMax members sorted by `steps`, descending (members with fewer coarse steps drop
+// out of the later ones: ragged step counts); passed by value in kernel parameter space.
+struct AmrPersist {
+    int count = 0, maxsteps = 0;
+    long long limit_ns = 0;    // longest wait at one grid barrier before the launch gives up
+    PersistSync* sync = nullptr;
+    PersistMember m[kAmrBatchMax];
+};
+// the block edge, fine-step mapping and flags the persistent coarse step implements (MB = 8, rows
+// of four cells, restrictions fused into the last substeps, preparations and restrictions on)
+bool amr_persist_supported(int mb, int vec, bool fuse, bool skip_prep);
+// Cooperative launch of the persistent coarse steps on `st` with `grid` CTAs (0: every CTA that can
+// be resident; capped there).  *grid_used (optional) returns the grid.
+cudaError_t amr_persist_launch(int storage, int mb, const AmrPersist& P, int grid, cudaStream_t st, int* grid_used);
+template <class ST> cudaError_t amr_persist_launch_st(int mb, const AmrPersist& P, int grid, cudaStream_t st,
+                                                      int* grid_used);
+
 // storage: 0 FP32, 1 shifted FP16, 2 shifted BF16 (jp_storage)
 cudaError_t amr_launch(int storage, int mb, int op, const AmrLaunch& L);
 // op as in AmrLaunch; tpb: threads per CTA of the steps (0: default); fuse: the fine steps restrict

@@ -83,6 +83,14 @@ struct jp_ensemble {
     cudaEvent_t done = nullptr;
     AmrFork fk;  // the level-0 branch of the AMR members' coarse steps
     std::vector<jp_solver*> members;
+    // persistent AMR coarse steps (jp_ensemble_set_persistent): barrier state of each launch of a
+    // jp_ensemble_step (one per kAmrBatchMax members), its error fields kept until jp_ensemble_sync
+    int persist = 0, persist_grid = 0;
+    long long limit_ns = kPersistLimitNs;
+    amr::PersistSync* sync = nullptr;
+    amr::PersistSync* sync_host = nullptr;  // pinned copy read by jp_ensemble_sync
+    static constexpr int kSyncSlots = 64;
+    static constexpr long long kPersistLimitNs = 2000000000LL;
 };
 
 extern "C" {
@@ -113,7 +121,44 @@ void jp_ensemble_destroy(jp_ensemble* e) {
     }
     e->fk.destroy();
     if (e->done) cudaEventDestroy(e->done);
+    if (e->sync) cudaFree(e->sync);
+    if (e->sync_host) cudaFreeHost(e->sync_host);
     delete e;
+}
+
+jp_status jp_ensemble_set_persistent(jp_ensemble* e, int32_t mode, int64_t wait_limit_ns, int32_t grid) {
+    if (!e) return fail(JP_ERR_INVALID, "null ensemble");
+    if (mode != 0 && mode != 1) return fail(JP_ERR_INVALID, "persistent mode %d (0 or 1)", mode);
+    if (wait_limit_ns < 0 || grid < 0) return fail(JP_ERR_INVALID, "negative wait limit or grid");
+    ECK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (mode && !e->sync) {
+        const size_t bytes = sizeof(amr::PersistSync) * jp_ensemble::kSyncSlots;
+        ECK(cudaMalloc(&e->sync, bytes), "cudaMalloc barrier state");
+        ECK(cudaMallocHost(&e->sync_host, bytes), "cudaMallocHost barrier state");
+        ECK(cudaMemsetAsync(e->sync, 0, bytes, e->stream), "barrier state");
+    }
+    e->persist = mode;
+    e->limit_ns = wait_limit_ns ? wait_limit_ns : jp_ensemble::kPersistLimitNs;
+    e->persist_grid = grid;
+    return JP_OK;
+}
+
+jp_status jp_ensemble_sync(jp_ensemble* e) {
+    if (!e) return fail(JP_ERR_INVALID, "null ensemble");
+    ECK(cudaSetDevice(e->device), "cudaSetDevice");
+    if (!e->sync) {
+        ECK(cudaStreamSynchronize(e->stream), "ensemble sync");
+        return JP_OK;
+    }
+    const size_t bytes = sizeof(amr::PersistSync) * jp_ensemble::kSyncSlots;
+    ECK(cudaMemcpyAsync(e->sync_host, e->sync, bytes, cudaMemcpyDeviceToHost, e->stream), "barrier state D2H");
+    ECK(cudaMemsetAsync(e->sync, 0, bytes, e->stream), "barrier state");
+    ECK(cudaStreamSynchronize(e->stream), "ensemble sync");
+    for (int c = 0; c < jp_ensemble::kSyncSlots; ++c)
+        if (e->sync_host[c].err)
+            return fail(JP_ERR_TIMEOUT, "persistent coarse steps: a grid barrier wait ran past %lld ns (launch %d, "
+                        "phase %d of coarse step %d)", e->limit_ns, c, e->sync_host[c].phase + 1, e->sync_host[c].step);
+    return JP_OK;
 }
 
 jp_status jp_ensemble_add(jp_ensemble* e, jp_solver* s) {
@@ -162,11 +207,24 @@ jp_status jp_ensemble_step(jp_ensemble* e, int64_t nsteps) {
             }
         if (!placed) amr.push_back({m});
     }
+    // persistent launches: all nsteps coarse steps of a group at once
+    std::vector<bool> in_persist(amr.size(), false);
+    if (e->persist && nsteps > 0)
+        for (size_t k = 0; k < amr.size(); ++k) {
+            bool ok = true;
+            for (jp_solver* m : amr[k]) ok = ok && amr_persist_ok(m);
+            if (!ok) continue;
+            jp_status st = amr_persist_steps(amr[k], std::vector<long long>(amr[k].size(), nsteps), e->stream, e->sync,
+                                             jp_ensemble::kSyncSlots, e->limit_ns, e->persist_grid);
+            if (st != JP_OK) return st;
+            in_persist[k] = true;
+        }
     for (int64_t i = 0; i < nsteps; ++i) {
         jp_status st = batched_step(uni, e->stream);
         if (st != JP_OK) return st;
-        for (auto& g : amr) {
-            st = amr_batch_step(g, e->stream, &e->fk);
+        for (size_t k = 0; k < amr.size(); ++k) {
+            if (in_persist[k]) continue;
+            st = amr_batch_step(amr[k], e->stream, &e->fk);
             if (st != JP_OK) return st;
         }
     }

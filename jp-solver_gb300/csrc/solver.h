@@ -12,6 +12,9 @@
 
 namespace jp {
 struct AmrState;
+namespace amr {
+struct PersistSync;
+}
 
 jp_status fail(jp_status st, const char* fmt, ...);
 jp_status cuda_fail(cudaError_t e, const char* what);
@@ -127,6 +130,16 @@ struct AmrFork {
 // stages on fork->side when a fork is given)
 jp_status amr_batch_step(const std::vector<jp_solver*>& members, cudaStream_t st, const AmrFork* fork = nullptr);
 bool amr_batch_compatible(const jp_solver* a, const jp_solver* b);
+// whether a solver's coarse step can run in the persistent launch (amr_persist_supported)
+bool amr_persist_ok(const jp_solver* s);
+// steps[i] coarse steps of members[i] (batch-compatible, amr_persist_ok) in persistent launches on
+// `st`, up to kAmrBatchMax members per launch; launch c waits at its grid barriers on sync[c] (of
+// nsync, zeroed by the caller once: the error fields stay set until the caller clears them), at most
+// limit_ns per wait; grid = CTAs per launch (0: all that can be resident).  *launches (optional)
+// counts the launches.
+jp_status amr_persist_steps(const std::vector<jp_solver*>& members, const std::vector<long long>& steps,
+                            cudaStream_t st, amr::PersistSync* sync, int nsync, long long limit_ns, int grid,
+                            int* launches = nullptr);
 jp_status amr_prepare_diag(jp_solver* s);
 jp_status amr_graph_step_on(jp_solver* s, cudaStream_t st);
 jp_status amr_save_state(jp_solver* s, std::FILE* f);

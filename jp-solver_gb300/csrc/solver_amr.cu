@@ -906,6 +906,94 @@ jp_status amr_batch_step(const std::vector<jp_solver*>& ms, cudaStream_t st, con
     return JP_OK;
 }
 
+bool amr_persist_ok(const jp_solver* s) {
+    const AmrState* a = s->amr;
+    const bool skip_restrict = s->cfg.flags & JP_FLAG_SKIP_RESTRICT;
+    return amr_persist_supported(a->MB, a->vec, !skip_restrict && can_fuse_restrict(a->MB),
+                                 (s->cfg.flags & JP_FLAG_SKIP_PREP) != 0);
+}
+
+// base_step's sequence for many solves and several coarse steps each in one cooperative launch per
+// kAmrBatchMax solves (amr_persist.cuh): the members' arrays and device counts, ordered by their step
+// counts (descending), and afterwards the coarse ping-pong of every member with an odd count swapped.
+jp_status amr_persist_steps(const std::vector<jp_solver*>& ms, const std::vector<long long>& steps, cudaStream_t st,
+                            PersistSync* sync, int nsync, long long limit_ns, int grid, int* launches) {
+    if (ms.size() != steps.size()) return fail(JP_ERR_INVALID, "persistent steps: %zu members, %zu step counts",
+                                               ms.size(), steps.size());
+    std::vector<size_t> order;
+    for (size_t i = 0; i < ms.size(); ++i) {
+        if (steps[i] < 0 || steps[i] > (1LL << 20)) return fail(JP_ERR_INVALID, "persistent steps: %lld coarse steps",
+                                                              steps[i]);
+        if (!amr_persist_ok(ms[i]) || !amr_batch_compatible(ms[0], ms[i]))
+            return fail(JP_ERR_UNSUPPORTED, "persistent coarse steps: MB=8, rows, fused restrictions, one storage");
+        if (steps[i] > 0) order.push_back(i);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return steps[x] > steps[y]; });
+    const size_t chunks = (order.size() + kAmrBatchMax - 1) / kAmrBatchMax;
+    if ((long long)chunks > nsync) return fail(JP_ERR_CAPACITY, "persistent steps: %zu launches, %d barrier slots",
+                                              chunks, nsync);
+    for (size_t c = 0; c < chunks; ++c) {
+        AmrPersist P;
+        P.sync = sync + c;
+        P.limit_ns = limit_ns;
+        for (size_t k = c * kAmrBatchMax; k < order.size() && k < (c + 1) * kAmrBatchMax; ++k) {
+            const AmrState* a = ms[order[k]]->amr;
+            PersistMember& M = P.m[P.count++];
+            std::memset(&M, 0, sizeof M);
+            M.c0[0] = a->c0a;
+            M.c0[1] = a->c0b;
+            M.prep0 = a->prep0;
+            M.gh1 = a->gh1;
+            M.f1a = a->f1a;
+            M.f1b = a->f1b;
+            M.prep1 = a->prep1;
+            M.gh2 = a->gh2;
+            M.f2a = a->f2a;
+            M.f2b = a->f2b;
+            M.pc0 = a->pc0;
+            M.pc1 = a->pc1;
+            M.fl1 = a->fl1;
+            M.fl2 = a->fl2;
+            M.pcb = a->pcb;
+            M.oct = a->oct;
+            M.l2pl1 = a->l2pl1;
+            M.l2oct = a->l2oct;
+            M.f1pos = a->f1pos;
+            M.l1grid = a->l1grid;
+            M.nb1 = a->nb1;
+            M.nb2 = a->nb2;
+            M.n_prep0 = a->step_cnt + SC_PREP0;
+            M.n_fill1 = a->step_cnt + SC_FILL1;
+            M.n_prep1 = a->step_cnt + SC_PREP1;
+            M.n_fill2 = a->step_cnt + SC_FILL2;
+            M.n_f1 = a->step_cnt + SC_NF1;
+            M.n_f2 = a->step_cnt + SC_NF2;
+            M.cgx = a->cgx;
+            M.n = a->N;
+            M.l1gx = a->l1gx;
+            M.n1 = a->N1;
+            M.cnb0 = a->cnb0;
+            M.steps = (int)steps[order[k]];
+            M.om0 = a->om0;
+            M.om1 = a->om1;
+            M.om2 = a->om2;
+            M.nqs01 = float(a->nqs01);
+            M.nqs12 = float(a->nqs12);
+            M.nqi21 = float(a->nqi21);
+            M.nqi10 = float(a->nqi10);
+            P.maxsteps = std::max(P.maxsteps, M.steps);
+        }
+        ACK(cudaMemsetAsync(P.sync, 0, kPersistResetBytes, st), "persistent barrier reset");
+        ACK(amr_persist_launch(ms[0]->amr->storage, ms[0]->amr->MB, P, grid, st, nullptr), "persistent coarse steps");
+        if (launches) ++*launches;
+    }
+    for (size_t i = 0; i < ms.size(); ++i) {
+        if (steps[i] & 1) std::swap(ms[i]->amr->c0a, ms[i]->amr->c0b);
+        ms[i]->step_count += steps[i];
+    }
+    return JP_OK;
+}
+
 bool amr_batch_compatible(const jp_solver* a, const jp_solver* b) {
     const int skip = JP_FLAG_SKIP_PREP | JP_FLAG_SKIP_RESTRICT;
     return a->amr->MB == b->amr->MB && a->amr->storage == b->amr->storage && a->amr->tpb == b->amr->tpb &&

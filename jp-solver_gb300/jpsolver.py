@@ -129,6 +129,8 @@ SIGNATURES = {
     "jp_ensemble_add": (C.c_int, [C.c_void_p, C.c_void_p]),
     "jp_ensemble_remove": (C.c_int, [C.c_void_p, C.c_void_p]),
     "jp_ensemble_step": (C.c_int, [C.c_void_p, C.c_int64]),
+    "jp_ensemble_set_persistent": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_int32]),
+    "jp_ensemble_sync": (C.c_int, [C.c_void_p]),
     "jp_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     "jp_server_destroy": (None, [C.c_void_p]),
     "jp_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request)]),
@@ -377,6 +379,14 @@ class Ensemble:
 
     def step(self, n: int = 1) -> None:
         _check(lib().jp_ensemble_step(self.h, n))
+
+    def set_persistent(self, mode: int = 1, wait_limit_ns: int = 0, grid: int = 0) -> None:
+        """mode 1: AMR members' coarse steps in one persistent launch per jp_ensemble_step."""
+        _check(lib().jp_ensemble_set_persistent(self.h, mode, wait_limit_ns, grid))
+
+    def sync(self) -> None:
+        """Wait for the queued steps; raises JPError (JP_ERR_TIMEOUT = 6) if a barrier gave up."""
+        _check(lib().jp_ensemble_sync(self.h))
 
     def close(self) -> None:
         if self.h:
