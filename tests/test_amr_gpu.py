@@ -398,6 +398,58 @@ def test_buffer_dilates_the_sensor_marks(layers):
     assert res[layers]["counts"]["nref1"] >= res[0]["counts"]["nref1"]
 
 
+def buffer_level2_spec(sen1, deep, f1pos, l1grid, l1gx, frac2, cap, layers):
+    """The level-2 marks of --buffer N, written out: the sensor threshold over the deep level-1
+    blocks (tgt = min(cap, max(1, int(frac2 * ndeep))), thr = the (ndeep - tgt)-th smallest, marks =
+    deep and sensor >= thr), then N dilation layers over the periodic level-1 grid, each marking a
+    deep block when it or one of its 26 neighbour positions holds a marked level-1 block."""
+    d = deep != 0
+    vals = np.sort(sen1[d])
+    nd = vals.size
+    tgt = max(1, int(frac2 * nd))
+    if cap is not None:
+        tgt = min(cap, tgt)
+    ref = (d & (sen1 >= vals[nd - tgt])).astype(np.int32)
+    px, py, pz = f1pos % l1gx, (f1pos // l1gx) % l1gx, f1pos // (l1gx * l1gx)
+    for _ in range(layers):
+        out = ref.copy()
+        for dz in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    q = (((pz + dz) % l1gx) * l1gx + (py + dy) % l1gx) * l1gx + (px + dx) % l1gx
+                    nb = l1grid[q]
+                    out |= np.where(nb >= 0, ref[np.maximum(nb, 0)], 0)
+        ref = np.where(d, out, 0).astype(np.int32)
+    return ref
+
+
+@pytest.mark.parametrize("layers", [1, 2])
+def test_buffer_level2_marks_match_written_spec(layers):
+    # --buffer N on level 2, pinned exactly: at the initial build (threshold without a cap) and at a
+    # regrid (capped by cap_nref1), the engine's level-2 marks equal the written specification
+    # computed from its own level-1 grid, sensor and deep mask; nf2 follows from them
+    n, f2 = 48, 0.1
+    with J.Solver("amr", n=n, re=800.0, l1_mode="sensor", l2_mode="sensor", frac1=0.2, frac2=f2, develop_steps=2,
+                  max_gb=64.0, buffer=layers, flags=J.FLAG_DEFER_INIT) as e:
+        e.set_sensor_override(*O.random_sensor_fields(n, seed=19))
+        e.init_tgv()
+        l1gx = 2 * n // 8
+        for where in ("initial build", "regrid"):
+            cap = None
+            if where == "regrid":
+                cap = e.counts()["cap_nref1"]          # the cap the regrid's threshold uses
+                e.step(1)
+                e.set_sensor_override(*O.random_sensor_fields(n, seed=23))
+                e.regrid()
+            c = e.counts()
+            want = buffer_level2_spec(e.sensor(1), e.table("deep"), e.table("f1pos"), e.table("l1grid"), l1gx, f2,
+                                      cap, layers)
+            got = e.table("ref1")
+            np.testing.assert_array_equal(got, want, err_msg=where)
+            assert c["nf2"] == 8 * int(want.sum()) and c["nref1"] == int(want.sum())
+            assert int(want.sum()) > int(np.sum(e.table("deep") != 0) * f2)   # the buffer added blocks
+
+
 @pytest.mark.parametrize("mb,storage", [(8, "fp32"), (8, "fp16"), (16, "fp32"), (16, "bf16")])
 def test_row_steps_bit_exact_with_cell_steps(mb, storage):
     # the fine steps on rows of four cells per thread (vector loads, shuffles at the row inside, the
