@@ -407,6 +407,83 @@ def bench_precision(J, args, device: int) -> dict:
     return out
 
 
+def precision_summary(J, device: int, every: int) -> dict:
+    """The storage precision figures of the headline line: the Re=1600, t*=12 run at N=256 in FP64,
+    FP32, shifted FP16 and shifted BF16 storage, each with its enstrophy-peak time error against the
+    FP64 run (bar for FP16: 0.05 t*), its largest energy-curve error and its mass drift."""
+    class Args:
+        pass
+
+    args = Args()
+    args.n, args.every = 256, every
+    pr = bench_precision(J, args, device)
+    out = {"n": 256, "re": RE, "tstar": 12.0, "every_steps": every, "dt_star_per_sample": pr["dt_star_per_sample"],
+           "fp64": {"peak_tstar": pr["fp64"]["peak_tstar"], "mass_drift": pr["fp64"]["mass_drift"],
+                    "seconds": pr["fp64"]["seconds"]}}
+    for st in ("fp32", "fp16", "bf16"):
+        out[st] = {k: pr[st][k] for k in ("peak_tstar", "peak_tstar_error", "energy_max_rel_error",
+                                          "enstrophy_max_rel_error", "mass_drift", "energy_monotonic")}
+    return out
+
+
+ENSEMBLE_SHAPES = {  # AMR ensembles of the served-ensemble shapes: (coarse N, count), sensor/sensor, 0.3/0.1
+    "served": [(16, 8), (24, 16), (32, 16), (48, 4)],
+    "n16x8": [(16, 8)],
+    "n24_32x32": [(24, 16), (32, 16)],
+    "n48x4": [(48, 4)],
+    "n96x1": [(96, 1)],
+}
+
+
+def bench_ensemble(J, shape: str, calls: int, k: int, device: int) -> dict:
+    """Coarse steps of an AMR ensemble (seeded sensor grids, FP32, MB=8) with one launch per stage
+    (per-stage) against one persistent launch per call of k coarse steps: device time per coarse step
+    of all members (host clock around the timed calls, synchronised at both ends) and GLUPS(work)."""
+    import numpy as np
+
+    out = {"shape": shape, "members": [list(x) for x in ENSEMBLE_SHAPES[shape]], "calls": calls,
+           "coarse_steps_per_call": k}
+    for mode, name in ((0, "per_stage"), (1, "persistent")):
+        solvers = []
+        seed = 0
+        for n0, cnt in ENSEMBLE_SHAPES[shape]:
+            for _ in range(cnt):
+                rng = np.random.default_rng(seed)
+                seed += 1
+                cgx = n0 // 8
+                s0 = rng.random(cgx ** 3, dtype=np.float32)
+                s1 = rng.random((2 * cgx) ** 3, dtype=np.float32)
+                s = J.Solver("amr", n=n0, re=1600.0, u0=U0, l1_mode="sensor", l2_mode="sensor", frac1=0.3, frac2=0.1,
+                             develop_steps=2, max_gb=64.0, device=device, flags=J.FLAG_DEFER_INIT)
+                s.set_sensor_override(s0, s1)
+                s.init_tgv()
+                solvers.append(s)
+        ens = J.Ensemble(device)
+        try:
+            ens.set_persistent(mode)
+            for s in solvers:
+                ens.add(s)
+            ens.step(2)
+            ens.sync()
+            l0 = J.launch_count()
+            t0 = time.perf_counter()
+            for _ in range(calls):
+                ens.step(k)
+            ens.sync()
+            dt = time.perf_counter() - t0
+            launches = J.launch_count() - l0
+            work = sum((c["cnb0"] + 2 * c["nf1"] + 4 * c["nf2"]) * 512 for c in (s.counts() for s in solvers))
+        finally:
+            ens.close()
+            for s in solvers:
+                s.close()
+        steps = calls * k
+        out[name] = {"us_per_coarse_step": dt / steps * 1e6, "glups_work": work * steps / dt / 1e9,
+                     "launches_per_coarse_step": launches / steps, "work_per_coarse_step": work}
+    out["speedup"] = out["per_stage"]["us_per_coarse_step"] / out["persistent"]["us_per_coarse_step"]
+    return out
+
+
 def cpu_baseline(n: int, steps: int) -> dict:
     """The oracle (CPU restatement of the reference's step, OpenMP) on this host's cores."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -423,7 +500,60 @@ def cpu_baseline(n: int, steps: int) -> dict:
     dt = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": n ** 3 * steps / dt / 1e9, "unit": "GLUPS", "cores": cores, "kind": "port",
+            "nproc": os.cpu_count(), "cpu_model": cpu_model(),
             "sample": "oracle FP32 step, N=%d cube, %d steps (%.1f s)" % (n, steps, dt)}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), read at run time."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        fields = dict(ln.split(":", 1) for ln in out.splitlines() if ":" in ln)
+        name = fields.get("Model name", "").strip()
+        vendor = fields.get("Vendor ID", "").strip()
+        if name:
+            return (vendor + " " + name).strip()
+    except (OSError, subprocess.SubprocessError, ValueError):
+        pass
+    import platform
+
+    return platform.machine() + " " + (platform.processor() or "unknown")
+
+
+def reference_gpu(n: int, steps: int) -> dict:
+    """The reference's own CUDA kernels (compiled from its checkout into oracle/_ref/*.cubin) rerun on
+    this GPU, timed with CUDA events: the uniform k_step at N=n (src/tgv3d_uniform.cu:41-61) and the
+    AMR base_step launch sequence (src/tgv3d_amr.cu:821-837) on the static gold case (N0=64 all/all,
+    Re=800) and on the dynamic case (N0=96 sensor/sensor, frac1 0.3, frac2 0.1, Re=1600, after the
+    300 develop steps; no regrid timed), work-normalised as the reference's --bench counts it."""
+    import ctypes as C
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    if not O.ref_amr_available():
+        return {"unavailable": "reference cubins not built (no reference checkout where build() ran)"}
+    p = O.params(n, RE, U0)
+    ms = O.ref_time(n, p["omega"], 3, steps, U0)
+    out = {"uniform": {"n": n, "kernel": "k_step (reference, MB=8)", "glups": n ** 3 * steps / (ms / 1e3) / 1e9,
+                       "ms_per_step": ms / steps, "steps": steps}}
+    cases = {"amr_static_gold": (64, 800.0, "all", "all", 0.35, 0.35),
+             "amr_dynamic": (96, 1600.0, "sensor", "sensor", 0.3, 0.1)}
+    for key, (n0, re, l1, l2, f1, f2) in cases.items():
+        b = O.AmrBackend("reference", n0, re, l1, l2, f1, f2, u0=U0, budget=float(1 << 40))
+        try:
+            c = b.counts()
+            work = (c["cnb0"] + 2 * c["nf1"] + 4 * c["nf2"]) * 512
+            t = C.c_float()
+            k = 10 if key == "amr_static_gold" else 100
+            rc = O.ref_amr().ref_amr_time(C.c_void_p(b.h), 2, k, C.byref(t))
+            if rc:
+                raise RuntimeError(O.ref().refrun_last_error().decode())
+        finally:
+            b.close()
+        out[key] = {"n0": n0, "glups_work": work * k / (t.value / 1e3) / 1e9, "ms_per_coarse_step": t.value / k,
+                    "work_per_coarse_step": work, "coarse_steps": k}
+    return out
 
 
 def main() -> int:
@@ -441,8 +571,14 @@ def main() -> int:
                     help="storage of the timed run (the headline is fp32)")
     ap.add_argument("--vec", type=int, default=0)
     ap.add_argument("--tpb", type=int, default=0)
-    ap.add_argument("--workload", default="uniform", choices=["uniform", "serve", "precision"])
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "serve", "precision", "ensemble"])
+    ap.add_argument("--shape", default="served", choices=list(ENSEMBLE_SHAPES),
+                    help="ensemble: the AMR members (coarse N x count)")
     ap.add_argument("--every", type=int, default=10, help="precision study: steps between diagnostics")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the storage precision study (FP16/BF16 against FP64 at N=256) in the headline line")
+    ap.add_argument("--reference-gpu", type=int, default=1,
+                    help="--impl reference: also time the reference's own CUDA kernels on this GPU (0: skip)")
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--seed", type=int, default=20261203)
@@ -466,12 +602,20 @@ def main() -> int:
             return 0
         steps = max(1, min(a.steps, 5))
         cb = cpu_baseline(n, steps)
+        rg = None
+        if a.reference_gpu:
+            try:
+                rg = reference_gpu(n, 20)
+            except Exception as exc:  # the CPU arm's line is still printed
+                rg = {"unavailable": "reference kernels failed: %s" % exc}
         line = {"metric": "GLUPS", "value": cb["value"], "unit": "GLUPS", "impl": "reference", "n_gpus": a.gpus,
                 "steps": steps, "warmup": a.warmup, "ms_per_step": 1e3 * n ** 3 / (cb["value"] * 1e9),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (analytic Taylor-Green initial state)", "config": config,
                 "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "GLUPS", "h2d_bytes_per_step": 0,
                                             "d2h_bytes_per_step": 0}}
+        if rg is not None:
+            line["reference_gpu"] = rg
         print(json.dumps(line))
         return 0
 
@@ -485,6 +629,19 @@ def main() -> int:
                 "data": "synthetic (analytic Taylor-Green initial state)",
                 "config": {"workload": "uniform TGV N=%d Re=%g t*=12, FP64/FP32/FP16/BF16 storage" % (pr["n"], RE)},
                 "precision": pr}
+        if rank == 0:
+            print(json.dumps(line))
+        return 0
+
+    if a.workload == "ensemble":
+        en = bench_ensemble(J, a.shape, max(1, a.steps // 8), 8, local)
+        line = {"metric": "AMR ensemble GLUPS(work)", "value": en["persistent"]["glups_work"], "unit": "GLUPS(work)",
+                "n_gpus": world, "steps": max(1, a.steps // 8) * 8, "warmup": 2,
+                "ms_per_step": en["persistent"]["us_per_coarse_step"] / 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded sensor grids of Taylor-Green solves)",
+                "config": {"workload": "AMR ensemble %s, sensor/sensor 0.3/0.1, FP32, MB=8" % a.shape},
+                "ensemble": en}
         if rank == 0:
             print(json.dumps(line))
         return 0
@@ -535,8 +692,9 @@ def main() -> int:
                      "bytes_per_update": BYTES_PER_UPDATE[a.storage],
                      "traffic": (traffic * n ** 3) if traffic else None},
         "variants": variants,
-        "e2e": ({"value": e2e["glups"] * world, "unit": "GLUPS", "h2d_bytes_per_step": e2e["h2d_bytes"],
-                 "d2h_bytes_per_step": e2e["d2h_bytes"], "lattice_steps_per_call": k,
+        "e2e": ({"value": e2e["glups"] * world, "unit": "GLUPS", "h2d_bytes_per_step": e2e["h2d_bytes"] // k,
+                 "d2h_bytes_per_step": e2e["d2h_bytes"] / k, "h2d_bytes_per_call": e2e["h2d_bytes"],
+                 "d2h_bytes_per_call": e2e["d2h_bytes"], "lattice_steps_per_call": k,
                  "calls": a.e2e_calls,
                  "overlap": "each call's H2D staged on a copy stream during the previous call's steps"}
                 if e2e else None),
@@ -545,6 +703,8 @@ def main() -> int:
     }
     if not a.no_amr and rank == 0:
         line["amr"] = bench_amr(J, local)
+    if not a.no_precision and rank == 0:
+        line["precision"] = precision_summary(J, local, a.every)
     if rank == 0 and world == 1 and a.cpu_steps > 0:
         line["cpu_baseline"] = cpu_baseline(n, a.cpu_steps)
     if rank == 0:
