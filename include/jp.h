@@ -324,7 +324,9 @@ typedef struct jp_server_config {
     double pool_gb;          /* HBM budget for admitted solves, GiB (0 = 75% of free memory) */
     int32_t tick_steps;      /* lattice steps the uniform solves advance per tick (default 64) */
     int32_t workers;         /* host threads that create and regrid AMR solves (0 = one per core, 4..32) */
-    int32_t reserved[6];
+    int32_t uniform_first;   /* 1: the uniform batches' stream at the highest priority and the AMR
+                                lanes at the lowest (the batches are the HBM-bound bulk); 0: equal */
+    int32_t reserved[5];
 } jp_server_config;
 typedef struct jp_request {
     int64_t id;

@@ -720,9 +720,14 @@ jp_status jp_server_create(const jp_server_config* cfg, jp_server** out) {
     if (sv->cfg.tick_steps <= 0) sv->cfg.tick_steps = 64;
     if (sv->cfg.workers <= 0) sv->cfg.workers = (int)std::min(32u, std::max(4u, std::thread::hardware_concurrency()));
     sv->t0 = std::chrono::steady_clock::now();
-    cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
+    // stream priorities: the solves' own streams (creation, regrids, read-backs) run at the highest;
+    // with uniform_first the uniform batches share it and the AMR lanes take the lowest
+    int lo = 0, hi = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithPriority(&sv->stream, cudaStreamNonBlocking, sv->cfg.uniform_first ? hi : lo);
     for (int l = 0; l < jp_server::kLanes && e == cudaSuccess; ++l) {
-        e = cudaStreamCreateWithFlags(&sv->lane[l].stream, cudaStreamNonBlocking);
+        e = cudaStreamCreateWithPriority(&sv->lane[l].stream, cudaStreamNonBlocking, lo);
         if (e == cudaSuccess) e = sv->lane[l].fk.create(sv->lane[l].stream);
         for (auto& d : sv->lane[l].adiag)
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d.done, cudaEventDisableTiming);

@@ -69,7 +69,8 @@ class AmrCounts(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("max_active", C.c_int32), ("pool_gb", C.c_double),
-                ("tick_steps", C.c_int32), ("workers", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("tick_steps", C.c_int32), ("workers", C.c_int32), ("uniform_first", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class ServerStats(C.Structure):
@@ -404,9 +405,10 @@ class Server:
     """Continuous-batching solve server (jp_server_*)."""
 
     def __init__(self, device: int = 0, max_active: int = 0, pool_gb: float = 0.0, tick_steps: int = 64,
-                 workers: int = 0):
+                 workers: int = 0, uniform_first: int = 0):
         c = ServerConfig()
         c.device, c.max_active, c.pool_gb, c.tick_steps, c.workers = device, max_active, pool_gb, tick_steps, workers
+        c.uniform_first = uniform_first
         h = C.c_void_p()
         _check(lib().jp_server_create(C.byref(c), C.byref(h)))
         self.h = h
