@@ -253,7 +253,7 @@ __global__ void k_dilate(const int* __restrict__ ref0, int cnb0, int cgx, const 
 // ordered compaction of the two flag ranges into the skin lists (copy_if over a counting iterator)
 __global__ void __launch_bounds__(kScanThreads) k_compact_skins(const int* __restrict__ flags, int cnb0, int nf1,
                                                                int* __restrict__ skin0, int* __restrict__ skin1,
-                                                               AdaptCounts* __restrict__ counts) {
+                                                               int* __restrict__ rest1, AdaptCounts* __restrict__ counts) {
     for (int part = 0; part < 2; ++part) {
         const int* fl = part == 0 ? flags : flags + cnb0;
         const int n = part == 0 ? cnb0 : nf1;
@@ -265,11 +265,15 @@ __global__ void __launch_bounds__(kScanThreads) k_compact_skins(const int* __res
             int tot;
             const int ex = block_exclusive_scan(v, tot);
             if (v) out[carry + ex] = i;
+            else if (part == 1 && rest1 && i < n) rest1[i - carry - ex] = i;  // i minus the skins before it
             carry += tot;
         }
         if (threadIdx.x == 0) {
             if (part == 0) counts->n_skin0 = carry;
-            else counts->n_skin1 = carry;
+            else {
+                counts->n_skin1 = carry;
+                counts->n_rest1 = n - carry;
+            }
         }
     }
 }
@@ -411,9 +415,10 @@ cudaError_t adapt_scatter_l2(const int* ref1, const int* rank, int nf1, int cap2
     return cudaGetLastError();
 }
 cudaError_t adapt_skins(const int* ref0, int cnb0, int cgx, const int* ref1, const int* f1pos, const int* l1grid,
-                        int nf1, int l1gx, int* flags, int* skin0, int* skin1, AdaptCounts* counts, cudaStream_t st) {
+                        int nf1, int l1gx, int* flags, int* skin0, int* skin1, AdaptCounts* counts, cudaStream_t st,
+                        int* rest1) {
     k_dilate<<<grid_for(cnb0 + nf1, 256), 256, 0, st>>>(ref0, cnb0, cgx, ref1, f1pos, l1grid, nf1, l1gx, flags);
-    k_compact_skins<<<1, kScanThreads, 0, st>>>(flags, cnb0, nf1, skin0, skin1, counts);
+    k_compact_skins<<<1, kScanThreads, 0, st>>>(flags, cnb0, nf1, skin0, skin1, rest1, counts);
     note_launch(2);
     return cudaGetLastError();
 }

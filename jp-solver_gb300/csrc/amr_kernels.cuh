@@ -458,14 +458,17 @@ struct RowGeo {
     static constexpr int TPB = SEGS < 256 ? SEGS : 256;          // threads per CTA
 };
 
-template <int MB, class ST, bool FUSE, bool WALK>
+// LIST: the blocks stepped are blist[0 .. *nlim) (a subset of the level, e.g. its skin blocks) instead
+// of 0 .. *nlim.
+template <int MB, class ST, bool FUSE, bool WALK, bool LIST = false>
 __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restrict__ fa,
                                                  typename ST::raw* __restrict__ fbuf,
                                                  const typename ST::raw* __restrict__ gh,
                                                  const int* __restrict__ nbtab, const int* __restrict__ parent,
                                                  const int* __restrict__ poct, float om,
                                                  typename ST::raw* __restrict__ parent_pool, float nqi,
-                                                 const int* __restrict__ nlim, int blk, int stride) {
+                                                 const int* __restrict__ nlim, int blk, int stride,
+                                                 const int* __restrict__ blist = nullptr) {
     using G = Geo<MB>;
     using RG = RowGeo<MB>;
     using raw = typename ST::raw;
@@ -476,7 +479,8 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
     // WALK: blocks blk, blk + gridDim.x, ... (a resident grid walks the level; the loop bound is
     // CTA-uniform, so the barriers of the fused restriction stay uniform); else the one block blk.
     // The count is re-read from L1 and the stride is gridDim.x, so the loop holds one register.
-    for (int b = blk; b < __ldg(nlim); b += (WALK ? (int)gridDim.x : stride)) {
+    for (int bi = blk; bi < __ldg(nlim); bi += (WALK ? (int)gridDim.x : stride)) {
+    const int b = LIST ? __ldg(blist + bi) : bi;
     const int* nbrow = nbtab + (size_t)b * 27;
     for (int seg = threadIdx.x; seg < RG::SEGS; seg += RG::TPB) {
         const int s = seg % RG::SPR, r = seg / RG::SPR, j = r % MB, k = r / MB, i0 = 4 * s;
@@ -543,7 +547,7 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
     if (FUSE) {
         __syncthreads();
         restrict_octant<MB, ST>(sf, parent_pool + (size_t)parent[b] * Q * G::MB3, poct[b], nqi);
-        if (WALK && b + (int)gridDim.x < __ldg(nlim)) __syncthreads();  // the next block stages into sf
+        if (WALK && bi + (int)gridDim.x < __ldg(nlim)) __syncthreads();  // the next block stages into sf
     }
     if (!WALK) break;
     }
@@ -560,6 +564,21 @@ __global__ void __launch_bounds__(RowGeo<MB>::TPB, (rows_min_blocks<MB, ST>())) 
     typename ST::raw* __restrict__ parent_pool, float nqi, const int* __restrict__ nlim) {
     d_step_fine_rows<MB, ST, FUSE, WALK>(fa, fbuf, gh, nbtab, parent, poct, om, parent_pool, nqi, nlim,
                                          (int)blockIdx.x, (int)gridDim.x);
+}
+
+// The non-fused walking rows step over a block list (blist[0 .. *nlim)): part of a level stepped on
+// its own, e.g. the level-1 blocks outside the skin beside the level-2 work that only the skin feeds.
+template <int MB, class ST>
+__global__ void __launch_bounds__(RowGeo<MB>::TPB, (rows_min_blocks<MB, ST>())) k_step_fine_rows_listed(
+    const typename ST::raw* __restrict__ fa, typename ST::raw* __restrict__ fbuf, const typename ST::raw* __restrict__ gh,
+    const int* __restrict__ nbtab, float om, const int* __restrict__ nlim, const int* __restrict__ blist) {
+    d_step_fine_rows<MB, ST, false, true, true>(fa, fbuf, gh, nbtab, nullptr, nullptr, om, nullptr, 0.f, nlim,
+                                               (int)blockIdx.x, (int)gridDim.x, blist);
+}
+template <int MB, class ST>
+static int rows_listed_grid_cap() {
+    static const int cap = resident_grid(k_step_fine_rows_listed<MB, ST>, RowGeo<MB>::TPB, 0);
+    return cap;
 }
 
 // The grid of the walking rows kernels (resident CTAs): each CTA walks the level's blocks, so the
@@ -880,6 +899,9 @@ static void launch_rows(const AmrLaunch& L) {
         else
             k_step_fine_rows<MB, ST, true, true><<<std::min(L.nblocks, cap), T, sm, L.st>>>(
                 CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.t0, L.t1, L.omega, POOL(L.out2), L.scale, L.nlim);
+    } else if (L.list) {  // the listed blocks only (L.nblocks: the list's capacity)
+        k_step_fine_rows_listed<MB, ST><<<std::min(L.nblocks, rows_listed_grid_cap<MB, ST>()), T, 0, L.st>>>(
+            CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.omega, L.nlim, L.list);
     } else {
         k_step_fine_rows<MB, ST, false, true><<<std::min(L.nblocks, rows_grid_cap<MB, ST, false>()), T, 0, L.st>>>(
             CPOOL(L.in), POOL(L.out), CPOOL(L.aux), L.nbt, L.t0, L.t1, L.omega, nullptr, 0.f, L.nlim);
@@ -967,6 +989,7 @@ static cudaError_t dispatch(const AmrLaunch& L, int op) {
             if constexpr (MB >= 8) {
                 if constexpr (MB <= 8) rows_grid_cap<MB, ST, true>();
                 rows_grid_cap<MB, ST, false>();
+                rows_listed_grid_cap<MB, ST>();
             }
             return cudaGetLastError();
         default:

@@ -16,7 +16,8 @@ enum AmrOp {
                        // nlim = its length, nblocks = its capacity
     OP_FILL_L2,        // in = prep1, out = gh2; t0 l2pl1, t1 l2oct, t2 f1pos, t3 l1grid; list, nlim, nblocks as
                        // OP_FILL_L1
-    OP_STEP_L1,        // in -> out, aux = gh1, nbt = level-1 table; t0 pcb, t1 oct; out2 = c0 restricts (scale nqi)
+    OP_STEP_L1,        // in -> out, aux = gh1, nbt = level-1 table; t0 pcb, t1 oct; out2 = c0 restricts (scale nqi);
+                       // list (rows mapping, no out2): only the blocks list[0 .. *nlim), nblocks = its capacity
     OP_STEP_L2,        // in -> out, aux = gh2, nbt = level-2 table; t0 l2pl1, t1 l2oct; out2 = f1 restricts
     OP_RESTRICT,       // out = coarse, in = fine; list = refined coarse blocks, t0 = fof; scale = nqi
     OP_SEED_L1,        // in = old f1 (migrate) , out = new f1, aux = c0; t0 pcb, t1 oct, t2 old ref0|null, t3 old fof0
@@ -142,7 +143,8 @@ int default_step_vec(int mb);
 struct AdaptCounts {
     int nref0, nf1, nref1, nf2, n_skin0, n_skin1, ndeep, err;
     float thr0, thr1;
-    int pad[6];
+    int n_rest1;  // level-1 blocks outside the skin (adapt_skins' rest1 list)
+    int pad[5];
 };
 enum { ADAPT_ERR_CAP1 = 1, ADAPT_ERR_CAP2 = 2 };
 
@@ -165,9 +167,11 @@ cudaError_t adapt_scan_l2(const int* ref1, int nf1, int* rank, AdaptCounts* coun
 // k_scatter_L2 from the ranks of adapt_scan_l2; error and no scatter if nf2 > cap2
 cudaError_t adapt_scatter_l2(const int* ref1, const int* rank, int nf1, int cap2, int* fof1, int* rl1, int* l2pl1,
                              int* l2oct, AdaptCounts* counts, cudaStream_t st);
-// skin lists: blocks that are refined or have a refined 26-neighbour, ascending (k_dilate + copy_if)
+// skin lists: blocks that are refined or have a refined 26-neighbour, ascending (k_dilate + copy_if);
+// rest1 (optional): the other level-1 blocks, ascending, their count in counts->n_rest1
 cudaError_t adapt_skins(const int* ref0, int cnb0, int cgx, const int* ref1, const int* f1pos, const int* l1grid,
-                        int nf1, int l1gx, int* flags, int* skin0, int* skin1, AdaptCounts* counts, cudaStream_t st);
+                        int nf1, int l1gx, int* flags, int* skin0, int* skin1, AdaptCounts* counts, cudaStream_t st,
+                        int* rest1 = nullptr);
 // set n ints to v
 cudaError_t adapt_fill(int* p, int v, long long n, cudaStream_t st);
 // fill list of a fine level: the ghost-shell cells (faces, edges) of the nf blocks whose slot of the

@@ -38,6 +38,7 @@ struct AmrState {
     int *ref0 = nullptr, *fof0 = nullptr, *rl0 = nullptr, *pcb = nullptr, *oct = nullptr, *f1pos = nullptr,
         *l1grid = nullptr, *ref1 = nullptr, *fof1 = nullptr, *rl1 = nullptr, *l2pl1 = nullptr, *l2oct = nullptr,
         *skin0 = nullptr, *skin1 = nullptr;
+    int* rest1 = nullptr;  // level-1 blocks outside the skin, ascending (adapt_skins), SC_REST1 of them
     int *o_ref0 = nullptr, *o_fof0 = nullptr, *o_l1grid = nullptr, *o_ref1 = nullptr, *o_fof1 = nullptr;
     int *rank = nullptr, *deep = nullptr, *flags = nullptr;
     int *nb1 = nullptr, *nb2 = nullptr;  // same-level neighbour tables of the fine levels (27 per block)
@@ -70,7 +71,7 @@ struct AmrState {
 // SC_COUNT entries come from the host (upload_counts); the fill-list lengths are written on the device
 // (SC_PREP0/1: interface cells of the prep lists, whose block counts are SC_PBLK0/1)
 enum { SC_NF1 = 0, SC_NF2, SC_SKIN0, SC_SKIN1, SC_NREF0, SC_NREF1, SC_COUNT, SC_FILL1 = SC_COUNT, SC_FILL2, SC_PREP0,
-       SC_PREP1, SC_PBLK0, SC_PBLK1, SC_ALL };
+       SC_PREP1, SC_PBLK0, SC_PBLK1, SC_REST1, SC_ALL };
 // CTAs per member of a batched prep or fill (its threads walk the member's cell list)
 constexpr int kBatchPrepCtas = 64;
 
@@ -214,10 +215,12 @@ static_assert(offsetof(AdaptCounts, n_skin1) == offsetof(AdaptCounts, n_skin0) +
 static jp_status skins(jp_solver* s) {
     AmrState* a = s->amr;
     ACK(adapt_skins(a->ref0, a->cnb0, a->cgx, a->ref1, a->f1pos, a->l1grid, a->nf1, a->l1gx, a->flags, a->skin0,
-                    a->skin1, a->cnt_dev, s->stream), "skins");
+                    a->skin1, a->cnt_dev, s->stream, a->rest1), "skins");
     TRY(upload_counts(s));
     ACK(cudaMemcpyAsync(a->step_cnt + SC_SKIN0, &a->cnt_dev->n_skin0, 2 * sizeof(int), cudaMemcpyDeviceToDevice,
                         s->stream), "skin counts");
+    ACK(cudaMemcpyAsync(a->step_cnt + SC_REST1, &a->cnt_dev->n_rest1, sizeof(int), cudaMemcpyDeviceToDevice,
+                        s->stream), "rest count");
     TRY(prep_lists(s));
     ACK(cudaMemcpyAsync(a->cnt_host, a->cnt_dev, sizeof(AdaptCounts), cudaMemcpyDeviceToHost, s->stream), "counts D2H");
     a->skins_pending = true;
@@ -288,7 +291,8 @@ static jp_status set_cap1(jp_solver* s, int cap, bool keep) {
     TRY(regrow(s, a->prep1, pf(a, cap * blk), 0));
     TRY(regrow(s, a->o_ref1, cap, old));           // snapshots of the previous grid
     TRY(regrow(s, a->o_fof1, cap, old));
-    int** scratch[] = {&a->pcb, &a->oct, &a->rl0, &a->f1pos, &a->ref1, &a->fof1, &a->rl1, &a->skin1, &a->deep};
+    int** scratch[] = {&a->pcb, &a->oct, &a->rl0, &a->f1pos, &a->ref1, &a->fof1, &a->rl1, &a->skin1, &a->rest1,
+                       &a->deep};
     for (int** t : scratch) TRY(regrow(s, *t, cap, 0));
     TRY(regrow(s, a->sen1, cap, 0));
     TRY(regrow(s, a->rank, std::max(a->cnb0, cap), 0));
@@ -577,6 +581,8 @@ cudaError_t AmrFork::create(cudaStream_t like) {
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, prio);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork2, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join2, cudaEventDisableTiming);
     return e;
 }
 
@@ -585,9 +591,11 @@ void AmrFork::destroy() {
     if (side) cudaStreamSynchronize(side);
     if (fork) cudaEventDestroy(fork);
     if (join) cudaEventDestroy(join);
+    if (fork2) cudaEventDestroy(fork2);
+    if (join2) cudaEventDestroy(join2);
     if (side) cudaStreamDestroy(side);
     side = nullptr;
-    fork = join = nullptr;
+    fork = join = fork2 = join2 = nullptr;
 }
 
 // Takes a side branch back into a stream (or a capture) on every return, errors included.
@@ -656,6 +664,12 @@ static jp_status base_step(jp_solver* s) {
     ACK(cudaEventRecord(a->fk.join, a->fk.side), "join");
     JoinOnExit join{s->stream, a->fk.join};
     TRY(st0);
+    // The first level-1 substep in two parts: its skin blocks (the only ones the next level-2 pair
+    // reads, through the prep cells, and the only ones that pair restricts into), then the others on
+    // the side branch, beside the whole second level-2 pair; they join before the last level-1
+    // substep.  Each block is stepped as in one launch (rows mapping).
+    const bool split = a->MB >= 8 && (a->vec ? a->vec : default_step_vec(a->MB)) == 4;
+    JoinOnExit join2{s->stream, a->fk.join2, false};
     for (int s1 = 0; s1 < 2; ++s1) {
         if (!skip_prep) {
             AmrLaunch L;
@@ -713,6 +727,7 @@ static jp_status base_step(jp_solver* s) {
             TRY(launch(s, OP_RESTRICT, R));
         }
         if (s1 == 0) TRY(join.now());
+        if (s1 == 1 && join2.pending) TRY(join2.now());
         AmrLaunch S;
         S.nblocks = a->cap1;
         S.nlim = cnt + SC_NF1;
@@ -729,7 +744,23 @@ static jp_status base_step(jp_solver* s) {
             S.out2 = a->c0a;
             S.scale = float(a->nqi10);
         }
-        TRY(launch(s, OP_STEP_L1, S));
+        if (s1 == 0 && split) {
+            AmrLaunch K = S;  // the skin blocks
+            K.list = a->skin1;
+            K.nlim = cnt + SC_SKIN1;
+            TRY(launch(s, OP_STEP_L1, K));
+            ACK(cudaEventRecord(a->fk.fork2, s->stream), "fork");
+            ACK(cudaStreamWaitEvent(a->fk.side, a->fk.fork2, 0), "fork");
+            AmrLaunch R = S;  // the others, on the side branch
+            R.list = a->rest1;
+            R.nlim = cnt + SC_REST1;
+            const jp_status sr = launch(s, OP_STEP_L1, R, a->fk.side);
+            ACK(cudaEventRecord(a->fk.join2, a->fk.side), "join");
+            join2.pending = true;
+            TRY(sr);
+        } else {
+            TRY(launch(s, OP_STEP_L1, S));
+        }
         std::swap(a->f1a, a->f1b);
     }
     if (skip_restrict || fuse) return JP_OK;
@@ -1108,7 +1139,7 @@ jp_status amr_create(jp_solver* s) {
     int** cnb_tabs[] = {&a->ref0, &a->fof0, &a->o_ref0, &a->o_fof0, &a->skin0};
     for (int** t : cnb_tabs) TRY(dalloc(a, t, (size_t)a->cnb0, "cudaMalloc table"));
     int** cap_tabs[] = {&a->pcb, &a->oct, &a->rl0, &a->f1pos, &a->ref1, &a->fof1, &a->o_ref1, &a->o_fof1,
-                        &a->rl1, &a->skin1, &a->deep};
+                        &a->rl1, &a->skin1, &a->rest1, &a->deep};
     for (int** t : cap_tabs) TRY(dalloc(a, t, (size_t)a->cap1, "cudaMalloc table"));
     TRY(dalloc(a, &a->l1grid, (size_t)a->NG1, "cudaMalloc l1grid"));
     TRY(dalloc(a, &a->o_l1grid, (size_t)a->NG1, "cudaMalloc l1grid"));
@@ -1417,10 +1448,10 @@ jp_status amr_load_state(jp_solver* s, std::FILE* f) {
         if (!fread_all(f, raw.data(), pl.second)) return fail(JP_ERR_INVALID, "state file truncated");
         if (pl.second) ACK(cudaMemcpy(pl.first, raw.data(), pl.second, cudaMemcpyHostToDevice), "pool H2D");
     }
-    TRY(upload_counts(s));
     TRY(fill_lists(s));
-    TRY(prep_lists(s));
+    TRY(skins(s));  // the skin lists again (the same as stored) with the level-1 rest list, counts, prep lists
     ACK(wait_stream(s), "load");
+    skins_landed(a);
     reset_graphs(a);
     update_bytes(s);
     return JP_OK;
