@@ -110,7 +110,8 @@ jp_status jp_load_state(jp_solver* s, const char* path) {
         }
         JP_CK(cudaStreamSynchronize(s->stream), "load");
         JP_CK(cudaMemcpy(s->fa, raw.data(), bytes, cudaMemcpyHostToDevice), "populations H2D");
-        s->staged = false;  // the loaded state replaces any populations staged before it
+        const jp_status ds = uniform_discard_staged(s);  // the loaded state replaces them
+        if (ds != JP_OK) return ds;
     }
     s->step_count = h.step_count;
     s->initialized = true;

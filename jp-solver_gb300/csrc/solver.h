@@ -100,6 +100,8 @@ jp_status uniform_get_output_fields(jp_solver* s, float* q, float* speed, float*
 jp_status output_fields_from(jp_solver* s, const void* field, bool field_is_double, bool float_diff, int n, float* q,
                              float* speed, float* vel);
 jp_status common_setup(jp_solver* s);
+// drop populations staged for the next step, after their copy has finished reading the host buffer
+jp_status uniform_discard_staged(jp_solver* s);
 // element of fa that holds population q of cell (x, y, z) at the current step count
 size_t uniform_slot(const jp_solver* s, int q, int x, int y, int z);
 // fa as stored <-> the flat [q][z][y][x] order of the two-array step (host copies; identity unless in place)
@@ -123,6 +125,7 @@ jp_status amr_set_step_map(jp_solver* s, int vec, int tpb);
 struct AmrFork {
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t fork2 = nullptr, join2 = nullptr;  // the second branch: level-1 blocks outside the skin
     cudaError_t create(cudaStream_t like);
     void destroy();
 };

@@ -128,8 +128,20 @@ void uniform_free(jp_solver* s) {
     s->partials = s->diag_dev = s->diag_host = nullptr;
 }
 
+// An explicit new state discards populations staged before it.  The staged copy may still be
+// reading the caller's pinned buffer: wait for it, so the buffer is free once the call returns.
+jp_status uniform_discard_staged(jp_solver* s) {
+    if (!s->staged) return JP_OK;
+    s->staged = false;
+    JP_CK(cudaEventSynchronize(s->ev_staged), "staged copy");
+    return JP_OK;
+}
+
 jp_status uniform_init(jp_solver* s) {
-    s->staged = false;  // an explicit new state discards populations staged before it
+    {
+        const jp_status ds = uniform_discard_staged(s);
+        if (ds != JP_OK) return ds;
+    }
     // the per-axis trigonometry table of the initial state lives in the diagnostic partials buffer
     // (3n <= 3 * kDiagBlocks doubles for n <= kDiagBlocks), which is free between diagnostics
     double* tab = s->partials;
@@ -324,7 +336,10 @@ jp_status uniform_set_populations(jp_solver* s, int level, int layout, int dtype
     if (count != (int64_t)Q * s->cells) return fail(JP_ERR_INVALID, "count %lld != 19*n^3", (long long)count);
     if (layout != JP_LAYOUT_FLAT && layout != JP_LAYOUT_BLOCKED) return fail(JP_ERR_INVALID, "bad layout %d", layout);
     const size_t bytes = (size_t)count * s->elem;
-    s->staged = false;  // an explicit new state discards populations staged before it
+    {
+        const jp_status ds = uniform_discard_staged(s);
+        if (ds != JP_OK) return ds;
+    }
     const bool native = layout == JP_LAYOUT_FLAT && !s->inplace &&
                         ((dtype == JP_F32 && s->storage == JP_FP32) || (dtype == JP_F64 && s->storage == JP_FP64));
     if (native) {
