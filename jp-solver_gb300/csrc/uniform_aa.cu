@@ -43,6 +43,13 @@ constexpr int aa_min_blocks() {
     return (sizeof(typename ST::raw) * V >= 8 && sizeof(typename ST::raw) <= 4) ? (384 / TPB > 0 ? 384 / TPB : 1) : 1;
 }
 
+// The stream step in 16-bit storage moves half the bytes per access of FP32 (8-byte vectors), so it
+// needs more warps in flight: 512 threads per SM (128 registers at 128 threads per CTA).
+template <class ST, int V, int TPB>
+constexpr int aa_stream_min_blocks() {
+    return sizeof(typename ST::raw) == 2 && V == 4 ? (512 / TPB > 0 ? 512 / TPB : 1) : aa_min_blocks<ST, V, TPB>();
+}
+
 __device__ __forceinline__ int solve_of(const UniBatch& b) {
     int si = 0;
 #pragma unroll 1
@@ -98,7 +105,7 @@ __global__ void __launch_bounds__(TPB, (aa_min_blocks<ST, V, TPB>())) k_aa_local
 
 // Stream step: gather population q from A[opp q][x - c_q], relax, scatter to A[q][x + c_q].
 template <class ST, int V, int TPB>
-__global__ void __launch_bounds__(TPB, (aa_min_blocks<ST, V, TPB>())) k_aa_stream(const __grid_constant__ UniBatch b) {
+__global__ void __launch_bounds__(TPB, (aa_stream_min_blocks<ST, V, TPB>())) k_aa_stream(const __grid_constant__ UniBatch b) {
     using raw = typename ST::raw;
     using R = typename ST::real;
     constexpr bool SH = ST::shifted;
