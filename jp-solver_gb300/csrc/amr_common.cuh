@@ -81,11 +81,6 @@ __host__ __device__ __forceinline__ int shell_slot(int i, int j, int k) {
     return (k < 0 ? 0 : (k >= MB ? 2 : 1)) * 9 + (j < 0 ? 0 : (j >= MB ? 2 : 1)) * 3 + (i < 0 ? 0 : (i >= MB ? 2 : 1));
 }
 
-__device__ __forceinline__ int pmod(int a, int n) {
-    const int r = a % n;
-    return r < 0 ? r + n : r;
-}
-
 // rho, u of one cell, summed in q order as the reference's loops do
 __device__ __forceinline__ void moments(const float (&f)[Q], float& rho, float& ux, float& uy, float& uz) {
     float r = f[0];
@@ -252,13 +247,17 @@ __device__ __forceinline__ void pull_cell(const typename ST::raw* __restrict__ f
 #endif
 
 // Trilinear weights of the cell-centred 2:1 prolongation: fine index g maps to the parent position
-// (g+0.5)/2-0.5, so the lower parent is floor of that and the weight of the upper one is 0.25 or
-// 0.75 (src/tgv3d_amr.cu:71-73).  Both are exact in float.
+// (g+0.5)/2-0.5 = (2g-1)/4 (src/tgv3d_amr.cu:71-73), so the lower parent is floor((g-1)/2) and the
+// weight of the upper one is 0.75 for even g, 0.25 for odd g: the reference's double expression's
+// values, exactly, in integer arithmetic (GB300's FP64 rate is a small fraction of its FP32 rate).
 __device__ __forceinline__ void tri_axis(int g, int& lo, float& t) {
-    const double xc = (double(g) + 0.5) / 2.0 - 0.5;
-    lo = int(floor(xc));
-    t = float(xc - lo);
+    lo = (g - 1) >> 1;  // arithmetic shift: floor for g = 0 too
+    t = (g & 1) ? 0.25f : 0.75f;
 }
+
+// a mod n for a in [-n, 2n): a wrap without a division (the corner and shell coordinates of the
+// fills are at most one cell outside the periodic box)
+__device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
 }  // namespace amr
 }  // namespace jp

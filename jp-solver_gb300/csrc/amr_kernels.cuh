@@ -141,7 +141,7 @@ __device__ __forceinline__ void corners_l0(const typename ST::raw* __restrict__ 
     for (int c = 0; c < 8; ++c) {
         const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
         w[c] = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
-        const int ci = pmod(ib + di, N), cj = pmod(jb + dj, N), ck = pmod(kb + dk, N);
+        const int ci = wrap1(ib + di, N), cj = wrap1(jb + dj, N), ck = wrap1(kb + dk, N);
         const int cb = ((ck / MB) * cgx + cj / MB) * cgx + ci / MB;
         const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
         p[c] = pr + (size_t)cb * Q * MB3 + cc;
@@ -161,7 +161,7 @@ __device__ __forceinline__ float corners_l1(const typename ST::raw* __restrict__
     for (int c = 0; c < 8; ++c) {
         const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
         w[c] = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
-        const int ci = pmod(ib + di, N1), cj = pmod(jb + dj, N1), ck = pmod(kb + dk, N1);
+        const int ci = wrap1(ib + di, N1), cj = wrap1(jb + dj, N1), ck = wrap1(kb + dk, N1);
         const int lb = __ldg(l1grid + ((ck / MB) * l1gx + cj / MB) * l1gx + ci / MB);
         const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
         p[c] = lb < 0 ? nullptr : pr + (size_t)lb * Q * MB3 + cc;
@@ -235,7 +235,7 @@ __device__ __forceinline__ void d_fill_l1(const typename ST::raw* __restrict__ p
                   oz = cbz * 2 * MB + (oct >> 2) * MB;
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
-        const int gfi = pmod(ox + i, N1), gfj = pmod(oy + j, N1), gfk = pmod(oz + k, N1);
+        const int gfi = wrap1(ox + i, N1), gfj = wrap1(oy + j, N1), gfk = wrap1(oz + k, N1);
         const typename ST::raw* p[8];
         float w[8];
         corners_l0<MB, ST>(pr, cgx, N, gfi, gfj, gfk, p, w);
@@ -274,7 +274,7 @@ __device__ __forceinline__ void d_fill_l2(const typename ST::raw* __restrict__ p
                   oz = pz * 2 * MB + (oct >> 2) * MB;
         int i, j, k;
         shell_coord<MB>(t, i, j, k);
-        const int g2i = pmod(ox + i, N2), g2j = pmod(oy + j, N2), g2k = pmod(oz + k, N2);
+        const int g2i = wrap1(ox + i, N2), g2j = wrap1(oy + j, N2), g2k = wrap1(oz + k, N2);
         const typename ST::raw* p[8];
         float w[8];
         const float wsum = corners_l1<MB, ST>(pr, l1grid, l1gx, N1, g2i, g2j, g2k, p, w);
@@ -655,7 +655,7 @@ __device__ __forceinline__ void prolong_l0(const typename ST::raw* __restrict__ 
     for (int c = 0; c < 8; ++c) {
         const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
         const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
-        const int ci = pmod(ib + di, N), cj = pmod(jb + dj, N), ck = pmod(kb + dk, N);
+        const int ci = wrap1(ib + di, N), cj = wrap1(jb + dj, N), ck = wrap1(kb + dk, N);
         const int cb = ((ck / MB) * cgx + cj / MB) * cgx + ci / MB;
         const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
         float f[Q];
@@ -681,7 +681,7 @@ __device__ __forceinline__ void prolong_l1(const typename ST::raw* __restrict__ 
     for (int c = 0; c < 8; ++c) {
         const int di = c & 1, dj = (c >> 1) & 1, dk = c >> 2;
         const float wgt = (di ? tx : 1 - tx) * (dj ? ty : 1 - ty) * (dk ? tz : 1 - tz);
-        const int ci = pmod(ib + di, N1), cj = pmod(jb + dj, N1), ck = pmod(kb + dk, N1);
+        const int ci = wrap1(ib + di, N1), cj = wrap1(jb + dj, N1), ck = wrap1(kb + dk, N1);
         const int lb = __ldg(l1grid + ((ck / MB) * l1gx + cj / MB) * l1gx + ci / MB);
         if (lb < 0) continue;
         const int cc = ((ck % MB) * MB + cj % MB) * MB + ci % MB;
