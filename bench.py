@@ -153,12 +153,18 @@ def bench_storage(J, n: int, storage: str, steps: int, warmup: int, device: int,
         barrier(pg)
         ms = max_over_ranks(pg, ms)
         d = s.diag()
+        diag_s = []
+        for _ in range(3):  # one diagnostic (macro field + reduction + read-back), host clock
+            t0 = time.perf_counter()
+            s.diag()
+            diag_s.append(time.perf_counter() - t0)
     finally:
         s.close()
     cells = n ** 3
     per_launch_s = ms / 1e3 / steps
     return {"ms_per_step": ms / steps, "glups": cells * steps / (ms / 1e3) / 1e9, "launches": launches,
-            "per_launch_s": per_launch_s, "clocks": clocks, "diag": d, "bytes_state": bytes_state,
+            "per_launch_s": per_launch_s, "clocks": clocks, "diag": d, "diag_ms": 1e3 * min(diag_s),
+            "bytes_state": bytes_state,
             "achieved_gbs": BYTES_PER_UPDATE[storage] * cells / per_launch_s / 1e9}
 
 
@@ -700,6 +706,8 @@ def main() -> int:
                 if e2e else None),
         "gpu_launches": main_r["launches"],
         "clocks": main_r["clocks"],
+        "diagnostic": {"ms": main_r["diag_ms"], "step_equivalents": main_r["diag_ms"] / main_r["ms_per_step"],
+                       "what": "one jp_diag (macro field, energy/enstrophy/mass reduction, read-back), host clock"},
     }
     if not a.no_amr and rank == 0:
         line["amr"] = bench_amr(J, local)
