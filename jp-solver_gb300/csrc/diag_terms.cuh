@@ -69,34 +69,23 @@ __device__ __forceinline__ FF half(FF x) { return {__fmul_rn(x.hi, 0.5f), __fmul
 
 __device__ __forceinline__ double to_double(FF x) { return double(x.hi) + double(x.lo); }
 
-// 1/2|u|^2, 1/2|curl u|^2 and rho of cell c (i fastest) of an n^3 field F[cell][4].  FLOAT_DIFF takes
-// each velocity difference in float (rounded) before halving, as the uniform program's host loop
-// does; otherwise the difference of the two floats is exact, as in the AMR diagnostic kernel.  VEC
-// reads each cell record (rho, ux, uy, uz) with one 16-byte load (F 16-byte aligned), else per float.
-template <bool FLOAT_DIFF, bool VEC>
-__device__ __forceinline__ void cell_terms(const float* __restrict__ F, int n, int i, int j, int k, FF& e, FF& ens,
-                                           float& rho) {
-    const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
-    const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
-    const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
-    auto rec = [&](int a, int b, int cc) -> float4 {
-        const float* p = F + (((size_t)cc * n + b) * n + a) * 4;
-        if (VEC) return __ldg(reinterpret_cast<const float4*>(p));
-        return make_float4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
-    };
+// 1/2|u|^2 and 1/2|curl u|^2 of a cell from its velocity (u, v, w) and its six face neighbours'
+// components that the curl uses: v, w at x+1 / x-1, u, w at y+1 / y-1, u, v at z+1 / z-1.
+// FLOAT_DIFF takes each velocity difference in float (rounded) before halving, as the uniform
+// program's host loop does; otherwise the difference of the two floats is exact, as in the AMR
+// diagnostic kernel.
+template <bool FLOAT_DIFF>
+__device__ __forceinline__ void velocity_terms(float u, float v, float w, float vxp, float vxm, float wxp, float wxm,
+                                               float uyp, float uym, float wyp, float wym, float uzp, float uzm,
+                                               float vzp, float vzm, FF& e, FF& ens) {
     auto dif = [&](float a, float b) -> FF {
         if (FLOAT_DIFF) return {__fmul_rn(__fsub_rn(a, b), 0.5f), 0.f};
         return half(two_sum(a, -b));
     };
-    const float4 me = rec(i, j, k);
-    const float4 xp = rec(ip, j, k), xm = rec(im, j, k), yp = rec(i, jp, k), ym = rec(i, jm, k);
-    const float4 zp = rec(i, j, kp), zm = rec(i, j, km);
-    rho = me.x;
-    const float u = me.y, v = me.z, w = me.w;
     e = half(add_same_sign(add_same_sign(two_prod(u, u), two_prod(v, v)), two_prod(w, w)));
-    const FF dudy = dif(yp.y, ym.y), dudz = dif(zp.y, zm.y);
-    const FF dvdx = dif(xp.z, xm.z), dvdz = dif(zp.z, zm.z);
-    const FF dwdx = dif(xp.w, xm.w), dwdy = dif(yp.w, ym.w);
+    const FF dudy = dif(uyp, uym), dudz = dif(uzp, uzm);
+    const FF dvdx = dif(vxp, vxm), dvdz = dif(vzp, vzm);
+    const FF dwdx = dif(wxp, wxm), dwdy = dif(wyp, wym);
     FF ox, oy, oz;
     if (FLOAT_DIFF) {  // differences of single floats: exact
         ox = two_sum(dwdy.hi, -dvdz.hi);
@@ -108,6 +97,28 @@ __device__ __forceinline__ void cell_terms(const float* __restrict__ F, int n, i
         oz = add(dvdx, {-dudy.hi, -dudy.lo});
     }
     ens = half(add_same_sign(add_same_sign(sq(ox), sq(oy)), sq(oz)));
+}
+
+// 1/2|u|^2, 1/2|curl u|^2 and rho of cell (i, j, k) of an n^3 field F[cell][4] (rho, ux, uy, uz;
+// i fastest), periodic.  VEC reads each cell record with one 16-byte load (F 16-byte aligned), else
+// per float.
+template <bool FLOAT_DIFF, bool VEC>
+__device__ __forceinline__ void cell_terms(const float* __restrict__ F, int n, int i, int j, int k, FF& e, FF& ens,
+                                           float& rho) {
+    const int ip = i + 1 == n ? 0 : i + 1, im = i == 0 ? n - 1 : i - 1;
+    const int jp = j + 1 == n ? 0 : j + 1, jm = j == 0 ? n - 1 : j - 1;
+    const int kp = k + 1 == n ? 0 : k + 1, km = k == 0 ? n - 1 : k - 1;
+    auto rec = [&](int a, int b, int cc) -> float4 {
+        const float* p = F + (((size_t)cc * n + b) * n + a) * 4;
+        if (VEC) return __ldg(reinterpret_cast<const float4*>(p));
+        return make_float4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
+    };
+    const float4 me = rec(i, j, k);
+    const float4 xp = rec(ip, j, k), xm = rec(im, j, k), yp = rec(i, jp, k), ym = rec(i, jm, k);
+    const float4 zp = rec(i, j, kp), zm = rec(i, j, km);
+    rho = me.x;
+    velocity_terms<FLOAT_DIFF>(me.y, me.z, me.w, xp.z, xm.z, xp.w, xm.w, yp.y, ym.y, yp.w, ym.w, zp.y, zm.y, zp.z,
+                               zm.z, e, ens);
 }
 
 // The cells c0, c0 + S, c0 + 2S, ... of an n^3 grid (i fastest) as (i, j, k), advanced by adding the
@@ -155,6 +166,73 @@ struct Acc {
     __device__ __forceinline__ void flush() {
         de += to_double(e);
         dens += to_double(ens);
+        dmass += to_double(mass);
+        e = ens = mass = FF{0.f, 0.f};
+        k = 0;
+    }
+};
+
+// Running sums for the diagnostic straight from the populations, cheaper per cell than Acc.  A cell
+// adds its three energy products u*u, v*v, w*w (exact pairs from two_prod) into a double-float
+// partial (hi by TwoSum, the low parts and TwoSum's errors gathered in lo), that partial into the
+// energy sum with add_same_sign; the enstrophy likewise from the three exact vorticity components
+// (hi^2 + 2 hi lo; lo^2 < 2^-48 of it is dropped); the mass with TwoSum and a renormalisation per
+// cell, so any sign of rho keeps it exact to ~2^-47.  The 1/2 of the energy and the enstrophy is
+// applied once, in FP64, at the flush (halving is exact).  Error per cell below ~2^-46 of the
+// running sum; kFlush cells per FP64 flush keep the sums within ~32 * 2^-46 ~ 5e-13 relative in the
+// worst case, ~1e-14 in practice.
+struct CellSums {
+    static constexpr int kFlush = 32;
+    FF e{0.f, 0.f}, ens{0.f, 0.f}, mass{0.f, 0.f};
+    double de = 0.0, dens = 0.0, dmass = 0.0;
+    int k = 0;
+
+    // the first square of a partial, then the next ones
+    __device__ static __forceinline__ FF sq1(float a) {
+        const float p = __fmul_rn(a, a);
+        return {p, __fmaf_rn(a, a, -p)};
+    }
+    __device__ static __forceinline__ void sq_add(FF& s, float a) {
+        const float p = __fmul_rn(a, a);
+        const float lo = __fmaf_rn(a, a, -p);
+        const FF t = two_sum(s.hi, p);
+        s = {t.hi, __fadd_rn(s.lo, __fadd_rn(t.lo, lo))};
+    }
+    // x^2 of an exact double-float x, to ~2^-47
+    __device__ static __forceinline__ FF dsq1(FF x) {
+        const float p = __fmul_rn(x.hi, x.hi);
+        return {p, __fmaf_rn(__fadd_rn(x.hi, x.hi), x.lo, __fmaf_rn(x.hi, x.hi, -p))};
+    }
+    __device__ static __forceinline__ void dsq_add(FF& s, FF x) {
+        const FF q = dsq1(x);
+        const FF t = two_sum(s.hi, q.hi);
+        s = {t.hi, __fadd_rn(s.lo, __fadd_rn(t.lo, q.lo))};
+    }
+
+    // the cell with velocity (u, v, w), density rho and the neighbour components velocity_terms takes;
+    // velocity differences in float (rounded), as the uniform program's host loop takes them
+    __device__ __forceinline__ void add_cell(float u, float v, float w, float rho, float vxp, float vxm, float wxp,
+                                             float wxm, float uyp, float uym, float wyp, float wym, float uzp,
+                                             float uzm, float vzp, float vzm) {
+        FF pe = sq1(u);
+        sq_add(pe, v);
+        sq_add(pe, w);
+        e = add_same_sign(e, pe);
+        auto dif = [](float a, float b) { return __fmul_rn(__fsub_rn(a, b), 0.5f); };
+        const float dudy = dif(uyp, uym), dudz = dif(uzp, uzm);
+        const float dvdx = dif(vxp, vxm), dvdz = dif(vzp, vzm);
+        const float dwdx = dif(wxp, wxm), dwdy = dif(wyp, wym);
+        FF pz = dsq1(two_sum(dwdy, -dvdz));
+        dsq_add(pz, two_sum(dudz, -dwdx));
+        dsq_add(pz, two_sum(dvdx, -dudy));
+        ens = add_same_sign(ens, pz);
+        const FF t = two_sum(mass.hi, rho);
+        mass = fast_two_sum(t.hi, __fadd_rn(mass.lo, t.lo));
+        if (++k == kFlush) flush();
+    }
+    __device__ __forceinline__ void flush() {
+        de += 0.5 * to_double(e);
+        dens += 0.5 * to_double(ens);
         dmass += to_double(mass);
         e = ens = mass = FF{0.f, 0.f};
         k = 0;

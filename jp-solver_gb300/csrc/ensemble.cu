@@ -269,7 +269,7 @@ long long estimate_bytes(const jp_config& c) {
     const int Qn = 19;
     if (c.kind == JP_UNIFORM) {
         const long long elem = c.storage == JP_FP64 ? 8 : (c.storage == JP_FP32 ? 4 : 2);
-        const long long field = (c.storage == JP_FP64 ? 32 : 16) * n * n * n;
+        const long long field = diag_pop_ok(c.storage, (int)n) ? 0 : (c.storage == JP_FP64 ? 32 : 16) * n * n * n;
         const long long arrays = (c.flags & JP_FLAG_INPLACE) ? 1 : 2;  // in place: one population array
         return arrays * Qn * elem * n * n * n + field + (1 << 20);
     }
@@ -933,10 +933,13 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
         jp_get_info(s, &j->info);
         j->steps = j->info.steps;
         j->diagK = j->req.diag_every > 0 ? j->req.diag_every : std::max(1LL, j->steps / 240);
-        // the macro field of the diagnostics, ready before the server's stream uses it
-        const size_t fb = (s->storage == JP_FP64 ? 8 : 4) * 4 * (size_t)s->cells;
-        cudaError_t e = dev_alloc(s, &s->field, fb);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        // an FP64 solve's diagnostics read a macro field, ready before the server's stream uses it
+        // (the float storages' diagnostics read the populations)
+        cudaError_t e = cudaSuccess;
+        if (!diag_pop_ok(s->storage, s->n)) {
+            e = dev_alloc(s, &s->field, (s->storage == JP_FP64 ? 8 : 4) * 4 * (size_t)s->cells);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        }
         if (e != cudaSuccess) {
             finish(sv, j, cuda_fail(e, "macro field"));
             continue;
@@ -973,10 +976,14 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             if (j->error != JP_OK || !j->need_diag) continue;
             if ((int)cur.entries.size() >= cur.cap) return fail(JP_ERR_CAPACITY, "diagnostic slots exhausted");
             jp_solver* s = j->s;
-            const bool dbl = s->storage == JP_FP64;
             double* slot = cur.dev + 3 * cur.entries.size();
-            ECK(launch_macro(s->storage, s->fa, s->field, s->n, sv->stream, s->aa_layout()), "macro");
-            ECK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, slot, sv->stream), "diag");
+            if (diag_pop_ok(s->storage, s->n)) {
+                ECK(launch_diag_pop(s->storage, s->aa_layout(), s->fa, s->n, s->partials, slot, sv->stream), "diag");
+            } else {
+                const bool dbl = s->storage == JP_FP64;
+                ECK(launch_macro(s->storage, s->fa, s->field, s->n, sv->stream, s->aa_layout()), "macro");
+                ECK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, slot, sv->stream), "diag");
+            }
             cur.entries.push_back({j, j->step});
             j->need_diag = false;
             ++j->inflight;

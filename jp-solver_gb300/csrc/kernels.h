@@ -66,6 +66,15 @@ constexpr int kDiagThreads = 256;
 cudaError_t launch_diag_field(bool field_is_double, bool float_diff, const void* field, int n,
                               double* partials_dev, double* out_dev, cudaStream_t st);
 
+// Energy, enstrophy, mass of a float-storage cube (storage 0 FP32, 1 FP16, 2 BF16) straight from its
+// populations f in layout 0 / 1 / 2 (as launch_macro), with no macro field: the per-cell terms of
+// launch_macro + launch_diag_field(float_diff=true), summed another way (double-float partials in a
+// fixed order) to ~1e-13 of the result.
+// Cubes it takes: even n (pairs of cells), n <= 1600 (32-bit cell indices).
+cudaError_t launch_diag_pop(int storage, int layout, const void* f, int n, double* partials_dev, double* out_dev,
+                            cudaStream_t st);
+inline bool diag_pop_ok(int storage, int n) { return storage >= 0 && storage <= 2 && n % 2 == 0 && n <= 1600; }
+
 // Q-criterion, speed and (vel != nullptr) velocity of a macro field of edge n into device arrays.
 cudaError_t launch_qspeed(bool field_is_double, bool float_diff, const void* field, int n, float* Q, float* speed,
                           float* vel, cudaStream_t st);

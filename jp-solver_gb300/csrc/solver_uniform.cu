@@ -236,11 +236,15 @@ static jp_status ensure_field(jp_solver* s) {
 }
 
 jp_status uniform_diag(jp_solver* s, double out[3]) {
-    jp_status st = ensure_field(s);
-    if (st != JP_OK) return st;
-    JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream, s->aa_layout()), "macro");
-    const bool dbl = s->storage == JP_FP64;
-    JP_CK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, s->diag_dev, s->stream), "diag");
+    if (diag_pop_ok(s->storage, s->n)) {  // float storages: straight from the populations
+        JP_CK(launch_diag_pop(s->storage, s->aa_layout(), s->fa, s->n, s->partials, s->diag_dev, s->stream), "diag");
+    } else {  // FP64 terms from an FP64 macro field (or a cube beyond 32-bit cell indices)
+        const jp_status st = ensure_field(s);
+        if (st != JP_OK) return st;
+        const bool dbl = s->storage == JP_FP64;
+        JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream, s->aa_layout()), "macro");
+        JP_CK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, s->diag_dev, s->stream), "diag");
+    }
     JP_CK(cudaMemcpyAsync(s->diag_host, s->diag_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "diag D2H");
     JP_CK(cudaStreamSynchronize(s->stream), "diag");
     out[0] = s->diag_host[0];

@@ -14,6 +14,7 @@
 #include "diag_terms.cuh"
 #include "uniform_common.cuh"
 
+#include <algorithm>
 #include <atomic>
 
 namespace jp {
@@ -278,6 +279,23 @@ cudaError_t launch_init_tgv(int storage, void* f, int n, double u0, double kf, d
 // ---- macro field ---------------------------------------------------------------------------------
 // layout 0: population q of cell x at [q][x]; the in-place layouts: 1 (even step count) at
 // [q][x + c_q], 2 (odd step count) at [opp q][x]
+// rho and u = j / rho of one cell from its 19 populations (shifted storage adds the rest density 1)
+template <class ST>
+__device__ __forceinline__ void cell_macro(const typename ST::real (&v)[Q], typename ST::real& rho,
+                                           typename ST::real& ux, typename ST::real& uy, typename ST::real& uz) {
+    using R = typename ST::real;
+    R sm = v[0];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) sm += v[q];
+    const R jx = v[1] - v[2] + v[7] - v[8] + v[9] - v[10] + v[11] - v[12] + v[13] - v[14];
+    const R jy = v[3] - v[4] + v[7] - v[8] - v[9] + v[10] + v[15] - v[16] + v[17] - v[18];
+    const R jz = v[5] - v[6] + v[11] - v[12] - v[13] + v[14] + v[15] - v[16] - v[17] + v[18];
+    rho = ST::shifted ? R(1) + sm : sm;
+    ux = jx / rho;
+    uy = jy / rho;
+    uz = jz / rho;
+}
+
 template <class ST, class FT>
 __global__ void k_macro(const typename ST::raw* __restrict__ f, FT* __restrict__ out, int n, int layout) {
     using R = typename ST::real;
@@ -296,18 +314,13 @@ __global__ void k_macro(const typename ST::raw* __restrict__ f, FT* __restrict__
             o = (size_t)opp(q) * cells + c;
         v[q] = ST::load(f[o]);
     }
-    R sm = v[0];
-#pragma unroll
-    for (int q = 1; q < Q; ++q) sm += v[q];
-    const R jx = v[1] - v[2] + v[7] - v[8] + v[9] - v[10] + v[11] - v[12] + v[13] - v[14];
-    const R jy = v[3] - v[4] + v[7] - v[8] - v[9] + v[10] + v[15] - v[16] + v[17] - v[18];
-    const R jz = v[5] - v[6] + v[11] - v[12] - v[13] + v[14] + v[15] - v[16] - v[17] + v[18];
-    const R rho = ST::shifted ? R(1) + sm : sm;
+    R rho, ux, uy, uz;
+    cell_macro<ST>(v, rho, ux, uy, uz);
     FT* o = out + 4 * c;
     o[0] = FT(rho);
-    o[1] = FT(jx / rho);
-    o[2] = FT(jy / rho);
-    o[3] = FT(jz / rho);
+    o[1] = FT(ux);
+    o[2] = FT(uy);
+    o[3] = FT(uz);
 }
 
 cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStream_t st, int layout) {
@@ -415,6 +428,223 @@ __global__ void __launch_bounds__(256) k_diag_finish(const double* __restrict__ 
         double t = 0.0;
         for (int i = 0; i < 8; ++i) t += sh[threadIdx.x][i];
         out[threadIdx.x] = t * inv_cells;
+    }
+}
+
+// ---- energy / enstrophy / mass straight from the populations ---------------------------------------
+// The float storages' diagnostic without a macro field in HBM (k_macro writes 16 B per cell that
+// k_diag_field reads back with its neighbours).  A CTA takes a tile of kPopTx x kPopTy cells of the
+// x-y plane and marches it along z over a chunk of planes, reading each cell's 19 populations once
+// per plane.  A thread owns two x-adjacent cells (one 8-byte FP32 or 4-byte 16-bit load per
+// population); the tile's one-cell halo in x and y is loaded too (its populations come mostly from
+// L2: the neighbouring tiles' CTAs run beside it over the same planes).  The velocities of a plane
+// land in a ring of three planes in shared memory, the z neighbours of a thread's own cells stay in
+// its registers, and once plane z+1 is in, the tile's cells add the terms of plane z.  rho and u
+// come from cell_macro (k_macro's arithmetic) and the velocity differences are taken in float, as in
+// the two-pass path, so each cell's terms are the same numbers; dterm::CellSums adds them (to
+// ~1e-13 of the sums) in a fixed order: items dealt to CTAs in a fixed order, fixed trees.  The next
+// plane's loads are issued before the current plane's terms, so they are in flight across the
+// barrier.  One 608-thread CTA per SM (96 registers) with this tile measured faster than two
+// 336-thread CTAs of 64 x 8 (a quarter of the loads in the halo, spills at 80 registers).
+constexpr int kPopTx = 64, kPopTy = 16;
+constexpr int kPopCols = kPopTx + 4;                          // x0-2 .. x0+kPopTx+1: whole pairs
+constexpr int kPopRows = kPopTy + 2;                          // y0-1 .. y0+kPopTy
+constexpr int kPopInner = kPopTx / 2 * kPopTy;                // threads on the tile's own pairs
+constexpr int kPopThreads = kPopInner + kPopTx + 2 * kPopTy;  // + the rows y0-1, y0+kPopTy, the x pairs
+
+// the 19 population arrays of a cube, in the order the kernel reads them (layout 2 permuted here)
+template <class RAW>
+struct PopPtrs {
+    const RAW* q[Q];
+};
+
+template <class RAW> struct PopPair;
+template <> struct PopPair<float> {
+    using word = float2;
+    __device__ static __forceinline__ float lo(word w) { return w.x; }
+    __device__ static __forceinline__ float hi(word w) { return w.y; }
+    __device__ static __forceinline__ word make(float a, float b) { return make_float2(a, b); }
+};
+template <> struct PopPair<uint16_t> {
+    using word = unsigned int;  // the cell at the lower address in the low half
+    __device__ static __forceinline__ uint16_t lo(word w) { return (uint16_t)(w & 0xffffu); }
+    __device__ static __forceinline__ uint16_t hi(word w) { return (uint16_t)(w >> 16); }
+    __device__ static __forceinline__ word make(uint16_t a, uint16_t b) { return (unsigned)a | ((unsigned)b << 16); }
+};
+
+// SHIFTED: the in-place layout after an even step count (population q of cell x at [q][x + c_q]).
+template <class ST, bool SHIFTED>
+__global__ void __launch_bounds__(kPopThreads, 1)
+    k_diag_pop(const PopPtrs<typename ST::raw> P, int n, int ntx, int ntiles, int zc, int items,
+               double* __restrict__ partials) {
+    using RAW = typename ST::raw;
+    using PP = PopPair<RAW>;
+    using W = typename PP::word;
+    __shared__ __align__(16) float ring[3][3][kPopRows][kPopCols];
+    const int t = threadIdx.x;
+    // this thread's pair (x, x+1) relative to the tile origin: the tile's pairs, the rows y = -1 and
+    // y = kPopTy, then the pairs x = -2 and x = kPopTx of the tile's rows
+    int ox, oy;
+    if (t < kPopInner) {
+        ox = 2 * (t % 32);
+        oy = t / 32;
+    } else if (t < kPopInner + kPopTx) {
+        const int l = t - kPopInner;
+        ox = 2 * (l % 32);
+        oy = l < 32 ? -1 : kPopTy;
+    } else {
+        const int l = t - kPopInner - kPopTx;
+        ox = l < kPopTy ? -2 : kPopTx;
+        oy = l < kPopTy ? l : l - kPopTy;
+    }
+    const int row = oy + 1, col = ox + 2;
+    auto wrap = [n](int a) {
+        a %= n;
+        return a < 0 ? a + n : a;
+    };
+    dterm::CellSums sums;
+    for (int it = blockIdx.x; it < items; it += gridDim.x) {
+        const int zci = it / ntiles, tile = it - zci * ntiles;
+        const int ty = tile / ntx, tx = tile - ty * ntx;
+        const int x0 = tx * kPopTx, y0 = ty * kPopTy;
+        const int zs = zci * zc, m = min(n, zs + zc) - zs;
+        const int gx = wrap(x0 + ox), gy = wrap(y0 + oy);  // gx even (n is even), gx + 1 < n
+        const bool valid = t < kPopInner && x0 + ox < n && y0 + oy < n;
+        W a[Q];
+        auto load_plane = [&](int z) {
+            if (!SHIFTED) {
+                const unsigned c = ((unsigned)z * n + gy) * n + gx;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) a[q] = __ldg(reinterpret_cast<const W*>(P.q[q] + c));
+            } else {
+                const int zm = z == 0 ? n - 1 : z - 1, zp = z + 1 == n ? 0 : z + 1;
+                const int gym = gy == 0 ? n - 1 : gy - 1, gyp = gy + 1 == n ? 0 : gy + 1;
+                const int xm = gx == 0 ? n - 1 : gx - 1, xp2 = gx + 2 == n ? 0 : gx + 2;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    const int zz = cz(q) > 0 ? zp : cz(q) < 0 ? zm : z;
+                    const int yy = cy(q) > 0 ? gyp : cy(q) < 0 ? gym : gy;
+                    const unsigned r = ((unsigned)zz * n + yy) * n;
+                    const int xa = cx(q) > 0 ? gx + 1 : cx(q) < 0 ? xm : gx;        // cell gx + c_q
+                    const int xb = cx(q) > 0 ? xp2 : cx(q) < 0 ? gx : gx + 1;       // cell gx + 1 + c_q
+                    a[q] = PP::make(ld_one<RAW>(P.q[q] + r + xa), ld_one<RAW>(P.q[q] + r + xb));
+                }
+            }
+        };
+        load_plane(zs == 0 ? n - 1 : zs - 1);
+        // the thread's two cells one plane back (u, v, w, rho) and two planes back (u, v)
+        float u1a = 0.f, v1a = 0.f, w1a = 0.f, r1a = 0.f, u2a = 0.f, v2a = 0.f;
+        float u1b = 0.f, v1b = 0.f, w1b = 0.f, r1b = 0.f, u2b = 0.f, v2b = 0.f;
+        int cur = 0;                                       // ring slot of plane zs - 1 + r
+        for (int r = 0; r <= m + 1; ++r) {
+            float rhoa, ua, va, wa, rhob, ub, vb, wb;
+            {
+                float fa[Q], fb[Q];
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    fa[q] = ST::load(PP::lo(a[q]));
+                    fb[q] = ST::load(PP::hi(a[q]));
+                }
+                cell_macro<ST>(fa, rhoa, ua, va, wa);
+                cell_macro<ST>(fb, rhob, ub, vb, wb);
+            }
+            if (r <= m) load_plane(zs + r == n ? 0 : zs + r);
+            *reinterpret_cast<float2*>(&ring[cur][0][row][col]) = make_float2(ua, ub);
+            *reinterpret_cast<float2*>(&ring[cur][1][row][col]) = make_float2(va, vb);
+            *reinterpret_cast<float2*>(&ring[cur][2][row][col]) = make_float2(wa, wb);
+            if (r >= 2) {
+                __syncthreads();
+                if (valid) {  // the terms of plane zs + r - 2, from the slot before cur
+                    const int pv = cur == 0 ? 2 : cur - 1;
+                    auto ld2 = [&](int comp, int rr, int cc) {
+                        return *reinterpret_cast<const float2*>(&ring[pv][comp][rr][cc]);
+                    };
+                    const float2 vl = ld2(1, row, col - 2), vr = ld2(1, row, col + 2), vc = ld2(1, row, col);
+                    const float2 wl = ld2(2, row, col - 2), wr = ld2(2, row, col + 2), wc = ld2(2, row, col);
+                    const float2 un = ld2(0, row + 1, col), us = ld2(0, row - 1, col);
+                    const float2 wn = ld2(2, row + 1, col), ws = ld2(2, row - 1, col);
+                    // cell x: x-1 at col-1, x+1 at col+1; cell x+1: x at col, x+2 at col+2
+                    sums.add_cell(u1a, v1a, w1a, r1a, vc.y, vl.y, wc.y, wl.y, un.x, us.x, wn.x, ws.x, ua, u2a, va, v2a);
+                    sums.add_cell(u1b, v1b, w1b, r1b, vr.x, vc.x, wr.x, wc.x, un.y, us.y, wn.y, ws.y, ub, u2b, vb, v2b);
+                }
+            }
+            u2a = u1a;
+            v2a = v1a;
+            u1a = ua;
+            v1a = va;
+            w1a = wa;
+            r1a = rhoa;
+            u2b = u1b;
+            v2b = v1b;
+            u1b = ub;
+            v1b = vb;
+            w1b = wb;
+            r1b = rhob;
+            cur = cur == 2 ? 0 : cur + 1;
+        }
+        __syncthreads();  // the next item writes the ring from its first plane on
+    }
+    sums.flush();
+    double e = warp_sum(sums.de), ens = warp_sum(sums.dens), mass = warp_sum(sums.dmass);
+    __shared__ double sh[3][kPopThreads / 32];
+    const int wid = t >> 5, lane = t & 31;
+    if (lane == 0) {
+        sh[0][wid] = e;
+        sh[1][wid] = ens;
+        sh[2][wid] = mass;
+    }
+    __syncthreads();
+    if (t < 3) {
+        double sum = 0.0;
+        for (int i = 0; i < kPopThreads / 32; ++i) sum += sh[t][i];
+        partials[blockIdx.x * 3 + t] = sum;
+    }
+}
+
+template <class ST>
+static cudaError_t launch_diag_pop_t(int layout, const void* f, int n, double* partials_dev, double* out_dev,
+                                     cudaStream_t st) {
+    using RAW = typename ST::raw;
+    auto kern = layout == 1 ? k_diag_pop<ST, true> : k_diag_pop<ST, false>;
+    PopPtrs<RAW> P;
+    const size_t cells = (size_t)n * n * n;
+    for (int q = 0; q < Q; ++q) P.q[q] = (const RAW*)f + (size_t)(layout == 2 ? opp(q) : q) * cells;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPopThreads, 0);
+    if (e != cudaSuccess) return e;
+    const long long cap = std::min<long long>(kDiagBlocks, std::max(1, sms * std::max(1, per_sm)));
+    const int ntx = (n + kPopTx - 1) / kPopTx, nty = (n + kPopTy - 1) / kPopTy, ntiles = ntx * nty;
+    // z chunk: a CTA walks rounds x (chunk + 2 halo planes) planes, rounds = items over the resident
+    // CTA slots; take the chunk with the fewest (the longest on a tie)
+    int best_zc = n;
+    long long best = -1;
+    for (int zc = n; zc >= 4; --zc) {
+        const long long items = (long long)ntiles * ((n + zc - 1) / zc);
+        const long long planes = (items + cap - 1) / cap * (zc + 2);
+        if (best < 0 || planes < best) {
+            best = planes;
+            best_zc = zc;
+        }
+    }
+    const long long nzc = (n + best_zc - 1) / best_zc, items = (long long)ntiles * nzc;
+    const int grid = (int)std::min(items, cap);
+    kern<<<grid, kPopThreads, 0, st>>>(P, n, ntx, ntiles, best_zc, (int)items, partials_dev);
+    k_diag_finish<<<1, 256, 0, st>>>(partials_dev, grid, 1.0 / double(cells), out_dev);
+    note_launch(2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diag_pop(int storage, int layout, const void* f, int n, double* partials_dev, double* out_dev,
+                            cudaStream_t st) {
+    // pairs of cells at even x need an even n; cell indices are 32-bit
+    if (n < 2 || n % 2 != 0 || n > 1600 || layout < 0 || layout > 2) return cudaErrorInvalidValue;
+    switch (storage) {
+        case 0: return launch_diag_pop_t<StF32>(layout, f, n, partials_dev, out_dev, st);
+        case 1: return launch_diag_pop_t<StF16>(layout, f, n, partials_dev, out_dev, st);
+        case 2: return launch_diag_pop_t<StBF16>(layout, f, n, partials_dev, out_dev, st);
+        default: return cudaErrorInvalidValue;
     }
 }
 
