@@ -978,7 +978,8 @@ static jp_status server_tick(jp_server* sv, int32_t* n_active, int32_t* n_queued
             jp_solver* s = j->s;
             double* slot = cur.dev + 3 * cur.entries.size();
             if (diag_pop_ok(s->storage, s->n)) {
-                ECK(launch_diag_pop(s->storage, s->aa_layout(), s->fa, s->n, s->partials, slot, sv->stream), "diag");
+                ECK(launch_diag_pop(s->storage, s->aa_layout(), s->fa, s->n, s->partials, slot, nullptr, sv->stream),
+                    "diag");  // a wait that gave up leaves NaN diagnostics, which fail the solve's check
             } else {
                 const bool dbl = s->storage == JP_FP64;
                 ECK(launch_macro(s->storage, s->fa, s->field, s->n, sv->stream, s->aa_layout()), "macro");

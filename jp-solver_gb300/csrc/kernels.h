@@ -63,6 +63,8 @@ cudaError_t launch_macro(int storage, const void* f, void* field, int n, cudaStr
 // be 16-byte aligned (every solver's own field is).
 constexpr int kDiagBlocks = 1216;   // 152 SMs x 8
 constexpr int kDiagThreads = 256;
+constexpr int kDiagPartials = kDiagBlocks * 3 + 1;  // block partials + the error word of launch_diag_pop
+inline int* diag_err_word(double* partials) { return reinterpret_cast<int*>(partials + kDiagBlocks * 3); }
 cudaError_t launch_diag_field(bool field_is_double, bool float_diff, const void* field, int n,
                               double* partials_dev, double* out_dev, cudaStream_t st);
 
@@ -70,9 +72,12 @@ cudaError_t launch_diag_field(bool field_is_double, bool float_diff, const void*
 // populations f in layout 0 / 1 / 2 (as launch_macro), with no macro field: the per-cell terms of
 // launch_macro + launch_diag_field(float_diff=true), summed another way (double-float partials in a
 // fixed order) to ~1e-13 of the result.
-// Cubes it takes: even n (pairs of cells), n <= 1600 (32-bit cell indices).
+// Cubes it takes: even n (pairs of cells), n <= 1600 (32-bit cell indices).  partials_dev holds
+// kDiagPartials doubles: the last is the kernel's error word (zero when allocated; set if a bounded
+// wait between its warps gave up, cleared by the launch's final sum, which copies it to *flag_out
+// when flag_out is given and then writes NaN diagnostics).
 cudaError_t launch_diag_pop(int storage, int layout, const void* f, int n, double* partials_dev, double* out_dev,
-                            cudaStream_t st);
+                            double* flag_out, cudaStream_t st);
 inline bool diag_pop_ok(int storage, int n) { return storage >= 0 && storage <= 2 && n % 2 == 0 && n <= 1600; }
 
 // Q-criterion, speed and (vel != nullptr) velocity of a macro field of edge n into device arrays.

@@ -63,9 +63,9 @@ struct jp_solver {
     void* fb = nullptr;        // next state (null when in place)
     bool inplace = false;      // JP_FLAG_INPLACE: one array, AA steps (uniform_aa.cu)
     void* field = nullptr;     // macro field (float4 or double4 per cell), allocated on first use
-    double* partials = nullptr;  // diagnostic block partials (kDiagBlocks*3)
-    double* diag_dev = nullptr;  // 3 doubles
-    double* diag_host = nullptr; // 3 doubles, pinned
+    double* partials = nullptr;  // diagnostic block partials + error word (kDiagPartials)
+    double* diag_dev = nullptr;  // 3 doubles (+ the error word's copy, uniform)
+    double* diag_host = nullptr; // 4 doubles, pinned
     int vec = 0, tpb = 0;
     float* outbuf = nullptr;   // device Q / speed / velocity for output frames, allocated on first use
     // populations staged for the next step (jp_stage_populations): uploaded into `staging` on

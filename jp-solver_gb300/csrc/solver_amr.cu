@@ -1160,7 +1160,7 @@ jp_status amr_create(jp_solver* s) {
     a->cnt_host = (AdaptCounts*)pinned_slot_alloc();
     s->diag_host = (double*)pinned_slot_alloc();
     if (!a->cnt_host || !s->diag_host) return fail(JP_ERR_NOMEM, "pinned host slot");
-    ACK(dev_alloc(s, (void**)&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
+    ACK(dev_alloc(s, (void**)&s->partials, sizeof(double) * kDiagPartials), "cudaMalloc partials");
     ACK(dev_alloc(s, (void**)&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
     ACK(a->fk.create(s->stream), "side stream");
     ACK(cudaMemsetAsync(a->fof1, 0xFF, sizeof(int) * a->cap1, s->stream), "memset");

@@ -98,8 +98,9 @@ jp_status uniform_create(jp_solver* s) {
     s->info.bytes_state = (int64_t)((s->inplace ? 1 : 2) * bytes);
     JP_CK(dev_alloc(s, &s->fa, bytes), "cudaMalloc populations");
     if (!s->inplace) JP_CK(dev_alloc(s, &s->fb, bytes), "cudaMalloc populations");
-    JP_CK(dev_alloc(s, (void**)&s->partials, sizeof(double) * kDiagBlocks * 3), "cudaMalloc partials");
-    JP_CK(dev_alloc(s, (void**)&s->diag_dev, sizeof(double) * 3), "cudaMalloc diag");
+    JP_CK(dev_alloc(s, (void**)&s->partials, sizeof(double) * kDiagPartials), "cudaMalloc partials");
+    JP_CK(cudaMemsetAsync(diag_err_word(s->partials), 0, sizeof(int), s->stream), "clear diag error word");
+    JP_CK(dev_alloc(s, (void**)&s->diag_dev, sizeof(double) * 4), "cudaMalloc diag");
     s->diag_host = (double*)pinned_slot_alloc();
     if (!s->diag_host) return fail(JP_ERR_NOMEM, "pinned host slot");
     if (s->cfg.flags & JP_FLAG_DEFER_INIT) return JP_OK;
@@ -236,8 +237,11 @@ static jp_status ensure_field(jp_solver* s) {
 }
 
 jp_status uniform_diag(jp_solver* s, double out[3]) {
-    if (diag_pop_ok(s->storage, s->n)) {  // float storages: straight from the populations
-        JP_CK(launch_diag_pop(s->storage, s->aa_layout(), s->fa, s->n, s->partials, s->diag_dev, s->stream), "diag");
+    const bool pop = diag_pop_ok(s->storage, s->n);
+    if (pop) {  // float storages: straight from the populations; diag_dev[3] takes the error word
+        JP_CK(launch_diag_pop(s->storage, s->aa_layout(), s->fa, s->n, s->partials, s->diag_dev, s->diag_dev + 3,
+                              s->stream),
+              "diag");
     } else {  // FP64 terms from an FP64 macro field (or a cube beyond 32-bit cell indices)
         const jp_status st = ensure_field(s);
         if (st != JP_OK) return st;
@@ -245,8 +249,12 @@ jp_status uniform_diag(jp_solver* s, double out[3]) {
         JP_CK(launch_macro(s->storage, s->fa, s->field, s->n, s->stream, s->aa_layout()), "macro");
         JP_CK(launch_diag_field(dbl, !dbl, s->field, s->n, s->partials, s->diag_dev, s->stream), "diag");
     }
-    JP_CK(cudaMemcpyAsync(s->diag_host, s->diag_dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "diag D2H");
+    JP_CK(cudaMemcpyAsync(s->diag_host, s->diag_dev, (pop ? 4 : 3) * sizeof(double), cudaMemcpyDeviceToHost,
+                          s->stream),
+          "diag D2H");
     JP_CK(cudaStreamSynchronize(s->stream), "diag");
+    if (pop && s->diag_host[3] != 0.0)
+        return fail(JP_ERR_TIMEOUT, "diagnostic: a wait between the kernel's warps gave up (its sums are NaN)");
     out[0] = s->diag_host[0];
     out[1] = s->diag_host[1];
     out[2] = s->diag_host[2];

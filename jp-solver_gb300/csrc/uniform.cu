@@ -407,9 +407,12 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_field(const FT* __restric
     }
 }
 
-// Sum `nparts` partial triples in a fixed order and scale by 1/cells.
+// Sum `nparts` partial triples in a fixed order and scale by 1/cells.  err (optional): the error word
+// of the kernel that wrote the partials, copied to *flag_out (when given) and cleared for the next one.
 __global__ void __launch_bounds__(256) k_diag_finish(const double* __restrict__ partials, int nparts,
-                                                     double inv_cells, double* __restrict__ out) {
+                                                     double inv_cells, double* __restrict__ out,
+                                                     int* __restrict__ err = nullptr,
+                                                     double* __restrict__ flag_out = nullptr) {
     double a[3] = {0.0, 0.0, 0.0};
     for (int p = threadIdx.x; p < nparts; p += 256) {
         a[0] += partials[p * 3 + 0];
@@ -429,6 +432,10 @@ __global__ void __launch_bounds__(256) k_diag_finish(const double* __restrict__ 
         for (int i = 0; i < 8; ++i) t += sh[threadIdx.x][i];
         out[threadIdx.x] = t * inv_cells;
     }
+    if (threadIdx.x == 0 && err) {
+        if (flag_out) *flag_out = double(*err);
+        *err = 0;
+    }
 }
 
 // ---- energy / enstrophy / mass straight from the populations ---------------------------------------
@@ -439,18 +446,71 @@ __global__ void __launch_bounds__(256) k_diag_finish(const double* __restrict__ 
 // population); the tile's one-cell halo in x and y is loaded too (its populations come mostly from
 // L2: the neighbouring tiles' CTAs run beside it over the same planes).  The velocities of a plane
 // land in a ring of three planes in shared memory, the z neighbours of a thread's own cells stay in
-// its registers, and once plane z+1 is in, the tile's cells add the terms of plane z.  rho and u
+// its registers, and once plane z+1 is in, the tile's cells add the terms of plane z.  The planes
+// are handed over by a split barrier: a warp arrives on an mbarrier once its velocities of plane g
+// are in the ring and then waits for plane g-1 only, so no warp waits for the slowest warp of the
+// plane it has just written; a ring of four planes keeps a slot from being rewritten while a slow
+// warp still reads it (a warp writing plane g has seen every warp arrive for plane g-2, after its
+// terms of plane g-3, the slot's last reader).  Every wait is bounded: past kPopWaitNs the warp
+// sets the CTA's abort flag, every warp leaves at its next wait, the CTA's partials become NaN and
+// the error word is set.  rho and u
 // come from cell_macro (k_macro's arithmetic) and the velocity differences are taken in float, as in
 // the two-pass path, so each cell's terms are the same numbers; dterm::CellSums adds them (to
 // ~1e-13 of the sums) in a fixed order: items dealt to CTAs in a fixed order, fixed trees.  The next
 // plane's loads are issued before the current plane's terms, so they are in flight across the
-// barrier.  One 608-thread CTA per SM (96 registers) with this tile measured faster than two
-// 336-thread CTAs of 64 x 8 (a quarter of the loads in the halo, spills at 80 registers).
+// wait.  One 608-thread CTA per SM (96 registers) with this tile measured faster than two 336-thread
+// CTAs of 64 x 8 (a quarter of the loads in the halo, spills at 80 registers).
 constexpr int kPopTx = 64, kPopTy = 16;
 constexpr int kPopCols = kPopTx + 4;                          // x0-2 .. x0+kPopTx+1: whole pairs
 constexpr int kPopRows = kPopTy + 2;                          // y0-1 .. y0+kPopTy
 constexpr int kPopInner = kPopTx / 2 * kPopTy;                // threads on the tile's own pairs
 constexpr int kPopThreads = kPopInner + kPopTx + 2 * kPopTy;  // + the rows y0-1, y0+kPopTy, the x pairs
+constexpr int kPopWarps = kPopThreads / 32;
+constexpr int kPopSlots = 4;
+constexpr size_t kPopRingBytes = sizeof(float) * kPopSlots * 3 * kPopRows * kPopCols;  // 58,752 B, dynamic
+constexpr unsigned long long kPopWaitNs = 2000000000ull;  // a plane hand-over takes microseconds
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(b))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_done(unsigned long long* b, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long pop_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Warp-collective (every lane calls it): true once the phase of parity `parity` of *b has completed;
+// false, the same in every lane, when *abort is set or the wait outlives kPopWaitNs (then it sets it).
+__device__ __forceinline__ bool pop_wait(unsigned long long* b, unsigned parity, volatile int* abort) {
+    unsigned long long t0 = 0;
+    for (;;) {
+        const bool ok = mbar_done(b, parity);
+        if (__all_sync(0xffffffffu, ok)) return true;
+        bool bad = *abort != 0;
+        if (!bad) {
+            const unsigned long long t = pop_ns();
+            if (t0 == 0) t0 = t;
+            else bad = t - t0 > kPopWaitNs;
+        }
+        if (__any_sync(0xffffffffu, bad)) {
+            *abort = 1;
+            return false;
+        }
+    }
+}
 
 // the 19 population arrays of a cube, in the order the kernel reads them (layout 2 permuted here)
 template <class RAW>
@@ -476,12 +536,22 @@ template <> struct PopPair<uint16_t> {
 template <class ST, bool SHIFTED>
 __global__ void __launch_bounds__(kPopThreads, 1)
     k_diag_pop(const PopPtrs<typename ST::raw> P, int n, int ntx, int ntiles, int zc, int items,
-               double* __restrict__ partials) {
+               double* __restrict__ partials, int* __restrict__ err) {
     using RAW = typename ST::raw;
     using PP = PopPair<RAW>;
     using W = typename PP::word;
-    __shared__ __align__(16) float ring[3][3][kPopRows][kPopCols];
-    const int t = threadIdx.x;
+    extern __shared__ __align__(16) float pop_ring[];
+    auto ring = reinterpret_cast<float(*)[3][kPopRows][kPopCols]>(pop_ring);  // [slot][u, v, w][row][col]
+    __shared__ unsigned long long mb[2];  // plane g complete: mb[g & 1], phase g >> 1
+    __shared__ int abort_flag;
+    volatile int* abort = &abort_flag;
+    const int t = threadIdx.x, lane = t & 31;
+    if (t == 0) {
+        mbar_init(&mb[0], kPopWarps);
+        mbar_init(&mb[1], kPopWarps);
+        abort_flag = 0;
+    }
+    __syncthreads();
     // this thread's pair (x, x+1) relative to the tile origin: the tile's pairs, the rows y = -1 and
     // y = kPopTy, then the pairs x = -2 and x = kPopTx of the tile's rows
     int ox, oy;
@@ -503,7 +573,9 @@ __global__ void __launch_bounds__(kPopThreads, 1)
         return a < 0 ? a + n : a;
     };
     dterm::CellSums sums;
-    for (int it = blockIdx.x; it < items; it += gridDim.x) {
+    unsigned g = 0;  // planes this CTA has walked, over all its items
+    bool ok = true;
+    for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
         const int zci = it / ntiles, tile = it - zci * ntiles;
         const int ty = tile / ntx, tx = tile - ty * ntx;
         const int x0 = tx * kPopTx, y0 = ty * kPopTy;
@@ -535,8 +607,7 @@ __global__ void __launch_bounds__(kPopThreads, 1)
         // the thread's two cells one plane back (u, v, w, rho) and two planes back (u, v)
         float u1a = 0.f, v1a = 0.f, w1a = 0.f, r1a = 0.f, u2a = 0.f, v2a = 0.f;
         float u1b = 0.f, v1b = 0.f, w1b = 0.f, r1b = 0.f, u2b = 0.f, v2b = 0.f;
-        int cur = 0;                                       // ring slot of plane zs - 1 + r
-        for (int r = 0; r <= m + 1; ++r) {
+        for (int r = 0; r <= m + 1; ++r, ++g) {  // plane zs - 1 + r, ring slot g & 3
             float rhoa, ua, va, wa, rhob, ub, vb, wb;
             {
                 float fa[Q], fb[Q];
@@ -549,13 +620,19 @@ __global__ void __launch_bounds__(kPopThreads, 1)
                 cell_macro<ST>(fb, rhob, ub, vb, wb);
             }
             if (r <= m) load_plane(zs + r == n ? 0 : zs + r);
+            const int cur = g & 3;
             *reinterpret_cast<float2*>(&ring[cur][0][row][col]) = make_float2(ua, ub);
             *reinterpret_cast<float2*>(&ring[cur][1][row][col]) = make_float2(va, vb);
             *reinterpret_cast<float2*>(&ring[cur][2][row][col]) = make_float2(wa, wb);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&mb[g & 1]);
+            if (g > 0 && !pop_wait(&mb[(g - 1) & 1], ((g - 1) >> 1) & 1, abort)) {
+                ok = false;
+                break;
+            }
             if (r >= 2) {
-                __syncthreads();
-                if (valid) {  // the terms of plane zs + r - 2, from the slot before cur
-                    const int pv = cur == 0 ? 2 : cur - 1;
+                if (valid) {  // the terms of plane zs + r - 2, from the slot of plane g - 1
+                    const int pv = (g - 1) & 3;
                     auto ld2 = [&](int comp, int rr, int cc) {
                         return *reinterpret_cast<const float2*>(&ring[pv][comp][rr][cc]);
                     };
@@ -580,14 +657,12 @@ __global__ void __launch_bounds__(kPopThreads, 1)
             v1b = vb;
             w1b = wb;
             r1b = rhob;
-            cur = cur == 2 ? 0 : cur + 1;
         }
-        __syncthreads();  // the next item writes the ring from its first plane on
     }
     sums.flush();
     double e = warp_sum(sums.de), ens = warp_sum(sums.dens), mass = warp_sum(sums.dmass);
     __shared__ double sh[3][kPopThreads / 32];
-    const int wid = t >> 5, lane = t & 31;
+    const int wid = t >> 5;
     if (lane == 0) {
         sh[0][wid] = e;
         sh[1][wid] = ens;
@@ -597,22 +672,24 @@ __global__ void __launch_bounds__(kPopThreads, 1)
     if (t < 3) {
         double sum = 0.0;
         for (int i = 0; i < kPopThreads / 32; ++i) sum += sh[t][i];
-        partials[blockIdx.x * 3 + t] = sum;
+        partials[blockIdx.x * 3 + t] = *abort ? __longlong_as_double(0x7ff8000000000000ll) : sum;
     }
+    if (t == 0 && *abort) atomicExch(err, 1);
 }
 
 template <class ST>
 static cudaError_t launch_diag_pop_t(int layout, const void* f, int n, double* partials_dev, double* out_dev,
-                                     cudaStream_t st) {
+                                     int* err_dev, double* flag_out, cudaStream_t st) {
     using RAW = typename ST::raw;
     auto kern = layout == 1 ? k_diag_pop<ST, true> : k_diag_pop<ST, false>;
     PopPtrs<RAW> P;
     const size_t cells = (size_t)n * n * n;
     for (int q = 0; q < Q; ++q) P.q[q] = (const RAW*)f + (size_t)(layout == 2 ? opp(q) : q) * cells;
     int dev = 0, sms = 0, per_sm = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPopRingBytes);
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPopThreads, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPopThreads, kPopRingBytes);
     if (e != cudaSuccess) return e;
     const long long cap = std::min<long long>(kDiagBlocks, std::max(1, sms * std::max(1, per_sm)));
     const int ntx = (n + kPopTx - 1) / kPopTx, nty = (n + kPopTy - 1) / kPopTy, ntiles = ntx * nty;
@@ -630,20 +707,21 @@ static cudaError_t launch_diag_pop_t(int layout, const void* f, int n, double* p
     }
     const long long nzc = (n + best_zc - 1) / best_zc, items = (long long)ntiles * nzc;
     const int grid = (int)std::min(items, cap);
-    kern<<<grid, kPopThreads, 0, st>>>(P, n, ntx, ntiles, best_zc, (int)items, partials_dev);
-    k_diag_finish<<<1, 256, 0, st>>>(partials_dev, grid, 1.0 / double(cells), out_dev);
+    kern<<<grid, kPopThreads, kPopRingBytes, st>>>(P, n, ntx, ntiles, best_zc, (int)items, partials_dev, err_dev);
+    k_diag_finish<<<1, 256, 0, st>>>(partials_dev, grid, 1.0 / double(cells), out_dev, err_dev, flag_out);
     note_launch(2);
     return cudaGetLastError();
 }
 
 cudaError_t launch_diag_pop(int storage, int layout, const void* f, int n, double* partials_dev, double* out_dev,
-                            cudaStream_t st) {
+                            double* flag_out, cudaStream_t st) {
     // pairs of cells at even x need an even n; cell indices are 32-bit
     if (n < 2 || n % 2 != 0 || n > 1600 || layout < 0 || layout > 2) return cudaErrorInvalidValue;
+    int* err = diag_err_word(partials_dev);
     switch (storage) {
-        case 0: return launch_diag_pop_t<StF32>(layout, f, n, partials_dev, out_dev, st);
-        case 1: return launch_diag_pop_t<StF16>(layout, f, n, partials_dev, out_dev, st);
-        case 2: return launch_diag_pop_t<StBF16>(layout, f, n, partials_dev, out_dev, st);
+        case 0: return launch_diag_pop_t<StF32>(layout, f, n, partials_dev, out_dev, err, flag_out, st);
+        case 1: return launch_diag_pop_t<StF16>(layout, f, n, partials_dev, out_dev, err, flag_out, st);
+        case 2: return launch_diag_pop_t<StBF16>(layout, f, n, partials_dev, out_dev, err, flag_out, st);
         default: return cudaErrorInvalidValue;
     }
 }
