@@ -173,6 +173,12 @@ def ref_run(f: np.ndarray, n: int, omega: float, nsteps: int) -> np.ndarray:
     return a
 
 
+def ref_run_inplace(f: np.ndarray, n: int, omega: float, nsteps: int) -> None:
+    """ref_run on f itself (no host copy: the N=512 state is 10.2 GB)."""
+    assert f.dtype == np.float32 and f.flags.c_contiguous
+    _rck(ref().ref_uniform_run(_fp(f), n, omega, nsteps))
+
+
 def ref_macro(f: np.ndarray, n: int) -> np.ndarray:
     F = np.empty(4 * n ** 3, dtype=np.float32)
     _rck(ref().ref_uniform_macro(_fp(np.ascontiguousarray(f, dtype=np.float32)), n, _fp(F)))

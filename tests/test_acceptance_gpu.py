@@ -14,6 +14,8 @@ per test); the gold criteria are checked on both sides as well.
       sensor, populations within 1e-5 relative per coarse step from a shared state, and the whole
       t*=20 run of both sides on the same grids against the dynamic gold criteria
   N=256 one FP32 step from the reference's state against the reference's k_step
+  N=512 the same at the benchmark size (10.2 GB of state; skipped where the host or the GPU lacks the
+        memory for two copies on each)
 """
 import numpy as np
 import pytest
@@ -341,4 +343,32 @@ def test_uniform_n256_step_from_reference_state():
         s.step(1)
         err = rel_err(s.get_populations(layout="blocked"), g)
     print("\nN=256 one step from the reference's state: max relative error %.2e" % err)
+    assert err < 1e-5
+
+
+def test_uniform_n512_step_from_reference_state():
+    # the per-step bar at the benchmark size: one engine step from the reference's state after 20
+    # steps, against the reference's k_step, on every population of 512^3 cells
+    import torch
+    n = 512
+    need = 19 * n ** 3 * 4                      # one state, 10.2 GB
+    avail = 0
+    with open("/proc/meminfo") as fh:
+        for line in fh:
+            if line.startswith("MemAvailable:"):
+                avail = int(line.split()[1]) * 1024
+    if avail < 5 * need:
+        pytest.skip("host memory: %.0f GB available, the test holds up to 4 states of 10.2 GB" % (avail / 1e9))
+    if torch.cuda.mem_get_info()[0] < 5 * need:
+        pytest.skip("device memory: two states on each side")
+    p = O.params(n, 1600.0)
+    f = O.ref_init(n)
+    O.ref_run_inplace(f, n, p["omega"], 20)
+    with J.Solver("uniform", n=n, re=1600.0) as s:
+        s.set_populations(f, layout="blocked")
+        s.step(1)
+        e = s.get_populations(layout="blocked")
+    O.ref_run_inplace(f, n, p["omega"], 1)
+    err = rel_err(e, f)
+    print("\nN=512 one step from the reference's state: max relative error %.2e" % err)
     assert err < 1e-5
