@@ -150,9 +150,12 @@ jp_status jp_sync(jp_solver* s);
 
 /* Mean kinetic energy 1/2|u|^2, mean enstrophy 1/2|omega|^2 (central differences, periodic) and
  * mean density of the current state, computed on the device with a deterministic reduction: per-cell
- * terms of a float field in double-float (within ~1e-14 relative of FP64), sums in FP64.
- * out[0]=E, out[1]=enstrophy, out[2]=mass.  Replaces k_macro + the host loop of
- * src/tgv3d_uniform.cu:169-189 and k_composite + k_diag_reduce of src/tgv3d_amr.cu:882-888. */
+ * terms of a float field in double-float (within ~1e-13 relative of FP64), sums in FP64.  A uniform
+ * cube in FP32/FP16/BF16 storage is reduced in one pass over its populations (no macro field); its
+ * kernel's waits between warps are bounded, and JP_ERR_TIMEOUT reports one that gave up (never seen
+ * in practice; out then holds NaN).  out[0]=E, out[1]=enstrophy, out[2]=mass.  Replaces k_macro +
+ * the host loop of src/tgv3d_uniform.cu:169-189 and k_composite + k_diag_reduce of
+ * src/tgv3d_amr.cu:882-888. */
 jp_status jp_diag(jp_solver* s, double out[3]);
 
 /* ---- population I/O (parity checks, checkpoint/restart, host-resident workloads) ----------- */
