@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(TPB, (min_blocks<ST, V, TPB>())) k_stream_coll
 
     // 4. moments, 5. relax and store, one population pair at a time
     const R om = sizeof(R) == 8 ? R(d.omega_d) : R(d.omega);
-    CellBgk<R, V, SA> c(om);
+    CellBgk<R, V, SA, SH> c(om);
     c.moments(f);
     const size_t orow = ((size_t)z * n + y) * n + x0;
     {
@@ -532,6 +532,23 @@ template <> struct PopPair<uint16_t> {
     __device__ static __forceinline__ word make(uint16_t a, uint16_t b) { return (unsigned)a | ((unsigned)b << 16); }
 };
 
+// the two cells of a pair word in the collision type: both halves of a 16-bit pair in one conversion
+template <class ST>
+__device__ __forceinline__ void pop_unpack(typename PopPair<typename ST::raw>::word w, float& a, float& b) {
+    if constexpr (ST::id == 1) {
+        const float2 t = __half22float2(*reinterpret_cast<const __half2*>(&w));
+        a = t.x;
+        b = t.y;
+    } else if constexpr (ST::id == 2) {
+        const float2 t = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w));
+        a = t.x;
+        b = t.y;
+    } else {
+        a = ST::load(PopPair<typename ST::raw>::lo(w));
+        b = ST::load(PopPair<typename ST::raw>::hi(w));
+    }
+}
+
 // SHIFTED: the in-place layout after an even step count (population q of cell x at [q][x + c_q]).
 template <class ST, bool SHIFTED>
 __global__ void __launch_bounds__(kPopThreads, 1)
@@ -612,10 +629,7 @@ __global__ void __launch_bounds__(kPopThreads, 1)
             {
                 float fa[Q], fb[Q];
 #pragma unroll
-                for (int q = 0; q < Q; ++q) {
-                    fa[q] = ST::load(PP::lo(a[q]));
-                    fb[q] = ST::load(PP::hi(a[q]));
-                }
+                for (int q = 0; q < Q; ++q) pop_unpack<ST>(a[q], fa[q], fb[q]);
                 cell_macro<ST>(fa, rhoa, ua, va, wa);
                 cell_macro<ST>(fb, rhob, ub, vb, wb);
             }

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(TPB, (aa_min_blocks<ST, V, TPB>())) k_aa_local
         for (int v = 0; v < V; ++v) f[v][q] = (SA && !SH) ? ST::load(L[q].v[v]) - wgt<R>(q) : ST::load(L[q].v[v]);
 
     const R om = sizeof(R) == 8 ? R(d.omega_d) : R(d.omega);
-    CellBgk<R, V, SA> c(om);
+    CellBgk<R, V, SA, SH> c(om);
     c.moments(f);
     {
         R o0[V];
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(TPB, (aa_stream_min_blocks<ST, V, TPB>())) k_a
         }
     // 4. relax in place
     const R om = sizeof(R) == 8 ? R(d.omega_d) : R(d.omega);
-    CellBgk<R, V, SA> c(om);
+    CellBgk<R, V, SA, SH> c(om);
     c.moments(f);
 #pragma unroll
     for (int v = 0; v < V; ++v) f[v][0] = c.rest(f, v);

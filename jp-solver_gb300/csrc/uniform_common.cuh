@@ -82,7 +82,9 @@ constexpr int min_blocks() {
 // (FP32 shifts on load, the 16-bit formats store shifts), f itself for FP64.  BGK as
 // out = (1 - omega) f + omega feq with omega*w*rho folded per weight class: with a = c.u,
 // feq_pm = w rho (1 - 1.5|u|^2 + 4.5 a^2) +- 3 w rho a (shifted: the -w part cancels against g).
-template <class R, int V, bool SA>
+// PACK: the FP32 relaxation on pairs of cells (CellBgk<float, V, true, true> below), for the 16-bit
+// storages, whose steps are issue-bound; FP32 and FP64 storage keep this one.
+template <class R, int V, bool SA, bool PACK = false>
 struct CellBgk {
     R om, omc;
     R s[V], rho[V], ux[V], uy[V], uz[V], usq[V];
@@ -141,6 +143,135 @@ struct CellBgk {
             const R oasym = (q < 7 ? owr3a[v] : owr3b[v]) * a;           // omega * antisymmetric part
             oa[v] = omc * f[v][q] + (osym + oasym);
             ob[v] = omc * f[v][q + 1] + (osym - oasym);
+        }
+    }
+};
+
+// ---- the same relaxation in FP32 on pairs of cells ------------------------------------------------
+// Blackwell issues two FP32 adds, multiplies or FMAs in one instruction (f32x2; __fadd2_rn,
+// __fmul2_rn, __ffma2_rn, each lane rounded to nearest like its scalar op).  The FP32 steps hold V = 2,
+// 4 or 8 cells per thread, so the relaxation runs on pairs of cells and issues half the FP32
+// instructions; an odd V runs the same sequence on single floats.  The 16-bit storages use it (their
+// steps are issue-bound); FP32 storage, bound by HBM, keeps the scalar code above.  Every operation is spelled out
+// (no contraction left to the compiler), so a cell's result does not depend on V, and the pull and
+// in-place steps, which share this code, produce the same bits.  The sequence per cell:
+//   s = g0 + g1 + ... + g18, j = the signed sums in q order, rho = 1 + s, inv = 1/rho (IEEE), u = j inv
+//   t = ux ux + uy uy + uz uz (two FMAs), base = -1.5 t, feq0 = w0 (s + rho base)
+//   out0 = (1 - om) g0 + om feq0, and per odd q with a = c_q . u (two terms at most):
+//   sym = om w s + om w rho (4.5 a a + base), asym = 3 om w rho a, out_q = (1 - om) g_q + (sym + asym),
+//   out_opp(q) = (1 - om) g_opp(q) + (sym - asym).
+template <class T> struct Lanes;
+template <> struct Lanes<float> {
+    static __device__ __forceinline__ float bc(float s) { return s; }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fmaf_rn(b, -1.f, a); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+    static __device__ __forceinline__ float rcp(float a) { return __frcp_rn(a); }
+};
+template <> struct Lanes<float2> {
+    static __device__ __forceinline__ float2 bc(float s) { return make_float2(s, s); }
+    static __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+    // a - b exactly rounded: b * -1 is exact, so the FMA rounds once, as a subtraction does
+    static __device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+    static __device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+    static __device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+    static __device__ __forceinline__ float2 rcp(float2 a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
+};
+
+template <int V>
+struct CellBgk<float, V, true, true> {
+    static constexpr bool PAIR = V % 2 == 0;
+    static constexpr int NP = PAIR ? V / 2 : V;  // lanes
+    using T = typename std::conditional<PAIR, float2, float>::type;
+    using L = Lanes<T>;
+    float om, omc;
+    T s[NP], rho[NP], ux[NP], uy[NP], uz[NP], base[NP];
+    T owr1[NP], owr2[NP], owr3a[NP], owr3b[NP], ows1[NP], ows2[NP];
+    T orest[NP];
+
+    __device__ __forceinline__ explicit CellBgk(float omega) : om(omega), omc(1.f - omega) {}
+
+    static __device__ __forceinline__ T get(const float (&f)[V][Q], int p, int q) {
+        if constexpr (PAIR) return make_float2(f[2 * p][q], f[2 * p + 1][q]);
+        else return f[p][q];
+    }
+    static __device__ __forceinline__ void put(float (&o)[V], int p, T v) {
+        if constexpr (PAIR) {
+            o[2 * p] = v.x;
+            o[2 * p + 1] = v.y;
+        } else {
+            o[p] = v;
+        }
+    }
+    // c_q . u for odd q (its first non-zero component is positive)
+    __device__ __forceinline__ T cdot_odd(int q, int p) const {
+        T a = cx(q) != 0 ? ux[p] : (cy(q) != 0 ? uy[p] : uz[p]);
+        if (cx(q) != 0 && cy(q) != 0) a = cy(q) > 0 ? L::add(a, uy[p]) : L::sub(a, uy[p]);
+        if ((cx(q) != 0 || cy(q) != 0) && cz(q) != 0) a = cz(q) > 0 ? L::add(a, uz[p]) : L::sub(a, uz[p]);
+        return a;
+    }
+
+    __device__ __forceinline__ void moments(const float (&f)[V][Q]) {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            T g[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) g[q] = get(f, p, q);
+            T sm = g[0];
+#pragma unroll
+            for (int q = 1; q < Q; ++q) sm = L::add(sm, g[q]);
+            // j in q order: a signed sum of the populations with that velocity component
+            constexpr int kx[10] = {1, 2, 7, 8, 9, 10, 11, 12, 13, 14}, ky[10] = {3, 4, 7, 8, 9, 10, 15, 16, 17, 18},
+                          kz[10] = {5, 6, 11, 12, 13, 14, 15, 16, 17, 18};
+            T jx = g[1], jy = g[3], jz = g[5];
+#pragma unroll
+            for (int i = 1; i < 10; ++i) {
+                jx = cx(kx[i]) > 0 ? L::add(jx, g[kx[i]]) : L::sub(jx, g[kx[i]]);
+                jy = cy(ky[i]) > 0 ? L::add(jy, g[ky[i]]) : L::sub(jy, g[ky[i]]);
+                jz = cz(kz[i]) > 0 ? L::add(jz, g[kz[i]]) : L::sub(jz, g[kz[i]]);
+            }
+            const T rh = L::add(L::bc(1.f), sm);
+            const T inv = L::rcp(rh);
+            s[p] = sm;
+            rho[p] = rh;
+            ux[p] = L::mul(jx, inv);
+            uy[p] = L::mul(jy, inv);
+            uz[p] = L::mul(jz, inv);
+            T t = L::mul(ux[p], ux[p]);
+            t = L::fma(uy[p], uy[p], t);
+            t = L::fma(uz[p], uz[p], t);
+            base[p] = L::mul(L::bc(-1.5f), t);
+            // the folded per-class terms and the rest population
+            const T feq0 = L::mul(L::bc(wf(0)), L::fma(rh, base[p], sm));
+            orest[p] = L::fma(L::bc(omc), g[0], L::mul(L::bc(om), feq0));
+            const T orho = L::mul(L::bc(om), rh);
+            owr1[p] = L::mul(orho, L::bc(wf(1)));
+            owr2[p] = L::mul(orho, L::bc(wf(7)));
+            owr3a[p] = L::mul(L::bc(3.f), owr1[p]);
+            owr3b[p] = L::mul(L::bc(3.f), owr2[p]);
+            ows1[p] = L::mul(L::bc(__fmul_rn(om, wf(1))), sm);
+            ows2[p] = L::mul(L::bc(__fmul_rn(om, wf(7))), sm);
+        }
+    }
+
+    // relaxed rest population of cell v (moments() computed it)
+    __device__ __forceinline__ float rest(const float (&)[V][Q], int v) const {
+        if constexpr (PAIR) return (v & 1) ? orest[v / 2].y : orest[v / 2].x;
+        else return orest[v];
+    }
+
+    // relaxed populations q and q+1 = opp(q) (q odd) of every cell
+    __device__ __forceinline__ void pair(const float (&f)[V][Q], int q, float (&oa)[V], float (&ob)[V]) const {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const T a = cdot_odd(q, p);
+            const T owr = q < 7 ? owr1[p] : owr2[p];
+            const T t = L::mul(owr, L::fma(L::mul(L::bc(4.5f), a), a, base[p]));
+            const T osym = L::add(q < 7 ? ows1[p] : ows2[p], t);
+            const T oasym = L::mul(q < 7 ? owr3a[p] : owr3b[p], a);
+            put(oa, p, L::fma(L::bc(omc), get(f, p, q), L::add(osym, oasym)));
+            put(ob, p, L::fma(L::bc(omc), get(f, p, q + 1), L::sub(osym, oasym)));
         }
     }
 };
