@@ -144,37 +144,62 @@ __device__ __forceinline__ void bgk(float (&f)[Q], float om) {
 // g = f - w_q (every AMR step works on them, PoolIO), rho = 1 + sum g, and the result is shifted too
 // (feq_q - w_q = w_q (s + rho (3a + 4.5a^2 - 1.5|u|^2)) with s = sum g), which keeps the round-off at
 // the level of the deviations: sum feq - rho then carries no bias of the O(w_q) terms, and mass
-// drifts ~1e3 times less.
-template <bool SH = false>
-__device__ __forceinline__ void bgk_fast(float (&f)[Q], float om) {
-    float sm = f[0];
+// drifts ~1e3 times less.  Written once over the lane type (Lanes): T = float relaxes one cell,
+// T = float2 two cells with packed FP32 instructions, every operation spelled out in the same order,
+// so a cell gets the same bits either way (the rows kernel relaxes its four cells as two pairs).
+#ifdef __CUDACC__
+template <class T, bool SH = false>
+__device__ __forceinline__ void bgk_lanes(T (&f)[Q], float om) {
+    using L = Lanes<T>;
+    T sm = f[0];
 #pragma unroll
-    for (int q = 1; q < Q; ++q) sm += f[q];
-    const float jx = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
-    const float jy = f[3] - f[4] + f[7] - f[8] - f[9] + f[10] + f[15] - f[16] + f[17] - f[18];
-    const float jz = f[5] - f[6] + f[11] - f[12] - f[13] + f[14] + f[15] - f[16] - f[17] + f[18];
-    const float rho = SH ? 1.f + sm : sm;
-    const float inv = 1.f / rho;
-    const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-    const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
-    const float base = SH ? -usq : 1.f - usq;
-    const float omc = 1.f - om, orho = om * rho;
-    const float owr1 = orho * wf(1), owr2 = orho * wf(7), owr3a = 3.f * owr1, owr3b = 3.f * owr2;
-    if constexpr (SH) {
-        f[0] = omc * f[0] + om * wf(0) * (sm - rho * usq);
+    for (int q = 1; q < Q; ++q) sm = L::add(sm, f[q]);
+    // j in q order: a signed sum of the populations with that velocity component
+    constexpr int kx[10] = {1, 2, 7, 8, 9, 10, 11, 12, 13, 14}, ky[10] = {3, 4, 7, 8, 9, 10, 15, 16, 17, 18},
+                  kz[10] = {5, 6, 11, 12, 13, 14, 15, 16, 17, 18};
+    T jx = f[1], jy = f[3], jz = f[5];
+#pragma unroll
+    for (int i = 1; i < 10; ++i) {
+        jx = cx(kx[i]) > 0 ? L::add(jx, f[kx[i]]) : L::sub(jx, f[kx[i]]);
+        jy = cy(ky[i]) > 0 ? L::add(jy, f[ky[i]]) : L::sub(jy, f[ky[i]]);
+        jz = cz(kz[i]) > 0 ? L::add(jz, f[kz[i]]) : L::sub(jz, f[kz[i]]);
+    }
+    const T rho = SH ? L::add(L::bc(1.f), sm) : sm;
+    const T inv = L::rcp(rho);
+    const T ux = L::mul(jx, inv), uy = L::mul(jy, inv), uz = L::mul(jz, inv);
+    T t2 = L::mul(ux, ux);
+    t2 = L::fma(uy, uy, t2);
+    t2 = L::fma(uz, uz, t2);
+    const T usq = L::mul(L::bc(1.5f), t2);
+    const T base = SH ? L::mul(L::bc(-1.5f), t2) : L::sub(L::bc(1.f), usq);  // -usq exactly when SH
+    const float omc = 1.f - om;
+    const T orho = L::mul(L::bc(om), rho);
+    const T owr1 = L::mul(orho, L::bc(wf(1))), owr2 = L::mul(orho, L::bc(wf(7)));
+    const T owr3a = L::mul(L::bc(3.f), owr1), owr3b = L::mul(L::bc(3.f), owr2);
+    if constexpr (SH) {  // (omega w0) (s - rho usq)
+        f[0] = L::fma(L::bc(omc), f[0], L::mul(L::bc(om * wf(0)), L::fma(rho, base, sm)));
     } else {
-        f[0] = omc * f[0] + orho * wf(0) * base;
+        f[0] = L::fma(L::bc(omc), f[0], L::mul(L::mul(orho, L::bc(wf(0))), base));
     }
 #pragma unroll
-    for (int q = 1; q < Q; q += 2) {
-        const float a = cdot<float>(q, ux, uy, uz);
-        float t = (q < 7 ? owr1 : owr2) * (4.5f * a * a + base);
-        if constexpr (SH) t += om * wf(q) * sm;  // omega * w * s, the shifted part of the equilibrium
-        const float as = (q < 7 ? owr3a : owr3b) * a;
-        f[q] = omc * f[q] + (t + as);
-        f[q + 1] = omc * f[q + 1] + (t - as);
+    for (int q = 1; q < Q; q += 2) {  // q odd: the first non-zero component of c_q is positive
+        T a = cx(q) != 0 ? ux : (cy(q) != 0 ? uy : uz);
+        if (cx(q) != 0 && cy(q) != 0) a = cy(q) > 0 ? L::add(a, uy) : L::sub(a, uy);
+        if ((cx(q) != 0 || cy(q) != 0) && cz(q) != 0) a = cz(q) > 0 ? L::add(a, uz) : L::sub(a, uz);
+        T t = L::mul(q < 7 ? owr1 : owr2, L::fma(L::mul(L::bc(4.5f), a), a, base));
+        // + omega w s, the shifted part, as one FMA: a product by a broadcast constant followed by an add
+        // is not compiled alike for one lane and for two, an FMA is
+        if constexpr (SH) t = L::fma(L::bc(om * wf(q)), sm, t);
+        const T as = L::mul(q < 7 ? owr3a : owr3b, a);
+        f[q] = L::fma(L::bc(omc), f[q], L::add(t, as));
+        f[q + 1] = L::fma(L::bc(omc), f[q + 1], L::sub(t, as));
     }
 }
+template <bool SH = false>
+__device__ __forceinline__ void bgk_fast(float (&f)[Q], float om) {
+    bgk_lanes<float, SH>(f, om);
+}
+#endif
 
 // Where population q of cell (i, j, k) is pulled from: the neighbour slot e = (dz+1)*9 + (dy+1)*3 +
 // (dx+1) of the same-level block at offset (dx, dy, dz) (13: the block itself) and the cell sc inside

@@ -158,27 +158,8 @@ struct CellBgk {
 //   s = g0 + g1 + ... + g18, j = the signed sums in q order, rho = 1 + s, inv = 1/rho (IEEE), u = j inv
 //   t = ux ux + uy uy + uz uz (two FMAs), base = -1.5 t, feq0 = w0 (s + rho base)
 //   out0 = (1 - om) g0 + om feq0, and per odd q with a = c_q . u (two terms at most):
-//   sym = om w s + om w rho (4.5 a a + base), asym = 3 om w rho a, out_q = (1 - om) g_q + (sym + asym),
+//   sym = fma(om w, s, om w rho (4.5 a a + base)), asym = 3 om w rho a, out_q = (1 - om) g_q + (sym + asym),
 //   out_opp(q) = (1 - om) g_opp(q) + (sym - asym).
-template <class T> struct Lanes;
-template <> struct Lanes<float> {
-    static __device__ __forceinline__ float bc(float s) { return s; }
-    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-    static __device__ __forceinline__ float sub(float a, float b) { return __fmaf_rn(b, -1.f, a); }
-    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-    static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-    static __device__ __forceinline__ float rcp(float a) { return __frcp_rn(a); }
-};
-template <> struct Lanes<float2> {
-    static __device__ __forceinline__ float2 bc(float s) { return make_float2(s, s); }
-    static __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-    // a - b exactly rounded: b * -1 is exact, so the FMA rounds once, as a subtraction does
-    static __device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
-    static __device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-    static __device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-    static __device__ __forceinline__ float2 rcp(float2 a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
-};
-
 template <int V>
 struct CellBgk<float, V, true, true> {
     static constexpr bool PAIR = V % 2 == 0;
@@ -187,7 +168,7 @@ struct CellBgk<float, V, true, true> {
     using L = Lanes<T>;
     float om, omc;
     T s[NP], rho[NP], ux[NP], uy[NP], uz[NP], base[NP];
-    T owr1[NP], owr2[NP], owr3a[NP], owr3b[NP], ows1[NP], ows2[NP];
+    T owr1[NP], owr2[NP], owr3a[NP], owr3b[NP];
     T orest[NP];
 
     __device__ __forceinline__ explicit CellBgk(float omega) : om(omega), omc(1.f - omega) {}
@@ -250,8 +231,7 @@ struct CellBgk<float, V, true, true> {
             owr2[p] = L::mul(orho, L::bc(wf(7)));
             owr3a[p] = L::mul(L::bc(3.f), owr1[p]);
             owr3b[p] = L::mul(L::bc(3.f), owr2[p]);
-            ows1[p] = L::mul(L::bc(__fmul_rn(om, wf(1))), sm);
-            ows2[p] = L::mul(L::bc(__fmul_rn(om, wf(7))), sm);
+
         }
     }
 
@@ -268,7 +248,9 @@ struct CellBgk<float, V, true, true> {
             const T a = cdot_odd(q, p);
             const T owr = q < 7 ? owr1[p] : owr2[p];
             const T t = L::mul(owr, L::fma(L::mul(L::bc(4.5f), a), a, base[p]));
-            const T osym = L::add(q < 7 ? ows1[p] : ows2[p], t);
+            // + omega w s as one FMA (a product by a broadcast constant then an add is not compiled
+            // alike in every kernel; an FMA is)
+            const T osym = L::fma(L::bc(om * wf(q)), s[p], t);
             const T oasym = L::mul(q < 7 ? owr3a[p] : owr3b[p], a);
             put(oa, p, L::fma(L::bc(omc), get(f, p, q), L::add(osym, oasym)));
             put(ob, p, L::fma(L::bc(omc), get(f, p, q + 1), L::sub(osym, oasym)));
