@@ -521,49 +521,53 @@ __device__ __forceinline__ void d_step_fine_rows(const typename ST::raw* __restr
         }
         // 3. the pulled values of the four cells, converted once, and relaxed.  FP32: as two pairs of
         // cells (v, v + 1) in packed FP32 instructions (bgk_lanes: each cell gets the per-cell steps'
-        // bits), which shortens the latency-bound FP32 rows; 16-bit rows, which hold five CTAs per SM in
-        // fewer registers, relax cell by cell (packed pairs spilled there and measured no faster).
-        constexpr bool PACK = sizeof(raw) == 4;
-        float2 g[2][Q];
-        float f[PACK ? 1 : 4][Q];
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            float fv[4];
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                const raw x = cx(q) > 0 ? (v == 0 ? E[q] : L[q].v[v - 1])
-                                        : (cx(q) < 0 ? (v == 3 ? E[q] : L[q].v[v + 1]) : L[q].v[v]);
-                fv[v] = PoolIO<ST>::g_of(x, q);
-            }
-            if constexpr (PACK) {
-                g[0][q] = make_float2(fv[0], fv[1]);
-                g[1][q] = make_float2(fv[2], fv[3]);
-            } else {
-#pragma unroll
-                for (int v = 0; v < 4; ++v) f[PACK ? 0 : v][q] = fv[v];
-            }
-        }
-        if constexpr (PACK) {
-            bgk_lanes<float2, true>(g[0], om);
-            bgk_lanes<float2, true>(g[1], om);
-        } else {
-#pragma unroll
-            for (int v = 0; v < 4; ++v) bgk_fast<true>(f[PACK ? 0 : v], om);
-        }
-        auto out = [&](int v, int q) -> float {
-            if constexpr (PACK) return (v & 1) ? g[v >> 1][q].y : g[v >> 1][q].x;
-            else return f[PACK ? 0 : v][q];
+        // bits), which shortens the latency-bound FP32 rows.  The 16-bit rows, which hold five CTAs per
+        // SM in fewer registers, relax cell by cell: in packed pairs they spilled and ran slower (also
+        // one pair at a time with 4-byte stores).
+        auto pulled = [&](int q, int v) -> raw {
+            return cx(q) > 0 ? (v == 0 ? E[q] : L[q].v[v - 1]) : (cx(q) < 0 ? (v == 3 ? E[q] : L[q].v[v + 1]) : L[q].v[v]);
         };
         const int cell0 = (k * MB + j) * MB + i0;
+        if constexpr (sizeof(raw) == 4) {
+            float2 g[2][Q];
 #pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            Vec4<ST> o;
+            for (int q = 0; q < Q; ++q) {
+                g[0][q] = make_float2(PoolIO<ST>::g_of(pulled(q, 0), q), PoolIO<ST>::g_of(pulled(q, 1), q));
+                g[1][q] = make_float2(PoolIO<ST>::g_of(pulled(q, 2), q), PoolIO<ST>::g_of(pulled(q, 3), q));
+            }
+            bgk_lanes<float2, true>(g[0], om);
+            bgk_lanes<float2, true>(g[1], om);
 #pragma unroll
-            for (int v = 0; v < 4; ++v) o.v[v] = PoolIO<ST>::of_g(out(v, q), q);
-            o.store(fbuf + ((size_t)b * Q + q) * MB3 + cell0);
-            if (FUSE) {  // the restriction works on unshifted populations of the values as stored
+            for (int q = 0; q < Q; ++q) {
+                Vec4<ST> o;
+                o.v[0] = PoolIO<ST>::of_g(g[0][q].x, q);
+                o.v[1] = PoolIO<ST>::of_g(g[0][q].y, q);
+                o.v[2] = PoolIO<ST>::of_g(g[1][q].x, q);
+                o.v[3] = PoolIO<ST>::of_g(g[1][q].y, q);
+                o.store(fbuf + ((size_t)b * Q + q) * MB3 + cell0);
+                if (FUSE) {  // the restriction works on unshifted populations of the values as stored
 #pragma unroll
-                for (int v = 0; v < 4; ++v) sf[q * MB3 + cell0 + v] = PoolIO<ST>::f_of(o.v[v], q);
+                    for (int v = 0; v < 4; ++v) sf[q * MB3 + cell0 + v] = PoolIO<ST>::f_of(o.v[v], q);
+                }
+            }
+        } else {
+            float f[4][Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) f[v][q] = PoolIO<ST>::g_of(pulled(q, v), q);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) bgk_fast<true>(f[v], om);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                Vec4<ST> o;
+#pragma unroll
+                for (int v = 0; v < 4; ++v) o.v[v] = PoolIO<ST>::of_g(f[v][q], q);
+                o.store(fbuf + ((size_t)b * Q + q) * MB3 + cell0);
+                if (FUSE) {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) sf[q * MB3 + cell0 + v] = PoolIO<ST>::f_of(o.v[v], q);
+                }
             }
         }
     }
