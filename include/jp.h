@@ -211,7 +211,7 @@ jp_status jp_memory_info(jp_solver* s, int64_t* free_bytes, int64_t* total_bytes
  * uniform solver's jp_diag), 0 exactly (the AMR composite).  Scratch lives in a fixed 384 KiB device
  * array inside the library, so fields above 268,435,456 cells (n > 645) are rejected with
  * JP_ERR_CAPACITY.  The first call on each device looks up that array's address (again after the
- * device's context was replaced, e.g. by cudaDeviceReset) and should come before any stream capture.
+ * device's context was replaced, e.g. by cudaDeviceReset).
  * Calls share the array: calls that overlap on the GPU race and must be serialised by the caller. */
 jp_status jp_diag_field_noalloc(const float* field_dev, int32_t n, int32_t float_diff, double* out_dev,
                                 void* stream);

@@ -18,9 +18,7 @@
 // Host code cannot use the array's name as a device address (it names a host-side stand-in); the
 // device address is looked up with cudaGetSymbolAddress on the first call made with a device's
 // context current, and looked up again when that context has been replaced (cudaDeviceReset tears
-// the primary context down and the next one loads the module anew, possibly elsewhere).  The
-// lookup may load the module, so the first call on each device should come before any stream
-// capture.
+// the primary context down and the next one loads the module anew, possibly elsewhere).
 #include <cuda.h>
 #include <cuda_runtime.h>
 
